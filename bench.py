@@ -1,0 +1,311 @@
+"""Benchmark: RAW->RGB MPix/s on one GB300, with the CPU oracle beside it.
+
+Workload (default): the phone-resolution plain pipeline -- three 4032x3024 RGGB 12-bit
+synthetic frames at read-noise/gain {2/1, 6/4, 12/16} (the last one takes the high-noise
+raw branch), 5-level pyramid, fp32 intermediates, local tone mapping on, RGBA8 output.
+One step = those three frames through RawConverter::demosaicImage.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+value: MPix/s with the raw frames already in HBM, CUDA-event timed per step with an L2
+flush (a 256 MB write) between steps, max over ranks.  e2e: the same frames through the
+host-buffer entry point (pinned uint16 in, RGBA8 out, copies inside the timed region).
+--impl reference times the CPU restatement of the reference pipeline (the oracle; the
+reference's OpenCL kernels cannot run on this machine) with every host thread.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "RAW→RGB MPix/s on 1 GB300 (plain vs batched/learned) at PSNR vs FP64 oracle"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gls", choices=["gls", "reference"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile-only", action="store_true", help="a short run for ncu: no clocks, no cpu leg")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def make_frames(cfg, rank):
+    from climage_gb300 import configs, synthetic
+    frames = []
+    for i, (sigma, gain, nl) in enumerate(cfg["noise"]):
+        raw, scene, meta = synthetic.make_frame(cfg["width"], cfg["height"], bayer=cfg["bayer"], bits=cfg["bits"],
+                                                black=cfg["black"], white=cfg["white"], wb=cfg["wb"], gain=gain,
+                                                read_sigma=sigma, seed=1000 * rank + i)
+        spec = configs.make_spec(meta, levels=cfg["levels"], storage=cfg["storage"], noise_level=nl)
+        frames.append((raw, scene, spec))
+    return frames
+
+
+def algorithmic_bytes_per_px(S, O, L):
+    """Compulsory traffic of the reference dataflow: 8 + 5S + O + 7S*G."""
+    G = sum(4.0 ** -l for l in range(1, L))
+    return 8 + 5 * S + O + 7 * S * G
+
+
+# algorithmic bytes per pixel of each single-stage kernel (fp32 storage S=16 B RGBA, 4 B single)
+def stage_bytes(name, s1, s4):
+    table = {
+        "scaleRawData": 2 + s1, "interpolateGreen": 2 * s1, "interpolateRedBlue": 2 * s1 + s4,
+        "blendHighlights": 2 * s4, "transformImage": 2 * s4, "despeckleImage": 2 * s4,
+        "denoise L0": 2 * s4, "reassemble L0": 2 * s4, "localToneMappingMask": s4 + s1,
+        "convertTosRGB": s4 + s1 + 4, "noiseStatistics+fit L0": s4, "rawNoiseStatistics+fit": s1,
+    }
+    return table.get(name)
+
+
+class ClockSampler:
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for s in self.samples:
+            for k, n in enumerate(names):
+                if len(s) > 5 + k and s[5 + k].lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.samples)}
+
+
+def measured_peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def cpu_leg(frames, max_seconds=30.0):
+    """The oracle on the host cores over a bounded sample: the first frame, full size."""
+    from oracle import oracle as orc
+    from tests.helpers import oracle_params
+    raw, _, spec = frames[0]
+    threads = orc.threads()
+    t0 = time.perf_counter()
+    n = 0
+    while True:
+        orc.demosaic(raw, oracle_params(spec), orc.F32, want=("rgba8",))
+        n += 1
+        if time.perf_counter() - t0 > max_seconds * 0.3 or n >= 3:
+            break
+    dt = (time.perf_counter() - t0) / n
+    mpix = raw.size / 1e6
+    return {"value": round(mpix / dt, 3), "unit": "MPix/s", "cores": threads, "kind": "port",
+            "sample": "%d frame(s) of %dx%d (read sigma %.0f DN, gain %.0f), oracle fp32, %d threads, %.2f s/frame"
+                      % (n, raw.shape[1], raw.shape[0], 2.0, 1.0, threads, dt)}
+
+
+def run_reference(args, cfg):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import oracle as orc
+    from tests.helpers import oracle_params
+    frames = make_frames(cfg, 0)
+    threads = orc.threads()
+    times = []
+    for i in range(args.warmup + args.steps):
+        raw, _, spec = frames[i % len(frames)]
+        t0 = time.perf_counter()
+        orc.demosaic(raw, oracle_params(spec), orc.F32, want=("rgba8",))
+        dt = time.perf_counter() - t0
+        if i >= args.warmup:
+            times.append(dt)
+    mpix = cfg["width"] * cfg["height"] / 1e6
+    value = mpix * len(times) / sum(times)
+    line = {"metric": METRIC, "value": round(value, 3), "unit": "MPix/s", "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1000 * sum(times) / len(times), 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": cfg["name"] + " (one frame per step)", "frames_per_step": 1,
+                       "width": cfg["width"], "height": cfg["height"], "levels": cfg["levels"]},
+            "cpu_baseline": {"value": round(value, 3), "unit": "MPix/s", "cores": threads, "kind": "port",
+                             "sample": "one full frame per step, cycling the three noise levels"},
+            "e2e": {"value": round(value, 3), "unit": "MPix/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    from climage_gb300 import configs
+    cfg = configs.CONFIG2
+    if args.impl == "reference":
+        run_reference(args, cfg)
+        return
+    import torch
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local if world > 1 else 0)
+    torch.cuda.set_device(dev)
+    from climage_gb300 import gls
+
+    frames = make_frames(cfg, rank)
+    ctx = gls.Context(dev.index)
+    conv = gls.RawConverter(ctx)
+    h, w = cfg["height"], cfg["width"]
+    raws = [torch.from_numpy(f[0]).to(dev) for f in frames]
+    params = [configs.to_gls_params(f[2]) for f in frames]
+    outs = [torch.empty((h, w, 4), dtype=torch.uint8, device=dev) for _ in frames]
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        for r, p, o in zip(raws, params, outs):
+            conv.demosaicImage(r, p, o, defer_noise_model=True)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    launches0 = ctx.kernel_launches()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    sampler = ClockSampler(dev.index)
+    with sampler:
+        torch.cuda.synchronize()
+        for k in range(args.steps):
+            flush.fill_(k & 0xFF)
+            starts[k].record(stream)
+            step()
+            ends[k].record(stream)
+        torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    launches = ctx.kernel_launches() - launches0
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_ms = float(sum(step_ms))
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    mpix_per_step = len(frames) * w * h / 1e6
+    value = world * mpix_per_step * args.steps / (total_ms / 1e3)
+
+    # ---- per-stage profile (separate pass) and roofline of the dominant kernel ----
+    conv.profile(True)
+    for _ in range(2):
+        step()
+    torch.cuda.synchronize()
+    prof = conv.profileReport()
+    conv.profile(False)
+    peak, peak_kind = measured_peak_hbm()
+    S1, S4 = 4, 16
+    dom = max((k for k in prof if stage_bytes(k, S1, S4)), key=lambda k: prof[k][0])
+    dom_ms = prof[dom][0] / prof[dom][1]
+    dom_bytes = stage_bytes(dom, S1, S4) * w * h
+    achieved = dom_bytes / (dom_ms / 1e3) / 1e9
+    bpp = algorithmic_bytes_per_px(16, 4, cfg["levels"])
+    frame_ms = total_ms / args.steps / len(frames)
+    pipe_achieved = bpp * w * h / (frame_ms / 1e3) / 1e9
+
+    # ---- end to end through the host-buffer entry point ----
+    e2e = None
+    if not args.no_e2e and not args.profile_only:
+        hosts = [torch.from_numpy(f[0]).pin_memory() for f in frames]
+        houts = [torch.empty((h, w, 4), dtype=torch.uint8).pin_memory() for _ in frames]
+        for hr, ho, p in zip(hosts, houts, params):
+            conv.demosaicImageHostPtr(hr.data_ptr(), w, h, p, ho.data_ptr(), 4)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            for hr, ho, p in zip(hosts, houts, params):
+                conv.demosaicImageHostPtr(hr.data_ptr(), w, h, p, ho.data_ptr(), 4)
+        e2e_s = time.perf_counter() - t0
+        e2e = {"value": round(world * mpix_per_step * args.steps / e2e_s, 3), "unit": "MPix/s",
+               "h2d_bytes_per_step": int(sum(f[0].nbytes for f in frames)),
+               "d2h_bytes_per_step": int(len(frames) * w * h * 4 + len(frames) * 9 * 8 * 4)}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu and not args.profile_only:
+        cpu = cpu_leg(frames)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": "MPix/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": cfg["name"], "frames_per_step": len(frames), "width": w, "height": h,
+                       "levels": cfg["levels"], "storage": "fp32", "output": "rgba8", "local_tone_mapping": True,
+                       "noise": cfg["noise"], "l2": "flushed between steps (256 MB write)",
+                       "parallelism": "replicas" if world > 1 else "single"},
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
+                         "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+                         "algorithmic_bytes_per_px": stage_bytes(dom, S1, S4)},
+            "pipeline_roofline": {"algorithmic_bytes_per_px": round(bpp, 2), "achieved": round(pipe_achieved, 1),
+                                  "unit": "GB/s", "frac": round(pipe_achieved / peak, 4), "ms_per_frame": round(frame_ms, 4)},
+            "stages_ms_per_frame": {k: round(v[0] / (2 * len(frames)), 4) for k, v in prof.items()},
+            "gpu_launches": int(launches),
+            "clocks": sampler.summary(),
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    conv.close()
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

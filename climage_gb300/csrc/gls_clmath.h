@@ -1,0 +1,332 @@
+// Copyright (c) 2026 gls-cuda authors. Licensed under the Apache License, Version 2.0.
+//
+// gls_clmath.h -- the OpenCL C built-in functions used by the RAW pipeline kernels,
+// with their semantics fixed once for every compiler that builds this project.
+//
+// The reference kernels (CLImage/app/src/main/cpp/OpenCL/demosaic.cl) are built with
+// -cl-fast-relaxed-math (src/gls_cl.cpp:161-165), so their transcendentals, min/max on
+// signed zeros and texture filtering are implementation-defined.  This header pins one
+// definition of each built-in so that the CUDA kernels and the CPU restatement produce
+// bit-identical float results:
+//
+//   * arithmetic is IEEE-754 binary32 with round-to-nearest-even, no contraction of
+//     a*b+c into fused multiply-add (nvcc --fmad=false, g++ -ffp-contract=off);
+//   * sqrt and division are correctly rounded (nvcc -prec-sqrt=true -prec-div=true);
+//   * atan2pi, tanh, exp2, log2 and pow are evaluated by the polynomial approximations
+//     below, derived by climage_gb300/csrc/fit_clmath_coeffs.py (Lawson-refined
+//     least squares on Chebyshev nodes), using only +, -, *, / and exact bit operations;
+//   * min/max/clamp follow the OpenCL fmin/fmax rules (a NaN operand yields the other
+//     operand) and, for equal operands, return the first one;
+//   * float -> half conversion rounds to nearest even (what write_imageh / half image
+//     storage does), with overflow to infinity.
+//
+// Accuracy of the approximations against correctly rounded results is checked by
+// tests/test_clmath.py (a few ulp); nothing in this header calls the platform libm
+// for a transcendental.
+#ifndef GLS_CLMATH_H
+#define GLS_CLMATH_H
+
+#include <stdint.h>
+#include <string.h>
+
+#if defined(__CUDACC__)
+#include <cuda_fp16.h>
+#endif
+
+#if defined(__CUDACC__)
+#define GLS_HD __host__ __device__ __forceinline__
+#else
+#define GLS_HD static inline
+#endif
+
+namespace glsm {
+
+GLS_HD uint32_t f2u(float f) {
+#if defined(__CUDA_ARCH__)
+    return __float_as_uint(f);
+#else
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    return u;
+#endif
+}
+
+GLS_HD float u2f(uint32_t u) {
+#if defined(__CUDA_ARCH__)
+    return __uint_as_float(u);
+#else
+    float f;
+    memcpy(&f, &u, 4);
+    return f;
+#endif
+}
+
+GLS_HD bool isnan_(float x) { return x != x; }
+GLS_HD float inf_() { return u2f(0x7f800000u); }
+GLS_HD float nan_() { return u2f(0x7fc00000u); }
+GLS_HD bool signbit_(float x) { return (f2u(x) >> 31) != 0; }
+GLS_HD float fabs_(float x) { return u2f(f2u(x) & 0x7fffffffu); }
+GLS_HD float copysign_(float x, float s) { return u2f((f2u(x) & 0x7fffffffu) | (f2u(s) & 0x80000000u)); }
+
+GLS_HD float sqrt_(float x) {
+#if defined(__CUDA_ARCH__)
+    return __fsqrt_rn(x);
+#else
+    return __builtin_sqrtf(x);
+#endif
+}
+
+GLS_HD float div_(float a, float b) {
+#if defined(__CUDA_ARCH__)
+    return __fdiv_rn(a, b);
+#else
+    return a / b;
+#endif
+}
+
+GLS_HD float floor_(float x) {
+#if defined(__CUDA_ARCH__)
+    return floorf(x);
+#else
+    return __builtin_floorf(x);
+#endif
+}
+
+GLS_HD float rint_(float x) {
+#if defined(__CUDA_ARCH__)
+    return rintf(x);
+#else
+    return __builtin_rintf(x);
+#endif
+}
+
+// OpenCL fmax/fmin: a NaN argument yields the other argument; ties keep the first.
+GLS_HD float fmax_(float a, float b) { return isnan_(a) ? b : (isnan_(b) ? a : (a < b ? b : a)); }
+GLS_HD float fmin_(float a, float b) { return isnan_(a) ? b : (isnan_(b) ? a : (b < a ? b : a)); }
+
+// OpenCL clamp(x, lo, hi) == fmin(fmax(x, lo), hi)
+GLS_HD float clamp_(float x, float lo, float hi) { return fmin_(fmax_(x, lo), hi); }
+
+// OpenCL mix(x, y, a) == x + (y - x) * a
+GLS_HD float mix_(float x, float y, float a) { return x + (y - x) * a; }
+
+// OpenCL step(edge, x) == x < edge ? 0 : 1
+GLS_HD float step_(float edge, float x) { return x < edge ? 0.0f : 1.0f; }
+
+// OpenCL smoothstep(e0, e1, x): t = clamp((x - e0) / (e1 - e0), 0, 1); t * t * (3 - 2 * t)
+GLS_HD float smoothstep_(float e0, float e1, float x) {
+    float t = clamp_(div_(x - e0, e1 - e0), 0.0f, 1.0f);
+    return t * t * (3.0f - 2.0f * t);
+}
+
+// The reference's own min/max/abs macros (demosaic.cl:56-65): plain selects.
+GLS_HD float mmin(float a, float b) { return a < b ? a : b; }
+GLS_HD float mmax(float a, float b) { return a > b ? a : b; }
+GLS_HD float mabs(float a) { return a > 0 ? a : -a; }
+
+// OpenCL length(): square root of the dot product, summed left to right.
+GLS_HD float length2_(float x, float y) { return sqrt_(x * x + y * y); }
+GLS_HD float length3_(float x, float y, float z) { return sqrt_(x * x + y * y + z * z); }
+GLS_HD float length4_(float x, float y, float z, float w) { return sqrt_(x * x + y * y + z * z + w * w); }
+
+// ---- binary16 storage rounding ----
+
+// float -> IEEE binary16 bits, round to nearest even; NaN -> quiet NaN, overflow -> inf.
+GLS_HD uint16_t f32_to_f16_bits(float f) {
+    const uint32_t b = f2u(f);
+    const uint32_t sign = (b >> 16) & 0x8000u;
+    const uint32_t a = b & 0x7fffffffu;
+    if (a >= 0x7f800000u) return (uint16_t)(sign | (a > 0x7f800000u ? 0x7e00u : 0x7c00u));
+    if (a >= 0x477ff000u) return (uint16_t)(sign | 0x7c00u);  // >= 65520 rounds to inf
+    if (a < 0x38800000u) {                                     // below 2^-14: subnormal half
+        // |f| * 2^24 is exact and < 2^10; rint rounds to nearest even.
+        const uint32_t r = (uint32_t)rint_(fabs_(f) * 16777216.0f);
+        return (uint16_t)(sign | r);
+    }
+    uint32_t h = ((((a >> 23) - 112u) << 10) | ((a >> 13) & 0x3ffu));
+    const uint32_t rem = a & 0x1fffu;
+    if (rem > 0x1000u || (rem == 0x1000u && (h & 1u))) h += 1u;
+    return (uint16_t)(sign | h);
+}
+
+GLS_HD float f16_bits_to_f32(uint16_t h) {
+    const uint32_t sign = ((uint32_t)h & 0x8000u) << 16;
+    const uint32_t e = ((uint32_t)h >> 10) & 0x1fu;
+    const uint32_t m = (uint32_t)h & 0x3ffu;
+    if (e == 0) {
+        // subnormal or zero: m * 2^-24, exact in float
+        const float v = (float)m * 5.9604644775390625e-8f;
+        return u2f(f2u(v) | sign);
+    }
+    if (e == 31) return u2f(sign | 0x7f800000u | (m << 13));
+    return u2f(sign | ((e + 112u) << 23) | (m << 13));
+}
+
+// Round a float to the nearest binary16 value (as a float).
+GLS_HD float round_half(float f) {
+#if defined(__CUDA_ARCH__)
+    return __half2float(__float2half_rn(f));
+#else
+    return f16_bits_to_f32(f32_to_f16_bits(f));
+#endif
+}
+
+// ---- transcendentals ----
+
+// atan2(y, x) / pi with the C99 special values.
+GLS_HD float atan2pi_(float y, float x) {
+    if (isnan_(x) || isnan_(y)) return x + y;
+    const float ax = fabs_(x), ay = fabs_(y);
+    const bool xneg = signbit_(x);
+    float r;
+    if (ay == 0.0f) {
+        r = xneg ? 1.0f : 0.0f;
+    } else if (ax == 0.0f) {
+        r = 0.5f;
+    } else if (ax == inf_() && ay == inf_()) {
+        r = xneg ? 0.75f : 0.25f;
+    } else if (ax == inf_()) {
+        r = xneg ? 1.0f : 0.0f;
+    } else if (ay == inf_()) {
+        r = 0.5f;
+    } else {
+        const bool swap = ay > ax;
+        const float a = swap ? div_(ax, ay) : div_(ay, ax);
+        const float s = a * a;
+        float p = -5.582857679e-04f;
+        p = p * s + 3.414458497e-03f;
+        p = p * s + -9.805344525e-03f;
+        p = p * s + 1.831933928e-02f;
+        p = p * s + -2.666578585e-02f;
+        p = p * s + 3.482955246e-02f;
+        p = p * s + -4.539714054e-02f;
+        p = p * s + 6.365645763e-02f;
+        p = p * s + -1.061031372e-01f;
+        p = p * s + 3.183098854e-01f;
+        r = a * p;
+        if (swap) r = 0.5f - r;
+        if (xneg) r = 1.0f - r;
+    }
+    return copysign_(r, y);
+}
+
+// 2^x
+GLS_HD float exp2_(float x) {
+    if (isnan_(x)) return x;
+    if (x >= 128.0f) return inf_();
+    if (x < -150.0f) return 0.0f;
+    const float n = floor_(x + 0.5f);
+    const float f = x - n;  // [-0.5, 0.5], exact
+    float p = 1.534580750e-04f;
+    p = p * f + 1.339993118e-03f;
+    p = p * f + 9.618488974e-03f;
+    p = p * f + 5.550328777e-02f;
+    p = p * f + 2.402264689e-01f;
+    p = p * f + 6.931472057e-01f;
+    p = p * f + 1.000000001e+00f;
+    int e = (int)n;
+    if (e > 127) {
+        p = p * 2.0f;
+        e -= 1;
+    }
+    if (e < -126) {
+        // scale in two exact steps to reach the subnormal range
+        p = p * u2f((uint32_t)(e + 126 + 127) << 23);
+        return p * u2f((uint32_t)(-126 + 127) << 23);
+    }
+    return p * u2f((uint32_t)(e + 127) << 23);
+}
+
+// log2(x)
+GLS_HD float log2_(float x) {
+    if (isnan_(x)) return x;
+    if (x < 0.0f) return nan_();
+    if (x == 0.0f) return -inf_();
+    if (x == inf_()) return x;
+    float k = 0.0f;
+    if (x < 1.17549435e-38f) {  // subnormal: scale by 2^24 (exact)
+        x = x * 16777216.0f;
+        k = -24.0f;
+    }
+    uint32_t b = f2u(x);
+    int e = (int)((b >> 23) & 0xffu) - 127;
+    float m = u2f((b & 0x007fffffu) | 0x3f800000u);  // [1, 2)
+    if (m > 1.41421356f) {
+        m = m * 0.5f;
+        e += 1;
+    }
+    const float z = div_(m - 1.0f, m + 1.0f);
+    const float s = z * z;
+    float p = 2.381667258e-02f;
+    p = p * s + 3.386064467e-01f;
+    p = p * s + 4.117443166e-01f;
+    p = p * s + 5.770824732e-01f;
+    p = p * s + 9.617966808e-01f;
+    p = p * s + 2.885390082e+00f;
+    return ((float)e + k) + z * p;
+}
+
+GLS_HD bool is_integer_(float y) { return floor_(y) == y; }
+
+// OpenCL pow(x, y) for the cases the pipeline meets: finite or infinite x, finite y.
+GLS_HD float pow_(float x, float y) {
+    if (y == 0.0f || x == 1.0f) return 1.0f;
+    if (isnan_(x) || isnan_(y)) return x + y;
+    if (x == 0.0f) return y < 0.0f ? inf_() : 0.0f;
+    if (x < 0.0f) {
+        if (!is_integer_(y)) return nan_();
+        const float r = exp2_(y * log2_(-x));
+        const float half_y = y * 0.5f;
+        return is_integer_(half_y) ? r : -r;
+    }
+    if (x == inf_()) return y < 0.0f ? 0.0f : x;
+    return exp2_(y * log2_(x));
+}
+
+// OpenCL powr(x, y): defined for x >= 0 only.
+GLS_HD float powr_(float x, float y) {
+    if (x < 0.0f || isnan_(x) || isnan_(y)) return nan_();
+    if (x == 0.0f) return y == 0.0f ? nan_() : (y < 0.0f ? inf_() : 0.0f);
+    if (x == 1.0f) return 1.0f;
+    if (y == 0.0f) return 1.0f;
+    return exp2_(y * log2_(x));
+}
+
+// tanh(x)
+GLS_HD float tanh_(float x) {
+    if (isnan_(x)) return x;
+    const float ax = fabs_(x);
+    float r;
+    if (ax < 0.625f) {
+        const float s = ax * ax;
+        float p = 6.422573784e-04f;
+        p = p * s + 1.535835834e-03f;
+        p = p * s + -8.009078423e-03f;
+        p = p * s + 2.170054290e-02f;
+        p = p * s + -5.395293793e-02f;
+        p = p * s + 1.333328214e-01f;
+        p = p * s + -3.333333306e-01f;
+        r = ax + ax * (s * p);
+    } else if (ax < 9.01f) {
+        const float e = exp2_(ax * 2.88539008f);  // e^(2|x|)
+        r = 1.0f - div_(2.0f, e + 1.0f);
+    } else {
+        r = 1.0f;
+    }
+    return copysign_(r, x);
+}
+
+// UNORM8 image write (write_imagef on CL_UNORM_INT8): convert_uchar_sat_rte(x * 255)
+GLS_HD uint8_t to_unorm8(float x) {
+    const float v = x * 255.0f;
+    if (!(v > 0.0f)) return 0;  // NaN and negatives
+    if (v >= 255.0f) return 255;
+    return (uint8_t)rint_(v);
+}
+
+// UNORM16 image read (read_imagef on CL_UNORM_INT16)
+GLS_HD float from_unorm16(uint16_t v) { return div_((float)v, 65535.0f); }
+
+}  // namespace glsm
+
+#endif  // GLS_CLMATH_H

@@ -1,0 +1,655 @@
+// gls_pixel_ops.cuh -- the per-pixel arithmetic of every stage of CLImage's RAW->RGB
+// pipeline, written once and shared by the single-stage kernels (global-memory
+// accessors) and the fused pipeline kernels (shared-memory tiles).
+//
+// Each function follows the reference kernel named in its comment operation by
+// operation, in the same order, so that the result is bit-identical to the CPU
+// restatement under the conventions of gls_clmath.h.  An accessor (Acc) is any type with
+// `float at(int x, int y)` (single channel) or `float4 at(int x, int y)` (RGBA) that
+// clamps to the image edge.
+#ifndef GLS_PIXEL_OPS_CUH
+#define GLS_PIXEL_OPS_CUH
+
+#include "gls_device.cuh"
+
+namespace gls {
+
+using glsm::clamp_;
+using glsm::div_;
+using glsm::length2_;
+using glsm::length3_;
+using glsm::length4_;
+using glsm::mabs;
+using glsm::mix_;
+using glsm::mmax;
+using glsm::mmin;
+using glsm::smoothstep_;
+using glsm::sqrt_;
+using glsm::step_;
+
+#define GLS_SQRT2_F 1.41421356237309504880f
+#define GLS_SQRT3_F 1.7320508f
+
+// ---- a4: scaleRawData (demosaic.cl:69-78) ----
+GLS_DI float scale_value(uint16_t raw, float scale_mul, float black) {
+    const float v = div_((float)raw, 65535.0f);
+    const float r = scale_mul * (v - black);
+    return r > 0.0f ? r : 0.0f;
+}
+
+// ---- a5: rawNoiseStatistics + readRAWQuad (demosaic.cl:1288-1324) ----
+template <class Acc>
+GLS_DI void raw_stats_quad(const Acc& raw, int qx, int qy, int bayer, float mean[4], float var[4]) {
+    float sum[4] = {0.0f, 0.0f, 0.0f, 0.0f}, sq[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+    for (int y = -2; y <= 2; y++) {
+#pragma unroll
+        for (int x = -2; x <= 2; x++) {
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                const float s = raw.at(2 * (qx + x) + bayer_dx(bayer, c), 2 * (qy + y) + bayer_dy(bayer, c));
+                sum[c] = sum[c] + s;
+                sq[c] = sq[c] + s * s;
+            }
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        mean[c] = div_(sum[c], 25.0f);
+        var[c] = div_(sq[c] - div_(sum[c] * sum[c], 25.0f), 25.0f);
+    }
+}
+
+// ---- a13: noiseStatistics (demosaic.cl:1267-1286): (mean Y, var Y, var Cb, var Cr) ----
+template <class Acc>
+GLS_DI float4 noise_stats_px(const Acc& im, int px, int py) {
+    float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, q0 = 0.0f, q1 = 0.0f, q2 = 0.0f;
+#pragma unroll
+    for (int y = -2; y <= 2; y++) {
+#pragma unroll
+        for (int x = -2; x <= 2; x++) {
+            const float4 s = im.at(px + x, py + y);
+            s0 = s0 + s.x;
+            q0 = q0 + s.x * s.x;
+            s1 = s1 + s.y;
+            q1 = q1 + s.y * s.y;
+            s2 = s2 + s.z;
+            q2 = q2 + s.z * s.z;
+        }
+    }
+    float4 r;
+    r.x = div_(s0, 25.0f);
+    r.y = div_(q0 - div_(s0 * s0, 25.0f), 25.0f);
+    r.z = div_(q1 - div_(s1 * s1, 25.0f), 25.0f);
+    r.w = div_(q2 - div_(s2 * s2, 25.0f), 25.0f);
+    return r;
+}
+
+// ---- a7: sobel / bilateralSobel / interpolateGreen (demosaic.cl:96-129, 160-227) ----
+struct SobelVal {
+    float gx, gy, len;  // |sobel| components and their length
+};
+
+template <class Acc>
+GLS_DI SobelVal sobel_abs(const Acc& im, int x, int y) {
+    const float kx[3][3] = {{1.0f, 0.0f, -1.0f}, {2.0f, 0.0f, -2.0f}, {1.0f, 0.0f, -1.0f}};
+    const float ky[3][3] = {{1.0f, 2.0f, 1.0f}, {0.0f, 0.0f, 0.0f}, {-1.0f, -2.0f, -1.0f}};
+    float vx = 0.0f, vy = 0.0f;
+#pragma unroll
+    for (int j = -1; j <= 1; j++) {
+#pragma unroll
+        for (int i = -1; i <= 1; i++) {
+            const float s = im.at(x + i, y + j);
+            vx = vx + kx[j + 1][i + 1] * s;
+            vy = vy + ky[j + 1][i + 1] * s;
+        }
+    }
+    const float r = sqrt_(4.5f);
+    SobelVal o;
+    o.gx = mabs(div_(vx, r));
+    o.gy = mabs(div_(vy, r));
+    o.len = length2_(o.gx, o.gy);
+    return o;
+}
+
+// Signed sobel of a single channel (used by denoiseImage's gradient boost).
+template <class Acc>
+GLS_DI float2 sobel_signed(const Acc& im, int x, int y) {
+    const float kx[3][3] = {{1.0f, 0.0f, -1.0f}, {2.0f, 0.0f, -2.0f}, {1.0f, 0.0f, -1.0f}};
+    const float ky[3][3] = {{1.0f, 2.0f, 1.0f}, {0.0f, 0.0f, 0.0f}, {-1.0f, -2.0f, -1.0f}};
+    float vx = 0.0f, vy = 0.0f;
+#pragma unroll
+    for (int j = -1; j <= 1; j++) {
+#pragma unroll
+        for (int i = -1; i <= 1; i++) {
+            const float s = im.at(x + i, y + j);
+            vx = vx + kx[j + 1][i + 1] * s;
+            vy = vy + ky[j + 1][i + 1] * s;
+        }
+    }
+    const float r = sqrt_(4.5f);
+    return make_float2(div_(vx, r), div_(vy, r));
+}
+
+// sob(i, j) returns the SobelVal at offset (i, j) from the centre.
+template <class SobF>
+GLS_DI float2 bilateral_sobel(const SobF& sob, float sigma) {
+    const SobelVal c = sob(0, 0);
+    float sx = 0.0f, sy = 0.0f, ws = 0.0f;
+    const float e0 = 4.0f * sigma, e1 = 16.0f * sigma;
+#pragma unroll
+    for (int j = -2; j <= 2; j++) {
+#pragma unroll
+        for (int i = -2; i <= 2; i++) {
+            const SobelVal g = sob(i, j);
+            const float w = 1.0f - smoothstep_(e0, e1, 0.05f * mabs(g.len - c.len));
+            sx = sx + w * g.gx;
+            sy = sy + w * g.gy;
+            ws = ws + w;
+        }
+    }
+    return make_float2(div_(sx, ws), div_(sy, ws));
+}
+
+// True when (x, y) is a red or blue site, where green has to be interpolated.
+GLS_DI bool green_needs_interp(int x, int y, int bayer) {
+    const int gx = bayer_dx(bayer, raw_green), gy = bayer_dy(bayer, raw_green);
+    const int x0 = (y & 1) == (gy & 1) ? gx + 1 : gx;
+    return (x0 & 1) == (x & 1);
+}
+
+// Green at a red/blue site; lumaVariance already clamped to >= 1e-4.
+template <class Acc, class SobF>
+GLS_DI float green_at(const Acc& raw, int x, int y, float lumaVariance, const SobF& sob) {
+    const float g_left = raw.at(x - 1, y), g_right = raw.at(x + 1, y);
+    const float g_up = raw.at(x, y - 1), g_down = raw.at(x, y + 1);
+    const float c_xy = raw.at(x, y);
+    const float c_left = raw.at(x - 2, y), c_right = raw.at(x + 2, y);
+    const float c_up = raw.at(x, y - 2), c_down = raw.at(x, y + 2);
+    const float c2_tl = raw.at(x - 1, y - 1), c2_tr = raw.at(x + 1, y - 1);
+    const float c2_bl = raw.at(x - 1, y + 1), c2_br = raw.at(x + 1, y + 1);
+    const float c2_ave = div_(c2_tl + c2_tr + c2_bl + c2_br, 4.0f);
+
+    const float g_ave = div_(g_left + g_right + g_up + g_down, 4.0f);
+    const float lumaStdDev = sqrt_(lumaVariance * g_ave);
+    const float2 grad = bilateral_sobel(sob, lumaStdDev);
+
+    const float g_lf_x = div_(g_left + g_right, 2.0f), g_lf_y = div_(g_up + g_down, 2.0f);
+    const float g_hf_x = div_(2.0f * c_xy - (c_left + c_right), 4.0f);
+    const float g_hf_y = div_(2.0f * c_xy - (c_up + c_down), 4.0f);
+
+    const float whiteness =
+        clamp_(div_(mmin(c_xy, mmin(g_ave, c2_ave)), mmax(c_xy, mmax(g_ave, c2_ave))), 0.0f, 1.0f);
+    const float glen = length2_(grad.x, grad.y);
+    const float lgt = smoothstep_(lumaStdDev, 4.0f * lumaStdDev, glen);
+    const float hf_gain = lgt * mmin(0.5f * whiteness + smoothstep_(0.0f, 0.3f, div_(glen, GLS_SQRT2_F)), 1.0f);
+    const float g_est_x = g_lf_x + hf_gain * g_hf_x;
+    const float g_est_y = g_lf_y + hf_gain * g_hf_y;
+
+    float direction = 2.0f * glsm::atan2pi_(grad.y, grad.x);
+    direction = direction < 0.5f
+                    ? mix_(direction, 0.0f, 1.0f - smoothstep_(0.3f * lgt, 0.45f * lgt, direction))
+                    : mix_(direction, 1.0f, smoothstep_((1.0f - 0.45f) * lgt, (1.0f - 0.3f) * lgt, direction));
+    direction = mix_(0.5f, direction, lgt);
+    return mix_(g_est_y, g_est_x, direction);
+}
+
+// ---- a8: interpolateRedBlue (demosaic.cl:229-318) -> (red, green, blue) ----
+template <class AccR, class AccG>
+GLS_DI float3 red_blue_at(const AccR& raw, const AccG& gi, int x, int y, int bayer, float chromaVariance) {
+    const int rx = bayer_dx(bayer, raw_red), ry = bayer_dy(bayer, raw_red);
+    const int gx = bayer_dx(bayer, raw_green), gy = bayer_dy(bayer, raw_green);
+    const int bx = bayer_dx(bayer, raw_blue), by = bayer_dy(bayer, raw_blue);
+    const int color = ((rx & 1) == (x & 1) && (ry & 1) == (y & 1))   ? raw_red
+                      : ((gx & 1) == (x & 1) && (gy & 1) == (y & 1)) ? raw_green
+                      : ((bx & 1) == (x & 1) && (by & 1) == (y & 1)) ? raw_blue
+                                                                     : raw_green2;
+    const float green = gi.at(x, y);
+    float red, blue;
+    if (color == raw_red || color == raw_blue) {
+        const float c1 = raw.at(x, y);
+        const float g_tl = gi.at(x - 1, y - 1), g_tr = gi.at(x + 1, y - 1);
+        const float g_bl = gi.at(x - 1, y + 1), g_br = gi.at(x + 1, y + 1);
+        const float c2_tl = g_tl - raw.at(x - 1, y - 1), c2_tr = g_tr - raw.at(x + 1, y - 1);
+        const float c2_bl = g_bl - raw.at(x - 1, y + 1), c2_br = g_br - raw.at(x + 1, y + 1);
+        const float chromaStdDev = sqrt_(chromaVariance * green);
+        const float dvx = glsm::fabs_(c2_tl - c2_br), dvy = glsm::fabs_(c2_tr - c2_bl);
+        const float flatness = 1.0f - smoothstep_(0.25f * chromaStdDev, chromaStdDev, length2_(dvx, dvy));
+        const float alpha = mix_(2.0f * glsm::atan2pi_(dvy, dvx), 0.5f, flatness);
+        const float c2 = green - mix_(div_(c2_tr + c2_bl, 2.0f), div_(c2_tl + c2_br, 2.0f), alpha);
+        if (color == raw_red) {
+            red = c1;
+            blue = c2;
+        } else {
+            blue = c1;
+            red = c2;
+        }
+    } else {
+        const float g_left = gi.at(x - 1, y), g_right = gi.at(x + 1, y);
+        const float g_up = gi.at(x, y - 1), g_down = gi.at(x, y + 1);
+        const float c1_left = g_left - raw.at(x - 1, y), c1_right = g_right - raw.at(x + 1, y);
+        const float c2_up = g_up - raw.at(x, y - 1), c2_down = g_down - raw.at(x, y + 1);
+        const float c1 = green - div_(c1_left + c1_right, 2.0f);
+        const float c2 = green - div_(c2_up + c2_down, 2.0f);
+        const int red_row_green = (bayer == bggr || bayer == grbg) ? raw_green : raw_green2;
+        if (color == red_row_green) {
+            red = c1;
+            blue = c2;
+        } else {
+            blue = c1;
+            red = c2;
+        }
+    }
+    return make_float3(red, green, blue);
+}
+
+// ---- a9: blendHighlightsImage (demosaic.cl:338-380) ----
+GLS_DI float3 blend_highlights_px(float3 p, float clip) {
+    if (p.x > clip || p.y > clip || p.z > clip) {
+        const float S3 = GLS_SQRT3_F;
+        const float h3 = S3 / 2.0f;
+        float c0[3] = {p.x, p.y, p.z};
+        float c1[3] = {mmin(p.x, clip), mmin(p.y, clip), mmin(p.z, clip)};
+        // lab = trans * cam, trans = {{1,1,1},{S3,-S3,0},{-1,-1,2}}
+        float l0[3], l1[3];
+        l0[0] = 1.0f * c0[0] + 1.0f * c0[1] + 1.0f * c0[2];
+        l0[1] = S3 * c0[0] + -S3 * c0[1] + 0.0f * c0[2];
+        l0[2] = -1.0f * c0[0] + -1.0f * c0[1] + 2.0f * c0[2];
+        l1[0] = 1.0f * c1[0] + 1.0f * c1[1] + 1.0f * c1[2];
+        l1[1] = S3 * c1[0] + -S3 * c1[1] + 0.0f * c1[2];
+        l1[2] = -1.0f * c1[0] + -1.0f * c1[1] + 2.0f * c1[2];
+        const float sum0 = l0[1] * l0[1] + l0[2] * l0[2];
+        const float sum1 = l1[1] * l1[1] + l1[2] * l1[2];
+        const float chratio = sum0 > 0.0f ? sqrt_(div_(sum1, sum0)) : 1.0f;
+        l0[1] = l0[1] * chratio;
+        l0[2] = l0[2] * chratio;
+        // itrans = {{1, S3/2, -0.5}, {1, -S3/2, -0.5}, {1, 0, 1}}
+        p.x = div_(1.0f * l0[0] + h3 * l0[1] + -0.5f * l0[2], 3.0f);
+        p.y = div_(1.0f * l0[0] + -h3 * l0[1] + -0.5f * l0[2], 3.0f);
+        p.z = div_(1.0f * l0[0] + 0.0f * l0[1] + 1.0f * l0[2], 3.0f);
+    }
+    return p;
+}
+
+// ---- a10: transformImage (demosaic.cl:728-733) ----
+struct Mat3 {
+    float m[9];
+};
+
+GLS_DI float3 transform_px(const Mat3& t, float3 v) {
+    return make_float3(t.m[0] * v.x + t.m[1] * v.y + t.m[2] * v.z, t.m[3] * v.x + t.m[4] * v.y + t.m[5] * v.z,
+                       t.m[6] * v.x + t.m[7] * v.y + t.m[8] * v.z);
+}
+
+// ---- a11: despeckleLumaMedianChromaImage (demosaic.cl:444-489), bound by the host
+// function despeckleImage (demosaic_cl.cpp:270-291).  Reads through read_imageh (values
+// rounded to binary16); every half-precision operation rounds to binary16. ----
+GLS_DI void cswap(float& a, float& b) {
+    const float t = a;
+    a = mmin(a, b);
+    b = mmax(t, b);
+}
+
+template <class Acc4>
+GLS_DI float4 despeckle_px(const Acc4& im, int px, int py, float va0, float vb0) {
+    using glsm::round_half;
+    float sample = 0.0f, firstMax = 0.0f, secMax = 0.0f;
+    const float hinf = glsm::inf_();  // (half)(float)0xffff overflows to +inf
+    float firstMin = hinf, secMin = hinf;
+    float acb[6], acr[6];
+    auto rd = [&](int dx, int dy, float& cb, float& cr) {
+        const float4 p = im.at(px + dx, py + dy);
+        const float v = round_half(p.x);
+        cb = round_half(p.y);
+        cr = round_half(p.z);
+        secMax = (v <= firstMax && v > secMax) ? v : secMax;
+        secMax = v > firstMax ? firstMax : secMax;
+        firstMax = v > firstMax ? v : firstMax;
+        secMin = (v >= firstMin && v < secMin) ? v : secMin;
+        secMin = v < firstMin ? firstMin : secMin;
+        firstMin = v < firstMin ? v : firstMin;
+        if (dx == 0 && dy == 0) sample = v;
+    };
+    rd(0, -1, acb[0], acr[0]);
+    rd(1, -1, acb[1], acr[1]);
+    rd(0, 0, acb[2], acr[2]);
+    rd(1, 0, acb[3], acr[3]);
+    rd(0, 1, acb[4], acr[4]);
+    rd(1, 1, acb[5], acr[5]);
+    // minMax6
+    cswap(acb[0], acb[1]); cswap(acb[2], acb[3]); cswap(acb[4], acb[5]);
+    cswap(acb[0], acb[2]); cswap(acb[1], acb[3]); cswap(acb[0], acb[4]); cswap(acb[3], acb[5]);
+    cswap(acr[0], acr[1]); cswap(acr[2], acr[3]); cswap(acr[4], acr[5]);
+    cswap(acr[0], acr[2]); cswap(acr[1], acr[3]); cswap(acr[0], acr[4]); cswap(acr[3], acr[5]);
+    rd(-1, 1, acb[0], acr[0]);
+    // minMax5
+    cswap(acb[0], acb[1]); cswap(acb[2], acb[3]); cswap(acb[0], acb[2]);
+    cswap(acb[1], acb[3]); cswap(acb[0], acb[4]); cswap(acb[3], acb[4]);
+    cswap(acr[0], acr[1]); cswap(acr[2], acr[3]); cswap(acr[0], acr[2]);
+    cswap(acr[1], acr[3]); cswap(acr[0], acr[4]); cswap(acr[3], acr[4]);
+    rd(-1, 0, acb[0], acr[0]);
+    // minMax4
+    cswap(acb[0], acb[1]); cswap(acb[2], acb[3]); cswap(acb[0], acb[2]); cswap(acb[1], acb[3]);
+    cswap(acr[0], acr[1]); cswap(acr[2], acr[3]); cswap(acr[0], acr[2]); cswap(acr[1], acr[3]);
+    rd(-1, -1, acb[0], acr[0]);
+    // minMax3
+    cswap(acb[0], acb[1]); cswap(acb[0], acb[2]); cswap(acb[1], acb[2]);
+    cswap(acr[0], acr[1]); cswap(acr[0], acr[2]); cswap(acr[1], acr[2]);
+
+    const float sigma = round_half(sqrt_(va0 + vb0 * sample));
+    const float four_sigma = round_half(4.0f * sigma);
+    auto hsmooth = [&](float e0, float e1, float x) {
+        const float t = clamp_(round_half(div_(round_half(x - e0), round_half(e1 - e0))), 0.0f, 1.0f);
+        return round_half(round_half(t * t) * round_half(3.0f - round_half(2.0f * t)));
+    };
+    auto hmix = [&](float x, float y, float t) { return round_half(x + round_half(round_half(y - x) * t)); };
+    const float minVal = hmix(secMin, firstMin, hsmooth(sigma, four_sigma, round_half(secMin - firstMin)));
+    const float maxVal = hmix(secMax, firstMax, hsmooth(sigma, four_sigma, round_half(firstMax - secMax)));
+    sample = clamp_(sample, minVal, maxVal);
+    return make_float4(sample, acb[1], acr[1], 0.0f);
+}
+
+// ---- a12: downsampleImage (demosaic.cl:853-865) ----
+template <class Acc4>
+GLS_DI float4 downsample_px(const Acc4& in, int x, int y, int ow, int oh, int iw, int ih) {
+    const float nx = div_(1.0f, (float)ow), ny = div_(1.0f, (float)oh);
+    const float px = ((float)x + 0.5f) * nx, py = ((float)y + 0.5f) * ny;
+    const float sx = 0.5f * nx, sy = 0.5f * ny;
+    const float4 t0 = sample4(in, px + -sx, py + -sy, iw, ih);
+    const float4 t1 = sample4(in, px + sx, py + -sy, iw, ih);
+    const float4 t2 = sample4(in, px + -sx, py + sy, iw, ih);
+    const float4 t3 = sample4(in, px + sx, py + sy, iw, ih);
+    float4 r;
+    r.x = 0.25f * (t0.x + t1.x + t2.x + t3.x);
+    r.y = 0.25f * (t0.y + t1.y + t2.y + t3.y);
+    r.z = 0.25f * (t0.z + t1.z + t2.z + t3.z);
+    r.w = 0.25f * (t0.w + t1.w + t2.w + t3.w);
+    return r;
+}
+
+// ---- a14: denoiseImage, bilateral (demosaic.cl:735-765) ----
+struct Nlf6 {
+    float a[3], b[3];
+};
+
+// Luma channel of an RGBA accessor, for the sobel of the gradient boost.
+template <class Acc4>
+struct LumaOf {
+    const Acc4& im;
+    GLS_DI float at(int x, int y) const { return im.at(x, y).x; }
+};
+
+template <class Acc4>
+GLS_DI float4 bilateral_px(const Acc4& im, int px, int py, const Nlf6& n, float chromaBoost, float gradientBoost) {
+    const float4 c = im.at(px, py);
+    const float sig0 = sqrt_(n.a[0] + n.b[0] * c.x);
+    const float sig1 = sqrt_(n.a[1] + n.b[1] * c.x);
+    const float sig2 = sqrt_(n.a[2] + n.b[2] * c.x);
+    float lumaBoost = 1.0f;
+    if (gradientBoost > 1.0f) {
+        LumaOf<Acc4> l{im};
+        const float2 g = sobel_signed(l, px, py);
+        lumaBoost = gradientBoost -
+                    (gradientBoost - 1.0f) * smoothstep_(0.5f, 2.0f, length2_(div_(g.x, sig0), div_(g.y, sig0)));
+    }
+    const float e0 = lumaBoost * GLS_SQRT2_F, e1 = chromaBoost * GLS_SQRT2_F;
+    float f0 = 0.0f, f1 = 0.0f, f2 = 0.0f, n0 = 0.0f, n1 = 0.0f, n2 = 0.0f;
+#pragma unroll
+    for (int y = -2; y <= 2; y++) {
+#pragma unroll
+        for (int x = -2; x <= 2; x++) {
+            const float4 s = im.at(px + x, py + y);
+            const float d0 = div_(s.x - c.x, sig0), d1 = div_(s.y - c.y, sig1), d2 = div_(s.z - c.z, sig2);
+            const float l = length3_(d0, d1, d2);
+            const float w0 = 1.0f - step_(e0, l), w1 = 1.0f - step_(e1, l);
+            f0 = f0 + w0 * s.x;
+            n0 = n0 + w0;
+            f1 = f1 + w1 * s.y;
+            n1 = n1 + w1;
+            f2 = f2 + w1 * s.z;
+            n2 = n2 + w1;
+        }
+    }
+    return make_float4(div_(f0, n0), div_(f1, n1), div_(f2, n2), 0.0f);
+}
+
+// ---- a15: denoiseImageGuided / denoiseLumaChromaGuided (demosaic.cl:767-851) ----
+template <class Acc4>
+GLS_DI float4 guided_fast_px(const Acc4& im, int px, int py, const Nlf6& n) {
+    const float4 I = im.at(px, py);
+    const float eps0 = n.a[0] + n.b[0] * I.x, eps1 = n.a[1] + n.b[1] * I.x, eps2 = n.a[2] + n.b[2] * I.x;
+    const float norm = div_(1.0f, 25.0f);
+    float m0 = 0.0f, m1 = 0.0f, m2 = 0.0f, rr = 0.0f, rg = 0.0f, rb = 0.0f, gg = 0.0f, gb = 0.0f, bb = 0.0f;
+#pragma unroll
+    for (int y = -2; y <= 2; y++) {
+#pragma unroll
+        for (int x = -2; x <= 2; x++) {
+            const float4 s = im.at(px + x, py + y);
+            m0 = m0 + s.x;
+            m1 = m1 + s.y;
+            m2 = m2 + s.z;
+            rr = rr + s.x * s.x;
+            rg = rg + s.x * s.y;
+            rb = rb + s.x * s.z;
+            gg = gg + s.y * s.y;
+            gb = gb + s.y * s.z;
+            bb = bb + s.z * s.z;
+        }
+    }
+    m0 = m0 * norm; m1 = m1 * norm; m2 = m2 * norm;
+    rr = rr * norm; rg = rg * norm; rb = rb * norm; gg = gg * norm; gb = gb * norm; bb = bb * norm;
+    const float vrr = rr - m0 * m0, vrg = rg - m0 * m1, vrb = rb - m0 * m2;
+    const float vgg = gg - m1 * m1, vgb = gb - m1 * m2, vbb = bb - m2 * m2;
+    const float vrre = vrr + eps0, vgge = vgg + eps1, vbbe = vbb + eps2;
+    float invrr = vgge * vbbe - vgb * vgb;
+    float invrg = vgb * vrb - vrg * vbbe;
+    float invrb = vrg * vgb - vgge * vrb;
+    float invgg = vrre * vbbe - vrb * vrb;
+    float invgb = vrb * vrg - vrre * vgb;
+    float invbb = vrre * vgge - vrg * vrg;
+    const float det = div_(1.0f, invrr * vrre + invrg * vrg + invrb * vrb);
+    invrr = invrr * det; invrg = invrg * det; invrb = invrb * det;
+    invgg = invgg * det; invgb = invgb * det; invbb = invbb * det;
+    const float cr[3] = {vrr, vrg, vrb}, cg[3] = {vrg, vgg, vgb}, cb[3] = {vrb, vgb, vbb};
+    const float mI[3] = {m0, m1, m2};
+    const float In[3] = {I.x, I.y, I.z};
+    float out[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const float ar = invrr * cr[k] + invrg * cg[k] + invrb * cb[k];
+        const float ag = invrg * cr[k] + invgg * cg[k] + invgb * cb[k];
+        const float ab = invrb * cr[k] + invgb * cg[k] + invbb * cb[k];
+        const float b = mI[k] - ar * mI[0] - ag * mI[1] - ab * mI[2];
+        out[k] = ar * In[0] + ag * In[1] + ab * In[2] + b;
+    }
+    return make_float4(out[0], out[1], out[2], 0.0f);
+}
+
+// ---- a17: reassembleImage (demosaic.cl:867-896) ----
+// d0: the denoised fine pixel; i1/d1: the coarse level before/after denoise; (w, h) the
+// fine level's size, (w1, h1) the coarse level's.
+template <class AccI, class AccD>
+GLS_DI float4 reassemble_px(float4 d0, const AccI& i1, const AccD& d1, int x, int y, int w, int h, int w1, int h1,
+                            float sharpening, float nlf0, float nlf1) {
+    const float nx = div_(1.0f, (float)w), ny = div_(1.0f, (float)h);
+    const float ipx = ((float)x + 0.5f) * nx, ipy = ((float)y + 0.5f) * ny;
+    const float4 p1 = sample4(i1, ipx, ipy, w1, h1);
+    const float4 pd1 = sample4(d1, ipx, ipy, w1, h1);
+    float4 dp;
+    dp.x = d0.x - (p1.x - pd1.x);
+    dp.y = d0.y - (p1.y - pd1.y);
+    dp.z = d0.z - (p1.z - pd1.z);
+    dp.w = d0.w - (p1.w - pd1.w);
+    if (sharpening > 1.0f) {
+        const float ax = sample4(d1, ipx + nx, ipy + 0.0f * ny, w1, h1).x;
+        const float bx = sample4(d1, ipx - nx, ipy - 0.0f * ny, w1, h1).x;
+        const float dx = div_(ax - bx, 2.0f);
+        const float ay = sample4(d1, ipx + 0.0f * nx, ipy + ny, w1, h1).x;
+        const float by = sample4(d1, ipx - 0.0f * nx, ipy - ny, w1, h1).x;
+        const float dy = div_(ay - by, 2.0f);
+        const float threshold = 0.25f * sqrt_(nlf0 + nlf1 * pd1.x);
+        const float detail = smoothstep_(0.25f * threshold, threshold, length2_(dx, dy)) *
+                             (1.0f - smoothstep_(0.95f, 1.0f, dp.x)) * (0.6f + 0.4f * smoothstep_(0.0f, 0.1f, dp.x));
+        sharpening = 1.0f + (sharpening - 1.0f) * detail;
+    }
+    dp.x = mix_(pd1.x, dp.x, sharpening);
+    return dp;
+}
+
+// ---- a18: localToneMappingMask (demosaic.cl:1026-1107) ----
+struct LtmParams {
+    float eps, shadows, highlights, detail;
+};
+
+template <class AccIn, class AccG>
+GLS_DI float ltm_mask_px(const AccIn& in, const AccG& guide, int x, int y, int w, int h, int gw, int gh,
+                         const LtmParams& lp, const Mat3& m) {
+    const float bw[9] = {0.16f, 0.16f, 0.08f, 0.16f, 0.16f, 0.08f, 0.08f, 0.08f, 0.04f};
+    const float bx[9] = {-1.5f, 0.5f, 2.0f, -1.5f, 0.5f, 2.0f, -1.5f, 0.5f, 2.0f};
+    const float by[9] = {-1.5f, -1.5f, -1.5f, 0.5f, 0.5f, 0.5f, 2.0f, 2.0f, 2.0f};
+    const float nx = div_(1.0f, (float)w), ny = div_(1.0f, (float)h);
+    const float px = (float)x * nx, py = (float)y * ny;
+    float gs[9];
+    float sum = 0.0f, sumSq = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 9; i++) {
+        gs[i] = sample4(guide, px + (bx[i] + 0.5f) * nx, py + (by[i] + 0.5f) * ny, gw, gh).x;
+        const float s = bw[i] * gs[i];
+        sum = sum + s;
+        sumSq = sumSq + s * s;
+    }
+    const float mean = sum, var = sumSq - sum * sum;
+    const float4 inp = sample4(in, px + 0.5f * nx, py + 0.5f * ny, w, h);
+    const float luma = inp.x;
+    float filtered = 0.0f, knorm = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 9; i++) {
+        const float wgt = bw[i] * (1.0f + div_((gs[i] - mean) * (luma - mean), var + lp.eps));
+        filtered = filtered + wgt * gs[i];
+        knorm = knorm + wgt;
+    }
+    const float illuminance = div_(filtered, knorm);
+    const float reflectance = div_(luma, illuminance);
+    const float3 rgb = transform_px(m, make_float3(inp.x, inp.y, inp.z));
+    const float hc = mmin(length3_(sqrt_(2.0f * rgb.x), sqrt_(2.0f * rgb.y), sqrt_(2.0f * rgb.z)), 1.0f);
+    const float tc = mix_(lp.shadows, lp.highlights, hc);
+    return div_(glsm::pow_(illuminance, div_(1.0f, tc)) * glsm::pow_(reflectance, lp.detail), luma);
+}
+
+// ---- a19: convertTosRGB + toneCurve & co (demosaic.cl:1380-1474) ----
+struct RgbParams {
+    float contrast, saturation, toneCurveSlope, exposureBias, blacks;
+    int localToneMapping;
+};
+
+GLS_DI float sigmoid_(float x, float s) { return 0.5f * (glsm::tanh_(s * x - 0.3f * s) + 1.0f); }
+
+GLS_DI float tone_curve_(float x, float s) {
+    return div_(sigmoid_(sqrt_(0.95f * x), s) - sigmoid_(0.0f, s), sigmoid_(1.0f, s) - sigmoid_(0.0f, s));
+}
+
+GLS_DI float3 srgb_px(float3 in, float ltm, const Mat3& m, const RgbParams& rp) {
+    float p[3] = {in.x, in.y, in.z};
+    const float eb = rp.exposureBias != 0.0f ? glsm::powr_(2.0f, rp.exposureBias) : 1.0f;
+#pragma unroll
+    for (int k = 0; k < 3; k++) p[k] = p[k] * eb;
+    if (rp.saturation != 1.0f) {
+        const float luma = 0.2126f * p[0] + 0.7152f * p[1] + 0.0722f * p[2];
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const float clip = smoothstep_(0.75f, 2.0f, p[k]);
+            p[k] = mix_(luma, p[k], mix_(rp.saturation, 1.0f, clip));
+        }
+    }
+    if (rp.contrast != 1.0f) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const float clip = smoothstep_(0.9f, 2.0f, p[k]);
+            p[k] = mix_(0.2f, p[k], mix_(rp.contrast, 1.0f, clip));
+        }
+    }
+    const float3 t = transform_px(m, make_float3(p[0], p[1], p[2]));
+    float rgb[3] = {t.x, t.y, t.z};
+#pragma unroll
+    for (int k = 0; k < 3; k++) rgb[k] = clamp_(tone_curve_(rgb[k], rp.toneCurveSlope), 0.0f, 1.0f);
+    if (rp.localToneMapping) {
+        const float boost = ltm;
+        if (boost > 1.0f) {
+            const float luma = 0.2126f * rgb[0] + 0.7152f * rgb[1] + 0.0722f * rgb[2];
+            const float tt = glsm::pow_(luma, 0.5f);
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                const float a = rgb[k] * boost;
+                const float b = luma < 1.0f ? 1.0f - div_((1.0f - rgb[k]) * (1.0f - boost * luma), 1.0f - luma) : rgb[k];
+                rgb[k] = mix_(a, b, tt);
+            }
+        } else if (boost < 1.0f) {
+#pragma unroll
+            for (int k = 0; k < 3; k++) rgb[k] = rgb[k] * boost;
+        }
+    }
+    if (rp.blacks > 0.0f) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) rgb[k] = div_(rgb[k] - rp.blacks, 1.0f - rp.blacks);
+    }
+    return make_float3(rgb[0], rgb[1], rgb[2]);
+}
+
+// ---- a6: high-noise raw branch (demosaic.cl:530-553, 930-949, 1187-1201) ----
+template <class Acc4>
+GLS_DI float4 despeckle_rgba_px(const Acc4& im, int px, int py) {
+    float s[4] = {0, 0, 0, 0}, fmx[4] = {0, 0, 0, 0}, smx[4] = {0, 0, 0, 0};
+    float fmn[4] = {65535.0f, 65535.0f, 65535.0f, 65535.0f}, smn[4] = {65535.0f, 65535.0f, 65535.0f, 65535.0f};
+#pragma unroll
+    for (int x = -1; x <= 1; x++) {
+#pragma unroll
+        for (int y = -1; y <= 1; y++) {
+            const float4 v4 = im.at(px + x, py + y);
+            const float vv[4] = {v4.x, v4.y, v4.z, v4.w};
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const float v = vv[k];
+                smx[k] = (v <= fmx[k] && v > smx[k]) ? v : smx[k];
+                smx[k] = v > fmx[k] ? fmx[k] : smx[k];
+                fmx[k] = v > fmx[k] ? v : fmx[k];
+                smn[k] = (v >= fmn[k] && v < smn[k]) ? v : smn[k];
+                smn[k] = v < fmn[k] ? fmn[k] : smn[k];
+                fmn[k] = v < fmn[k] ? v : fmn[k];
+                if (x == 0 && y == 0) s[k] = v;
+            }
+        }
+    }
+    return make_float4(clamp_(s[0], smn[0], smx[0]), clamp_(s[1], smn[1], smx[1]), clamp_(s[2], smn[2], smx[2]),
+                       clamp_(s[3], smn[3], smx[3]));
+}
+
+template <class Acc4>
+GLS_DI float4 denoise_rgba_px(const Acc4& im, int px, int py, const float rv[4]) {
+    const float4 c = im.at(px, py);
+    const float in[4] = {c.x, c.y, c.z, c.w};
+    float sg[4], f[4] = {0, 0, 0, 0}, nrm[4] = {0, 0, 0, 0};
+#pragma unroll
+    for (int k = 0; k < 4; k++) sg[k] = sqrt_(rv[k] * in[k]);
+#pragma unroll
+    for (int y = -2; y <= 2; y++) {
+#pragma unroll
+        for (int x = -2; x <= 2; x++) {
+            const float4 s4 = im.at(px + x, py + y);
+            const float s[4] = {s4.x, s4.y, s4.z, s4.w};
+            float d[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) d[k] = div_(s[k] - in[k], sg[k]);
+            const float w = 1.0f - step_(1.0f, length4_(d[0], d[1], d[2], d[3]));
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                f[k] = f[k] + w * s[k];
+                nrm[k] = nrm[k] + w;
+            }
+        }
+    }
+    return make_float4(div_(f[0], nrm[0]), div_(f[1], nrm[1]), div_(f[2], nrm[2]), div_(f[3], nrm[3]));
+}
+
+}  // namespace gls
+
+#endif  // GLS_PIXEL_OPS_CUH

@@ -1,0 +1,467 @@
+// raw_converter.cu -- RawConverter (CLImage/app/src/main/cpp/raw_converter.cpp:73-237) and
+// PyramidalDenoise<levels> (pyramidal_denoise.cpp:104-149) on the GPU.
+//
+// The stage order, the parameter plumbing and the image each stage reads follow the
+// reference exactly; the differences are in how the work is scheduled:
+//   * the noise-model regressions run on the device (k_nlf.cu), so one frame is a single
+//     stream of kernel launches with no host round trip;
+//   * working images are reallocated when the frame size, pyramid depth or storage
+//     precision changes (the reference sizes them once, by the first frame).
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "gls_internal.h"
+#include "gls_pipeline.h"
+#include "gls_pixel_ops.cuh"
+#include "gls_stages.h"
+
+using namespace gls;
+
+namespace {
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+// half -> float copies for the parity taps
+__global__ void tap_copy_kernel(const void* src, bool half, int channels, int w, int h, int spitch, float* dst,
+                                int dpitch) {
+    const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
+    if (x >= w || y >= h) return;
+    for (int c = 0; c < channels; c++) {
+        const size_t si = ((size_t)y * spitch + x) * channels + c;
+        const float v = half ? __half2float(((const __half*)src)[si]) : ((const float*)src)[si];
+        dst[((size_t)y * dpitch + x) * channels + c] = v;
+    }
+}
+
+__global__ void rgba8_to_rgb8_kernel(const uchar4* in, int w, int h, uint8_t* out) {
+    const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
+    if (x >= w || y >= h) return;
+    const uchar4 p = in[(size_t)y * w + x];
+    uint8_t* o = out + ((size_t)y * w + x) * 3;
+    o[0] = p.x;
+    o[1] = p.y;
+    o[2] = p.z;
+}
+
+}  // namespace
+
+struct gls_raw_converter {
+    gls_ctx* ctx = nullptr;
+    int w = 0, h = 0, L = 0;
+    bool half = false;
+    std::vector<DevBuf> owned;
+    ImgRef scaled{}, green{}, linA{}, linB{}, mask{}, hnA{}, hnB{};
+    ImgRef pyr[GLS_MAX_LEVELS]{}, den[GLS_MAX_LEVELS]{};
+    float* nlf_dev = nullptr;  // slot 0: raw {A0..A3, B0..B3}; slot 1+i: level i {A0..A2, B0..B2, -, -}
+    void* nlf_scratch = nullptr;
+    void* gf_scratch = nullptr;
+    size_t gf_scratch_bytes = 0;
+    float* nlf_host = nullptr;  // pinned
+    // host-buffer entry point
+    uint16_t* raw_dev = nullptr;
+    size_t raw_dev_bytes = 0;
+    uint8_t* out_dev = nullptr;
+    size_t out_dev_bytes = 0;
+    // parity taps
+    gls_image_desc taps[5]{};
+    bool tap_set[5]{};
+
+    ~gls_raw_converter() { release(); }
+
+    void release() {
+        for (auto& b : owned)
+            if (b.p) cudaFree(b.p);
+        owned.clear();
+        w = h = L = 0;
+    }
+
+    gls_status alloc(void** p, size_t bytes) {
+        GLS_CHECK(check_cuda(ctx, cudaMalloc(p, bytes), "cudaMalloc(working image)"));
+        owned.push_back(DevBuf{*p, bytes});
+        return GLS_OK;
+    }
+
+    gls_status img(ImgRef& r, int iw, int ih, int channels) {
+        const size_t es = half ? 2 : 4;
+        void* p = nullptr;
+        GLS_CHECK(alloc(&p, (size_t)iw * ih * channels * es));
+        r = ImgRef{p, iw, ih, iw, half};
+        return GLS_OK;
+    }
+
+    gls_status ensure(int width, int height, int levels, bool half_storage) {
+        if (width == w && height == h && levels == L && half_storage == half) return GLS_OK;
+        cudaStreamSynchronize(ctx->stream);
+        release();
+        half = half_storage;
+        GLS_CHECK(img(scaled, width, height, 1));
+        GLS_CHECK(img(green, width, height, 1));
+        GLS_CHECK(img(linA, width, height, 4));
+        GLS_CHECK(img(linB, width, height, 4));
+        GLS_CHECK(img(mask, width, height, 1));
+        GLS_CHECK(img(hnA, width / 2, height / 2, 4));
+        GLS_CHECK(img(hnB, width / 2, height / 2, 4));
+        for (int i = 0; i < levels - 1; i++) GLS_CHECK(img(pyr[i], width >> (i + 1), height >> (i + 1), 4));
+        for (int i = 0; i < levels; i++) GLS_CHECK(img(den[i], width >> i, height >> i, 4));
+        void* p = nullptr;
+        GLS_CHECK(alloc(&p, (1 + GLS_MAX_LEVELS) * 8 * sizeof(float)));
+        nlf_dev = (float*)p;
+        GLS_CHECK(alloc(&nlf_scratch, kNlfScratchBytes));
+        gf_scratch = nullptr;
+        gf_scratch_bytes = 0;
+        w = width;
+        h = height;
+        L = levels;
+        return GLS_OK;
+    }
+
+    void tap(int stage, const ImgRef& src, int channels) {
+        if (stage < 0 || stage >= 5 || !tap_set[stage]) return;
+        const gls_image_desc& d = taps[stage];
+        if (d.width != src.w || d.height != src.h) return;
+        tap_copy_kernel<<<dim3((src.w + 31) / 32, (src.h + 7) / 8), dim3(32, 8), 0, ctx->stream>>>(
+            src.ptr, src.half, channels, src.w, src.h, src.pitch, (float*)d.ptr, d.stride_bytes / (4 * channels));
+        ctx->launches++;
+    }
+
+    gls_status denoise_level(int algo, bool coarsest, const ImgRef& in, const ImgRef& out, int level,
+                             const gls_denoise_params& dp) {
+        NlfArg a;
+        a.dev = nlf_dev + 8 * (1 + level);
+        const float lm = dp.luma * dp.luma, cm = dp.chroma * dp.chroma;
+        const float mul[6] = {lm, cm, cm, lm, cm, cm};
+        for (int k = 0; k < 6; k++) {
+            a.host[k] = 0;
+            a.mul[k] = mul[k];
+        }
+        if (algo == GLS_DENOISE_BILATERAL || (algo == GLS_DENOISE_GUIDED_FAST && coarsest)) {
+            launch_bilateral(ctx, in, out, a, dp.chromaBoost, dp.gradientBoost);
+        } else if (algo == GLS_DENOISE_GUIDED_FAST) {
+            launch_guided_fast(ctx, in, out, a);
+        } else {
+            const size_t need = guided_filter_scratch_bytes(w, h);
+            if (gf_scratch_bytes < need) {
+                GLS_CHECK(alloc(&gf_scratch, need));
+                gf_scratch_bytes = need;
+            }
+            launch_guided_filter(ctx, in, out, 5, a, gf_scratch);
+        }
+        return GLS_OK;
+    }
+
+    // ---- per-stage timing ----
+    bool profiling = false;
+    cudaEvent_t ev_pool[64];
+    int ev_used = 0;
+    const char* ev_name[64];
+    std::vector<std::pair<std::string, std::pair<double, long>>> prof;
+
+    void mark(const char* name) {
+        if (!profiling || ev_used >= 64) return;
+        cudaEventRecord(ev_pool[ev_used], ctx->stream);
+        ev_name[ev_used++] = name;
+    }
+
+    void collect() {
+        if (!profiling || ev_used < 2) {
+            ev_used = 0;
+            return;
+        }
+        cudaEventSynchronize(ev_pool[ev_used - 1]);
+        for (int i = 1; i < ev_used; i++) {
+            float ms = 0;
+            cudaEventElapsedTime(&ms, ev_pool[i - 1], ev_pool[i]);
+            bool found = false;
+            for (auto& e : prof)
+                if (e.first == ev_name[i]) {
+                    e.second.first += ms;
+                    e.second.second += 1;
+                    found = true;
+                }
+            if (!found) prof.push_back({ev_name[i], {ms, 1L}});
+        }
+        ev_used = 0;
+    }
+
+    gls_status run(const uint16_t* raw, int rpitch, gls_demosaic_params* p, void* out, bool out_float, int opitch) {
+        const int Lv = L;
+        const int bayer = p->bayer_pattern;
+        const bool high_noise = p->noise_level > 0.6f;
+        ev_used = 0;
+        mark("start");
+
+        // --- image demosaicing (raw_converter.cpp:101-131) ---
+        launch_scale_raw(ctx, raw, w, h, rpitch, scaled, bayer, p->scale_mul, p->black_level / 0xffff);
+        mark("scaleRawData");
+        GLS_CHECK(nlf_fit_raw_scaled(ctx, scaled.ptr, half, w, h, scaled.pitch, bayer, nlf_scratch_at(nlf_scratch),
+                                     nlf_dev));
+        mark("rawNoiseStatistics+fit");
+        const float* rawB = nlf_dev + 4;
+        if (high_noise) {
+            launch_bayer_to_rgba(ctx, scaled, hnA, bayer);
+            launch_despeckle_rgba(ctx, hnA, hnB);
+            launch_denoise_rgba(ctx, hnB, hnA, p->raw_nlf, rawB);
+            launch_rgba_to_bayer(ctx, hnA, scaled, bayer);
+            mark("rawDenoise");
+        }
+        tap(0, scaled, 1);
+        launch_green(ctx, scaled, green, bayer, 0.0f, rawB + 1);
+        mark("interpolateGreen");
+        tap(1, green, 1);
+        launch_red_blue(ctx, scaled, green, linA, bayer, 0.0f, rawB);
+        mark("interpolateRedBlue");
+        launch_highlights(ctx, linA, linA, 1.0f);
+        mark("blendHighlights");
+
+        // --- image denoising (raw_converter.cpp:133-160) ---
+        float cam_to_ycbcr[9];
+        host_cam_ycbcr(p->rgb_cam, cam_to_ycbcr);
+        launch_transform(ctx, linA, linA, cam_to_ycbcr);
+        mark("transformImage");
+        launch_despeckle(ctx, linA, linB, p->pyramid_nlf[0][0], p->pyramid_nlf[0][3]);
+        mark("despeckleImage");
+        tap(2, linB, 4);
+
+        // PyramidalDenoise::denoise
+        for (int i = 0; i < Lv; i++) {
+            const ImgRef& src = i == 0 ? linB : pyr[i - 1];
+            if (i < Lv - 1) launch_downsample(ctx, src, pyr[i]);
+            mark("downsampleImage");
+            GLS_CHECK(nlf_fit_level(ctx, src.ptr, half, src.w, src.h, src.pitch, nlf_scratch_at(nlf_scratch),
+                                    nlf_dev + 8 * (1 + i)));
+            mark(i == 0 ? "noiseStatistics+fit L0" : "noiseStatistics+fit L1+");
+        }
+        const int algo = p->denoise_algorithm;
+        GLS_CHECK(denoise_level(algo, true, pyr[Lv - 2], den[Lv - 1], Lv - 1, p->denoise[Lv - 1]));
+        mark("denoise L1+");
+        for (int i = Lv - 2; i >= 0; i--) {
+            const ImgRef& input = i > 0 ? pyr[i - 1] : linB;
+            GLS_CHECK(denoise_level(algo, false, input, den[i], i, p->denoise[i]));
+            mark(i == 0 ? "denoise L0" : "denoise L1+");
+            NlfArg a;
+            a.dev = nlf_dev + 8 * (1 + i);
+            const float lm = p->denoise[i].luma * p->denoise[i].luma;
+            const float cm = p->denoise[i].chroma * p->denoise[i].chroma;
+            const float mul[6] = {lm, cm, cm, lm, cm, cm};
+            for (int k = 0; k < 6; k++) {
+                a.host[k] = 0;
+                a.mul[k] = mul[k];
+            }
+            launch_reassemble(ctx, den[i], pyr[i], den[i + 1], den[i], p->denoise[i].sharpening, a);
+            mark(i == 0 ? "reassemble L0" : "reassemble L1+");
+        }
+        const ImgRef& denoised = den[0];
+        tap(3, denoised, 4);
+
+        // --- local tone mapping and output (raw_converter.cpp:162-174) ---
+        float inv[9], icy_e[9];
+        if (!host_inverse3x3(cam_to_ycbcr, inv)) return set_error(ctx, GLS_ERR_INVALID_ARGUMENT, "singular cam_ycbcr");
+        for (int k = 0; k < 9; k++) icy_e[k] = inv[k] * p->exposure_multiplier;
+        const bool ltm = p->rgb_conversion.localToneMapping != 0;
+        if (ltm) {
+            LtmParams lp{p->ltm.guidedFilterEps, p->ltm.shadows, p->ltm.highlights, p->ltm.detail};
+            launch_ltm(ctx, denoised, den[3], mask, lp, icy_e);
+            mark("localToneMappingMask");
+            tap(4, mask, 1);
+        }
+        launch_transform(ctx, denoised, denoised, icy_e);
+        mark("transformImage");
+        const gls_rgb_conversion_params& rc = p->rgb_conversion;
+        RgbParams rp{rc.contrast, rc.saturation, rc.toneCurveSlope, rc.exposureBias, rc.blacks, rc.localToneMapping};
+        launch_srgb(ctx, denoised, ltm ? &mask : nullptr, out, out_float, opitch, p->rgb_cam, rp);
+        mark("convertTosRGB");
+        collect();
+        return check_launch(ctx, "RawConverter::demosaicImage");
+    }
+
+    gls_status fetch_noise_model(gls_demosaic_params* p) {
+        const size_t n = (1 + GLS_MAX_LEVELS) * 8;
+        GLS_CHECK(check_cuda(ctx, cudaMemcpyAsync(nlf_host, nlf_dev, n * sizeof(float), cudaMemcpyDeviceToHost,
+                                                  ctx->stream), "copy noise model"));
+        GLS_CHECK(check_cuda(ctx, cudaStreamSynchronize(ctx->stream), "synchronize"));
+        for (int c = 0; c < 4; c++) p->raw_nlf[c] = nlf_host[4 + c];
+        for (int i = 0; i < L; i++)
+            for (int k = 0; k < 6; k++) p->pyramid_nlf[i][k] = nlf_host[8 * (1 + i) + k];
+        return GLS_OK;
+    }
+};
+
+static gls_status validate_params(gls_ctx* ctx, const gls_demosaic_params* p, int w, int h) {
+    if (!p) return set_error(ctx, GLS_ERR_INVALID_ARGUMENT, "params is null");
+    if (p->bayer_pattern < 0 || p->bayer_pattern > 3)
+        return set_error(ctx, GLS_ERR_INVALID_ARGUMENT, "unknown bayer pattern %d", p->bayer_pattern);
+    if (p->pyramid_levels < 4 || p->pyramid_levels > GLS_MAX_LEVELS)
+        return set_error(ctx, GLS_ERR_INVALID_ARGUMENT, "pyramid_levels must be in [4, %d]", GLS_MAX_LEVELS);
+    if (p->storage != GLS_STORAGE_F32 && p->storage != GLS_STORAGE_F16)
+        return set_error(ctx, GLS_ERR_INVALID_ARGUMENT, "unknown storage %d", p->storage);
+    if (p->denoise_algorithm < 0 || p->denoise_algorithm > 2)
+        return set_error(ctx, GLS_ERR_INVALID_ARGUMENT, "unknown denoise algorithm %d", p->denoise_algorithm);
+    if (p->rotate_180) return set_error(ctx, GLS_ERR_UNSUPPORTED, "rotate_180 is not supported");
+    if (w <= 0 || h <= 0 || (w & 1) || (h & 1))
+        return set_error(ctx, GLS_ERR_INVALID_SIZE, "raw frames must have positive, even width and height");
+    if ((w >> (p->pyramid_levels - 1)) < 1 || (h >> (p->pyramid_levels - 1)) < 1)
+        return set_error(ctx, GLS_ERR_INVALID_SIZE, "frame too small for %d pyramid levels", p->pyramid_levels);
+    return GLS_OK;
+}
+
+extern "C" {
+
+gls_status gls_raw_converter_create(gls_ctx* ctx, gls_raw_converter** out) {
+    if (!ctx || !out) return GLS_ERR_INVALID_ARGUMENT;
+    gls_raw_converter* c = new gls_raw_converter();
+    c->ctx = ctx;
+    if (cudaMallocHost(&c->nlf_host, (1 + GLS_MAX_LEVELS) * 8 * sizeof(float)) != cudaSuccess) {
+        delete c;
+        return set_error(ctx, GLS_ERR_OUT_OF_MEMORY, "cudaMallocHost");
+    }
+    *out = c;
+    return GLS_OK;
+}
+
+gls_status gls_raw_converter_destroy(gls_raw_converter* c) {
+    if (!c) return GLS_ERR_INVALID_ARGUMENT;
+    cudaStreamSynchronize(c->ctx->stream);
+    if (c->nlf_host) cudaFreeHost(c->nlf_host);
+    if (c->raw_dev) cudaFree(c->raw_dev);
+    if (c->out_dev) cudaFree(c->out_dev);
+    delete c;
+    return GLS_OK;
+}
+
+gls_status gls_raw_converter_profile(gls_raw_converter* c, int enable) {
+    if (!c) return GLS_ERR_INVALID_ARGUMENT;
+    if (enable && !c->profiling) {
+        for (int i = 0; i < 64; i++)
+            GLS_CHECK(check_cuda(c->ctx, cudaEventCreate(&c->ev_pool[i]), "cudaEventCreate"));
+        c->prof.clear();
+        c->profiling = true;
+    } else if (!enable && c->profiling) {
+        cudaStreamSynchronize(c->ctx->stream);
+        for (int i = 0; i < 64; i++) cudaEventDestroy(c->ev_pool[i]);
+        c->profiling = false;
+    }
+    return GLS_OK;
+}
+
+gls_status gls_raw_converter_profile_report(gls_raw_converter* c, char* buf, size_t len) {
+    if (!c || !buf || len == 0) return GLS_ERR_INVALID_ARGUMENT;
+    std::string s = "{";
+    for (size_t i = 0; i < c->prof.size(); i++) {
+        char item[160];
+        snprintf(item, sizeof(item), "%s\"%s\": [%.6f, %ld]", i ? ", " : "", c->prof[i].first.c_str(),
+                 c->prof[i].second.first, c->prof[i].second.second);
+        s += item;
+    }
+    s += "}";
+    if (s.size() + 1 > len) return GLS_ERR_INVALID_SIZE;
+    memcpy(buf, s.c_str(), s.size() + 1);
+    return GLS_OK;
+}
+
+gls_status gls_raw_converter_set_tap(gls_raw_converter* c, int stage, const gls_image_desc* dst) {
+    if (!c || stage < 0 || stage >= 5) return GLS_ERR_INVALID_ARGUMENT;
+    if (!dst) {
+        c->tap_set[stage] = false;
+        return GLS_OK;
+    }
+    const int want = (stage == 0 || stage == 1 || stage == 4) ? GLS_R_F32 : GLS_RGBA_F32;
+    GLS_CHECK(check_desc(c->ctx, dst, "tap", want));
+    c->taps[stage] = *dst;
+    c->tap_set[stage] = true;
+    return GLS_OK;
+}
+
+gls_status gls_raw_converter_demosaic(gls_raw_converter* c, const gls_image_desc* raw, gls_demosaic_params* p,
+                                      const gls_image_desc* out, int defer) {
+    if (!c) return GLS_ERR_INVALID_ARGUMENT;
+    gls_ctx* ctx = c->ctx;
+    GLS_CHECK(check_desc(ctx, raw, "raw", GLS_R16_UNORM));
+    GLS_CHECK(check_desc(ctx, out, "out", GLS_RGBA8_UNORM, GLS_RGBA_F32));
+    if (out->width != raw->width || out->height != raw->height)
+        return set_error(ctx, GLS_ERR_INVALID_SIZE, "output size differs from the raw frame");
+    GLS_CHECK(validate_params(ctx, p, raw->width, raw->height));
+    GLS_CHECK(c->ensure(raw->width, raw->height, p->pyramid_levels, p->storage == GLS_STORAGE_F16));
+    GLS_CHECK(c->run((const uint16_t*)raw->ptr, pitch_elems(raw), p, out->ptr, out->format == GLS_RGBA_F32,
+                     pitch_elems(out)));
+    if (!defer) GLS_CHECK(c->fetch_noise_model(p));
+    return GLS_OK;
+}
+
+gls_status gls_raw_converter_noise_model(gls_raw_converter* c, gls_demosaic_params* p) {
+    if (!c || !p) return GLS_ERR_INVALID_ARGUMENT;
+    if (c->L == 0) return set_error(c->ctx, GLS_ERR_INVALID_ARGUMENT, "no frame processed yet");
+    return c->fetch_noise_model(p);
+}
+
+gls_status gls_raw_converter_demosaic_host(gls_raw_converter* c, const uint16_t* raw, int w, int h, int stride,
+                                           gls_demosaic_params* p, uint8_t* out, int out_channels) {
+    if (!c || !raw || !out) return GLS_ERR_INVALID_ARGUMENT;
+    gls_ctx* ctx = c->ctx;
+    if (out_channels != 3 && out_channels != 4)
+        return set_error(ctx, GLS_ERR_INVALID_ARGUMENT, "out_channels must be 3 or 4");
+    if (stride < w) return set_error(ctx, GLS_ERR_INVALID_SIZE, "raw stride smaller than width");
+    GLS_CHECK(validate_params(ctx, p, w, h));
+    const size_t rb = (size_t)w * h * 2, ob = (size_t)w * h * 4 + (size_t)w * h * 3;
+    if (c->raw_dev_bytes < rb) {
+        if (c->raw_dev) cudaFree(c->raw_dev);
+        c->raw_dev = nullptr;
+        c->raw_dev_bytes = 0;
+        GLS_CHECK(check_cuda(ctx, cudaMalloc(&c->raw_dev, rb), "cudaMalloc(raw)"));
+        c->raw_dev_bytes = rb;
+    }
+    if (c->out_dev_bytes < ob) {
+        if (c->out_dev) cudaFree(c->out_dev);
+        c->out_dev = nullptr;
+        c->out_dev_bytes = 0;
+        GLS_CHECK(check_cuda(ctx, cudaMalloc(&c->out_dev, ob), "cudaMalloc(output)"));
+        c->out_dev_bytes = ob;
+    }
+    GLS_CHECK(check_cuda(ctx, cudaMemcpy2DAsync(c->raw_dev, (size_t)w * 2, raw, (size_t)stride * 2, (size_t)w * 2, h,
+                                                cudaMemcpyHostToDevice, ctx->stream), "copy raw frame"));
+    GLS_CHECK(c->ensure(w, h, p->pyramid_levels, p->storage == GLS_STORAGE_F16));
+    GLS_CHECK(c->run(c->raw_dev, w, p, c->out_dev, false, w));
+    const void* src = c->out_dev;
+    if (out_channels == 3) {
+        uint8_t* rgb = c->out_dev + (size_t)w * h * 4;
+        rgba8_to_rgb8_kernel<<<dim3((w + 31) / 32, (h + 7) / 8), dim3(32, 8), 0, ctx->stream>>>(
+            (const uchar4*)c->out_dev, w, h, rgb);
+        ctx->launches++;
+        src = rgb;
+    }
+    GLS_CHECK(check_cuda(ctx, cudaMemcpyAsync(out, src, (size_t)w * h * out_channels, cudaMemcpyDeviceToHost,
+                                              ctx->stream), "copy output"));
+    return c->fetch_noise_model(p);
+}
+
+gls_status gls_raw_converter_fast_demosaic(gls_raw_converter* c, const gls_image_desc* raw,
+                                           const gls_demosaic_params* p, const gls_image_desc* out) {
+    if (!c) return GLS_ERR_INVALID_ARGUMENT;
+    gls_ctx* ctx = c->ctx;
+    GLS_CHECK(check_desc(ctx, raw, "raw", GLS_R16_UNORM));
+    GLS_CHECK(check_desc(ctx, out, "out", GLS_RGBA8_UNORM, GLS_RGBA_F32));
+    if (!p) return set_error(ctx, GLS_ERR_INVALID_ARGUMENT, "params is null");
+    if ((raw->width & 1) || (raw->height & 1)) return set_error(ctx, GLS_ERR_INVALID_SIZE, "odd raw frame size");
+    if (out->width != raw->width / 2 || out->height != raw->height / 2)
+        return set_error(ctx, GLS_ERR_INVALID_SIZE, "fastDemosaicImage output must be half size");
+    if (p->bayer_pattern < 0 || p->bayer_pattern > 3) return set_error(ctx, GLS_ERR_INVALID_ARGUMENT, "bayer pattern");
+    const bool half = p->storage == GLS_STORAGE_F16;
+    GLS_CHECK(c->ensure(raw->width, raw->height, c->L ? c->L : 4, half));
+    const int w = raw->width, h = raw->height;
+    launch_scale_raw(ctx, (const uint16_t*)raw->ptr, w, h, pitch_elems(raw), c->scaled, p->bayer_pattern, p->scale_mul,
+                     p->black_level / 0xffff);
+    ImgRef half_rgb{c->linA.ptr, w / 2, h / 2, w / 2, half};
+    launch_fast_debayer(ctx, c->scaled, half_rgb, p->bayer_pattern);
+    launch_highlights(ctx, half_rgb, half_rgb, 1.0f);
+    const gls_rgb_conversion_params& rc = p->rgb_conversion;
+    RgbParams rp{rc.contrast, rc.saturation, rc.toneCurveSlope, rc.exposureBias, rc.blacks, 0};
+    launch_srgb(ctx, half_rgb, nullptr, out->ptr, out->format == GLS_RGBA_F32, pitch_elems(out), p->rgb_cam, rp);
+    return check_launch(ctx, "RawConverter::fastDemosaicImage");
+}
+
+}  // extern "C"

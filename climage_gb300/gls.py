@@ -1,0 +1,394 @@
+"""ctypes bindings of libgls_cuda.so (include/gls_cuda.h) and a thin Python mirror of the
+reference's operator surface (demosaic_cl.hpp free functions, RawConverter).
+
+Device images are torch CUDA tensors: (H, W) for single-channel images, (H, W, 4) for
+RGBA, with dtype uint16 (raw), float32/float16 (storage precision) or uint8 (RGBA8).
+PyTorch only supplies device memory and the stream; every pixel is computed by the CUDA
+kernels of libgls_cuda.  There is no CPU fallback: without the built library every call
+raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libgls_cuda.so")
+
+GLS_OK = 0
+STATUS = {0: "ok", 1: "invalid argument", 2: "invalid size", 3: "unsupported", 4: "CUDA error",
+          5: "out of memory", 6: "timeout", 7: "unsupported pixel format"}
+
+R16_UNORM, R_F32, R_F16, RGBA_F32, RGBA_F16, RGBA8_UNORM, RGB8_UNORM = range(7)
+GRBG, GBRG, RGGB, BGGR = range(4)
+BILATERAL, GUIDED_FAST, GUIDED_PRECISE = range(3)
+STORAGE_F32, STORAGE_F16 = 0, 1
+MAX_LEVELS = 8
+
+
+class GlsError(RuntimeError):
+    def __init__(self, status, what, detail=""):
+        super().__init__("%s failed: %s%s" % (what, STATUS.get(status, status), (" (%s)" % detail) if detail else ""))
+        self.status = status
+
+
+class ImageDesc(ctypes.Structure):
+    _fields_ = [("ptr", ctypes.c_void_p), ("width", ctypes.c_int), ("height", ctypes.c_int),
+                ("stride_bytes", ctypes.c_int), ("format", ctypes.c_int)]
+
+
+class DenoiseParams(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_float) for n in ("luma", "chroma", "chromaBoost", "gradientBoost", "sharpening")]
+
+
+class RGBConversionParams(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_float) for n in ("contrast", "saturation", "toneCurveSlope", "exposureBias", "blacks")] + [
+        ("localToneMapping", ctypes.c_int)]
+
+
+class LTMParams(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_float) for n in ("guidedFilterEps", "shadows", "highlights", "detail")]
+
+
+class DemosaicParams(ctypes.Structure):
+    _fields_ = [
+        ("bayer_pattern", ctypes.c_int),
+        ("black_level", ctypes.c_float),
+        ("white_level", ctypes.c_float),
+        ("exposure_multiplier", ctypes.c_float),
+        ("scale_mul", ctypes.c_float * 4),
+        ("rgb_cam", ctypes.c_float * 9),
+        ("raw_nlf", ctypes.c_float * 4),
+        ("pyramid_nlf", (ctypes.c_float * 6) * MAX_LEVELS),
+        ("denoise", DenoiseParams * MAX_LEVELS),
+        ("noise_level", ctypes.c_float),
+        ("rgb_conversion", RGBConversionParams),
+        ("ltm", LTMParams),
+        ("pyramid_levels", ctypes.c_int),
+        ("denoise_algorithm", ctypes.c_int),
+        ("storage", ctypes.c_int),
+        ("rotate_180", ctypes.c_int),
+    ]
+
+
+_lib = None
+
+# (name, restype, argtypes) of every entry point declared in include/gls_cuda.h
+_P = ctypes.c_void_p
+_D = ctypes.POINTER(ImageDesc)
+_F = ctypes.c_float
+_I = ctypes.c_int
+_FP = ctypes.POINTER(ctypes.c_float)
+SIGNATURES = [
+    ("gls_ctx_create", _I, [_I, ctypes.POINTER(_P)]),
+    ("gls_ctx_destroy", _I, [_P]),
+    ("gls_ctx_set_stream", _I, [_P, _P]),
+    ("gls_ctx_synchronize", _I, [_P]),
+    ("gls_status_string", ctypes.c_char_p, [_I]),
+    ("gls_ctx_last_error", ctypes.c_char_p, [_P]),
+    ("gls_ctx_kernel_launches", ctypes.c_uint64, [_P]),
+    ("gls_version", ctypes.c_char_p, []),
+    ("gls_scale_raw_data", _I, [_P, _D, _D, _I, _FP, _F]),
+    ("gls_raw_noise_statistics", _I, [_P, _D, _I, _D, _D]),
+    ("gls_compute_raw_noise_statistics", _I, [_P, _D, _I, _FP]),
+    ("gls_interpolate_green", _I, [_P, _D, _D, _I, _F]),
+    ("gls_interpolate_red_blue", _I, [_P, _D, _D, _D, _I, _F, _I]),
+    ("gls_fast_debayer", _I, [_P, _D, _D, _I]),
+    ("gls_blend_highlights", _I, [_P, _D, _F, _D]),
+    ("gls_transform_image", _I, [_P, _D, _D, _FP]),
+    ("gls_despeckle_image", _I, [_P, _D, _FP, _FP, _D]),
+    ("gls_downsample_image", _I, [_P, _D, _D]),
+    ("gls_noise_statistics", _I, [_P, _D, _D]),
+    ("gls_compute_noise_statistics", _I, [_P, _D, _FP]),
+    ("gls_denoise_image", _I, [_P, _D, _FP, _FP, _F, _F, _D]),
+    ("gls_denoise_image_guided", _I, [_P, _D, _FP, _FP, _D]),
+    ("gls_guided_filter", _I, [_P, _D, _I, _FP, _D]),
+    ("gls_reassemble_image", _I, [_P, _D, _D, _D, _F, _FP, _D]),
+    ("gls_local_tone_mapping_mask", _I, [_P, _D, _D, ctypes.POINTER(LTMParams), _FP, _D]),
+    ("gls_convert_to_srgb", _I, [_P, _D, _D, _D, _FP, ctypes.POINTER(RGBConversionParams)]),
+    ("gls_bayer_to_raw_rgba", _I, [_P, _D, _D, _I]),
+    ("gls_raw_rgba_to_bayer", _I, [_P, _D, _D, _I]),
+    ("gls_despeckle_raw_rgba", _I, [_P, _D, _D]),
+    ("gls_denoise_raw_rgba", _I, [_P, _D, _FP, _D]),
+    ("gls_unpack_raw_bits", _I, [_P, _P, ctypes.c_size_t, _I, _P, ctypes.c_size_t]),
+    ("gls_cam_xyz_coeff", _I, [_FP, _FP, _FP]),
+    ("gls_cam_ycbcr", _I, [_FP, _FP]),
+    ("gls_inverse3x3", _I, [_FP, _FP]),
+    ("gls_raw_converter_create", _I, [_P, ctypes.POINTER(_P)]),
+    ("gls_raw_converter_destroy", _I, [_P]),
+    ("gls_raw_converter_demosaic", _I, [_P, _D, ctypes.POINTER(DemosaicParams), _D, _I]),
+    ("gls_raw_converter_noise_model", _I, [_P, ctypes.POINTER(DemosaicParams)]),
+    ("gls_raw_converter_demosaic_host", _I, [_P, _P, _I, _I, _I, ctypes.POINTER(DemosaicParams), _P, _I]),
+    ("gls_raw_converter_fast_demosaic", _I, [_P, _D, ctypes.POINTER(DemosaicParams), _D]),
+    ("gls_raw_converter_set_tap", _I, [_P, _I, _D]),
+    ("gls_raw_converter_profile", _I, [_P, _I]),
+    ("gls_raw_converter_profile_report", _I, [_P, ctypes.c_char_p, ctypes.c_size_t]),
+]
+
+
+def lib():
+    """Loads libgls_cuda.so; raises when it has not been built (there is no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libgls_cuda.so is not built: run climage_gb300.build.build() (nvcc, sm_103a)")
+        l = ctypes.CDLL(LIB_PATH)
+        for name, res, args in SIGNATURES:
+            fn = getattr(l, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = l
+    return _lib
+
+
+def farr(vals, n=None):
+    vals = [float(v) for v in np.ravel(vals)]
+    n = len(vals) if n is None else n
+    return (ctypes.c_float * n)(*vals)
+
+
+# ---- host colour math (no GPU needed) ----
+
+def cam_xyz_coeff(cam_xyz):
+    pre, out = (ctypes.c_float * 3)(), (ctypes.c_float * 9)()
+    s = lib().gls_cam_xyz_coeff(farr(cam_xyz, 9), pre, out)
+    if s != GLS_OK:
+        raise GlsError(s, "cam_xyz_coeff")
+    return np.array(pre[:], np.float32), np.array(out[:], np.float32).reshape(3, 3)
+
+
+def cam_ycbcr(rgb_cam):
+    out = (ctypes.c_float * 9)()
+    lib().gls_cam_ycbcr(farr(rgb_cam, 9), out)
+    return np.array(out[:], np.float32).reshape(3, 3)
+
+
+def inverse3x3(m):
+    out = (ctypes.c_float * 9)()
+    s = lib().gls_inverse3x3(farr(m, 9), out)
+    if s != GLS_OK:
+        raise GlsError(s, "inverse3x3")
+    return np.array(out[:], np.float32).reshape(3, 3)
+
+
+# ---- device images ----
+
+def _fmt_of(t, channels):
+    import torch
+    if t.dtype == torch.uint16:
+        return R16_UNORM
+    if t.dtype == torch.uint8:
+        return RGBA8_UNORM if channels == 4 else RGB8_UNORM
+    if t.dtype == torch.float32:
+        return R_F32 if channels == 1 else RGBA_F32
+    if t.dtype == torch.float16:
+        return R_F16 if channels == 1 else RGBA_F16
+    raise TypeError("unsupported tensor dtype %s" % t.dtype)
+
+
+def desc(t):
+    """gls_image_desc of a contiguous (H, W) or (H, W, C) CUDA tensor."""
+    if t is None:
+        return None
+    if not t.is_cuda:
+        raise ValueError("device images must be CUDA tensors")
+    if t.dim() == 2:
+        h, w = t.shape
+        c = 1
+    elif t.dim() == 3:
+        h, w, c = t.shape
+    else:
+        raise ValueError("images are (H, W) or (H, W, C) tensors")
+    if t.stride(-1) != 1 or (t.dim() == 3 and t.stride(1) != c):
+        raise ValueError("image rows must be contiguous")
+    es = t.element_size()
+    return ImageDesc(t.data_ptr(), w, h, t.stride(0) * es, _fmt_of(t, c))
+
+
+class Context:
+    """gls_ctx: one per host thread; launches go to the torch stream current at creation
+    unless set_stream is called."""
+
+    def __init__(self, device=0, stream=None):
+        import torch
+        self._lib = lib()
+        self.handle = ctypes.c_void_p()
+        s = self._lib.gls_ctx_create(device, ctypes.byref(self.handle))
+        if s != GLS_OK:
+            raise GlsError(s, "gls_ctx_create")
+        self.set_stream(stream if stream is not None else torch.cuda.current_stream(device))
+
+    def set_stream(self, stream):
+        self.stream = stream
+        self._lib.gls_ctx_set_stream(self.handle, ctypes.c_void_p(stream.cuda_stream))
+
+    def check(self, status, what):
+        if status != GLS_OK:
+            raise GlsError(status, what, self._lib.gls_ctx_last_error(self.handle).decode())
+
+    def synchronize(self):
+        self.check(self._lib.gls_ctx_synchronize(self.handle), "synchronize")
+
+    def kernel_launches(self):
+        return int(self._lib.gls_ctx_kernel_launches(self.handle))
+
+    def close(self):
+        if self.handle:
+            self._lib.gls_ctx_destroy(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- stages (demosaic_cl.hpp) ----
+    def scaleRawData(self, raw, scaled, bayer, scale_mul, black_level):
+        self.check(self._lib.gls_scale_raw_data(self.handle, desc(raw), desc(scaled), bayer, farr(scale_mul, 4),
+                                                float(black_level)), "scaleRawData")
+
+    def rawNoiseStatistics(self, scaled, bayer, mean, var):
+        self.check(self._lib.gls_raw_noise_statistics(self.handle, desc(scaled), bayer, desc(mean), desc(var)),
+                   "rawNoiseStatistics")
+
+    def computeRawNoiseStatistics(self, scaled, bayer):
+        out = (ctypes.c_float * 8)()
+        self.check(self._lib.gls_compute_raw_noise_statistics(self.handle, desc(scaled), bayer, out),
+                   "computeRawNoiseStatistics")
+        return np.array(out[:], np.float32)
+
+    def interpolateGreen(self, scaled, green, bayer, luma_variance):
+        self.check(self._lib.gls_interpolate_green(self.handle, desc(scaled), desc(green), bayer, float(luma_variance)),
+                   "interpolateGreen")
+
+    def interpolateRedBlue(self, scaled, green, rgb, bayer, chroma_variance, rotate_180=False):
+        self.check(self._lib.gls_interpolate_red_blue(self.handle, desc(scaled), desc(green), desc(rgb), bayer,
+                                                      float(chroma_variance), int(rotate_180)), "interpolateRedBlue")
+
+    def fastDebayer(self, scaled, rgb, bayer):
+        self.check(self._lib.gls_fast_debayer(self.handle, desc(scaled), desc(rgb), bayer), "fastDebayer")
+
+    def blendHighlightsImage(self, inp, clip, out):
+        self.check(self._lib.gls_blend_highlights(self.handle, desc(inp), float(clip), desc(out)), "blendHighlights")
+
+    def transformImage(self, inp, out, transform):
+        self.check(self._lib.gls_transform_image(self.handle, desc(inp), desc(out), farr(transform, 9)),
+                   "transformImage")
+
+    def despeckleImage(self, inp, var_a, var_b, out):
+        self.check(self._lib.gls_despeckle_image(self.handle, desc(inp), farr(var_a, 3), farr(var_b, 3), desc(out)),
+                   "despeckleImage")
+
+    def downsampleImage(self, inp, out):
+        self.check(self._lib.gls_downsample_image(self.handle, desc(inp), desc(out)), "downsampleImage")
+
+    def noiseStatistics(self, inp, out):
+        self.check(self._lib.gls_noise_statistics(self.handle, desc(inp), desc(out)), "noiseStatistics")
+
+    def computeNoiseStatistics(self, inp):
+        out = (ctypes.c_float * 6)()
+        self.check(self._lib.gls_compute_noise_statistics(self.handle, desc(inp), out), "computeNoiseStatistics")
+        return np.array(out[:], np.float32)
+
+    def denoiseImage(self, inp, var_a, var_b, chroma_boost, gradient_boost, out):
+        self.check(self._lib.gls_denoise_image(self.handle, desc(inp), farr(var_a, 3), farr(var_b, 3),
+                                               float(chroma_boost), float(gradient_boost), desc(out)), "denoiseImage")
+
+    def denoiseImageGuided(self, inp, var_a, var_b, out):
+        self.check(self._lib.gls_denoise_image_guided(self.handle, desc(inp), farr(var_a, 3), farr(var_b, 3),
+                                                      desc(out)), "denoiseImageGuided")
+
+    def guidedFilter(self, inp, filter_size, eps, out):
+        self.check(self._lib.gls_guided_filter(self.handle, desc(inp), int(filter_size), farr(eps, 3), desc(out)),
+                   "GuidedFilter::filter")
+
+    def reassembleImage(self, den0, img1, den1, sharpening, nlf, out):
+        self.check(self._lib.gls_reassemble_image(self.handle, desc(den0), desc(img1), desc(den1), float(sharpening),
+                                                  farr(nlf, 2), desc(out)), "reassembleImage")
+
+    def localToneMappingMask(self, inp, guide, ltm, transform, out):
+        self.check(self._lib.gls_local_tone_mapping_mask(self.handle, desc(inp), desc(guide), ctypes.byref(ltm),
+                                                         farr(transform, 9), desc(out)), "localToneMappingMask")
+
+    def convertTosRGB(self, linear, ltm_mask, out, rgb_cam, params):
+        self.check(self._lib.gls_convert_to_srgb(self.handle, desc(linear), desc(ltm_mask), desc(out),
+                                                 farr(rgb_cam, 9), ctypes.byref(params)), "convertTosRGB")
+
+    def bayerToRawRGBA(self, raw, rgba, bayer):
+        self.check(self._lib.gls_bayer_to_raw_rgba(self.handle, desc(raw), desc(rgba), bayer), "bayerToRawRGBA")
+
+    def rawRGBAToBayer(self, rgba, raw, bayer):
+        self.check(self._lib.gls_raw_rgba_to_bayer(self.handle, desc(rgba), desc(raw), bayer), "rawRGBAToBayer")
+
+    def despeckleRawRGBAImage(self, inp, out):
+        self.check(self._lib.gls_despeckle_raw_rgba(self.handle, desc(inp), desc(out)), "despeckleRawRGBAImage")
+
+    def denoiseRawRGBAImage(self, inp, raw_variance, out):
+        self.check(self._lib.gls_denoise_raw_rgba(self.handle, desc(inp), farr(raw_variance, 4), desc(out)),
+                   "denoiseRawRGBAImage")
+
+    def unpackRawBits(self, packed, bits, out):
+        n = out.numel()
+        self.check(self._lib.gls_unpack_raw_bits(self.handle, ctypes.c_void_p(packed.data_ptr()), packed.numel(),
+                                                 int(bits), ctypes.c_void_p(out.data_ptr()), n), "unpackRawBits")
+
+
+class RawConverter:
+    """RawConverter (raw_converter.hpp:22-62) over gls_raw_converter."""
+
+    def __init__(self, ctx):
+        self.ctx = ctx
+        self.handle = ctypes.c_void_p()
+        ctx.check(lib().gls_raw_converter_create(ctx.handle, ctypes.byref(self.handle)), "RawConverter")
+
+    def demosaicImage(self, raw, params, out, defer_noise_model=False):
+        """raw: (H, W) uint16 CUDA tensor; out: (H, W, 4) uint8 (RGBA8) or float32 CUDA tensor."""
+        self.ctx.check(lib().gls_raw_converter_demosaic(self.handle, desc(raw), ctypes.byref(params), desc(out),
+                                                        int(defer_noise_model)), "RawConverter::demosaicImage")
+        return out
+
+    def noiseModel(self, params):
+        self.ctx.check(lib().gls_raw_converter_noise_model(self.handle, ctypes.byref(params)), "noiseModel")
+
+    def demosaicImageHost(self, raw, params, out):
+        """raw: (H, W) uint16 numpy array (ideally pinned); out: (H, W, 3|4) uint8 numpy array."""
+        h, w = raw.shape
+        ch = out.shape[2]
+        self.ctx.check(lib().gls_raw_converter_demosaic_host(
+            self.handle, ctypes.c_void_p(raw.ctypes.data), w, h, raw.strides[0] // 2, ctypes.byref(params),
+            ctypes.c_void_p(out.ctypes.data), ch), "demosaicImage (host buffers)")
+        return out
+
+    def demosaicImageHostPtr(self, raw_ptr, w, h, params, out_ptr, channels):
+        self.ctx.check(lib().gls_raw_converter_demosaic_host(self.handle, ctypes.c_void_p(raw_ptr), w, h, w,
+                                                             ctypes.byref(params), ctypes.c_void_p(out_ptr), channels),
+                       "demosaicImage (host buffers)")
+
+    def fastDemosaicImage(self, raw, params, out):
+        self.ctx.check(lib().gls_raw_converter_fast_demosaic(self.handle, desc(raw), ctypes.byref(params), desc(out)),
+                       "RawConverter::fastDemosaicImage")
+        return out
+
+    def profile(self, enable=True):
+        self.ctx.check(lib().gls_raw_converter_profile(self.handle, int(enable)), "profile")
+
+    def profileReport(self):
+        import json
+        buf = ctypes.create_string_buffer(1 << 16)
+        self.ctx.check(lib().gls_raw_converter_profile_report(self.handle, buf, len(buf)), "profile report")
+        return json.loads(buf.value.decode())
+
+    def setTap(self, stage, tensor):
+        self.ctx.check(lib().gls_raw_converter_set_tap(self.handle, int(stage), desc(tensor)), "setTap")
+
+    def close(self):
+        if self.handle:
+            lib().gls_raw_converter_destroy(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,229 @@
+/*
+ * gls_cuda.h -- C ABI of the GB300-native (sm_103a) RAW->RGB pipeline.
+ *
+ * Drop-in boundary for CLImage's RAW pipeline: every stage that the reference binds as a
+ * C++ free function over gls::cl_image_2d<T> (CLImage/app/src/main/cpp/demosaic_cl.hpp,
+ * pyramidal_denoise.hpp, guided_filter.hpp, raw_converter.hpp) has one entry point here,
+ * taking plain device pointers and sizes.  The header-only C++ layer in
+ * include/gls_cuda.hpp restores the reference's signatures (gls::image<T>,
+ * gls::cuda_image_2d<T>, RawConverter) on top of it.
+ *
+ * Conventions
+ *  - Every call returns a gls_status; nothing throws across this boundary.
+ *  - Stage calls are asynchronous on the context's stream (gls_ctx_set_stream); calls that
+ *    return host values (noise models, the host-buffer pipeline) synchronise that stream.
+ *  - Images are described by gls_image_desc: a device pointer, width, height, row pitch
+ *    in bytes and a pixel format.  Pitches must be multiples of the pixel size.
+ *  - One gls_ctx per host thread; a context is not thread-safe.
+ */
+#ifndef GLS_CUDA_H
+#define GLS_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GLS_API __attribute__((visibility("default")))
+
+typedef enum {
+    GLS_OK = 0,
+    GLS_ERR_INVALID_ARGUMENT = 1,
+    GLS_ERR_INVALID_SIZE = 2,
+    GLS_ERR_UNSUPPORTED = 3,
+    GLS_ERR_CUDA = 4,
+    GLS_ERR_OUT_OF_MEMORY = 5,
+    GLS_ERR_TIMEOUT = 6,
+    GLS_ERR_FORMAT = 7,
+} gls_status;
+
+/* Pixel formats (gls_cl_image.hpp:232-292 maps the same pixel types to OpenCL formats). */
+typedef enum {
+    GLS_R16_UNORM = 0,   /* luma_pixel_16: raw sensor data */
+    GLS_R_F32 = 1,       /* luma_pixel_float, fp32 storage */
+    GLS_R_F16 = 2,       /* luma_pixel_float, fp16 storage (the reference as built for ARM) */
+    GLS_RGBA_F32 = 3,    /* rgba_pixel_float, fp32 storage */
+    GLS_RGBA_F16 = 4,    /* rgba_pixel_float, fp16 storage */
+    GLS_RGBA8_UNORM = 5, /* rgba_pixel: the pipeline's product */
+    GLS_RGB8_UNORM = 6,  /* rgb_pixel: RawConverter::convertToRGBImage's product */
+} gls_pixel_format;
+
+typedef struct {
+    void* ptr;
+    int width;
+    int height;
+    int stride_bytes;
+    int format; /* gls_pixel_format */
+} gls_image_desc;
+
+typedef enum { GLS_GRBG = 0, GLS_GBRG = 1, GLS_RGGB = 2, GLS_BGGR = 3 } gls_bayer_pattern;
+
+/* DenoiseParameters, RGBConversionParameters, LTMParameters (demosaic.hpp:32-56); the
+ * two structs passed to kernels keep the layout of demosaic.cl:1026-1031, 1423-1430. */
+typedef struct {
+    float luma, chroma, chromaBoost, gradientBoost, sharpening;
+} gls_denoise_params;
+
+typedef struct {
+    float contrast, saturation, toneCurveSlope, exposureBias, blacks;
+    int localToneMapping;
+} gls_rgb_conversion_params;
+
+typedef struct {
+    float guidedFilterEps, shadows, highlights, detail;
+} gls_ltm_params;
+
+#define GLS_MAX_LEVELS 8
+
+typedef enum { GLS_DENOISE_BILATERAL = 0, GLS_DENOISE_GUIDED_FAST = 1, GLS_DENOISE_GUIDED_PRECISE = 2 } gls_denoise_algorithm;
+typedef enum { GLS_STORAGE_F32 = 0, GLS_STORAGE_F16 = 1 } gls_storage;
+
+/* DemosaicParameters (demosaic.hpp:61-81), generalised from 5 to pyramid_levels levels.
+ * raw_nlf and pyramid_nlf are in/out exactly as NoiseModel is in the reference:
+ * pyramid_nlf[0] on input parameterises the despeckle (raw_converter.cpp:144-145), and the
+ * pipeline overwrites both with the fitted noise model. */
+typedef struct {
+    int bayer_pattern;
+    float black_level;
+    float white_level;
+    float exposure_multiplier;
+    float scale_mul[4];
+    float rgb_cam[9];
+    float raw_nlf[4];
+    float pyramid_nlf[GLS_MAX_LEVELS][6];
+    gls_denoise_params denoise[GLS_MAX_LEVELS];
+    float noise_level;
+    gls_rgb_conversion_params rgb_conversion;
+    gls_ltm_params ltm;
+    int pyramid_levels;    /* 4..8 (the reference fixes 5) */
+    int denoise_algorithm; /* gls_denoise_algorithm (PyramidalDenoise::DenoiseAlgorithm) */
+    int storage;           /* gls_storage of the intermediate images */
+    int rotate_180;        /* must be 0 */
+} gls_demosaic_params;
+
+typedef struct gls_ctx gls_ctx;
+typedef struct gls_raw_converter gls_raw_converter;
+
+/* ---- context ---- */
+GLS_API gls_status gls_ctx_create(int device, gls_ctx** out);
+GLS_API gls_status gls_ctx_destroy(gls_ctx* ctx);
+GLS_API gls_status gls_ctx_set_stream(gls_ctx* ctx, void* cuda_stream);
+GLS_API gls_status gls_ctx_synchronize(gls_ctx* ctx);
+GLS_API const char* gls_status_string(gls_status s);
+GLS_API const char* gls_ctx_last_error(gls_ctx* ctx);
+/* Number of kernels this context has launched so far (all entry points). */
+GLS_API uint64_t gls_ctx_kernel_launches(gls_ctx* ctx);
+GLS_API const char* gls_version(void);
+
+/* ---- single stages (demosaic_cl.hpp:23-129) ---- */
+/* scaleRawData (demosaic_cl.cpp:26-44): raw R16_UNORM -> scaled R_F32/R_F16 */
+GLS_API gls_status gls_scale_raw_data(gls_ctx* ctx, const gls_image_desc* raw, const gls_image_desc* scaled,
+                                      int bayer_pattern, const float scale_mul[4], float black_level);
+/* rawNoiseStatistics (demosaic_cl.cpp:104-126): scaled -> mean, var (RGBA_F32, w/2 x h/2) */
+GLS_API gls_status gls_raw_noise_statistics(gls_ctx* ctx, const gls_image_desc* scaled, int bayer_pattern,
+                                            const gls_image_desc* mean, const gls_image_desc* var);
+/* computeRawNoiseStatistics (pyramidal_denoise.hpp:56-58): returns {A0..A3, B0..B3} */
+GLS_API gls_status gls_compute_raw_noise_statistics(gls_ctx* ctx, const gls_image_desc* scaled, int bayer_pattern,
+                                                    float out_nlf[8]);
+/* interpolateGreen (demosaic_cl.cpp:46-64) */
+GLS_API gls_status gls_interpolate_green(gls_ctx* ctx, const gls_image_desc* scaled, const gls_image_desc* green,
+                                         int bayer_pattern, float luma_variance);
+/* interpolateRedBlue (demosaic_cl.cpp:66-86); rotate_180 must be 0 */
+GLS_API gls_status gls_interpolate_red_blue(gls_ctx* ctx, const gls_image_desc* scaled, const gls_image_desc* green,
+                                            const gls_image_desc* rgb, int bayer_pattern, float chroma_variance,
+                                            int rotate_180);
+/* fasteDebayer (demosaic_cl.cpp:88-102): scaled -> RGBA at half resolution */
+GLS_API gls_status gls_fast_debayer(gls_ctx* ctx, const gls_image_desc* scaled, const gls_image_desc* rgb,
+                                    int bayer_pattern);
+/* blendHighlightsImage (demosaic_cl.cpp:506-522); in may equal out */
+GLS_API gls_status gls_blend_highlights(gls_ctx* ctx, const gls_image_desc* in, float clip, const gls_image_desc* out);
+/* transformImage (demosaic_cl.cpp:210-235); row-major 3x3; in may equal out */
+GLS_API gls_status gls_transform_image(gls_ctx* ctx, const gls_image_desc* in, const gls_image_desc* out,
+                                       const float transform[9]);
+/* despeckleImage (demosaic_cl.cpp:270-291, kernel despeckleLumaMedianChromaImage) */
+GLS_API gls_status gls_despeckle_image(gls_ctx* ctx, const gls_image_desc* in, const float var_a[3],
+                                       const float var_b[3], const gls_image_desc* out);
+/* resampleImage("downsampleImage") (demosaic_cl.cpp:157-180) */
+GLS_API gls_status gls_downsample_image(gls_ctx* ctx, const gls_image_desc* in, const gls_image_desc* out);
+/* applyKernel("noiseStatistics") (pyramidal_denoise.cpp:162-164): RGBA -> RGBA_F32 */
+GLS_API gls_status gls_noise_statistics(gls_ctx* ctx, const gls_image_desc* in, const gls_image_desc* out);
+/* computeNoiseStatistics (pyramidal_denoise.hpp:53-54): returns {A0..A2, B0..B2} */
+GLS_API gls_status gls_compute_noise_statistics(gls_ctx* ctx, const gls_image_desc* in, float out_nlf[6]);
+/* denoiseImage (demosaic_cl.cpp:296-319) */
+GLS_API gls_status gls_denoise_image(gls_ctx* ctx, const gls_image_desc* in, const float var_a[3],
+                                     const float var_b[3], float chroma_boost, float gradient_boost,
+                                     const gls_image_desc* out);
+/* denoiseImageGuided (demosaic_cl.cpp:321-337) */
+GLS_API gls_status gls_denoise_image_guided(gls_ctx* ctx, const gls_image_desc* in, const float var_a[3],
+                                            const float var_b[3], const gls_image_desc* out);
+/* GuidedFilter::filter (guided_filter.cpp:195-225) */
+GLS_API gls_status gls_guided_filter(gls_ctx* ctx, const gls_image_desc* in, int filter_size, const float eps[3],
+                                     const gls_image_desc* out);
+/* reassembleImage (demosaic_cl.cpp:182-208); den0 may equal out */
+GLS_API gls_status gls_reassemble_image(gls_ctx* ctx, const gls_image_desc* den0, const gls_image_desc* img1,
+                                        const gls_image_desc* den1, float sharpening, const float nlf[2],
+                                        const gls_image_desc* out);
+/* localToneMappingMask (demosaic_cl.cpp:339-370) */
+GLS_API gls_status gls_local_tone_mapping_mask(gls_ctx* ctx, const gls_image_desc* in, const gls_image_desc* guide,
+                                               const gls_ltm_params* ltm, const float transform[9],
+                                               const gls_image_desc* out);
+/* convertTosRGB (demosaic_cl.cpp:237-268): out RGBA8_UNORM (the product) or RGBA_F32 */
+GLS_API gls_status gls_convert_to_srgb(gls_ctx* ctx, const gls_image_desc* linear, const gls_image_desc* ltm_mask,
+                                       const gls_image_desc* out, const float rgb_cam[9],
+                                       const gls_rgb_conversion_params* params);
+/* bayerToRawRGBA / rawRGBAToBayer (demosaic_cl.cpp:372-406) */
+GLS_API gls_status gls_bayer_to_raw_rgba(gls_ctx* ctx, const gls_image_desc* raw, const gls_image_desc* rgba,
+                                         int bayer_pattern);
+GLS_API gls_status gls_raw_rgba_to_bayer(gls_ctx* ctx, const gls_image_desc* rgba, const gls_image_desc* raw,
+                                         int bayer_pattern);
+/* despeckleRawRGBAImage / denoiseRawRGBAImage (demosaic_cl.cpp:408-444) */
+GLS_API gls_status gls_despeckle_raw_rgba(gls_ctx* ctx, const gls_image_desc* in, const gls_image_desc* out);
+GLS_API gls_status gls_denoise_raw_rgba(gls_ctx* ctx, const gls_image_desc* in, const float raw_variance[4],
+                                        const gls_image_desc* out);
+/* unpack12BitsInto16Bits / unpack14BitsInto16Bits (src/gls_image_tiff.cpp:53-87), plus
+ * 10-bit: MSB-first packed samples (device bytes) -> uint16 (device), n_samples outputs. */
+GLS_API gls_status gls_unpack_raw_bits(gls_ctx* ctx, const void* packed, size_t n_bytes, int bits, uint16_t* out,
+                                       size_t n_samples);
+
+/* ---- host colour math (demosaic_utils.cpp:25-52, 809-822; gls_linalg.hpp:545-556) ---- */
+GLS_API gls_status gls_cam_xyz_coeff(const float cam_xyz[9], float pre_mul[3], float rgb_cam[9]);
+GLS_API gls_status gls_cam_ycbcr(const float rgb_cam[9], float out[9]);
+GLS_API gls_status gls_inverse3x3(const float m[9], float out[9]);
+
+/* ---- the pipeline: RawConverter (raw_converter.hpp:22-62) ---- */
+GLS_API gls_status gls_raw_converter_create(gls_ctx* ctx, gls_raw_converter** out);
+GLS_API gls_status gls_raw_converter_destroy(gls_raw_converter* conv);
+/* RawConverter::demosaicImage (raw_converter.cpp:73-186) on a device raw frame; out is
+ * RGBA8_UNORM (the reference product) or RGBA_F32.  params is updated with the fitted
+ * noise model (raw_nlf, pyramid_nlf) unless defer_noise_model is set, in which case the
+ * call does not synchronise and gls_raw_converter_noise_model() returns it later. */
+GLS_API gls_status gls_raw_converter_demosaic(gls_raw_converter* conv, const gls_image_desc* raw,
+                                              gls_demosaic_params* params, const gls_image_desc* out,
+                                              int defer_noise_model);
+GLS_API gls_status gls_raw_converter_noise_model(gls_raw_converter* conv, gls_demosaic_params* params);
+/* demosaicImage + convertToRGBImage on host buffers (demosaic.cpp:34-51): host uint16
+ * raw in, host RGBA8 (out_channels 4) or RGB8 (3) out; copies go through pinned staging. */
+GLS_API gls_status gls_raw_converter_demosaic_host(gls_raw_converter* conv, const uint16_t* raw, int width, int height,
+                                                   int raw_stride_px, gls_demosaic_params* params, uint8_t* out,
+                                                   int out_channels);
+/* RawConverter::fastDemosaicImage (raw_converter.cpp:188-224): half-resolution preview */
+GLS_API gls_status gls_raw_converter_fast_demosaic(gls_raw_converter* conv, const gls_image_desc* raw,
+                                                   const gls_demosaic_params* params, const gls_image_desc* out);
+/* Optional intermediate images of the last demosaic call (device RGBA_F32 unless noted),
+ * for parity checks: stage 0 scaled raw (R_F32), 1 green (R_F32), 2 level 0 after the
+ * despeckle, 3 denoised level 0 (YCbCr), 4 LTM mask (R_F32). */
+GLS_API gls_status gls_raw_converter_set_tap(gls_raw_converter* conv, int stage, const gls_image_desc* dst);
+/* Per-stage timing (the reference's PRINT_EXECUTION_TIME, raw_converter.cpp:22, 97-99,
+ * 176-183, with CUDA events instead of queue.finish()).  enable != 0 records an event
+ * after every stage of later demosaic calls; the report is a JSON object
+ * {"stage": [total_ms, calls], ...} accumulated since profiling was enabled. */
+GLS_API gls_status gls_raw_converter_profile(gls_raw_converter* conv, int enable);
+GLS_API gls_status gls_raw_converter_profile_report(gls_raw_converter* conv, char* buf, size_t buf_len);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GLS_CUDA_H */

@@ -1,0 +1,389 @@
+"""ctypes wrapper of the CPU oracle (liboracle.so) and of the reference-host shim.
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and bench.py's
+CPU-baseline leg as the checker of the CUDA pipeline; the product never imports it.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+REF_PATH = os.path.join(HERE, "_ref", "libref_host.so")
+
+F32, F16, F64 = 0, 1, 2
+MAX_LEVELS = 8
+
+
+class DenoiseParams(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_float) for n in ("luma", "chroma", "chromaBoost", "gradientBoost", "sharpening")]
+
+
+class RGBParams(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_float) for n in ("contrast", "saturation", "toneCurveSlope", "exposureBias", "blacks")] + [
+        ("localToneMapping", ctypes.c_int)
+    ]
+
+
+class LTMParams(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_float) for n in ("guidedFilterEps", "shadows", "highlights", "detail")]
+
+
+class Params(ctypes.Structure):
+    _fields_ = [
+        ("bayer_pattern", ctypes.c_int),
+        ("black_level", ctypes.c_float),
+        ("white_level", ctypes.c_float),
+        ("exposure_multiplier", ctypes.c_float),
+        ("scale_mul", ctypes.c_float * 4),
+        ("rgb_cam", ctypes.c_float * 9),
+        ("noise_level", ctypes.c_float),
+        ("pyramid_levels", ctypes.c_int),
+        ("denoise_algorithm", ctypes.c_int),
+        ("rotate_180", ctypes.c_int),
+        ("raw_nlf", ctypes.c_float * 4),
+        ("pyramid_nlf", (ctypes.c_float * 6) * MAX_LEVELS),
+        ("denoise", DenoiseParams * MAX_LEVELS),
+        ("rgb", RGBParams),
+        ("ltm", LTMParams),
+    ]
+
+
+class Taps(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_void_p) for n in
+                ("scaled_raw", "green", "linear_rgb", "ycbcr", "level0", "denoised0", "ltm_mask", "camera_rgb")]
+
+
+_lib = None
+_ref = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("oracle/liboracle.so is not built: run __graft_entry__.build() or make -C oracle")
+        _lib = ctypes.CDLL(LIB_PATH)
+        f = ctypes.c_float
+        for name, res, args in [
+            ("oracle_atan2pi", f, [f, f]),
+            ("oracle_tanh", f, [f]),
+            ("oracle_exp2", f, [f]),
+            ("oracle_log2", f, [f]),
+            ("oracle_pow", f, [f, f]),
+            ("oracle_f32_to_f16", ctypes.c_uint16, [f]),
+            ("oracle_f16_to_f32", f, [ctypes.c_uint16]),
+            ("oracle_unpack_bits", ctypes.c_long, [ctypes.c_void_p, ctypes.c_long, ctypes.c_int, ctypes.c_void_p, ctypes.c_long]),
+            ("oracle_regress", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_long, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]),
+        ]:
+            fn = getattr(_lib, name)
+            fn.restype = res
+            fn.argtypes = args
+    return _lib
+
+
+def ref_lib():
+    """The reference's own host code compiled from its sources, or None when absent."""
+    global _ref
+    if _ref is None and os.path.exists(REF_PATH):
+        _ref = ctypes.CDLL(REF_PATH, mode=os.RTLD_LAZY)
+    return _ref
+
+
+def _p(a):
+    return None if a is None else ctypes.c_void_p(a.ctypes.data)
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _arr(vals, n):
+    return (ctypes.c_float * n)(*[float(v) for v in vals])
+
+
+def set_threads(n):
+    lib().oracle_set_threads(int(n))
+
+
+def threads():
+    return lib().oracle_threads()
+
+
+# ---- whole pipeline ----
+
+def demosaic(raw, params, prec=F32, want=("rgba8",), taps=()):
+    """Runs the pipeline; returns a dict with 'rgba8'/'rgbaf', the taps asked for and the
+    updated params (raw_nlf, pyramid_nlf)."""
+    raw = np.ascontiguousarray(raw, dtype=np.uint16)
+    h, w = raw.shape
+    out = {}
+    o8 = np.zeros((h, w, 4), np.uint8) if "rgba8" in want else None
+    of = np.zeros((h, w, 4), np.float32) if "rgbaf" in want else None
+    t = Taps()
+    shapes = {"scaled_raw": (h, w), "green": (h, w), "linear_rgb": (h, w, 4), "ycbcr": (h, w, 4),
+              "level0": (h, w, 4), "denoised0": (h, w, 4), "ltm_mask": (h, w), "camera_rgb": (h, w, 4)}
+    bufs = {}
+    for name in taps:
+        bufs[name] = np.zeros(shapes[name], np.float32)
+        setattr(t, name, bufs[name].ctypes.data)
+    rc = lib().oracle_demosaic(_p(raw), w, h, w, ctypes.byref(params), prec, _p(o8), _p(of), ctypes.byref(t))
+    if rc != 0:
+        raise ValueError("oracle_demosaic failed: %d" % rc)
+    if o8 is not None:
+        out["rgba8"] = o8
+    if of is not None:
+        out["rgbaf"] = of
+    out.update(bufs)
+    out["raw_nlf"] = np.array(params.raw_nlf[:], np.float32)
+    out["pyramid_nlf"] = np.array([params.pyramid_nlf[i][:] for i in range(params.pyramid_levels)], np.float32)
+    return out
+
+
+def fast_demosaic(raw, params, prec=F32):
+    raw = np.ascontiguousarray(raw, dtype=np.uint16)
+    h, w = raw.shape
+    o8 = np.zeros((h // 2, w // 2, 4), np.uint8)
+    of = np.zeros((h // 2, w // 2, 4), np.float32)
+    rc = lib().oracle_fast_demosaic(_p(raw), w, h, w, ctypes.byref(params), prec, _p(o8), _p(of))
+    if rc != 0:
+        raise ValueError("oracle_fast_demosaic failed: %d" % rc)
+    return o8, of
+
+
+# ---- single stages ----
+
+def scale_raw(raw, bayer, scale_mul, black_norm, prec=F32):
+    raw = np.ascontiguousarray(raw, dtype=np.uint16)
+    h, w = raw.shape
+    out = np.zeros((h, w), np.float32)
+    lib().oracle_scale_raw(_p(raw), w, h, w, bayer, _arr(scale_mul, 4), ctypes.c_float(black_norm), prec, _p(out))
+    return out
+
+
+def raw_noise_statistics(scaled, bayer):
+    s = _f32(scaled)
+    h, w = s.shape
+    mean = np.zeros((h // 2, w // 2, 4), np.float32)
+    var = np.zeros((h // 2, w // 2, 4), np.float32)
+    lib().oracle_raw_noise_statistics(_p(s), w, h, bayer, _p(mean), _p(var))
+    return mean, var
+
+
+def compute_raw_nlf(scaled, bayer):
+    s = _f32(scaled)
+    h, w = s.shape
+    out = (ctypes.c_float * 8)()
+    lib().oracle_compute_raw_nlf(_p(s), w, h, bayer, out)
+    return np.array(out[:], np.float32)
+
+
+def interpolate_green(scaled, bayer, luma_variance, prec=F32):
+    s = _f32(scaled)
+    h, w = s.shape
+    out = np.zeros((h, w), np.float32)
+    lib().oracle_interpolate_green(_p(s), w, h, bayer, ctypes.c_float(luma_variance), prec, _p(out))
+    return out
+
+
+def interpolate_red_blue(scaled, green, bayer, chroma_variance, prec=F32):
+    s, g = _f32(scaled), _f32(green)
+    h, w = s.shape
+    out = np.zeros((h, w, 4), np.float32)
+    lib().oracle_interpolate_red_blue(_p(s), _p(g), w, h, bayer, ctypes.c_float(chroma_variance), prec, _p(out))
+    return out
+
+
+def blend_highlights(img, clip=1.0, prec=F32):
+    a = _f32(img)
+    h, w, _ = a.shape
+    out = np.zeros_like(a)
+    lib().oracle_blend_highlights(_p(a), w, h, ctypes.c_float(clip), prec, _p(out))
+    return out
+
+
+def transform(img, m, prec=F32):
+    a = _f32(img)
+    h, w, _ = a.shape
+    out = np.zeros_like(a)
+    lib().oracle_transform(_p(a), w, h, _arr(np.ravel(m), 9), prec, _p(out))
+    return out
+
+
+def despeckle(img, var_a, var_b, prec=F32):
+    a = _f32(img)
+    h, w, _ = a.shape
+    out = np.zeros_like(a)
+    lib().oracle_despeckle(_p(a), w, h, _arr(var_a, 3), _arr(var_b, 3), prec, _p(out))
+    return out
+
+
+def downsample(img, ow, oh, prec=F32):
+    a = _f32(img)
+    h, w, _ = a.shape
+    out = np.zeros((oh, ow, 4), np.float32)
+    lib().oracle_downsample(_p(a), w, h, ow, oh, prec, _p(out))
+    return out
+
+
+def noise_statistics(img):
+    a = _f32(img)
+    h, w, _ = a.shape
+    out = np.zeros_like(a)
+    lib().oracle_noise_statistics(_p(a), w, h, _p(out))
+    return out
+
+
+def compute_nlf(img):
+    a = _f32(img)
+    h, w, _ = a.shape
+    out = (ctypes.c_float * 6)()
+    lib().oracle_compute_nlf(_p(a), w, h, out)
+    return np.array(out[:], np.float32)
+
+
+def denoise_bilateral(img, var_a, var_b, chroma_boost, gradient_boost, prec=F32):
+    a = _f32(img)
+    h, w, _ = a.shape
+    out = np.zeros_like(a)
+    lib().oracle_denoise_bilateral(_p(a), w, h, _arr(var_a, 3), _arr(var_b, 3), ctypes.c_float(chroma_boost),
+                                   ctypes.c_float(gradient_boost), prec, _p(out))
+    return out
+
+
+def denoise_guided(img, var_a, var_b, prec=F32):
+    a = _f32(img)
+    h, w, _ = a.shape
+    out = np.zeros_like(a)
+    lib().oracle_denoise_guided(_p(a), w, h, _arr(var_a, 3), _arr(var_b, 3), prec, _p(out))
+    return out
+
+
+def guided_filter(img, filter_size, eps, prec=F32):
+    a = _f32(img)
+    h, w, _ = a.shape
+    out = np.zeros_like(a)
+    lib().oracle_guided_filter(_p(a), w, h, filter_size, _arr(eps, 3), prec, _p(out))
+    return out
+
+
+def reassemble(den0, img1, den1, sharpening, nlf, prec=F32):
+    d0, i1, d1 = _f32(den0), _f32(img1), _f32(den1)
+    h, w, _ = d0.shape
+    h1, w1, _ = i1.shape
+    out = np.zeros_like(d0)
+    lib().oracle_reassemble(_p(d0), w, h, _p(i1), _p(d1), w1, h1, ctypes.c_float(sharpening), _arr(nlf, 2), prec, _p(out))
+    return out
+
+
+def ltm_mask(img, guide, ltm, m, prec=F32):
+    a, g = _f32(img), _f32(guide)
+    h, w, _ = a.shape
+    gh, gw, _ = g.shape
+    out = np.zeros((h, w), np.float32)
+    lib().oracle_ltm_mask(_p(a), w, h, _p(g), gw, gh, ctypes.byref(ltm), _arr(np.ravel(m), 9), prec, _p(out))
+    return out
+
+
+def convert_to_srgb(img, mask, m, rgb):
+    a = _f32(img)
+    h, w, _ = a.shape
+    o8 = np.zeros((h, w, 4), np.uint8)
+    of = np.zeros((h, w, 4), np.float32)
+    mk = None if mask is None else _f32(mask)
+    lib().oracle_convert_to_srgb(_p(a), _p(mk), w, h, _arr(np.ravel(m), 9), ctypes.byref(rgb), _p(o8), _p(of))
+    return o8, of
+
+
+def bayer_to_rgba(scaled, bayer, prec=F32):
+    s = _f32(scaled)
+    h, w = s.shape
+    out = np.zeros((h // 2, w // 2, 4), np.float32)
+    lib().oracle_bayer_to_rgba(_p(s), w, h, bayer, prec, _p(out))
+    return out
+
+
+def rgba_to_bayer(rgba, bayer, prec=F32):
+    a = _f32(rgba)
+    qh, qw, _ = a.shape
+    out = np.zeros((2 * qh, 2 * qw), np.float32)
+    lib().oracle_rgba_to_bayer(_p(a), 2 * qw, 2 * qh, bayer, prec, _p(out))
+    return out
+
+
+def despeckle_rgba(img, prec=F32):
+    a = _f32(img)
+    h, w, _ = a.shape
+    out = np.zeros_like(a)
+    lib().oracle_despeckle_rgba(_p(a), w, h, prec, _p(out))
+    return out
+
+
+def denoise_rgba(img, raw_variance, prec=F32):
+    a = _f32(img)
+    h, w, _ = a.shape
+    out = np.zeros_like(a)
+    lib().oracle_denoise_rgba(_p(a), w, h, _arr(raw_variance, 4), prec, _p(out))
+    return out
+
+
+def fast_debayer(scaled, bayer, prec=F32):
+    s = _f32(scaled)
+    h, w = s.shape
+    out = np.zeros((h // 2, w // 2, 4), np.float32)
+    lib().oracle_fast_debayer(_p(s), w, h, bayer, prec, _p(out))
+    return out
+
+
+def regress(m, v):
+    m = _f32(m)
+    v = _f32(v)
+    n = v.shape[0]
+    mc = 1 if m.ndim == 1 else m.shape[1]
+    nc = v.shape[1]
+    out = np.zeros(2 * nc, np.float32)
+    lib().oracle_regress(_p(m), _p(v), n, mc, nc, _p(out))
+    return out
+
+
+def unpack_bits(packed, bits):
+    b = np.ascontiguousarray(np.frombuffer(bytes(packed), np.uint8))
+    n = (b.size * 8) // bits
+    out = np.zeros(n, np.uint16)
+    k = lib().oracle_unpack_bits(_p(b), b.size, bits, _p(out), n)
+    if k < 0:
+        raise ValueError("unsupported bit depth %d" % bits)
+    return out[:k]
+
+
+# ---- host colour math ----
+
+def _m9(fn, *mats):
+    args = [_arr(np.ravel(m), 9) for m in mats]
+    out = (ctypes.c_float * 9)()
+    fn(*args, out)
+    return np.array(out[:], np.float32).reshape(3, 3)
+
+
+def cam_xyz_coeff(cam_xyz):
+    pre = (ctypes.c_float * 3)()
+    out = (ctypes.c_float * 9)()
+    lib().oracle_cam_xyz_coeff(_arr(np.ravel(cam_xyz), 9), pre, out)
+    return np.array(pre[:], np.float32), np.array(out[:], np.float32).reshape(3, 3)
+
+
+def cam_ycbcr(rgb_cam):
+    return _m9(lib().oracle_cam_ycbcr, rgb_cam)
+
+
+def inverse3x3(m):
+    return _m9(lib().oracle_inverse3x3, m)
+
+
+def matmul3x3(a, b):
+    return _m9(lib().oracle_matmul3x3, a, b)
+
+
+def atan2pi(y, x):
+    return lib().oracle_atan2pi(y, x)

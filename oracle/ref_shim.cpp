@@ -1,0 +1,68 @@
+// ref_shim.cpp -- C entry points into the reference's own host code, compiled from the
+// reference sources where they lie (oracle/Makefile, target _ref).  Test infrastructure:
+// used only to pin the oracle's restatement of the host colour math and of the packed
+// raw unpack; never shipped, never built on a machine without the reference sources.
+#include <cstdint>
+#include <cstring>
+
+#include "demosaic.hpp"
+
+const char* BayerPatternName[4] = {"GRBG", "GBRG", "RGGB", "BGGR"};
+
+// The 12/14-bit unpack routines are file-local (static inline) in gls_image_tiff.cpp,
+// so that translation unit is included here; the libtiff entry points it references are
+// never called from this shim.
+#include "gls_image_tiff.cpp"
+
+extern "C" {
+
+void ref_cam_xyz_coeff(const float cam_xyz[9], float pre_mul[3], float rgb_cam[9]) {
+    gls::Matrix<3, 3> cx;
+    for (int i = 0; i < 9; i++) cx[i / 3][i % 3] = cam_xyz[i];
+    gls::Vector<3> pm;
+    const auto r = cam_xyz_coeff(&pm, cx);
+    for (int i = 0; i < 3; i++) pre_mul[i] = pm[i];
+    for (int i = 0; i < 9; i++) rgb_cam[i] = r[i / 3][i % 3];
+}
+
+void ref_cam_ycbcr(const float rgb_cam[9], float out[9]) {
+    gls::Matrix<3, 3> m;
+    for (int i = 0; i < 9; i++) m[i / 3][i % 3] = rgb_cam[i];
+    const auto r = cam_ycbcr(m);
+    for (int i = 0; i < 9; i++) out[i] = r[i / 3][i % 3];
+}
+
+void ref_inverse3x3(const float in[9], float out[9]) {
+    gls::Matrix<3, 3> m;
+    for (int i = 0; i < 9; i++) m[i / 3][i % 3] = in[i];
+    const auto r = gls::inverse(m);
+    for (int i = 0; i < 9; i++) out[i] = r[i / 3][i % 3];
+}
+
+void ref_matmul3x3(const float a[9], const float b[9], float out[9]) {
+    gls::Matrix<3, 3> x, y;
+    for (int i = 0; i < 9; i++) {
+        x[i / 3][i % 3] = a[i];
+        y[i / 3][i % 3] = b[i];
+    }
+    const auto r = x * y;
+    for (int i = 0; i < 9; i++) out[i] = r[i / 3][i % 3];
+}
+
+void ref_matscale3x3(const float a[9], float s, float out[9]) {
+    gls::Matrix<3, 3> x;
+    for (int i = 0; i < 9; i++) x[i / 3][i % 3] = a[i];
+    const auto r = x * s;
+    for (int i = 0; i < 9; i++) out[i] = r[i / 3][i % 3];
+}
+
+// in_words: big-endian 16-bit words as stored in the file (the routine swaps them)
+void ref_unpack12(const uint16_t* in_words, long n_words, uint16_t* out) {
+    gls::unpack12BitsInto16Bits(out, in_words, (size_t)n_words);
+}
+
+void ref_unpack14(const uint16_t* in_words, long n_words, uint16_t* out) {
+    gls::unpack14BitsInto16Bits(out, in_words, (size_t)n_words);
+}
+
+}  // extern "C"
