@@ -66,13 +66,22 @@ def algorithmic_bytes_per_px(S, O, L):
     return 8 + 5 * S + O + 7 * S * G
 
 
-# algorithmic bytes per pixel of each single-stage kernel (fp32 storage S=16 B RGBA, 4 B single)
+# Compulsory bytes per full-resolution pixel of each full-resolution kernel (what it must
+# read and write at least once; fp32 storage: s1 = 4 B single channel, s4 = 16 B RGBA).
+# Fused kernels: level 0 is stored in binary16 (8 B/px) because the despeckle that
+# produces it already rounds every value to binary16.
 def stage_bytes(name, s1, s4):
     table = {
+        # fused schedule
+        "rawNoiseStatistics+fit": 2,                      # uint16 raw in
+        "demosaic": 2 + 8,                                # raw in, level 0 out
+        "noiseStatistics+downsample L0": 8 + s4 / 4,      # level 0 in, level 1 out
+        "denoise L0+LTM+sRGB": 8 + 2 * s4 / 4 + s4 / 64 + 4,  # level 0, level 1 (both), level 3 guide, RGBA8 out
+        # single-stage schedule
         "scaleRawData": 2 + s1, "interpolateGreen": 2 * s1, "interpolateRedBlue": 2 * s1 + s4,
         "blendHighlights": 2 * s4, "transformImage": 2 * s4, "despeckleImage": 2 * s4,
         "denoise L0": 2 * s4, "reassemble L0": 2 * s4, "localToneMappingMask": s4 + s1,
-        "convertTosRGB": s4 + s1 + 4, "noiseStatistics+fit L0": s4, "rawNoiseStatistics+fit": s1,
+        "convertTosRGB": s4 + s1 + 4, "noiseStatistics+fit L0": s4,
     }
     return table.get(name)
 

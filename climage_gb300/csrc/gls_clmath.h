@@ -110,8 +110,12 @@ GLS_HD float clamp_(float x, float lo, float hi) { return fmin_(fmax_(x, lo), hi
 // OpenCL mix(x, y, a) == x + (y - x) * a
 GLS_HD float mix_(float x, float y, float a) { return x + (y - x) * a; }
 
-// OpenCL step(edge, x) == x < edge ? 0 : 1
-GLS_HD float step_(float edge, float x) { return x < edge ? 0.0f : 1.0f; }
+// OpenCL step(edge, x): 0 when x < edge, else 1 -- evaluated as x >= edge ? 1 : 0, which is
+// the same function for every non-NaN x.  The reference is compiled with
+// -cl-finite-math-only, so its result for a NaN x is undefined; this reading (NaN -> 0)
+// keeps the bilateral weights finite where the fitted noise model gives a negative
+// variance or a zero raw sample gives 0/0 (demosaic.cl:757, 940).
+GLS_HD float step_(float edge, float x) { return x >= edge ? 1.0f : 0.0f; }
 
 // OpenCL smoothstep(e0, e1, x): t = clamp((x - e0) / (e1 - e0), 0, 1); t * t * (3 - 2 * t)
 GLS_HD float smoothstep_(float e0, float e1, float x) {

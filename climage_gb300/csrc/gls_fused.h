@@ -1,0 +1,92 @@
+// gls_fused.h -- argument blocks and launchers of the fused pipeline kernels (k_fused.cu).
+#ifndef GLS_FUSED_H
+#define GLS_FUSED_H
+
+#include "gls_internal.h"
+#include "gls_pixel_ops.cuh"
+
+namespace gls {
+
+struct RawPass1Args {
+    const uint16_t* raw;
+    int w, h, pitch;
+    int bayer;
+    float sm[4];  // scale factor per (y & 1) * 2 + (x & 1)
+    float black;
+    NlfThresholds th;
+    double* part_d;
+    float* part_f;
+};
+
+struct DemosaicArgs {
+    const void* in;  // uint16 raw (scaled on the fly) or the scaled raw image
+    int w, h, in_pitch;
+    int bayer;
+    float sm[4];
+    float black;
+    const float* rawB_dev;  // fitted raw noise model B[0..3] (or null: lv_host / cv_host)
+    float lv_host, cv_host;
+    Mat3 cam_ycbcr;
+    float va0, vb0;  // luma despeckle noise model (pyramidNlf[0])
+    half4* level0;
+    int l0_pitch;
+    float* tap_scaled;
+    float* tap_green;
+    int tap_pitch;
+};
+
+struct LevelPass1Args {
+    const void* in;
+    int w, h, pitch;
+    void* out;  // downsampled level (null for the coarsest level)
+    int ow, oh, opitch;
+    NlfThresholds th;
+    double* part_d;
+    float* part_f;
+};
+
+struct DenoiseArgs {
+    const void* in;
+    int w, h, pitch;
+    void* out;
+    int opitch;
+    const void* coarse_img;
+    const void* coarse_den;
+    int cw, ch, cpitch;
+    const float* nlf_dev;
+    float mul[6];
+    float chroma_boost, gradient_boost, sharpening;
+};
+
+struct FinalArgs {
+    const half4* level0;
+    int w, h, l0_pitch;
+    const void* pyr0;
+    const void* den1;
+    int cw, ch, cpitch;
+    const void* guide;
+    int gw, gh, gpitch;
+    const float* nlf_dev;
+    float mul[6];
+    float chroma_boost, gradient_boost, sharpening;
+    LtmParams ltm;
+    Mat3 icy;
+    Mat3 rgb_cam;
+    RgbParams rgb;
+    void* out;
+    int opitch;
+    float* tap_den;
+    float* tap_mask;
+    int tap_pitch;
+};
+
+gls_status fused_raw_fit(gls_ctx* ctx, const RawPass1Args& a, bool half, NlfScratch s, float* out_dev);
+gls_status fused_demosaic(gls_ctx* ctx, const DemosaicArgs& a, bool raw_u16, bool half);
+gls_status fused_level_fit(gls_ctx* ctx, const LevelPass1Args& a, bool in_half, bool half, NlfScratch s,
+                           float* out_dev);
+gls_status fused_denoise(gls_ctx* ctx, const DenoiseArgs& a, bool in_half, bool half, int algo, bool reasm);
+gls_status fused_final(gls_ctx* ctx, const FinalArgs& a, bool half, int algo, bool ltm, bool out_f32);
+
+}  // namespace gls
+
+#endif  // GLS_FUSED_H

@@ -1,0 +1,552 @@
+// k_fused.cu -- the RAW pipeline as a handful of fused, shared-memory-tiled kernels.
+//
+// Each kernel reads its input tile (with the halo its stencils need) from HBM once,
+// runs several reference stages back to back out of shared memory, and writes only the
+// images that later passes need.  Every value that the reference stores in an
+// intermediate image is rounded to that image's storage precision at the same point,
+// and every image read outside the frame is clamped to the edge exactly as the
+// reference's sampler-less reads are, so the results equal the single-stage kernels
+// (k_stages.cu) and the CPU oracle bit for bit.
+//
+//   raw_pass1      scaleRawData on the fly + rawNoiseStatistics + pass-1 regression sums
+//   demosaic       scaleRawData + interpolateGreen (shared Sobel map) + interpolateRedBlue
+//                  + blendHighlights + transformImage(cam->YCbCr) + despeckleImage
+//                  -> level 0 of the pyramid (binary16: the despeckle already rounds
+//                  every value to binary16, so this storage is exact)
+//   level_pass1    noiseStatistics + pass-1 sums of level i, downsampleImage -> level i+1
+//   denoise_reasm  denoiseImage (+ reassembleImage) of levels >= 1
+//   final          denoiseImage + reassembleImage of level 0, localToneMappingMask,
+//                  transformImage(YCbCr->camera), convertTosRGB -> RGBA8 / RGBA fp32
+#include "gls_fused.h"
+#include "gls_nlf.cuh"
+
+namespace gls {
+namespace {
+
+constexpr int kT = 256;
+
+// ---- shared-memory accessors (coordinates in image space, origin at (x0, y0)) ----
+struct SAcc1 {
+    const float* s;
+    int x0, y0, ld;
+    GLS_DI float at(int x, int y) const { return s[(y - y0) * ld + (x - x0)]; }
+};
+
+struct SAcc4h {
+    const half4* s;
+    int x0, y0, ld;
+    GLS_DI float4 at(int x, int y) const { return Storage<__half>::cvt(s[(y - y0) * ld + (x - x0)]); }
+};
+
+struct SAcc4f {
+    const float4* s;
+    int x0, y0, ld;
+    GLS_DI float4 at(int x, int y) const { return s[(y - y0) * ld + (x - x0)]; }
+};
+
+struct SobelMap {
+    const float* base;
+    int plane;  // elements per plane (gx | gy | len)
+    int x0, y0, ld, x, y;
+    GLS_DI SobelVal operator()(int i, int j) const {
+        const int k = (y + j - y0) * ld + (x + i - x0);
+        SobelVal v;
+        v.gx = base[k];
+        v.gy = base[plane + k];
+        v.len = base[2 * plane + k];
+        return v;
+    }
+};
+
+GLS_DI half4 to_half4(float4 v) {
+    half4 h;
+    h.xy = __halves2half2(__float2half_rn(v.x), __float2half_rn(v.y));
+    h.zw = __halves2half2(__float2half_rn(v.z), __float2half_rn(v.w));
+    return h;
+}
+
+template <class S>
+GLS_DI float3 round3(float3 v) {
+    return make_float3(Storage<S>::round(v.x), Storage<S>::round(v.y), Storage<S>::round(v.z));
+}
+
+template <class S>
+GLS_DI float4 round4(float4 v) {
+    return make_float4(Storage<S>::round(v.x), Storage<S>::round(v.y), Storage<S>::round(v.z), Storage<S>::round(v.w));
+}
+
+// =========================================================================================
+// raw_pass1: per 2x2 quad, the 5x5-quad statistics of the scaled raw planes and the
+// pass-1 sums of computeRawNoiseStatistics.  Tiles of 32x32 quads, scaled values staged
+// in shared memory (one division per pixel instead of one per tap).
+// =========================================================================================
+constexpr int RQ = 32;               // quads per tile side
+constexpr int RP = 2 * RQ + 8;       // staged pixels per side (halo of 2 quads)
+
+template <class S>
+__global__ void __launch_bounds__(kT) raw_pass1_kernel(RawPass1Args a) {
+    __shared__ float s_raw[RP * RP];
+    Pass1Acc<4, 4> acc;
+    acc.init();
+    const int qw = a.w / 2, qh = a.h / 2;
+    const int tiles_x = (qw + RQ - 1) / RQ, tiles_y = (qh + RQ - 1) / RQ;
+    const int col = threadIdx.x & 31, row0 = (threadIdx.x >> 5) * 4;
+    for (int t = blockIdx.x; t < tiles_x * tiles_y; t += gridDim.x) {
+        const int qx0 = (t % tiles_x) * RQ, qy0 = (t / tiles_x) * RQ;
+        const int px0 = 2 * qx0 - 4, py0 = 2 * qy0 - 4;
+        for (int i = threadIdx.x; i < RP * RP; i += kT) {
+            const int r = i / RP, c = i - r * RP;
+            const int gx = clampi(px0 + c, 0, a.w - 1), gy = clampi(py0 + r, 0, a.h - 1);
+            const float v = scale_value(__ldg(a.raw + (size_t)gy * a.pitch + gx), a.sm[((gy & 1) << 1) | (gx & 1)],
+                                        a.black);
+            s_raw[i] = Storage<S>::round(v);
+        }
+        __syncthreads();
+        SAcc1 R{s_raw, px0, py0, RP};
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const int qx = qx0 + col, qy = qy0 + row0 + j;
+            if (qx < qw && qy < qh) {
+                float m[4], v[4];
+                raw_stats_quad(R, qx, qy, a.bayer, m, v);
+                acc.add(m, v, a.th);
+            }
+        }
+        __syncthreads();
+    }
+    acc.write(a.part_d, a.part_f);
+}
+
+// =========================================================================================
+// demosaic: TW x TH output tile, 256 threads.
+// =========================================================================================
+template <int TW, int TH, bool RAW_U16, class S>
+__global__ void __launch_bounds__(kT) demosaic_kernel(DemosaicArgs a) {
+    constexpr int RW = TW + 10, RH = TH + 10;  // scaled raw, origin (x0 - 5, y0 - 5)
+    constexpr int SW = TW + 8, SH = TH + 8;    // Sobel map, origin (x0 - 4, y0 - 4)
+    constexpr int GW = TW + 4, GH = TH + 4;    // green, origin (x0 - 2, y0 - 2)
+    constexpr int CW = TW + 2, CH = TH + 2;    // YCbCr (binary16), origin (x0 - 1, y0 - 1)
+    static_assert(CW * CH * 8 <= 3 * SW * SH * 4, "YCbCr tile must fit in the Sobel map space");
+    static_assert(GW % 2 == 0, "green region pairs");
+    __shared__ float s_raw[RH * RW];
+    __shared__ float s_green[GH * GW];
+    __shared__ __align__(16) float s_u[3 * SH * SW];
+    half4* s_ycc = reinterpret_cast<half4*>(s_u);
+
+    const int x0 = blockIdx.x * TW, y0 = blockIdx.y * TH;
+    const int w = a.w, h = a.h, bayer = a.bayer;
+    const int tid = threadIdx.x;
+    const bool border = x0 - 5 < 0 || y0 - 5 < 0 || x0 + TW + 5 > w || y0 + TH + 5 > h;
+
+    // 1. scaled raw tile (clamped reads)
+    for (int i = tid; i < RH * RW; i += kT) {
+        const int r = i / RW, c = i - r * RW;
+        const int gx = clampi(x0 - 5 + c, 0, w - 1), gy = clampi(y0 - 5 + r, 0, h - 1);
+        float v;
+        if (RAW_U16) {
+            v = Storage<S>::round(scale_value(__ldg((const uint16_t*)a.in + (size_t)gy * a.in_pitch + gx),
+                                              a.sm[((gy & 1) << 1) | (gx & 1)], a.black));
+        } else {
+            v = Storage<S>::ldg((const S*)a.in + (size_t)gy * a.in_pitch + gx);
+        }
+        s_raw[i] = v;
+    }
+    __syncthreads();
+    const SAcc1 R{s_raw, x0 - 5, y0 - 5, RW};
+
+    // 2. Sobel map (|gx|, |gy|, length) at every position a bilateralSobel may visit
+    for (int i = tid; i < SH * SW; i += kT) {
+        const int r = i / SW, c = i - r * SW;
+        const SobelVal sv = sobel_abs(R, x0 - 4 + c, y0 - 4 + r);
+        s_u[i] = sv.gx;
+        s_u[SH * SW + i] = sv.gy;
+        s_u[2 * SH * SW + i] = sv.len;
+    }
+    if (a.tap_scaled) {
+        for (int i = tid; i < TW * TH; i += kT) {
+            const int r = i / TW, c = i - r * TW, x = x0 + c, y = y0 + r;
+            if (x < w && y < h) a.tap_scaled[(size_t)y * a.tap_pitch + x] = R.at(x, y);
+        }
+    }
+    __syncthreads();
+
+    // 3. green at every in-frame position of the green region; pairs of pixels hold one
+    //    red/blue site and one green site, so the work is even across threads
+    {
+        const float lv = mmax(a.rawB_dev ? a.rawB_dev[1] : a.lv_host, 1e-4f);
+        for (int p = tid; p < GH * GW / 2; p += kT) {
+            const int r = p / (GW / 2), k = p - r * (GW / 2);
+            const int y = y0 - 2 + r;
+#pragma unroll
+            for (int e = 0; e < 2; e++) {
+                const int x = x0 - 2 + 2 * k + e;
+                if (x < 0 || x >= w || y < 0 || y >= h) continue;
+                float g;
+                if (green_needs_interp(x, y, bayer)) {
+                    const SobelMap sob{s_u, SH * SW, x0 - 4, y0 - 4, SW, x, y};
+                    g = green_at(R, x, y, lv, sob);
+                } else {
+                    g = R.at(x, y);
+                }
+                s_green[r * GW + 2 * k + e] = Storage<S>::round(g);
+            }
+        }
+    }
+    __syncthreads();
+    if (border) {  // out-of-frame green reads clamp to the frame
+        for (int i = tid; i < GH * GW; i += kT) {
+            const int r = i / GW, c = i - r * GW, x = x0 - 2 + c, y = y0 - 2 + r;
+            if (x >= 0 && x < w && y >= 0 && y < h) continue;
+            const int cx = clampi(x, 0, w - 1) - (x0 - 2), cy = clampi(y, 0, h - 1) - (y0 - 2);
+            s_green[i] = s_green[cy * GW + cx];
+        }
+        __syncthreads();
+    }
+    const SAcc1 G{s_green, x0 - 2, y0 - 2, GW};
+
+    // 4. red/blue, highlight recovery, camera -> YCbCr (the Sobel map is dead: reuse it)
+    {
+        const float cv = mmax(a.rawB_dev ? div_(a.rawB_dev[0] + a.rawB_dev[2], 2.0f) : a.cv_host, 1e-6f);
+        for (int i = tid; i < CH * CW; i += kT) {
+            const int r = i / CW, c = i - r * CW, x = x0 - 1 + c, y = y0 - 1 + r;
+            if (x < 0 || x >= w || y < 0 || y >= h) continue;
+            float3 p = round3<S>(red_blue_at(R, G, x, y, bayer, cv));
+            p = round3<S>(blend_highlights_px(p, 1.0f));
+            p = round3<S>(transform_px(a.cam_ycbcr, p));
+            s_ycc[i] = to_half4(make_float4(p.x, p.y, p.z, 0.0f));
+        }
+    }
+    if (a.tap_green) {
+        for (int i = tid; i < TW * TH; i += kT) {
+            const int r = i / TW, c = i - r * TW, x = x0 + c, y = y0 + r;
+            if (x < w && y < h) a.tap_green[(size_t)y * a.tap_pitch + x] = G.at(x, y);
+        }
+    }
+    __syncthreads();
+    if (border) {
+        for (int i = tid; i < CH * CW; i += kT) {
+            const int r = i / CW, c = i - r * CW, x = x0 - 1 + c, y = y0 - 1 + r;
+            if (x >= 0 && x < w && y >= 0 && y < h) continue;
+            const int cx = clampi(x, 0, w - 1) - (x0 - 1), cy = clampi(y, 0, h - 1) - (y0 - 1);
+            s_ycc[i] = s_ycc[cy * CW + cx];
+        }
+        __syncthreads();
+    }
+
+    // 5. luma despeckle / chroma median -> level 0
+    const SAcc4h Y{s_ycc, x0 - 1, y0 - 1, CW};
+    for (int i = tid; i < TW * TH; i += kT) {
+        const int r = i / TW, c = i - r * TW, x = x0 + c, y = y0 + r;
+        if (x >= w || y >= h) continue;
+        a.level0[(size_t)y * a.l0_pitch + x] = to_half4(despeckle_px(Y, x, y, a.va0, a.vb0));
+    }
+}
+
+// =========================================================================================
+// level_pass1: noiseStatistics + pass-1 sums of level i, and downsampleImage to level i+1.
+// Persistent blocks walk 32x32 tiles; each thread owns a column of 4 pixels and reuses
+// the loaded rows across them (each output still sums its 5x5 window in the reference's
+// row-major order).
+// =========================================================================================
+constexpr int LT = 32;
+constexpr int LP = LT + 4;
+
+template <class SIn, class SOut>
+__global__ void __launch_bounds__(kT) level_pass1_kernel(LevelPass1Args a) {
+    __shared__ float4 s_in[LP * LP];
+    Pass1Acc<1, 3> acc;
+    acc.init();
+    typedef typename Storage<SIn>::T4 TIn;
+    const TIn* in = (const TIn*)a.in;
+    const GImg4<SIn> gin{in, a.w, a.h, a.pitch};
+    const int tiles_x = (a.w + LT - 1) / LT, tiles_y = (a.h + LT - 1) / LT;
+    const int col = threadIdx.x & 31, row0 = (threadIdx.x >> 5) * 4;
+    for (int t = blockIdx.x; t < tiles_x * tiles_y; t += gridDim.x) {
+        const int x0 = (t % tiles_x) * LT, y0 = (t / tiles_x) * LT;
+        for (int i = threadIdx.x; i < LP * LP; i += kT) {
+            const int r = i / LP, c = i - r * LP;
+            s_in[i] = gin.at(x0 - 2 + c, y0 - 2 + r);
+        }
+        __syncthreads();
+        // statistics for pixels (x0 + col, y0 + row0 + j), j = 0..3
+        float s0[4], s1[4], s2[4], q0[4], q1[4], q2[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) s0[j] = s1[j] = s2[j] = q0[j] = q1[j] = q2[j] = 0.0f;
+#pragma unroll
+        for (int rr = 0; rr < 8; rr++) {
+#pragma unroll
+            for (int dx = 0; dx < 5; dx++) {
+                const float4 v = s_in[(row0 + rr) * LP + col + dx];
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    if (rr - j >= 0 && rr - j <= 4) {
+                        s0[j] = s0[j] + v.x;
+                        q0[j] = q0[j] + v.x * v.x;
+                        s1[j] = s1[j] + v.y;
+                        q1[j] = q1[j] + v.y * v.y;
+                        s2[j] = s2[j] + v.z;
+                        q2[j] = q2[j] + v.z * v.z;
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const int x = x0 + col, y = y0 + row0 + j;
+            if (x < a.w && y < a.h) {
+                float m[1], v[3];
+                m[0] = div_(s0[j], 25.0f);
+                v[0] = div_(q0[j] - div_(s0[j] * s0[j], 25.0f), 25.0f);
+                v[1] = div_(q1[j] - div_(s1[j] * s1[j], 25.0f), 25.0f);
+                v[2] = div_(q2[j] - div_(s2[j] * s2[j], 25.0f), 25.0f);
+                acc.add(m, v, a.th);
+            }
+        }
+        // downsample: the coarse 16x16 tile under this fine tile
+        if (a.out) {
+            const int ox = x0 / 2 + (threadIdx.x & 15), oy = y0 / 2 + (threadIdx.x >> 4);
+            if (ox < a.ow && oy < a.oh) {
+                typedef typename Storage<SOut>::T4 TOut;
+                Storage<SOut>::st4((TOut*)a.out + (size_t)oy * a.opitch + ox,
+                                   downsample_px(gin, ox, oy, a.ow, a.oh, a.w, a.h));
+            }
+        }
+        __syncthreads();
+    }
+    acc.write(a.part_d, a.part_f);
+}
+
+// =========================================================================================
+// denoise_reasm: denoiseImage (bilateral / guided fast) of a pyramid level and, below the
+// coarsest level, reassembleImage with the next coarser level.  32x16 output tiles.
+// =========================================================================================
+constexpr int DW = 32, DH = 16;
+
+template <class SIn, class S, int ALGO, bool REASM>
+__global__ void __launch_bounds__(kT) denoise_reasm_kernel(DenoiseArgs a) {
+    constexpr int PW = DW + 4, PH = DH + 4;
+    __shared__ float4 s_in[PW * PH];
+    const int x0 = blockIdx.x * DW, y0 = blockIdx.y * DH;
+    const GImg4<SIn> gin{(const typename Storage<SIn>::T4*)a.in, a.w, a.h, a.pitch};
+    for (int i = threadIdx.x; i < PW * PH; i += kT) {
+        const int r = i / PW, c = i - r * PW;
+        s_in[i] = gin.at(x0 - 2 + c, y0 - 2 + r);
+    }
+    __syncthreads();
+    const SAcc4f I{s_in, x0 - 2, y0 - 2, PW};
+    Nlf6 n;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        n.a[k] = a.nlf_dev[k] * a.mul[k];
+        n.b[k] = a.nlf_dev[3 + k] * a.mul[3 + k];
+    }
+    typedef typename Storage<S>::T4 T4;
+    const GImg4<S> i1{(const T4*)a.coarse_img, a.cw, a.ch, a.cpitch};
+    const GImg4<S> d1{(const T4*)a.coarse_den, a.cw, a.ch, a.cpitch};
+    for (int i = threadIdx.x; i < DW * DH; i += kT) {
+        const int r = i / DW, c = i - r * DW, x = x0 + c, y = y0 + r;
+        if (x >= a.w || y >= a.h) continue;
+        float4 d = ALGO == 0 ? bilateral_px(I, x, y, n, a.chroma_boost, a.gradient_boost) : guided_fast_px(I, x, y, n);
+        d = round4<S>(d);
+        if (REASM) d = round4<S>(reassemble_px(d, i1, d1, x, y, a.w, a.h, a.cw, a.ch, a.sharpening, n.a[0], n.b[0]));
+        Storage<S>::st4((T4*)a.out + (size_t)y * a.opitch + x, d);
+    }
+}
+
+// =========================================================================================
+// final: level-0 denoise + reassemble over the tile and a one-pixel ring (the local tone
+// mapping samples its input bilinearly), then the LTM mask, YCbCr -> camera and
+// convertTosRGB.  32x16 output tiles.
+// =========================================================================================
+constexpr int FW = 32, FH = 16;
+
+template <class S, int ALGO, bool LTM, bool OUT_F32>
+__global__ void __launch_bounds__(kT) final_kernel(FinalArgs a) {
+    constexpr int PW = FW + 6, PH = FH + 6;  // level 0 (binary16), origin (x0 - 3, y0 - 3)
+    constexpr int EW = FW + 2, EH = FH + 2;  // denoised level 0, origin (x0 - 1, y0 - 1)
+    __shared__ half4 s_l0[PW * PH];
+    __shared__ float4 s_den[EW * EH];
+    const int x0 = blockIdx.x * FW, y0 = blockIdx.y * FH;
+    const int w = a.w, h = a.h;
+    const GImg4<__half> gl0{a.level0, w, h, a.l0_pitch};
+    for (int i = threadIdx.x; i < PW * PH; i += kT) {
+        const int r = i / PW, c = i - r * PW;
+        const int gx = clampi(x0 - 3 + c, 0, w - 1), gy = clampi(y0 - 3 + r, 0, h - 1);
+        const uint2 u = __ldg(reinterpret_cast<const uint2*>(a.level0 + (size_t)gy * a.l0_pitch + gx));
+        *reinterpret_cast<uint2*>(&s_l0[i]) = u;
+    }
+    __syncthreads();
+    const SAcc4h L0{s_l0, x0 - 3, y0 - 3, PW};
+    Nlf6 n;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        n.a[k] = a.nlf_dev[k] * a.mul[k];
+        n.b[k] = a.nlf_dev[3 + k] * a.mul[3 + k];
+    }
+    typedef typename Storage<S>::T4 T4;
+    const GImg4<S> i1{(const T4*)a.pyr0, a.cw, a.ch, a.cpitch};
+    const GImg4<S> d1{(const T4*)a.den1, a.cw, a.ch, a.cpitch};
+    for (int i = threadIdx.x; i < EW * EH; i += kT) {
+        const int r = i / EW, c = i - r * EW, x = x0 - 1 + c, y = y0 - 1 + r;
+        if (x < 0 || x >= w || y < 0 || y >= h) continue;
+        float4 d = ALGO == 0 ? bilateral_px(L0, x, y, n, a.chroma_boost, a.gradient_boost) : guided_fast_px(L0, x, y, n);
+        d = round4<S>(d);
+        d = round4<S>(reassemble_px(d, i1, d1, x, y, w, h, a.cw, a.ch, a.sharpening, n.a[0], n.b[0]));
+        s_den[i] = d;
+    }
+    __syncthreads();
+    if (x0 - 1 < 0 || y0 - 1 < 0 || x0 + FW + 1 > w || y0 + FH + 1 > h) {
+        for (int i = threadIdx.x; i < EW * EH; i += kT) {
+            const int r = i / EW, c = i - r * EW, x = x0 - 1 + c, y = y0 - 1 + r;
+            if (x >= 0 && x < w && y >= 0 && y < h) continue;
+            const int cx = clampi(x, 0, w - 1) - (x0 - 1), cy = clampi(y, 0, h - 1) - (y0 - 1);
+            s_den[i] = s_den[cy * EW + cx];
+        }
+        __syncthreads();
+    }
+    const SAcc4f D{s_den, x0 - 1, y0 - 1, EW};
+    const GImg4<S> guide{(const T4*)a.guide, a.gw, a.gh, a.gpitch};
+    for (int i = threadIdx.x; i < FW * FH; i += kT) {
+        const int r = i / FW, c = i - r * FW, x = x0 + c, y = y0 + r;
+        if (x >= w || y >= h) continue;
+        const float4 den = D.at(x, y);
+        if (a.tap_den) reinterpret_cast<float4*>(a.tap_den)[(size_t)y * a.tap_pitch + x] = den;
+        float mask = 0.0f;
+        if (LTM) {
+            mask = Storage<S>::round(ltm_mask_px(D, guide, x, y, w, h, a.gw, a.gh, a.ltm, a.icy));
+            if (a.tap_mask) a.tap_mask[(size_t)y * a.tap_pitch + x] = mask;
+        }
+        const float3 cam = round3<S>(transform_px(a.icy, make_float3(den.x, den.y, den.z)));
+        const float3 o = srgb_px(cam, mask, a.rgb_cam, a.rgb);
+        if (OUT_F32) {
+            reinterpret_cast<float4*>(a.out)[(size_t)y * a.opitch + x] = make_float4(o.x, o.y, o.z, 0.0f);
+        } else {
+            reinterpret_cast<uchar4*>(a.out)[(size_t)y * a.opitch + x] =
+                make_uchar4(glsm::to_unorm8(o.x), glsm::to_unorm8(o.y), glsm::to_unorm8(o.z), 0);
+        }
+    }
+}
+
+int persistent_grid(gls_ctx* ctx, long tiles, int per_sm) {
+    long g = (long)(ctx->num_sms > 0 ? ctx->num_sms : 148) * per_sm;
+    if (g > kNlfMaxBlocks) g = kNlfMaxBlocks;
+    if (g > tiles) g = tiles;
+    return (int)(g < 1 ? 1 : g);
+}
+
+// Raw quads scaled on the fly, for the (rare) explicit regression passes.
+template <class S>
+struct RawU16SrcS {
+    GRaw16 raw;
+    float sm[4];
+    float black;
+    int bayer;
+    GLS_DI float at(int x, int y) const {
+        x = clampi(x, 0, raw.w - 1);
+        y = clampi(y, 0, raw.h - 1);
+        return Storage<S>::round(scale_value(__ldg(raw.p + (size_t)y * raw.pitch + x), sm[((y & 1) << 1) | (x & 1)], black));
+    }
+    GLS_DI void stats(int qx, int qy, float* m, float* v) const { raw_stats_quad(*this, qx, qy, bayer, m, v); }
+};
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------------
+// launchers
+// ------------------------------------------------------------------------------------------
+
+gls_status fused_raw_fit(gls_ctx* ctx, const RawPass1Args& args, bool half, NlfScratch s, float* out_dev) {
+    RawPass1Args a = args;
+    a.th = nlf_thresholds();
+    a.part_d = s.part_d;
+    a.part_f = s.part_f;
+    const int qw = a.w / 2, qh = a.h / 2;
+    const long tiles = (long)((qw + RQ - 1) / RQ) * ((qh + RQ - 1) / RQ);
+    const int grid = persistent_grid(ctx, tiles, 4);
+    if (half) {
+        raw_pass1_kernel<__half><<<grid, kT, 0, ctx->stream>>>(a);
+        RawU16SrcS<__half> src{{a.raw, a.w, a.h, a.pitch}, {a.sm[0], a.sm[1], a.sm[2], a.sm[3]}, a.black, a.bayer};
+        ctx->launches++;
+        nlf_finish<4, 4>(ctx, src, qw, qh, grid, s, out_dev);
+    } else {
+        raw_pass1_kernel<float><<<grid, kT, 0, ctx->stream>>>(a);
+        RawU16SrcS<float> src{{a.raw, a.w, a.h, a.pitch}, {a.sm[0], a.sm[1], a.sm[2], a.sm[3]}, a.black, a.bayer};
+        ctx->launches++;
+        nlf_finish<4, 4>(ctx, src, qw, qh, grid, s, out_dev);
+    }
+    return check_launch(ctx, "raw noise statistics (fused)");
+}
+
+gls_status fused_demosaic(gls_ctx* ctx, const DemosaicArgs& a, bool raw_u16, bool half) {
+    constexpr int TW = 28, TH = 28;
+    const dim3 grid((a.w + TW - 1) / TW, (a.h + TH - 1) / TH);
+    if (raw_u16) {
+        if (half) demosaic_kernel<TW, TH, true, __half><<<grid, kT, 0, ctx->stream>>>(a);
+        else demosaic_kernel<TW, TH, true, float><<<grid, kT, 0, ctx->stream>>>(a);
+    } else {
+        if (half) demosaic_kernel<TW, TH, false, __half><<<grid, kT, 0, ctx->stream>>>(a);
+        else demosaic_kernel<TW, TH, false, float><<<grid, kT, 0, ctx->stream>>>(a);
+    }
+    ctx->launches++;
+    return check_launch(ctx, "demosaic (fused)");
+}
+
+gls_status fused_level_fit(gls_ctx* ctx, const LevelPass1Args& args, bool in_half, bool half, NlfScratch s,
+                           float* out_dev) {
+    LevelPass1Args a = args;
+    a.th = nlf_thresholds();
+    a.part_d = s.part_d;
+    a.part_f = s.part_f;
+    const long tiles = (long)((a.w + LT - 1) / LT) * ((a.h + LT - 1) / LT);
+    const int grid = persistent_grid(ctx, tiles, 4);
+    if (in_half) {
+        if (half) level_pass1_kernel<__half, __half><<<grid, kT, 0, ctx->stream>>>(a);
+        else level_pass1_kernel<__half, float><<<grid, kT, 0, ctx->stream>>>(a);
+        LevelSrc<__half> src{{(const half4*)a.in, a.w, a.h, a.pitch}};
+        ctx->launches++;
+        nlf_finish<1, 3>(ctx, src, a.w, a.h, grid, s, out_dev);
+    } else {
+        level_pass1_kernel<float, float><<<grid, kT, 0, ctx->stream>>>(a);
+        LevelSrc<float> src{{(const float4*)a.in, a.w, a.h, a.pitch}};
+        ctx->launches++;
+        nlf_finish<1, 3>(ctx, src, a.w, a.h, grid, s, out_dev);
+    }
+    return check_launch(ctx, "level statistics (fused)");
+}
+
+gls_status fused_denoise(gls_ctx* ctx, const DenoiseArgs& a, bool in_half, bool half, int algo, bool reasm) {
+    const dim3 grid((a.w + DW - 1) / DW, (a.h + DH - 1) / DH);
+    cudaStream_t st = ctx->stream;
+#define GLS_DEN(SIN, SS, AL, RE) denoise_reasm_kernel<SIN, SS, AL, RE><<<grid, kT, 0, st>>>(a)
+    if (in_half && half) {
+        if (algo == 0) { if (reasm) GLS_DEN(__half, __half, 0, true); else GLS_DEN(__half, __half, 0, false); }
+        else { if (reasm) GLS_DEN(__half, __half, 1, true); else GLS_DEN(__half, __half, 1, false); }
+    } else if (in_half) {
+        if (algo == 0) { if (reasm) GLS_DEN(__half, float, 0, true); else GLS_DEN(__half, float, 0, false); }
+        else { if (reasm) GLS_DEN(__half, float, 1, true); else GLS_DEN(__half, float, 1, false); }
+    } else {
+        if (algo == 0) { if (reasm) GLS_DEN(float, float, 0, true); else GLS_DEN(float, float, 0, false); }
+        else { if (reasm) GLS_DEN(float, float, 1, true); else GLS_DEN(float, float, 1, false); }
+    }
+#undef GLS_DEN
+    ctx->launches++;
+    return check_launch(ctx, "denoise/reassemble (fused)");
+}
+
+gls_status fused_final(gls_ctx* ctx, const FinalArgs& a, bool half, int algo, bool ltm, bool out_f32) {
+    const dim3 grid((a.w + FW - 1) / FW, (a.h + FH - 1) / FH);
+    cudaStream_t st = ctx->stream;
+#define GLS_FIN(SS, AL) \
+    if (ltm) { if (out_f32) final_kernel<SS, AL, true, true><<<grid, kT, 0, st>>>(a); else final_kernel<SS, AL, true, false><<<grid, kT, 0, st>>>(a); } \
+    else { if (out_f32) final_kernel<SS, AL, false, true><<<grid, kT, 0, st>>>(a); else final_kernel<SS, AL, false, false><<<grid, kT, 0, st>>>(a); }
+    if (half) {
+        if (algo == 0) { GLS_FIN(__half, 0) } else { GLS_FIN(__half, 1) }
+    } else {
+        if (algo == 0) { GLS_FIN(float, 0) } else { GLS_FIN(float, 1) }
+    }
+#undef GLS_FIN
+    ctx->launches++;
+    return check_launch(ctx, "final (fused)");
+}
+
+}  // namespace gls

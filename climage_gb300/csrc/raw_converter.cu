@@ -16,6 +16,7 @@
 #include "gls_internal.h"
 #include "gls_pipeline.h"
 #include "gls_pixel_ops.cuh"
+#include "gls_fused.h"
 #include "gls_stages.h"
 
 using namespace gls;
@@ -95,20 +96,23 @@ struct gls_raw_converter {
         return GLS_OK;
     }
 
+    // level 0 of the pyramid in binary16 (the fused path: the despeckle output is binary16)
+    ImgRef level0{};
+    bool staged_alloc = false, high_noise_alloc = false;
+
     gls_status ensure(int width, int height, int levels, bool half_storage) {
         if (width == w && height == h && levels == L && half_storage == half) return GLS_OK;
         cudaStreamSynchronize(ctx->stream);
         release();
+        staged_alloc = high_noise_alloc = false;
         half = half_storage;
-        GLS_CHECK(img(scaled, width, height, 1));
-        GLS_CHECK(img(green, width, height, 1));
-        GLS_CHECK(img(linA, width, height, 4));
-        GLS_CHECK(img(linB, width, height, 4));
-        GLS_CHECK(img(mask, width, height, 1));
-        GLS_CHECK(img(hnA, width / 2, height / 2, 4));
-        GLS_CHECK(img(hnB, width / 2, height / 2, 4));
+        {
+            void* p = nullptr;
+            GLS_CHECK(alloc(&p, (size_t)width * height * 8));
+            level0 = ImgRef{p, width, height, width, true};
+        }
         for (int i = 0; i < levels - 1; i++) GLS_CHECK(img(pyr[i], width >> (i + 1), height >> (i + 1), 4));
-        for (int i = 0; i < levels; i++) GLS_CHECK(img(den[i], width >> i, height >> i, 4));
+        for (int i = 1; i < levels; i++) GLS_CHECK(img(den[i], width >> i, height >> i, 4));
         void* p = nullptr;
         GLS_CHECK(alloc(&p, (1 + GLS_MAX_LEVELS) * 8 * sizeof(float)));
         nlf_dev = (float*)p;
@@ -118,6 +122,27 @@ struct gls_raw_converter {
         w = width;
         h = height;
         L = levels;
+        return GLS_OK;
+    }
+
+    // working images of the single-stage pipeline, allocated on first use
+    gls_status ensure_staged() {
+        if (staged_alloc) return GLS_OK;
+        GLS_CHECK(img(green, w, h, 1));
+        GLS_CHECK(img(linA, w, h, 4));
+        GLS_CHECK(img(linB, w, h, 4));
+        GLS_CHECK(img(mask, w, h, 1));
+        GLS_CHECK(img(den[0], w, h, 4));
+        staged_alloc = true;
+        return ensure_high_noise();
+    }
+
+    gls_status ensure_high_noise() {
+        if (high_noise_alloc) return GLS_OK;
+        GLS_CHECK(img(scaled, w, h, 1));
+        GLS_CHECK(img(hnA, w / 2, h / 2, 4));
+        GLS_CHECK(img(hnB, w / 2, h / 2, 4));
+        high_noise_alloc = true;
         return GLS_OK;
     }
 
@@ -189,7 +214,174 @@ struct gls_raw_converter {
         ev_used = 0;
     }
 
+    int mode = 0;  // 0 fused kernels, 1 one kernel per reference stage
+
     gls_status run(const uint16_t* raw, int rpitch, gls_demosaic_params* p, void* out, bool out_float, int opitch) {
+        if (mode == 0 && p->denoise_algorithm != GLS_DENOISE_GUIDED_PRECISE)
+            return run_fused(raw, rpitch, p, out, out_float, opitch);
+        return run_staged(raw, rpitch, p, out, out_float, opitch);
+    }
+
+    float* tap_ptr(int stage) { return tap_set[stage] ? (float*)taps[stage].ptr : nullptr; }
+
+    gls_status run_fused(const uint16_t* raw, int rpitch, gls_demosaic_params* p, void* out, bool out_float,
+                         int opitch) {
+        const int Lv = L;
+        const int bayer = p->bayer_pattern;
+        const bool high_noise = p->noise_level > 0.6f;
+        ev_used = 0;
+        mark("start");
+        float sm[4];
+        for (int c = 0; c < 4; c++) sm[bayer_dy(bayer, c) * 2 + bayer_dx(bayer, c)] = p->scale_mul[c];
+        const float black = p->black_level / 0xffff;
+
+        // raw noise model, fitted on the fly from the uint16 frame
+        RawPass1Args ra{};
+        ra.raw = raw;
+        ra.w = w;
+        ra.h = h;
+        ra.pitch = rpitch;
+        ra.bayer = bayer;
+        memcpy(ra.sm, sm, sizeof(sm));
+        ra.black = black;
+        GLS_CHECK(fused_raw_fit(ctx, ra, half, nlf_scratch_at(nlf_scratch), nlf_dev));
+        mark("rawNoiseStatistics+fit");
+        const float* rawB = nlf_dev + 4;
+
+        DemosaicArgs da{};
+        da.w = w;
+        da.h = h;
+        da.bayer = bayer;
+        memcpy(da.sm, sm, sizeof(sm));
+        da.black = black;
+        da.rawB_dev = rawB;
+        float cam_to_ycbcr[9];
+        host_cam_ycbcr(p->rgb_cam, cam_to_ycbcr);
+        memcpy(da.cam_ycbcr.m, cam_to_ycbcr, sizeof(cam_to_ycbcr));
+        da.va0 = p->pyramid_nlf[0][0];
+        da.vb0 = p->pyramid_nlf[0][3];
+        da.level0 = (half4*)level0.ptr;
+        da.l0_pitch = level0.pitch;
+        da.tap_scaled = tap_ptr(0);
+        da.tap_green = tap_ptr(1);
+        da.tap_pitch = w;
+        if (high_noise) {
+            // raw-domain despeckle and bilateral on the quarter-resolution CFA planes
+            GLS_CHECK(ensure_high_noise());
+            launch_scale_raw(ctx, raw, w, h, rpitch, scaled, bayer, p->scale_mul, black);
+            launch_bayer_to_rgba(ctx, scaled, hnA, bayer);
+            launch_despeckle_rgba(ctx, hnA, hnB);
+            launch_denoise_rgba(ctx, hnB, hnA, p->raw_nlf, rawB);
+            launch_rgba_to_bayer(ctx, hnA, scaled, bayer);
+            mark("rawDenoise");
+            da.in = scaled.ptr;
+            da.in_pitch = scaled.pitch;
+            GLS_CHECK(fused_demosaic(ctx, da, false, half));
+        } else {
+            da.in = raw;
+            da.in_pitch = rpitch;
+            GLS_CHECK(fused_demosaic(ctx, da, true, half));
+        }
+        mark("demosaic");
+        tap(2, level0, 4);
+
+        // pyramid: noise model of every level, downsampled levels
+        for (int i = 0; i < Lv; i++) {
+            const ImgRef& src = i == 0 ? level0 : pyr[i - 1];
+            LevelPass1Args la{};
+            la.in = src.ptr;
+            la.w = src.w;
+            la.h = src.h;
+            la.pitch = src.pitch;
+            if (i < Lv - 1) {
+                la.out = pyr[i].ptr;
+                la.ow = pyr[i].w;
+                la.oh = pyr[i].h;
+                la.opitch = pyr[i].pitch;
+            }
+            GLS_CHECK(fused_level_fit(ctx, la, src.half, half, nlf_scratch_at(nlf_scratch), nlf_dev + 8 * (1 + i)));
+            mark(i == 0 ? "noiseStatistics+downsample L0" : "noiseStatistics+downsample L1+");
+        }
+
+        // denoise coarse to fine
+        const int algo = p->denoise_algorithm;
+        for (int i = Lv - 1; i >= 1; i--) {
+            const gls_denoise_params& dp = p->denoise[i];
+            DenoiseArgs a{};
+            const ImgRef& in = pyr[i - 1];
+            a.in = in.ptr;
+            a.w = in.w;
+            a.h = in.h;
+            a.pitch = in.pitch;
+            a.out = den[i].ptr;
+            a.opitch = den[i].pitch;
+            const bool reasm = i < Lv - 1;
+            if (reasm) {
+                a.coarse_img = pyr[i].ptr;
+                a.coarse_den = den[i + 1].ptr;
+                a.cw = pyr[i].w;
+                a.ch = pyr[i].h;
+                a.cpitch = pyr[i].pitch;
+            }
+            a.nlf_dev = nlf_dev + 8 * (1 + i);
+            const float lm = dp.luma * dp.luma, cm = dp.chroma * dp.chroma;
+            const float mul[6] = {lm, cm, cm, lm, cm, cm};
+            memcpy(a.mul, mul, sizeof(mul));
+            a.chroma_boost = dp.chromaBoost;
+            a.gradient_boost = dp.gradientBoost;
+            a.sharpening = dp.sharpening;
+            const int level_algo = (algo == GLS_DENOISE_GUIDED_FAST && i < Lv - 1) ? 1 : 0;
+            GLS_CHECK(fused_denoise(ctx, a, in.half, half, level_algo, reasm));
+            mark("denoise+reassemble L1+");
+        }
+
+        // level 0 + local tone mapping + output
+        FinalArgs f{};
+        f.level0 = (const half4*)level0.ptr;
+        f.w = w;
+        f.h = h;
+        f.l0_pitch = level0.pitch;
+        f.pyr0 = pyr[0].ptr;
+        f.den1 = den[1].ptr;
+        f.cw = pyr[0].w;
+        f.ch = pyr[0].h;
+        f.cpitch = pyr[0].pitch;
+        f.guide = den[3].ptr;
+        f.gw = den[3].w;
+        f.gh = den[3].h;
+        f.gpitch = den[3].pitch;
+        f.nlf_dev = nlf_dev + 8;
+        {
+            const gls_denoise_params& dp = p->denoise[0];
+            const float lm = dp.luma * dp.luma, cm = dp.chroma * dp.chroma;
+            const float mul[6] = {lm, cm, cm, lm, cm, cm};
+            memcpy(f.mul, mul, sizeof(mul));
+            f.chroma_boost = dp.chromaBoost;
+            f.gradient_boost = dp.gradientBoost;
+            f.sharpening = dp.sharpening;
+        }
+        f.ltm = LtmParams{p->ltm.guidedFilterEps, p->ltm.shadows, p->ltm.highlights, p->ltm.detail};
+        float inv[9];
+        if (!host_inverse3x3(cam_to_ycbcr, inv)) return set_error(ctx, GLS_ERR_INVALID_ARGUMENT, "singular cam_ycbcr");
+        for (int k = 0; k < 9; k++) f.icy.m[k] = inv[k] * p->exposure_multiplier;
+        memcpy(f.rgb_cam.m, p->rgb_cam, sizeof(f.rgb_cam.m));
+        const gls_rgb_conversion_params& rc = p->rgb_conversion;
+        f.rgb = RgbParams{rc.contrast, rc.saturation, rc.toneCurveSlope, rc.exposureBias, rc.blacks, rc.localToneMapping};
+        f.out = out;
+        f.opitch = opitch;
+        f.tap_den = tap_ptr(3);
+        f.tap_mask = tap_ptr(4);
+        f.tap_pitch = w;
+        const int algo0 = (algo == GLS_DENOISE_GUIDED_FAST) ? 1 : 0;
+        GLS_CHECK(fused_final(ctx, f, half, algo0, rc.localToneMapping != 0, out_float));
+        mark("denoise L0+LTM+sRGB");
+        collect();
+        return GLS_OK;
+    }
+
+    gls_status run_staged(const uint16_t* raw, int rpitch, gls_demosaic_params* p, void* out, bool out_float,
+                          int opitch) {
+        GLS_CHECK(ensure_staged());
         const int Lv = L;
         const int bayer = p->bayer_pattern;
         const bool high_noise = p->noise_level > 0.6f;
@@ -334,6 +526,12 @@ gls_status gls_raw_converter_destroy(gls_raw_converter* c) {
     return GLS_OK;
 }
 
+gls_status gls_raw_converter_set_mode(gls_raw_converter* c, int mode) {
+    if (!c || (mode != 0 && mode != 1)) return GLS_ERR_INVALID_ARGUMENT;
+    c->mode = mode;
+    return GLS_OK;
+}
+
 gls_status gls_raw_converter_profile(gls_raw_converter* c, int enable) {
     if (!c) return GLS_ERR_INVALID_ARGUMENT;
     if (enable && !c->profiling) {
@@ -452,6 +650,7 @@ gls_status gls_raw_converter_fast_demosaic(gls_raw_converter* c, const gls_image
     if (p->bayer_pattern < 0 || p->bayer_pattern > 3) return set_error(ctx, GLS_ERR_INVALID_ARGUMENT, "bayer pattern");
     const bool half = p->storage == GLS_STORAGE_F16;
     GLS_CHECK(c->ensure(raw->width, raw->height, c->L ? c->L : 4, half));
+    GLS_CHECK(c->ensure_staged());
     const int w = raw->width, h = raw->height;
     launch_scale_raw(ctx, (const uint16_t*)raw->ptr, w, h, pitch_elems(raw), c->scaled, p->bayer_pattern, p->scale_mul,
                      p->black_level / 0xffff);

@@ -121,6 +121,7 @@ SIGNATURES = [
     ("gls_raw_converter_demosaic_host", _I, [_P, _P, _I, _I, _I, ctypes.POINTER(DemosaicParams), _P, _I]),
     ("gls_raw_converter_fast_demosaic", _I, [_P, _D, ctypes.POINTER(DemosaicParams), _D]),
     ("gls_raw_converter_set_tap", _I, [_P, _I, _D]),
+    ("gls_raw_converter_set_mode", _I, [_P, _I]),
     ("gls_raw_converter_profile", _I, [_P, _I]),
     ("gls_raw_converter_profile_report", _I, [_P, ctypes.c_char_p, ctypes.c_size_t]),
 ]
@@ -369,6 +370,10 @@ class RawConverter:
         self.ctx.check(lib().gls_raw_converter_fast_demosaic(self.handle, desc(raw), ctypes.byref(params), desc(out)),
                        "RawConverter::fastDemosaicImage")
         return out
+
+    def setMode(self, mode):
+        """0: fused tile kernels (default); 1: one kernel per reference stage."""
+        self.ctx.check(lib().gls_raw_converter_set_mode(self.handle, int(mode)), "setMode")
 
     def profile(self, enable=True):
         self.ctx.check(lib().gls_raw_converter_profile(self.handle, int(enable)), "profile")

@@ -215,6 +215,10 @@ GLS_API gls_status gls_raw_converter_fast_demosaic(gls_raw_converter* conv, cons
  * for parity checks: stage 0 scaled raw (R_F32), 1 green (R_F32), 2 level 0 after the
  * despeckle, 3 denoised level 0 (YCbCr), 4 LTM mask (R_F32). */
 GLS_API gls_status gls_raw_converter_set_tap(gls_raw_converter* conv, int stage, const gls_image_desc* dst);
+/* Kernel schedule: 0 (default) runs the fused tile kernels; 1 runs one kernel per
+ * reference stage (the same arithmetic, every intermediate image materialised).  Both
+ * give identical results; GuidedPrecise denoising always uses the single-stage schedule. */
+GLS_API gls_status gls_raw_converter_set_mode(gls_raw_converter* conv, int mode);
 /* Per-stage timing (the reference's PRINT_EXECUTION_TIME, raw_converter.cpp:22, 97-99,
  * 176-183, with CUDA events instead of queue.finish()).  enable != 0 records an event
  * after every stage of later demosaic calls; the report is a JSON object

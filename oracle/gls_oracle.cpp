@@ -102,8 +102,9 @@ C smoothstepc(C e0, C e1, C x) {
     C t = clampc<C>(M<C>::div(x - e0, e1 - e0), C(0), C(1));
     return t * t * (C(3) - C(2) * t);
 }
+// step(edge, x) with NaN x giving 0 (the finite-math reading pinned in gls_clmath.h)
 template <class C>
-C stepc(C edge, C x) { return x < edge ? C(0) : C(1); }
+C stepc(C edge, C x) { return x >= edge ? C(1) : C(0); }
 template <class C>
 C mminc(C a, C b) { return a < b ? a : b; }
 template <class C>

@@ -18,10 +18,16 @@ pytestmark = pytest.mark.gpu
 TAPS = {0: "scaled_raw", 1: "green", 2: "level0", 3: "denoised0", 4: "ltm_mask"}
 
 
-def run_gpu(ctx, raw, spec, out_float=False, taps=True):
+@pytest.fixture(params=[0, 1], ids=["fused", "staged"])
+def mode(request):
+    return request.param
+
+
+def run_gpu(ctx, raw, spec, out_float=False, taps=True, mode=0):
     import torch
     h, w = raw.shape
     conv = gls.RawConverter(ctx)
+    conv.setMode(mode)
     bufs = {}
     if taps:
         for k, name in TAPS.items():
@@ -40,11 +46,11 @@ def run_gpu(ctx, raw, spec, out_float=False, taps=True):
     return res
 
 
-def check(ctx, raw, spec, out_float=False):
+def check(ctx, raw, spec, out_float=False, mode=0):
     prec = orc.F16 if spec["storage"] == gls.STORAGE_F16 else orc.F32
     ref = orc.demosaic(raw, oracle_params(spec), prec, want=("rgbaf" if out_float else "rgba8",),
                        taps=tuple(TAPS.values()))
-    got = run_gpu(ctx, raw, spec, out_float)
+    got = run_gpu(ctx, raw, spec, out_float, mode=mode)
     np.testing.assert_array_equal(got["raw_nlf"], ref["raw_nlf"])
     np.testing.assert_array_equal(got["pyramid_nlf"], ref["pyramid_nlf"])
     for name in TAPS.values():
@@ -62,37 +68,37 @@ def check(ctx, raw, spec, out_float=False):
 
 
 @pytest.mark.parametrize("bayer", [0, 1, 2, 3], ids=["grbg", "gbrg", "rggb", "bggr"])
-def test_pipeline_cfa_phases(ctx, bayer):
+def test_pipeline_cfa_phases(ctx, bayer, mode):
     raw, _, meta = synthetic.make_frame(256, 192, bayer=bayer, seed=100 + bayer)
-    check(ctx, raw, configs.make_spec(meta, levels=4))
+    check(ctx, raw, configs.make_spec(meta, levels=4), mode=mode)
 
 
-def test_pipeline_config1_float_output(ctx):
+def test_pipeline_config1_float_output(ctx, mode):
     c = configs.CONFIG1
     raw, _, meta = synthetic.make_frame(c["width"], c["height"], bayer=c["bayer"], bits=c["bits"], black=c["black"],
                                         white=c["white"], wb=c["wb"], read_sigma=3.0, gain=2.0, seed=1)
-    check(ctx, raw, configs.make_spec(meta, levels=4), out_float=True)
+    check(ctx, raw, configs.make_spec(meta, levels=4), out_float=True, mode=mode)
 
 
-def test_pipeline_fp16_storage(ctx):
+def test_pipeline_fp16_storage(ctx, mode):
     raw, _, meta = synthetic.make_frame(320, 240, bayer=0, bits=14, seed=3)
-    check(ctx, raw, configs.make_spec(meta, levels=6, storage=gls.STORAGE_F16))
+    check(ctx, raw, configs.make_spec(meta, levels=6, storage=gls.STORAGE_F16), mode=mode)
 
 
-def test_pipeline_high_noise_branch(ctx):
+def test_pipeline_high_noise_branch(ctx, mode):
     raw, _, meta = synthetic.make_frame(256, 192, bayer=2, gain=16.0, read_sigma=12.0, seed=4)
-    check(ctx, raw, configs.make_spec(meta, levels=5, noise_level=0.7))
+    check(ctx, raw, configs.make_spec(meta, levels=5, noise_level=0.7), mode=mode)
 
 
 @pytest.mark.parametrize("algo", [1, 2], ids=["guided_fast", "guided_precise"])
-def test_pipeline_guided_denoisers(ctx, algo):
+def test_pipeline_guided_denoisers(ctx, algo, mode):
     raw, _, meta = synthetic.make_frame(192, 128, bayer=3, seed=5)
-    check(ctx, raw, configs.make_spec(meta, levels=4, algorithm=algo))
+    check(ctx, raw, configs.make_spec(meta, levels=4, algorithm=algo), mode=mode)
 
 
-def test_pipeline_strong_denoise_no_ltm(ctx):
+def test_pipeline_strong_denoise_no_ltm(ctx, mode):
     raw, _, meta = synthetic.make_frame(256, 160, bayer=1, seed=6, gain=4.0, read_sigma=6.0)
-    check(ctx, raw, configs.make_spec(meta, levels=5, ltm=False, denoise="strong"))
+    check(ctx, raw, configs.make_spec(meta, levels=5, ltm=False, denoise="strong"), mode=mode)
 
 
 def test_pipeline_host_buffers_and_rgb(ctx):
