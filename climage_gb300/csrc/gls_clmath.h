@@ -118,10 +118,101 @@ GLS_HD float mix_(float x, float y, float a) { return x + (y - x) * a; }
 GLS_HD float step_(float edge, float x) { return x >= edge ? 1.0f : 0.0f; }
 
 // OpenCL smoothstep(e0, e1, x): t = clamp((x - e0) / (e1 - e0), 0, 1); t * t * (3 - 2 * t)
-GLS_HD float smoothstep_(float e0, float e1, float x) {
+GLS_HD float smoothstep_ref(float e0, float e1, float x) {
     float t = clamp_(div_(x - e0, e1 - e0), 0.0f, 1.0f);
     return t * t * (3.0f - 2.0f * t);
 }
+
+// ---- exact shortcuts (results identical to the literal expressions) ----
+
+GLS_HD float fma_(float a, float b, float c) {
+#if defined(__CUDA_ARCH__)
+    return __fmaf_rn(a, b, c);
+#else
+    return __builtin_fmaf(a, b, c);
+#endif
+}
+
+GLS_HD float rcp_(float d) {
+#if defined(__CUDA_ARCH__)
+    return __frcp_rn(d);
+#else
+    return 1.0f / d;
+#endif
+}
+
+// Division by a value shared by many numerators.  With y = RN(1/d) and q0 = RN(x*y), the
+// residual r = x - q0*d is exact and RN(q0 + r*y) is the correctly rounded x/d
+// (Markstein's correction, P. Markstein, "IA-64 and Elementary Functions", 2000); the
+// shortcut is taken only where no intermediate can overflow or underflow, and zero, NaN
+// and infinite numerators take the literal division.
+struct FastDiv {
+    float d, y;
+    bool ok;
+    GLS_HD void init(float den) {
+        d = den;
+        const float ad = fabs_(den);
+        ok = ad >= 8.67361738e-19f && ad <= 1.15292150e18f;  // [2^-60, 2^60]
+        y = ok ? rcp_(den) : 0.0f;
+    }
+    GLS_HD float operator()(float x) const {
+        const float ax = fabs_(x);
+        if (!ok || !(ax >= 8.67361738e-19f && ax <= 1.15292150e18f)) return div_(x, d);
+        const float q0 = x * y;
+        const float r = fma_(-q0, d, x);
+        return fma_(r, y, q0);
+    }
+};
+
+// smoothstep with the interpolation denominator e1 - e0 shared by many evaluations: the
+// division is only evaluated where the clamp does not decide the result by itself
+// (num <= 0 or NaN clamps to 0, num >= den > 0 clamps to 1, exactly as the literal form).
+GLS_HD float smoothstep_den(float e0, const FastDiv& den, float x) {
+    const float num = x - e0;
+    float t;
+    if (den.d > 0.0f && den.d <= 3.4e38f) {
+        t = !(num > 0.0f) ? 0.0f : (num >= den.d ? 1.0f : den(num));
+    } else {
+        t = clamp_(div_(num, den.d), 0.0f, 1.0f);
+    }
+    return t * t * (3.0f - 2.0f * t);
+}
+
+// smoothstep(e0, e1, x), identical to smoothstep_ref, skipping the division when the
+// clamp decides the value.
+GLS_HD float smoothstep_(float e0, float e1, float x) {
+    const float den = e1 - e0;
+    const float num = x - e0;
+    float t;
+    if (den > 0.0f && den <= 3.4e38f) {
+        t = !(num > 0.0f) ? 0.0f : (num >= den ? 1.0f : div_(num, den));
+    } else {
+        t = clamp_(div_(num, den), 0.0f, 1.0f);
+    }
+    return t * t * (3.0f - 2.0f * t);
+}
+
+// sqrt_rn(q) >= e decided without the square root when q is clearly on one side of e^2
+// (|q - e^2| > 2^-20 e^2); e must be positive and moderate, otherwise the literal test.
+struct SqrtGe {
+    float e, lo, hi;
+    bool ok;
+    GLS_HD void init(float edge) {
+        e = edge;
+        ok = edge > 1e-15f && edge < 1e15f;
+        const float t = edge * edge;
+        lo = t * (1.0f - 9.5367431640625e-07f);  // 1 - 2^-20, exact
+        hi = t * (1.0f + 9.5367431640625e-07f);  // 1 + 2^-20, exact
+    }
+    // returns sqrt_rn(q) >= e (false for NaN q)
+    GLS_HD bool operator()(float q) const {
+        if (ok) {
+            if (q < lo) return false;
+            if (q > hi) return true;
+        }
+        return sqrt_(q) >= e;
+    }
+};
 
 // The reference's own min/max/abs macros (demosaic.cl:56-65): plain selects.
 GLS_HD float mmin(float a, float b) { return a < b ? a : b; }

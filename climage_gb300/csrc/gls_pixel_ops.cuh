@@ -30,6 +30,18 @@ using glsm::step_;
 #define GLS_SQRT2_F 1.41421356237309504880f
 #define GLS_SQRT3_F 1.7320508f
 
+using glsm::FastDiv;
+using glsm::SqrtGe;
+
+// x / 25 (the 5x5 box normalisation): 0.04f is RN(1/25)
+GLS_DI FastDiv div25() {
+    FastDiv f;
+    f.d = 25.0f;
+    f.y = 0.04f;
+    f.ok = true;
+    return f;
+}
+
 // ---- a4: scaleRawData (demosaic.cl:69-78) ----
 GLS_DI float scale_value(uint16_t raw, float scale_mul, float black) {
     const float v = div_((float)raw, 65535.0f);
@@ -53,10 +65,11 @@ GLS_DI void raw_stats_quad(const Acc& raw, int qx, int qy, int bayer, float mean
             }
         }
     }
+    const FastDiv d25 = div25();
 #pragma unroll
     for (int c = 0; c < 4; c++) {
-        mean[c] = div_(sum[c], 25.0f);
-        var[c] = div_(sq[c] - div_(sum[c] * sum[c], 25.0f), 25.0f);
+        mean[c] = d25(sum[c]);
+        var[c] = d25(sq[c] - d25(sum[c] * sum[c]));
     }
 }
 
@@ -77,11 +90,12 @@ GLS_DI float4 noise_stats_px(const Acc& im, int px, int py) {
             q2 = q2 + s.z * s.z;
         }
     }
+    const FastDiv d25 = div25();
     float4 r;
-    r.x = div_(s0, 25.0f);
-    r.y = div_(q0 - div_(s0 * s0, 25.0f), 25.0f);
-    r.z = div_(q1 - div_(s1 * s1, 25.0f), 25.0f);
-    r.w = div_(q2 - div_(s2 * s2, 25.0f), 25.0f);
+    r.x = d25(s0);
+    r.y = d25(q0 - d25(s0 * s0));
+    r.z = d25(q1 - d25(s1 * s1));
+    r.w = d25(q2 - d25(s2 * s2));
     return r;
 }
 
@@ -104,10 +118,11 @@ GLS_DI SobelVal sobel_abs(const Acc& im, int x, int y) {
             vy = vy + ky[j + 1][i + 1] * s;
         }
     }
-    const float r = sqrt_(4.5f);
+    FastDiv r;
+    r.init(sqrt_(4.5f));
     SobelVal o;
-    o.gx = mabs(div_(vx, r));
-    o.gy = mabs(div_(vy, r));
+    o.gx = mabs(r(vx));
+    o.gy = mabs(r(vy));
     o.len = length2_(o.gx, o.gy);
     return o;
 }
@@ -127,8 +142,9 @@ GLS_DI float2 sobel_signed(const Acc& im, int x, int y) {
             vy = vy + ky[j + 1][i + 1] * s;
         }
     }
-    const float r = sqrt_(4.5f);
-    return make_float2(div_(vx, r), div_(vy, r));
+    FastDiv r;
+    r.init(sqrt_(4.5f));
+    return make_float2(r(vx), r(vy));
 }
 
 // sob(i, j) returns the SobelVal at offset (i, j) from the centre.
@@ -137,12 +153,14 @@ GLS_DI float2 bilateral_sobel(const SobF& sob, float sigma) {
     const SobelVal c = sob(0, 0);
     float sx = 0.0f, sy = 0.0f, ws = 0.0f;
     const float e0 = 4.0f * sigma, e1 = 16.0f * sigma;
+    FastDiv den;
+    den.init(e1 - e0);
 #pragma unroll
     for (int j = -2; j <= 2; j++) {
 #pragma unroll
         for (int i = -2; i <= 2; i++) {
             const SobelVal g = sob(i, j);
-            const float w = 1.0f - smoothstep_(e0, e1, 0.05f * mabs(g.len - c.len));
+            const float w = 1.0f - glsm::smoothstep_den(e0, den, 0.05f * mabs(g.len - c.len));
             sx = sx + w * g.gx;
             sy = sy + w * g.gy;
             ws = ws + w;
@@ -168,15 +186,15 @@ GLS_DI float green_at(const Acc& raw, int x, int y, float lumaVariance, const So
     const float c_up = raw.at(x, y - 2), c_down = raw.at(x, y + 2);
     const float c2_tl = raw.at(x - 1, y - 1), c2_tr = raw.at(x + 1, y - 1);
     const float c2_bl = raw.at(x - 1, y + 1), c2_br = raw.at(x + 1, y + 1);
-    const float c2_ave = div_(c2_tl + c2_tr + c2_bl + c2_br, 4.0f);
+    const float c2_ave = ((c2_tl + c2_tr + c2_bl + c2_br) * 0.25f);
 
-    const float g_ave = div_(g_left + g_right + g_up + g_down, 4.0f);
+    const float g_ave = ((g_left + g_right + g_up + g_down) * 0.25f);
     const float lumaStdDev = sqrt_(lumaVariance * g_ave);
     const float2 grad = bilateral_sobel(sob, lumaStdDev);
 
-    const float g_lf_x = div_(g_left + g_right, 2.0f), g_lf_y = div_(g_up + g_down, 2.0f);
-    const float g_hf_x = div_(2.0f * c_xy - (c_left + c_right), 4.0f);
-    const float g_hf_y = div_(2.0f * c_xy - (c_up + c_down), 4.0f);
+    const float g_lf_x = ((g_left + g_right) * 0.5f), g_lf_y = ((g_up + g_down) * 0.5f);
+    const float g_hf_x = ((2.0f * c_xy - (c_left + c_right)) * 0.25f);
+    const float g_hf_y = ((2.0f * c_xy - (c_up + c_down)) * 0.25f);
 
     const float whiteness =
         clamp_(div_(mmin(c_xy, mmin(g_ave, c2_ave)), mmax(c_xy, mmax(g_ave, c2_ave))), 0.0f, 1.0f);
@@ -216,7 +234,7 @@ GLS_DI float3 red_blue_at(const AccR& raw, const AccG& gi, int x, int y, int bay
         const float dvx = glsm::fabs_(c2_tl - c2_br), dvy = glsm::fabs_(c2_tr - c2_bl);
         const float flatness = 1.0f - smoothstep_(0.25f * chromaStdDev, chromaStdDev, length2_(dvx, dvy));
         const float alpha = mix_(2.0f * glsm::atan2pi_(dvy, dvx), 0.5f, flatness);
-        const float c2 = green - mix_(div_(c2_tr + c2_bl, 2.0f), div_(c2_tl + c2_br, 2.0f), alpha);
+        const float c2 = green - mix_(((c2_tr + c2_bl) * 0.5f), ((c2_tl + c2_br) * 0.5f), alpha);
         if (color == raw_red) {
             red = c1;
             blue = c2;
@@ -229,8 +247,8 @@ GLS_DI float3 red_blue_at(const AccR& raw, const AccG& gi, int x, int y, int bay
         const float g_up = gi.at(x, y - 1), g_down = gi.at(x, y + 1);
         const float c1_left = g_left - raw.at(x - 1, y), c1_right = g_right - raw.at(x + 1, y);
         const float c2_up = g_up - raw.at(x, y - 1), c2_down = g_down - raw.at(x, y + 1);
-        const float c1 = green - div_(c1_left + c1_right, 2.0f);
-        const float c2 = green - div_(c2_up + c2_down, 2.0f);
+        const float c1 = green - ((c1_left + c1_right) * 0.5f);
+        const float c2 = green - ((c2_up + c2_down) * 0.5f);
         const int red_row_green = (bayer == bggr || bayer == grbg) ? raw_green : raw_green2;
         if (color == red_row_green) {
             red = c1;
@@ -392,21 +410,30 @@ GLS_DI float4 bilateral_px(const Acc4& im, int px, int py, const Nlf6& n, float 
         lumaBoost = gradientBoost -
                     (gradientBoost - 1.0f) * smoothstep_(0.5f, 2.0f, length2_(div_(g.x, sig0), div_(g.y, sig0)));
     }
-    const float e0 = lumaBoost * GLS_SQRT2_F, e1 = chromaBoost * GLS_SQRT2_F;
+    // weight = 1 - step(edge, length(diff)) = !(sqrt_rn(|diff|^2) >= edge), decided on the
+    // squared length; the divisions by sigma share their divisor; the weights are 0 or 1,
+    // so w * s is exact and the multiply-add can be fused without changing a bit.
+    SqrtGe ge0, ge1;
+    ge0.init(lumaBoost * GLS_SQRT2_F);
+    ge1.init(chromaBoost * GLS_SQRT2_F);
+    FastDiv dv0, dv1, dv2;
+    dv0.init(sig0);
+    dv1.init(sig1);
+    dv2.init(sig2);
     float f0 = 0.0f, f1 = 0.0f, f2 = 0.0f, n0 = 0.0f, n1 = 0.0f, n2 = 0.0f;
 #pragma unroll
     for (int y = -2; y <= 2; y++) {
 #pragma unroll
         for (int x = -2; x <= 2; x++) {
             const float4 s = im.at(px + x, py + y);
-            const float d0 = div_(s.x - c.x, sig0), d1 = div_(s.y - c.y, sig1), d2 = div_(s.z - c.z, sig2);
-            const float l = length3_(d0, d1, d2);
-            const float w0 = 1.0f - step_(e0, l), w1 = 1.0f - step_(e1, l);
-            f0 = f0 + w0 * s.x;
+            const float d0 = dv0(s.x - c.x), d1 = dv1(s.y - c.y), d2 = dv2(s.z - c.z);
+            const float q = d0 * d0 + d1 * d1 + d2 * d2;
+            const float w0 = ge0(q) ? 0.0f : 1.0f, w1 = ge1(q) ? 0.0f : 1.0f;
+            f0 = glsm::fma_(w0, s.x, f0);
             n0 = n0 + w0;
-            f1 = f1 + w1 * s.y;
+            f1 = glsm::fma_(w1, s.y, f1);
             n1 = n1 + w1;
-            f2 = f2 + w1 * s.z;
+            f2 = glsm::fma_(w1, s.z, f2);
             n2 = n2 + w1;
         }
     }
@@ -483,10 +510,10 @@ GLS_DI float4 reassemble_px(float4 d0, const AccI& i1, const AccD& d1, int x, in
     if (sharpening > 1.0f) {
         const float ax = sample4(d1, ipx + nx, ipy + 0.0f * ny, w1, h1).x;
         const float bx = sample4(d1, ipx - nx, ipy - 0.0f * ny, w1, h1).x;
-        const float dx = div_(ax - bx, 2.0f);
+        const float dx = ((ax - bx) * 0.5f);
         const float ay = sample4(d1, ipx + 0.0f * nx, ipy + ny, w1, h1).x;
         const float by = sample4(d1, ipx - 0.0f * nx, ipy - ny, w1, h1).x;
-        const float dy = div_(ay - by, 2.0f);
+        const float dy = ((ay - by) * 0.5f);
         const float threshold = 0.25f * sqrt_(nlf0 + nlf1 * pd1.x);
         const float detail = smoothstep_(0.25f * threshold, threshold, length2_(dx, dy)) *
                              (1.0f - smoothstep_(0.95f, 1.0f, dp.x)) * (0.6f + 0.4f * smoothstep_(0.0f, 0.1f, dp.x));
@@ -522,9 +549,11 @@ GLS_DI float ltm_mask_px(const AccIn& in, const AccG& guide, int x, int y, int w
     const float4 inp = sample4(in, px + 0.5f * nx, py + 0.5f * ny, w, h);
     const float luma = inp.x;
     float filtered = 0.0f, knorm = 0.0f;
+    FastDiv dv;
+    dv.init(var + lp.eps);
 #pragma unroll
     for (int i = 0; i < 9; i++) {
-        const float wgt = bw[i] * (1.0f + div_((gs[i] - mean) * (luma - mean), var + lp.eps));
+        const float wgt = bw[i] * (1.0f + dv((gs[i] - mean) * (luma - mean)));
         filtered = filtered + wgt * gs[i];
         knorm = knorm + wgt;
     }
@@ -630,6 +659,11 @@ GLS_DI float4 denoise_rgba_px(const Acc4& im, int px, int py, const float rv[4])
     float sg[4], f[4] = {0, 0, 0, 0}, nrm[4] = {0, 0, 0, 0};
 #pragma unroll
     for (int k = 0; k < 4; k++) sg[k] = sqrt_(rv[k] * in[k]);
+    FastDiv dv[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) dv[k].init(sg[k]);
+    SqrtGe ge;
+    ge.init(1.0f);
 #pragma unroll
     for (int y = -2; y <= 2; y++) {
 #pragma unroll
@@ -638,8 +672,8 @@ GLS_DI float4 denoise_rgba_px(const Acc4& im, int px, int py, const float rv[4])
             const float s[4] = {s4.x, s4.y, s4.z, s4.w};
             float d[4];
 #pragma unroll
-            for (int k = 0; k < 4; k++) d[k] = div_(s[k] - in[k], sg[k]);
-            const float w = 1.0f - step_(1.0f, length4_(d[0], d[1], d[2], d[3]));
+            for (int k = 0; k < 4; k++) d[k] = dv[k](s[k] - in[k]);
+            const float w = ge(d[0] * d[0] + d[1] * d[1] + d[2] * d[2] + d[3] * d[3]) ? 0.0f : 1.0f;
 #pragma unroll
             for (int k = 0; k < 4; k++) {
                 f[k] = f[k] + w * s[k];

@@ -587,3 +587,87 @@ void launch_unpack(gls_ctx* ctx, const void* packed, size_t n_bytes, int bits, u
 }
 
 }  // namespace gls
+
+// ------------------------------------------------------------------------------------------
+// Self-test of the exact shortcuts against the literal operations (gls_selftest).
+// ------------------------------------------------------------------------------------------
+namespace gls {
+namespace {
+
+__device__ uint32_t hash32(uint64_t x) {
+    x ^= x >> 33;
+    x *= 0xff51afd7ed558ccdULL;
+    x ^= x >> 33;
+    x *= 0xc4ceb9fe1a85ec53ULL;
+    x ^= x >> 33;
+    return (uint32_t)x;
+}
+
+// a float with a random sign, mantissa and an exponent in [emin, emax]
+__device__ float rand_float(uint64_t key, int emin, int emax) {
+    const uint32_t h = hash32(key);
+    const uint32_t h2 = hash32(key ^ 0x9e3779b97f4a7c15ULL);
+    const int e = emin + (int)(h2 % (uint32_t)(emax - emin + 1));
+    const uint32_t bits = ((uint32_t)(e + 127) << 23) | (h & 0x7fffffu) | (h2 & 0x80000000u);
+    return __uint_as_float(bits);
+}
+
+__global__ void selftest_kernel(uint64_t n, uint64_t seed, unsigned long long* bad) {
+    unsigned long long b0 = 0, b1 = 0, b2 = 0, b3 = 0;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t k = seed * 0x100000001b3ULL + 4 * i;
+        // division: random and near-halfway numerators
+        const float d = fabsf(rand_float(k, -40, 40)) * ((i & 1) ? 1.0f : -1.0f);
+        float x = rand_float(k + 1, -40, 40);
+        if (i & 2) x = __fmul_rn(d, 1.0f + (float)(hash32(k + 2) & 0xffff) * 1.1920929e-07f);
+        FastDiv fd;
+        fd.init(d);
+        const float q1 = fd(x), q2 = div_(x, d);
+        if (__float_as_uint(q1) != __float_as_uint(q2) && !(q1 != q1 && q2 != q2)) b0++;
+        // smoothstep: edges and samples of the magnitudes the kernels see
+        const float e0 = fabsf(rand_float(k + 3, -20, 2)), e1 = e0 * (1.0f + (float)(hash32(k) & 15));
+        const float xs = rand_float(k + 2, -22, 3);
+        const float s1 = glsm::smoothstep_(e0, e1, xs), s2 = glsm::smoothstep_ref(e0, e1, xs);
+        FastDiv den;
+        den.init(e1 - e0);
+        const float s3 = glsm::smoothstep_den(e0, den, xs);
+        if (__float_as_uint(s1) != __float_as_uint(s2) || __float_as_uint(s3) != __float_as_uint(s2)) b1++;
+        // squared-length edge test, including q within a few ulps of e^2
+        const float e = fabsf(rand_float(k + 4, -10, 10));
+        SqrtGe ge;
+        ge.init(e);
+        float qv = e * e;
+        const int off = (int)(hash32(k + 5) % 64) - 32;
+        qv = __uint_as_float(__float_as_uint(qv) + off);
+        if ((i & 7) == 0) qv = fabsf(rand_float(k + 6, -25, 25));
+        if (ge(qv) != (sqrt_(qv) >= e)) b2++;
+        // float -> half rounding
+        const float hv = rand_float(k + 7, -26, 16);
+        const float h1 = glsm::round_half(hv);
+        const float h2 = glsm::f16_bits_to_f32(glsm::f32_to_f16_bits(hv));
+        if (__float_as_uint(h1) != __float_as_uint(h2)) b3++;
+    }
+    if (b0) atomicAdd(&bad[0], b0);
+    if (b1) atomicAdd(&bad[1], b1);
+    if (b2) atomicAdd(&bad[2], b2);
+    if (b3) atomicAdd(&bad[3], b3);
+}
+
+}  // namespace
+}  // namespace gls
+
+extern "C" gls_status gls_selftest(gls_ctx* ctx, uint64_t n, uint64_t seed, uint64_t mismatches[4]) {
+    using namespace gls;
+    if (!ctx || !mismatches) return GLS_ERR_INVALID_ARGUMENT;
+    unsigned long long* d = nullptr;
+    GLS_CHECK(check_cuda(ctx, cudaMalloc(&d, 4 * sizeof(unsigned long long)), "cudaMalloc(selftest)"));
+    cudaMemsetAsync(d, 0, 4 * sizeof(unsigned long long), ctx->stream);
+    selftest_kernel<<<4 * (ctx->num_sms > 0 ? ctx->num_sms : 148), 256, 0, ctx->stream>>>(n, seed, d);
+    ctx->launches++;
+    unsigned long long h[4] = {0, 0, 0, 0};
+    gls_status s = check_cuda(ctx, cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream), "selftest copy");
+    if (s == GLS_OK) s = check_cuda(ctx, cudaStreamSynchronize(ctx->stream), "selftest");
+    cudaFree(d);
+    for (int i = 0; i < 4; i++) mismatches[i] = h[i];
+    return s;
+}

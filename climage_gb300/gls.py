@@ -111,6 +111,7 @@ SIGNATURES = [
     ("gls_despeckle_raw_rgba", _I, [_P, _D, _D]),
     ("gls_denoise_raw_rgba", _I, [_P, _D, _FP, _D]),
     ("gls_unpack_raw_bits", _I, [_P, _P, ctypes.c_size_t, _I, _P, ctypes.c_size_t]),
+    ("gls_selftest", _I, [_P, ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)]),
     ("gls_cam_xyz_coeff", _I, [_FP, _FP, _FP]),
     ("gls_cam_ycbcr", _I, [_FP, _FP]),
     ("gls_inverse3x3", _I, [_FP, _FP]),
@@ -229,6 +230,11 @@ class Context:
 
     def synchronize(self):
         self.check(self._lib.gls_ctx_synchronize(self.handle), "synchronize")
+
+    def selftest(self, n=1 << 24, seed=1):
+        out = (ctypes.c_uint64 * 4)()
+        self.check(self._lib.gls_selftest(self.handle, int(n), int(seed), out), "selftest")
+        return [int(v) for v in out]
 
     def kernel_launches(self):
         return int(self._lib.gls_ctx_kernel_launches(self.handle))

@@ -187,6 +187,13 @@ GLS_API gls_status gls_denoise_raw_rgba(gls_ctx* ctx, const gls_image_desc* in, 
 GLS_API gls_status gls_unpack_raw_bits(gls_ctx* ctx, const void* packed, size_t n_bytes, int bits, uint16_t* out,
                                        size_t n_samples);
 
+/* Device self-test of the exact arithmetic shortcuts the kernels use (no reference
+ * counterpart): over n pseudo-random inputs derived from seed, counts the results that
+ * differ from the literal operation -- [0] shared-divisor division vs IEEE division,
+ * [1] the clamped smoothstep vs its literal form, [2] the squared-length edge test vs
+ * sqrt-then-compare, [3] hardware float->half rounding vs the portable conversion. */
+GLS_API gls_status gls_selftest(gls_ctx* ctx, uint64_t n, uint64_t seed, uint64_t mismatches[4]);
+
 /* ---- host colour math (demosaic_utils.cpp:25-52, 809-822; gls_linalg.hpp:545-556) ---- */
 GLS_API gls_status gls_cam_xyz_coeff(const float cam_xyz[9], float pre_mul[3], float rgb_cam[9]);
 GLS_API gls_status gls_cam_ycbcr(const float rgb_cam[9], float out[9]);

@@ -299,6 +299,14 @@ def test_unpack(ctx):
         np.testing.assert_array_equal(orc.unpack_bits(packed, bits), samples)
 
 
+def test_exact_shortcuts_selftest(ctx):
+    """The kernels replace some literal operations by exact equivalents (shared-divisor
+    division, clamped smoothstep, squared-length edge tests, hardware binary16 rounding);
+    over 2^26 random and adversarial inputs each must equal the literal operation."""
+    for seed in (1, 2):
+        assert ctx.selftest(1 << 26, seed) == [0, 0, 0, 0]
+
+
 def test_invalid_arguments(ctx):
     import torch
     raw = torch.zeros((9, 8), dtype=torch.uint16, device="cuda")
