@@ -72,5 +72,21 @@ def build(verbose=False):
     return LIB
 
 
+def build_cpp_test():
+    """Compiles tests/cpp/test_cpp_layer.cpp (a C++ client of include/gls_cuda.hpp)."""
+    lib = build()
+    src = os.path.join(HERE, "..", "tests", "cpp", "test_cpp_layer.cpp")
+    exe = os.path.join(BUILD, "test_cpp_layer")
+    hdrs = [os.path.join(HERE, "..", "include", f) for f in ("gls_cuda.h", "gls_cuda.hpp")]
+    if _newer(exe, [src, lib] + hdrs):
+        return exe
+    cmd = [nvcc(), "-std=c++20", "-O2", "-x", "cu", src, "-o", exe, "-L" + HERE, "-lgls_cuda",
+           "-Xlinker", "-rpath=" + HERE] + ARCH
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("C++ layer test build failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
+    return exe
+
+
 if __name__ == "__main__":
     print(build(verbose=True))

@@ -35,8 +35,10 @@
 
 #if defined(__CUDACC__)
 #define GLS_HD __host__ __device__ __forceinline__
+#define GLS_HDM __host__ __device__ __forceinline__
 #else
 #define GLS_HD static inline
+#define GLS_HDM inline
 #endif
 
 namespace glsm {
@@ -149,13 +151,13 @@ GLS_HD float rcp_(float d) {
 struct FastDiv {
     float d, y;
     bool ok;
-    GLS_HD void init(float den) {
+    GLS_HDM void init(float den) {
         d = den;
         const float ad = fabs_(den);
         ok = ad >= 8.67361738e-19f && ad <= 1.15292150e18f;  // [2^-60, 2^60]
         y = ok ? rcp_(den) : 0.0f;
     }
-    GLS_HD float operator()(float x) const {
+    GLS_HDM float operator()(float x) const {
         const float ax = fabs_(x);
         if (!ok || !(ax >= 8.67361738e-19f && ax <= 1.15292150e18f)) return div_(x, d);
         const float q0 = x * y;
@@ -197,7 +199,7 @@ GLS_HD float smoothstep_(float e0, float e1, float x) {
 struct SqrtGe {
     float e, lo, hi;
     bool ok;
-    GLS_HD void init(float edge) {
+    GLS_HDM void init(float edge) {
         e = edge;
         ok = edge > 1e-15f && edge < 1e15f;
         const float t = edge * edge;
@@ -205,7 +207,7 @@ struct SqrtGe {
         hi = t * (1.0f + 9.5367431640625e-07f);  // 1 + 2^-20, exact
     }
     // returns sqrt_rn(q) >= e (false for NaN q)
-    GLS_HD bool operator()(float q) const {
+    GLS_HDM bool operator()(float q) const {
         if (ok) {
             if (q < lo) return false;
             if (q > hi) return true;

@@ -1,0 +1,79 @@
+// Drives the header-only C++ layer (include/gls_cuda.hpp) the way a port of CLImage's
+// RawPipeline driver would: host gls::image<luma_pixel_16> in, RawConverter::demosaicImage,
+// RawConverter::convertToRGBImage out.  Reads a raw frame and its parameters from files
+// written by tests/test_gpu_cpp_layer.py and writes the RGB result next to them.
+//
+//   test_cpp_layer <dir>     reads <dir>/raw.u16 <dir>/params.txt, writes <dir>/rgb.u8
+#include <cstdio>
+#include <fstream>
+#include <iostream>
+#include <string>
+#include <vector>
+
+#include "../../include/gls_cuda.hpp"
+
+int main(int argc, char** argv) {
+    if (argc < 2) {
+        std::cerr << "usage: test_cpp_layer <dir>\n";
+        return 2;
+    }
+    const std::string dir = argv[1];
+    std::ifstream pf(dir + "/params.txt");
+    int w, h, bayer, levels, ltm;
+    gls::DemosaicParametersT<4> p;
+    pf >> w >> h >> bayer >> levels >> ltm;
+    pf >> p.black_level >> p.white_level >> p.exposure_multiplier >> p.noiseLevel;
+    for (auto& v : p.scale_mul) pf >> v;
+    for (auto& r : p.rgb_cam)
+        for (auto& v : r) pf >> v;
+    for (auto& v : p.noiseModel.rawNlf) pf >> v;
+    for (auto& r : p.noiseModel.pyramidNlf)
+        for (auto& v : r) pf >> v;
+    for (auto& d : p.denoiseParameters) pf >> d.luma >> d.chroma >> d.chromaBoost >> d.gradientBoost >> d.sharpening;
+    auto& rc = p.rgbConversionParameters;
+    pf >> rc.contrast >> rc.saturation >> rc.toneCurveSlope >> rc.exposureBias >> rc.blacks;
+    rc.localToneMapping = ltm;
+    pf >> p.ltmParameters.guidedFilterEps >> p.ltmParameters.shadows >> p.ltmParameters.highlights >>
+        p.ltmParameters.detail;
+    p.bayerPattern = (gls::BayerPattern)bayer;
+    if (!pf || levels != 4) {
+        std::cerr << "bad params\n";
+        return 2;
+    }
+    gls::image<gls::luma_pixel_16> raw(w, h);
+    {
+        std::ifstream rf(dir + "/raw.u16", std::ios::binary);
+        rf.read(reinterpret_cast<char*>(raw[0]), (std::streamsize)w * h * 2);
+        if (!rf) {
+            std::cerr << "bad raw\n";
+            return 2;
+        }
+    }
+    try {
+        gls::CudaContext ctx(0);
+        gls::RawConverter conv(&ctx);
+        auto* rgba = conv.demosaicImage(raw, &p, nullptr, false);
+        auto rgb = gls::RawConverter::convertToRGBImage(*rgba);
+        std::ofstream of(dir + "/rgb.u8", std::ios::binary);
+        of.write(reinterpret_cast<const char*>((*rgb)[0]), (std::streamsize)w * h * 3);
+        std::ofstream nf(dir + "/nlf.txt");
+        nf.precision(9);
+        for (float v : p.noiseModel.rawNlf) nf << v << " ";
+        nf << "\n";
+        // the C++ layer rejects what the reference cannot do
+        bool threw = false;
+        try {
+            conv.demosaicImage(raw, &p, nullptr, true);
+        } catch (const gls::cuda_error& e) {
+            threw = e.status == GLS_ERR_UNSUPPORTED;
+        }
+        if (!threw) {
+            std::cerr << "rotate_180 did not throw\n";
+            return 1;
+        }
+    } catch (const std::exception& e) {
+        std::cerr << "error: " << e.what() << "\n";
+        return 1;
+    }
+    return 0;
+}

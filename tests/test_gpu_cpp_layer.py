@@ -1,0 +1,43 @@
+"""The header-only C++ layer (include/gls_cuda.hpp): a C++ program written against the
+reference's API (gls::image, RawConverter::demosaicImage, convertToRGBImage) produces the
+oracle's RGB output."""
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+import pytest
+
+from climage_gb300 import build, configs, synthetic
+from oracle import oracle as orc
+from tests.helpers import oracle_params
+
+pytestmark = pytest.mark.gpu
+
+
+def test_cpp_layer_raw_converter(cuda):
+    exe = build.build_cpp_test()
+    raw, _, meta = synthetic.make_frame(192, 128, bayer=2, seed=31)
+    spec = configs.make_spec(meta, levels=4)
+    with tempfile.TemporaryDirectory() as d:
+        raw.tofile(os.path.join(d, "raw.u16"))
+        vals = [192, 128, spec["bayer_pattern"], 4, spec["rgb"]["localToneMapping"], spec["black_level"],
+                spec["white_level"], spec["exposure_multiplier"], spec["noise_level"]]
+        vals += spec["scale_mul"] + spec["rgb_cam"] + spec["raw_nlf"]
+        for row in spec["pyramid_nlf"]:
+            vals += row
+        for dp in spec["denoise"]:
+            vals += [dp["luma"], dp["chroma"], dp["chromaBoost"], dp["gradientBoost"], dp["sharpening"]]
+        r = spec["rgb"]
+        vals += [r["contrast"], r["saturation"], r["toneCurveSlope"], r["exposureBias"], r["blacks"]]
+        l = spec["ltm"]
+        vals += [l["guidedFilterEps"], l["shadows"], l["highlights"], l["detail"]]
+        with open(os.path.join(d, "params.txt"), "w") as f:
+            f.write(" ".join(repr(float(v)) if isinstance(v, float) else str(v) for v in vals))
+        res = subprocess.run([exe, d], capture_output=True, text=True, timeout=300)
+        assert res.returncode == 0, res.stderr
+        got = np.fromfile(os.path.join(d, "rgb.u8"), np.uint8).reshape(128, 192, 3)
+        nlf = np.array(open(os.path.join(d, "nlf.txt")).read().split(), np.float32)
+    ref = orc.demosaic(raw, oracle_params(spec), orc.F32, want=("rgba8",))
+    np.testing.assert_array_equal(got, ref["rgba8"][..., :3])
+    np.testing.assert_allclose(nlf, ref["raw_nlf"], rtol=1e-6)
