@@ -511,7 +511,7 @@ gls_status gls_convert_to_srgb(gls_ctx* ctx, const gls_image_desc* linear, const
         GLS_CHECK(same_size(ctx, linear, ltm_mask, "convertTosRGB"));
         mk = ref_of(ltm_mask);
     }
-    RgbParams rp{p->contrast, p->saturation, p->toneCurveSlope, p->exposureBias, p->blacks, p->localToneMapping};
+    const RgbParams rp = rgb_params_init(p->contrast, p->saturation, p->toneCurveSlope, p->exposureBias, p->blacks, p->localToneMapping);
     launch_srgb(ctx, ref_of(linear), p->localToneMapping ? &mk : nullptr, out->ptr, out->format == GLS_RGBA_F32,
                 pitch_elems(out), rgb_cam, rp);
     return check_launch(ctx, "convertTosRGB");

@@ -36,9 +36,11 @@
 #if defined(__CUDACC__)
 #define GLS_HD __host__ __device__ __forceinline__
 #define GLS_HDM __host__ __device__ __forceinline__
+#define GLS_HDN static __host__ __device__ __noinline__
 #else
 #define GLS_HD static inline
 #define GLS_HDM inline
+#define GLS_HDN static __attribute__((noinline))
 #endif
 
 namespace glsm {
@@ -151,32 +153,52 @@ GLS_HD float rcp_(float d) {
 struct FastDiv {
     float d, y;
     bool ok;
+    // divisor range [2^-60, 2^30] and numerator range {0} u [2^-83, 2^60] keep the quotient
+    // in [2^-113, 2^120] and the residual above 2^-107: every intermediate is normal
     GLS_HDM void init(float den) {
         d = den;
         const float ad = fabs_(den);
-        ok = ad >= 8.67361738e-19f && ad <= 1.15292150e18f;  // [2^-60, 2^60]
+        ok = ad >= 8.67361738e-19f && ad <= 1073741824.0f;
         y = ok ? rcp_(den) : 0.0f;
     }
     GLS_HDM float operator()(float x) const {
-        const float ax = fabs_(x);
-        if (!ok || !(ax >= 8.67361738e-19f && ax <= 1.15292150e18f)) return div_(x, d);
+        if (!ok || !in_range(x)) return div_(x, d);
+        return fast(x);
+    }
+    // the shortcut alone: exact when ok and in_range(x) (x == 0 gives a zero of either sign)
+    GLS_HDM float fast(float x) const {
         const float q0 = x * y;
         const float r = fma_(-q0, d, x);
         return fma_(r, y, q0);
+    }
+    GLS_HDM static bool in_range(float x) {
+        const float ax = fabs_(x);
+        return ax <= 1.15292150e18f && (ax >= 1.03397577e-25f || ax == 0.0f);
+    }
+    // a value whose differences with any other such value stay in_range
+    GLS_HDM static bool operand_ok(float v) {
+        const float av = fabs_(v);
+        return av <= 5.76460752e17f && (av >= 8.67361738e-19f || av == 0.0f);  // [2^-60, 2^59]
     }
 };
 
 // smoothstep with the interpolation denominator e1 - e0 shared by many evaluations: the
 // division is only evaluated where the clamp does not decide the result by itself
 // (num <= 0 or NaN clamps to 0, num >= den > 0 clamps to 1, exactly as the literal form).
+// out-of-line literal operations for the rare paths (keeps the unrolled loops compact)
+GLS_HDN float div_slow(float a, float b) { return div_(a, b); }
+GLS_HDN float sqrt_slow(float a) { return sqrt_(a); }
+GLS_HDN float smoothstep_slow(float num, float den) {
+    const float t = clamp_(div_(num, den), 0.0f, 1.0f);
+    return t * t * (3.0f - 2.0f * t);
+}
+
 GLS_HD float smoothstep_den(float e0, const FastDiv& den, float x) {
     const float num = x - e0;
-    float t;
-    if (den.d > 0.0f && den.d <= 3.4e38f) {
-        t = !(num > 0.0f) ? 0.0f : (num >= den.d ? 1.0f : den(num));
-    } else {
-        t = clamp_(div_(num, den.d), 0.0f, 1.0f);
-    }
+    if (!(den.ok && den.d > 0.0f)) return smoothstep_slow(num, den.d);
+    // 0 < num < den <= 2^60: num >= 2^-60 makes the shortcut exact
+    const float t = !(num > 0.0f) ? 0.0f
+                    : (num >= den.d ? 1.0f : (num >= 8.67361738e-19f ? den.fast(num) : div_slow(num, den.d)));
     return t * t * (3.0f - 2.0f * t);
 }
 
@@ -185,12 +207,8 @@ GLS_HD float smoothstep_den(float e0, const FastDiv& den, float x) {
 GLS_HD float smoothstep_(float e0, float e1, float x) {
     const float den = e1 - e0;
     const float num = x - e0;
-    float t;
-    if (den > 0.0f && den <= 3.4e38f) {
-        t = !(num > 0.0f) ? 0.0f : (num >= den ? 1.0f : div_(num, den));
-    } else {
-        t = clamp_(div_(num, den), 0.0f, 1.0f);
-    }
+    if (!(den > 0.0f && den <= 3.4e38f)) return smoothstep_slow(num, den);
+    const float t = !(num > 0.0f) ? 0.0f : (num >= den ? 1.0f : div_slow(num, den));
     return t * t * (3.0f - 2.0f * t);
 }
 
@@ -212,8 +230,10 @@ struct SqrtGe {
             if (q < lo) return false;
             if (q > hi) return true;
         }
-        return sqrt_(q) >= e;
+        return sqrt_slow(q) >= e;
     }
+    // true when q is close enough to e^2 that only the literal test decides
+    GLS_HDM bool ambiguous(float q) const { return q >= lo && q <= hi; }
 };
 
 // The reference's own min/max/abs macros (demosaic.cl:56-65): plain selects.

@@ -397,8 +397,35 @@ struct LumaOf {
     GLS_DI float at(int x, int y) const { return im.at(x, y).x; }
 };
 
+// The bilateral sum with the literal divisions and square roots (rare path).
 template <class Acc4>
-GLS_DI float4 bilateral_px(const Acc4& im, int px, int py, const Nlf6& n, float chromaBoost, float gradientBoost) {
+__device__ __noinline__ float4 bilateral_literal(const Acc4& im, int px, int py, float sig0, float sig1, float sig2,
+                                                 float e0, float e1) {
+    const float4 c = im.at(px, py);
+    float f0 = 0.0f, f1 = 0.0f, f2 = 0.0f, n0 = 0.0f, n1 = 0.0f, n2 = 0.0f;
+    for (int y = -2; y <= 2; y++) {
+        for (int x = -2; x <= 2; x++) {
+            const float4 s = im.at(px + x, py + y);
+            const float d0 = div_(s.x - c.x, sig0), d1 = div_(s.y - c.y, sig1), d2 = div_(s.z - c.z, sig2);
+            const float l = length3_(d0, d1, d2);
+            const float w0 = 1.0f - step_(e0, l), w1 = 1.0f - step_(e1, l);
+            f0 = f0 + w0 * s.x;
+            n0 = n0 + w0;
+            f1 = f1 + w1 * s.y;
+            n1 = n1 + w1;
+            f2 = f2 + w1 * s.z;
+            n2 = n2 + w1;
+        }
+    }
+    return make_float4(div_(f0, n0), div_(f1, n1), div_(f2, n2), 0.0f);
+}
+
+// CHECK: test every sample difference against the division shortcut's exact range; a
+// caller that has verified every value of the 5x5 window with FastDiv::operand_ok passes
+// CHECK = false and values_ok = true instead.
+template <bool CHECK, class Acc4>
+GLS_DI float4 bilateral_px(const Acc4& im, int px, int py, const Nlf6& n, float chromaBoost, float gradientBoost,
+                           bool values_ok = true) {
     const float4 c = im.at(px, py);
     const float sig0 = sqrt_(n.a[0] + n.b[0] * c.x);
     const float sig1 = sqrt_(n.a[1] + n.b[1] * c.x);
@@ -412,7 +439,9 @@ GLS_DI float4 bilateral_px(const Acc4& im, int px, int py, const Nlf6& n, float 
     }
     // weight = 1 - step(edge, length(diff)) = !(sqrt_rn(|diff|^2) >= edge), decided on the
     // squared length; the divisions by sigma share their divisor; the weights are 0 or 1,
-    // so w * s is exact and the multiply-add can be fused without changing a bit.
+    // so w * s is exact and the multiply-add can be fused without changing a bit.  Any
+    // sample outside the shortcuts' exact range, or too close to an edge to decide
+    // without the square root, sends the pixel to the literal evaluation.
     SqrtGe ge0, ge1;
     ge0.init(lumaBoost * GLS_SQRT2_F);
     ge1.init(chromaBoost * GLS_SQRT2_F);
@@ -420,15 +449,21 @@ GLS_DI float4 bilateral_px(const Acc4& im, int px, int py, const Nlf6& n, float 
     dv0.init(sig0);
     dv1.init(sig1);
     dv2.init(sig2);
+    if (!(values_ok && dv0.ok && dv1.ok && dv2.ok && ge0.ok && ge1.ok))
+        return bilateral_literal(im, px, py, sig0, sig1, sig2, ge0.e, ge1.e);
     float f0 = 0.0f, f1 = 0.0f, f2 = 0.0f, n0 = 0.0f, n1 = 0.0f, n2 = 0.0f;
-#pragma unroll
+    bool redo = false;
+#pragma unroll 1
     for (int y = -2; y <= 2; y++) {
 #pragma unroll
         for (int x = -2; x <= 2; x++) {
             const float4 s = im.at(px + x, py + y);
-            const float d0 = dv0(s.x - c.x), d1 = dv1(s.y - c.y), d2 = dv2(s.z - c.z);
+            const float x0 = s.x - c.x, x1 = s.y - c.y, x2 = s.z - c.z;
+            if (CHECK) redo |= !(FastDiv::in_range(x0) && FastDiv::in_range(x1) && FastDiv::in_range(x2));
+            const float d0 = dv0.fast(x0), d1 = dv1.fast(x1), d2 = dv2.fast(x2);
             const float q = d0 * d0 + d1 * d1 + d2 * d2;
-            const float w0 = ge0(q) ? 0.0f : 1.0f, w1 = ge1(q) ? 0.0f : 1.0f;
+            redo |= ge0.ambiguous(q) || ge1.ambiguous(q);
+            const float w0 = q < ge0.lo ? 1.0f : 0.0f, w1 = q < ge1.lo ? 1.0f : 0.0f;
             f0 = glsm::fma_(w0, s.x, f0);
             n0 = n0 + w0;
             f1 = glsm::fma_(w1, s.y, f1);
@@ -437,6 +472,7 @@ GLS_DI float4 bilateral_px(const Acc4& im, int px, int py, const Nlf6& n, float 
             n2 = n2 + w1;
         }
     }
+    if (redo) return bilateral_literal(im, px, py, sig0, sig1, sig2, ge0.e, ge1.e);
     return make_float4(div_(f0, n0), div_(f1, n1), div_(f2, n2), 0.0f);
 }
 
@@ -569,17 +605,35 @@ GLS_DI float ltm_mask_px(const AccIn& in, const AccG& guide, int x, int y, int w
 struct RgbParams {
     float contrast, saturation, toneCurveSlope, exposureBias, blacks;
     int localToneMapping;
+    // per-frame constants of convertTosRGB, evaluated once (rgb_params_init): the exposure
+    // factor powr(2, exposureBias) and the tone curve's sigmoid(0, s), sigmoid(1, s) - sigmoid(0, s)
+    float eb, sig0, sig_den;
 };
 
-GLS_DI float sigmoid_(float x, float s) { return 0.5f * (glsm::tanh_(s * x - 0.3f * s) + 1.0f); }
+__host__ __device__ inline float sigmoid_(float x, float s) { return 0.5f * (glsm::tanh_(s * x - 0.3f * s) + 1.0f); }
 
-GLS_DI float tone_curve_(float x, float s) {
-    return div_(sigmoid_(sqrt_(0.95f * x), s) - sigmoid_(0.0f, s), sigmoid_(1.0f, s) - sigmoid_(0.0f, s));
+__host__ __device__ inline RgbParams rgb_params_init(float contrast, float saturation, float toneCurveSlope,
+                                                     float exposureBias, float blacks, int localToneMapping) {
+    RgbParams r;
+    r.contrast = contrast;
+    r.saturation = saturation;
+    r.toneCurveSlope = toneCurveSlope;
+    r.exposureBias = exposureBias;
+    r.blacks = blacks;
+    r.localToneMapping = localToneMapping;
+    r.eb = exposureBias != 0.0f ? glsm::powr_(2.0f, exposureBias) : 1.0f;
+    r.sig0 = sigmoid_(0.0f, toneCurveSlope);
+    r.sig_den = sigmoid_(1.0f, toneCurveSlope) - r.sig0;
+    return r;
+}
+
+GLS_DI float tone_curve_(float x, float s, float sig0, const FastDiv& den) {
+    return den(sigmoid_(sqrt_(0.95f * x), s) - sig0);
 }
 
 GLS_DI float3 srgb_px(float3 in, float ltm, const Mat3& m, const RgbParams& rp) {
     float p[3] = {in.x, in.y, in.z};
-    const float eb = rp.exposureBias != 0.0f ? glsm::powr_(2.0f, rp.exposureBias) : 1.0f;
+    const float eb = rp.eb;
 #pragma unroll
     for (int k = 0; k < 3; k++) p[k] = p[k] * eb;
     if (rp.saturation != 1.0f) {
@@ -599,8 +653,10 @@ GLS_DI float3 srgb_px(float3 in, float ltm, const Mat3& m, const RgbParams& rp) 
     }
     const float3 t = transform_px(m, make_float3(p[0], p[1], p[2]));
     float rgb[3] = {t.x, t.y, t.z};
+    FastDiv tden;
+    tden.init(rp.sig_den);
 #pragma unroll
-    for (int k = 0; k < 3; k++) rgb[k] = clamp_(tone_curve_(rgb[k], rp.toneCurveSlope), 0.0f, 1.0f);
+    for (int k = 0; k < 3; k++) rgb[k] = clamp_(tone_curve_(rgb[k], rp.toneCurveSlope, rp.sig0, tden), 0.0f, 1.0f);
     if (rp.localToneMapping) {
         const float boost = ltm;
         if (boost > 1.0f) {

@@ -177,19 +177,16 @@ __global__ void __launch_bounds__(kT) demosaic_kernel(DemosaicArgs a) {
         for (int p = tid; p < GH * GW / 2; p += kT) {
             const int r = p / (GW / 2), k = p - r * (GW / 2);
             const int y = y0 - 2 + r;
-#pragma unroll
-            for (int e = 0; e < 2; e++) {
-                const int x = x0 - 2 + 2 * k + e;
-                if (x < 0 || x >= w || y < 0 || y >= h) continue;
-                float g;
-                if (green_needs_interp(x, y, bayer)) {
-                    const SobelMap sob{s_u, SH * SW, x0 - 4, y0 - 4, SW, x, y};
-                    g = green_at(R, x, y, lv, sob);
-                } else {
-                    g = R.at(x, y);
-                }
-                s_green[r * GW + 2 * k + e] = Storage<S>::round(g);
+            const int xa = x0 - 2 + 2 * k;
+            // every thread interpolates the red/blue site of its pair at the same time
+            const int e_rb = green_needs_interp(xa, y, bayer) ? 0 : 1;
+            const int xr = xa + e_rb, xg = xa + (1 - e_rb);
+            const bool yin = y >= 0 && y < h;
+            if (yin && xr >= 0 && xr < w) {
+                const SobelMap sob{s_u, SH * SW, x0 - 4, y0 - 4, SW, xr, y};
+                s_green[r * GW + 2 * k + e_rb] = Storage<S>::round(green_at(R, xr, y, lv, sob));
             }
+            if (yin && xg >= 0 && xg < w) s_green[r * GW + 2 * k + 1 - e_rb] = Storage<S>::round(R.at(xg, y));
         }
     }
     __syncthreads();
@@ -328,11 +325,14 @@ __global__ void __launch_bounds__(kT) denoise_reasm_kernel(DenoiseArgs a) {
     __shared__ float4 s_in[PW * PH];
     const int x0 = blockIdx.x * DW, y0 = blockIdx.y * DH;
     const GImg4<SIn> gin{(const typename Storage<SIn>::T4*)a.in, a.w, a.h, a.pitch};
+    bool ok = true;
     for (int i = threadIdx.x; i < PW * PH; i += kT) {
         const int r = i / PW, c = i - r * PW;
-        s_in[i] = gin.at(x0 - 2 + c, y0 - 2 + r);
+        const float4 v = gin.at(x0 - 2 + c, y0 - 2 + r);
+        ok &= FastDiv::operand_ok(v.x) && FastDiv::operand_ok(v.y) && FastDiv::operand_ok(v.z);
+        s_in[i] = v;
     }
-    __syncthreads();
+    const bool tile_ok = __syncthreads_and(ok);
     const SAcc4f I{s_in, x0 - 2, y0 - 2, PW};
     Nlf6 n;
 #pragma unroll
@@ -346,7 +346,8 @@ __global__ void __launch_bounds__(kT) denoise_reasm_kernel(DenoiseArgs a) {
     for (int i = threadIdx.x; i < DW * DH; i += kT) {
         const int r = i / DW, c = i - r * DW, x = x0 + c, y = y0 + r;
         if (x >= a.w || y >= a.h) continue;
-        float4 d = ALGO == 0 ? bilateral_px(I, x, y, n, a.chroma_boost, a.gradient_boost) : guided_fast_px(I, x, y, n);
+        float4 d = ALGO == 0 ? bilateral_px<false>(I, x, y, n, a.chroma_boost, a.gradient_boost, tile_ok)
+                             : guided_fast_px(I, x, y, n);
         d = round4<S>(d);
         if (REASM) d = round4<S>(reassemble_px(d, i1, d1, x, y, a.w, a.h, a.cw, a.ch, a.sharpening, n.a[0], n.b[0]));
         Storage<S>::st4((T4*)a.out + (size_t)y * a.opitch + x, d);
@@ -358,7 +359,8 @@ __global__ void __launch_bounds__(kT) denoise_reasm_kernel(DenoiseArgs a) {
 // mapping samples its input bilinearly), then the LTM mask, YCbCr -> camera and
 // convertTosRGB.  32x16 output tiles.
 // =========================================================================================
-constexpr int FW = 32, FH = 16;
+// 30x14 outputs: the denoised tile with its ring is 32x16 = 2 positions per thread
+constexpr int FW = 30, FH = 14;
 
 template <class S, int ALGO, bool LTM, bool OUT_F32>
 __global__ void __launch_bounds__(kT) final_kernel(FinalArgs a) {
@@ -368,14 +370,18 @@ __global__ void __launch_bounds__(kT) final_kernel(FinalArgs a) {
     __shared__ float4 s_den[EW * EH];
     const int x0 = blockIdx.x * FW, y0 = blockIdx.y * FH;
     const int w = a.w, h = a.h;
-    const GImg4<__half> gl0{a.level0, w, h, a.l0_pitch};
+    bool ok = true;
     for (int i = threadIdx.x; i < PW * PH; i += kT) {
         const int r = i / PW, c = i - r * PW;
         const int gx = clampi(x0 - 3 + c, 0, w - 1), gy = clampi(y0 - 3 + r, 0, h - 1);
         const uint2 u = __ldg(reinterpret_cast<const uint2*>(a.level0 + (size_t)gy * a.l0_pitch + gx));
-        *reinterpret_cast<uint2*>(&s_l0[i]) = u;
+        half4 hv;
+        *reinterpret_cast<uint2*>(&hv) = u;
+        const float4 v = Storage<__half>::cvt(hv);
+        ok &= FastDiv::operand_ok(v.x) && FastDiv::operand_ok(v.y) && FastDiv::operand_ok(v.z);
+        s_l0[i] = hv;
     }
-    __syncthreads();
+    const bool tile_ok = __syncthreads_and(ok);
     const SAcc4h L0{s_l0, x0 - 3, y0 - 3, PW};
     Nlf6 n;
 #pragma unroll
@@ -389,7 +395,8 @@ __global__ void __launch_bounds__(kT) final_kernel(FinalArgs a) {
     for (int i = threadIdx.x; i < EW * EH; i += kT) {
         const int r = i / EW, c = i - r * EW, x = x0 - 1 + c, y = y0 - 1 + r;
         if (x < 0 || x >= w || y < 0 || y >= h) continue;
-        float4 d = ALGO == 0 ? bilateral_px(L0, x, y, n, a.chroma_boost, a.gradient_boost) : guided_fast_px(L0, x, y, n);
+        float4 d = ALGO == 0 ? bilateral_px<false>(L0, x, y, n, a.chroma_boost, a.gradient_boost, tile_ok)
+                             : guided_fast_px(L0, x, y, n);
         d = round4<S>(d);
         d = round4<S>(reassemble_px(d, i1, d1, x, y, w, h, a.cw, a.ch, a.sharpening, n.a[0], n.b[0]));
         s_den[i] = d;

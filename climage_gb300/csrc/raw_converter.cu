@@ -366,7 +366,7 @@ struct gls_raw_converter {
         for (int k = 0; k < 9; k++) f.icy.m[k] = inv[k] * p->exposure_multiplier;
         memcpy(f.rgb_cam.m, p->rgb_cam, sizeof(f.rgb_cam.m));
         const gls_rgb_conversion_params& rc = p->rgb_conversion;
-        f.rgb = RgbParams{rc.contrast, rc.saturation, rc.toneCurveSlope, rc.exposureBias, rc.blacks, rc.localToneMapping};
+        f.rgb = rgb_params_init(rc.contrast, rc.saturation, rc.toneCurveSlope, rc.exposureBias, rc.blacks, rc.localToneMapping);
         f.out = out;
         f.opitch = opitch;
         f.tap_den = tap_ptr(3);
@@ -465,7 +465,7 @@ struct gls_raw_converter {
         launch_transform(ctx, denoised, denoised, icy_e);
         mark("transformImage");
         const gls_rgb_conversion_params& rc = p->rgb_conversion;
-        RgbParams rp{rc.contrast, rc.saturation, rc.toneCurveSlope, rc.exposureBias, rc.blacks, rc.localToneMapping};
+        const RgbParams rp = rgb_params_init(rc.contrast, rc.saturation, rc.toneCurveSlope, rc.exposureBias, rc.blacks, rc.localToneMapping);
         launch_srgb(ctx, denoised, ltm ? &mask : nullptr, out, out_float, opitch, p->rgb_cam, rp);
         mark("convertTosRGB");
         collect();
@@ -658,7 +658,7 @@ gls_status gls_raw_converter_fast_demosaic(gls_raw_converter* c, const gls_image
     launch_fast_debayer(ctx, c->scaled, half_rgb, p->bayer_pattern);
     launch_highlights(ctx, half_rgb, half_rgb, 1.0f);
     const gls_rgb_conversion_params& rc = p->rgb_conversion;
-    RgbParams rp{rc.contrast, rc.saturation, rc.toneCurveSlope, rc.exposureBias, rc.blacks, 0};
+    const RgbParams rp = rgb_params_init(rc.contrast, rc.saturation, rc.toneCurveSlope, rc.exposureBias, rc.blacks, 0);
     launch_srgb(ctx, half_rgb, nullptr, out->ptr, out->format == GLS_RGBA_F32, pitch_elems(out), p->rgb_cam, rp);
     return check_launch(ctx, "RawConverter::fastDemosaicImage");
 }
