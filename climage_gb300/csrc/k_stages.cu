@@ -521,8 +521,9 @@ void launch_fast_debayer(gls_ctx* ctx, const ImgRef& raw, const ImgRef& rgb, int
 size_t guided_filter_scratch_bytes(int w, int h) {
     const size_t n = (size_t)w * h;
     // meanI (+ transposed temp) in storage precision (<= 16 B/px each), p1, p2, ipr, ipg,
-    // ipb, inv1, inv2 and an fp32 transposed temp
-    return n * (16 + 16 + 16 + 8 + 16 * 3 + 16 + 8 + 16) + 1024;
+    // ipb, inv1, inv2 and an fp32 transposed temp; each of the 10 buffers starts on a
+    // 256-byte boundary, so up to 255 bytes of padding follow each one
+    return n * (16 + 16 + 16 + 8 + 16 * 3 + 16 + 8 + 16) + 10 * 256;
 }
 
 void launch_guided_filter(gls_ctx* ctx, const ImgRef& in, const ImgRef& out, int fs, const NlfArg& eps, void* scratch) {

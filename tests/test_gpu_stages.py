@@ -278,6 +278,9 @@ def test_odd_sizes_rgba_stages(ctx, w, h):
     ctx.despeckleImage(dev(img), va, vb, out)
     torch.cuda.synchronize()
     assert mismatch(host(out), orc.despeckle(img, va, vb)) == 0
+    ctx.guidedFilter(dev(img), 3, [4e-4, 1e-4, 1.2e-4], out)
+    torch.cuda.synchronize()
+    assert mismatch(host(out), orc.guided_filter(img, 3, [4e-4, 1e-4, 1.2e-4])) == 0
     ow, oh = max(1, w // 2), max(1, h // 2)
     ds = empty((oh, ow, 4))
     ctx.downsampleImage(dev(img), ds)
