@@ -16,6 +16,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libgls_cuda.so")
 
 GLS_OK = 0
+GLS_ERR_INVALID_SIZE = 2
+# image size limit of Context.guidedFilterNoAlloc (gls_cuda.h)
+GUIDED_FILTER_NOALLOC_MAX_PIXELS = 116490
 STATUS = {0: "ok", 1: "invalid argument", 2: "invalid size", 3: "unsupported", 4: "CUDA error",
           5: "out of memory", 6: "timeout", 7: "unsupported pixel format"}
 
@@ -103,6 +106,7 @@ SIGNATURES = [
     ("gls_denoise_image", _I, [_P, _D, _FP, _FP, _F, _F, _D]),
     ("gls_denoise_image_guided", _I, [_P, _D, _FP, _FP, _D]),
     ("gls_guided_filter", _I, [_P, _D, _I, _FP, _D]),
+    ("gls_guided_filter_noalloc", _I, [_P, _D, _I, _FP, _D]),
     ("gls_reassemble_image", _I, [_P, _D, _D, _D, _F, _FP, _D]),
     ("gls_local_tone_mapping_mask", _I, [_P, _D, _D, ctypes.POINTER(LTMParams), _FP, _D]),
     ("gls_convert_to_srgb", _I, [_P, _D, _D, _D, _FP, ctypes.POINTER(RGBConversionParams)]),
@@ -309,6 +313,12 @@ class Context:
     def guidedFilter(self, inp, filter_size, eps, out):
         self.check(self._lib.gls_guided_filter(self.handle, desc(inp), int(filter_size), farr(eps, 3), desc(out)),
                    "GuidedFilter::filter")
+
+    def guidedFilterNoAlloc(self, inp, filter_size, eps, out):
+        """guidedFilter over the library's static scratch: allocates nothing, images of at
+        most GUIDED_FILTER_NOALLOC_MAX_PIXELS pixels; overlapping calls race."""
+        self.check(self._lib.gls_guided_filter_noalloc(self.handle, desc(inp), int(filter_size), farr(eps, 3),
+                                                        desc(out)), "GuidedFilter::filter (no allocation)")
 
     def reassembleImage(self, den0, img1, den1, sharpening, nlf, out):
         self.check(self._lib.gls_reassemble_image(self.handle, desc(den0), desc(img1), desc(den1), float(sharpening),

@@ -161,6 +161,26 @@ GLS_API gls_status gls_denoise_image_guided(gls_ctx* ctx, const gls_image_desc* 
 /* GuidedFilter::filter (guided_filter.cpp:195-225) */
 GLS_API gls_status gls_guided_filter(gls_ctx* ctx, const gls_image_desc* in, int filter_size, const float eps[3],
                                      const gls_image_desc* out);
+/* GuidedFilter::filter that allocates nothing.  It has no counterpart in the reference: it
+ * serves callers that must not allocate device memory while they run (a frame loop that
+ * shares the GPU with other streams, where cudaMalloc/cudaFree would synchronise or fail
+ * under memory pressure; a process whose device footprint is fixed after start-up).
+ * Arguments, checks and results are those of gls_guided_filter, bit for bit.  Its scratch
+ * is one static device array of GLS_GUIDED_FILTER_NOALLOC_SCRATCH_BYTES (16 MiB), not the
+ * context's cudaMalloc'd scratch, so the image may hold at most
+ * GLS_GUIDED_FILTER_NOALLOC_MAX_PIXELS pixels; a larger one is rejected with
+ * GLS_ERR_INVALID_SIZE and a message giving both sizes, and nothing is launched.
+ * Set-up: the first call on a device, with the context's device current (required on every
+ * call), looks up the array's address there with cudaGetSymbolAddress, which loads the array
+ * onto that device; make that first call before any stream capture.  Later calls only launch
+ * kernels on the context's stream.  All calls on a device share the one array: calls whose
+ * work overlaps on the GPU (other streams, other contexts or threads) race on it and corrupt
+ * each other's results, so serialise them.  Nothing in the array has to start at zero (each
+ * call writes every buffer in full before reading it), so no call clears it. */
+#define GLS_GUIDED_FILTER_NOALLOC_SCRATCH_BYTES (16u << 20)
+#define GLS_GUIDED_FILTER_NOALLOC_MAX_PIXELS 116490
+GLS_API gls_status gls_guided_filter_noalloc(gls_ctx* ctx, const gls_image_desc* in, int filter_size,
+                                             const float eps[3], const gls_image_desc* out);
 /* reassembleImage (demosaic_cl.cpp:182-208); den0 may equal out */
 GLS_API gls_status gls_reassemble_image(gls_ctx* ctx, const gls_image_desc* den0, const gls_image_desc* img1,
                                         const gls_image_desc* den1, float sharpening, const float nlf[2],
