@@ -14,8 +14,8 @@ struct RawPass1Args {
     float sm[4];  // scale factor per (y & 1) * 2 + (x & 1)
     float black;
     NlfThresholds th;
-    double* part_d;
-    float* part_f;
+    NlfScratch nlf;  // regression scratch (set by the launcher)
+    float* nlf_out;  // fitted {A0..3, B0..3}
 };
 
 struct DemosaicArgs {
@@ -41,8 +41,8 @@ struct LevelPass1Args {
     void* out;  // downsampled level (null for the coarsest level)
     int ow, oh, opitch;
     NlfThresholds th;
-    double* part_d;
-    float* part_f;
+    NlfScratch nlf;  // regression scratch (set by the launcher)
+    float* nlf_out;  // fitted {A0..2, B0..2}
 };
 
 struct DenoiseArgs {

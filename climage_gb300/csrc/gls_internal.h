@@ -69,24 +69,42 @@ struct NlfFit {
     int pad;
 };
 
-// Scratch layout for one regression: fit state + per-block partial sums.
+// Scratch layout for one regression: fit state, the block ticket, and per-block partial
+// sums (pass 1 and 3: 128-bit fixed point + NaN masks; pass 2: doubles; pass 1: min/max).
+// The ticket must be zero before a pass starts; the last block of every pass resets it.
 constexpr int kNlfMaxBlocks = 1024;
 constexpr int kNlfK = 1 + 5 * 4;   // N + 5 sums x 4 channels
 constexpr int kNlfKF = 4 * 4;      // min/max of m and v per channel
-constexpr size_t kNlfScratchBytes =
-    256 + sizeof(double) * kNlfMaxBlocks * kNlfK + sizeof(float) * kNlfMaxBlocks * kNlfKF;
+constexpr size_t kNlfHeaderBytes = 256;
+constexpr size_t kNlfPartIBytes = 16 * (size_t)kNlfMaxBlocks * kNlfK;
+constexpr size_t kNlfPartNanBytes = sizeof(unsigned) * (size_t)kNlfMaxBlocks;
+constexpr size_t kNlfPartDBytes = sizeof(double) * (size_t)kNlfMaxBlocks * kNlfK;
+constexpr size_t kNlfPartFBytes = sizeof(float) * (size_t)kNlfMaxBlocks * kNlfKF;
+constexpr size_t kNlfScratchBytes = kNlfHeaderBytes + kNlfPartIBytes + kNlfPartNanBytes + kNlfPartDBytes + kNlfPartFBytes;
+static_assert(sizeof(NlfFit) <= 128, "fit state and ticket share the 256-byte header");
 
 struct NlfScratch {
     NlfFit* fit;
-    double* part_d;
-    float* part_f;
+    unsigned* ticket;            // blocks of the current pass that have written their row
+    unsigned long long* part_i;  // [block][kNlfK] x {lo, hi}
+    unsigned* part_nan;          // [block]: bit k set when column k summed a NaN
+    double* part_d;              // [block][kNlfK]
+    float* part_f;               // [block][kNlfKF]
 };
 
 inline NlfScratch nlf_scratch_at(void* base) {
+    char* p = reinterpret_cast<char*>(base);
     NlfScratch s;
-    s.fit = reinterpret_cast<NlfFit*>(base);
-    s.part_d = reinterpret_cast<double*>(reinterpret_cast<char*>(base) + 256);
-    s.part_f = reinterpret_cast<float*>(reinterpret_cast<char*>(base) + 256 + sizeof(double) * kNlfMaxBlocks * kNlfK);
+    s.fit = reinterpret_cast<NlfFit*>(p);
+    s.ticket = reinterpret_cast<unsigned*>(p + 128);
+    p += kNlfHeaderBytes;
+    s.part_i = reinterpret_cast<unsigned long long*>(p);
+    p += kNlfPartIBytes;
+    s.part_nan = reinterpret_cast<unsigned*>(p);
+    p += kNlfPartNanBytes;
+    s.part_d = reinterpret_cast<double*>(p);
+    p += kNlfPartDBytes;
+    s.part_f = reinterpret_cast<float*>(p);
     return s;
 }
 

@@ -1,7 +1,7 @@
 // gls_nlf.cuh -- device side of the noise-model regressions (computeNoiseStatistics /
 // computeRawNoiseStatistics, CLImage/app/src/main/cpp/pyramidal_denoise.cpp:161-362):
-// statistics sources, the explicit FP64 passes, the parallel deterministic solve, and
-// the launcher that finishes a fit once pass-1 partial sums exist.  Included by k_nlf.cu
+// statistics sources, exact fixed-point partial sums, the solves run by the last block of
+// each pass, the explicit FP64 passes, and the launchers.  Included by k_nlf.cu
 // (single-stage regressions) and k_fused.cu (pass 1 fused into the pyramid kernels); the
 // kernels have internal linkage in each translation unit.
 #ifndef GLS_NLF_CUH
@@ -114,12 +114,128 @@ GLS_DI void block_minmax_write(float (&mn)[K], float (&mx)[K], float* out) {
     __syncthreads();
 }
 
-// Per-thread pass-1 accumulator.  Partial record (doubles): [0] N, then per channel c at
-// 1+5c: sx, sxx, sy, sxy, syy.  Float record: [0..2NC) minimum of (m_c, v_c),
-// [2NC..4NC) maximum.  All threads of the block must call write().
+// ---- exact fixed-point partial sums ----
+// Each thread sums its pixels in float-float pairs.  From there on the pass-1 and pass-3
+// sums travel as 128-bit two's-complement integers in units of 2^-R, R fixed per column, so
+// the block and grid reductions are exact: the totals depend neither on the order of the
+// additions nor on the number of blocks, and integer adds replace FP64 ones (GB300 runs FP64
+// at a small fraction of its FP32 rate).  Every selected term is bounded (0.001 <= m <= 0.5,
+// 0 <= v <= 0.001), so with fewer than 2^31 selected pixels no column total reaches 2^126
+// units, and the resolutions (2^-95 for sx ... 2^-114 for syy) lie far below the rounding
+// of the doubles the fit uses.
+struct I128 {
+    unsigned long long lo, hi;  // value = hi * 2^64 + lo, two's complement
+};
+
+// R of column k of a record [N, then per channel (sx, sxx, sy, sxy, syy)]
+GLS_DI int fixed_scale(int k) {
+    if (k == 0) return 0;
+    switch ((k - 1) % 5) {
+        case 0: return 95;
+        case 1: return 96;
+        case 2: return 104;
+        case 3: return 105;
+        default: return 114;
+    }
+}
+
+GLS_DI void i128_add(I128& a, const I128& b) {
+    const unsigned long long lo = a.lo + b.lo;
+    a.hi += b.hi + (lo < a.lo ? 1ull : 0ull);
+    a.lo = lo;
+}
+
+GLS_DI I128 i128_neg(I128 a) {
+    a.lo = ~a.lo + 1ull;
+    a.hi = ~a.hi + (a.lo == 0ull ? 1ull : 0ull);
+    return a;
+}
+
+// x * 2^R rounded to the nearest integer, ties to even.  x is finite with |x| * 2^R < 2^127
+// (a larger x is clamped to that range; the column bounds rule it out).
+GLS_DI I128 f32_to_fixed(float x, int R) {
+    const unsigned b = __float_as_uint(x);
+    const int ef = (int)((b >> 23) & 0xffu);
+    unsigned long long m = b & 0x7fffffu;
+    if (ef != 0) m |= 0x800000ull;
+    int s = (ef == 0 ? -149 : ef - 150) + R;  // |x| * 2^R = m * 2^s, m < 2^24
+    if (s > 103) s = 103;
+    I128 r{0ull, 0ull};
+    if (m == 0ull) return r;
+    if (s >= 64) {
+        r.hi = m << (s - 64);
+    } else if (s > 0) {
+        r.lo = m << s;
+        r.hi = m >> (64 - s);
+    } else if (s == 0) {
+        r.lo = m;
+    } else if (s > -25) {
+        const int k = -s;
+        unsigned long long q = m >> k;
+        const unsigned long long rem = m & ((1ull << k) - 1ull), half = 1ull << (k - 1);
+        if (rem > half || (rem == half && (q & 1ull))) q++;
+        r.lo = q;
+    }  // else m * 2^s < 1/2: rounds to 0
+    return (b >> 31) ? i128_neg(r) : r;
+}
+
+GLS_DI double pow2_d(int e) { return __longlong_as_double((long long)(e + 1023) << 52); }  // |e| <= 1022
+
+// a * 2^-R rounded once to the nearest double (ties to even)
+GLS_DI double fixed_to_f64(I128 a, int R) {
+    const bool neg = (long long)a.hi < 0;
+    if (neg) a = i128_neg(a);
+    double d;
+    if (a.hi == 0ull) {
+        d = __ull2double_rn(a.lo);
+    } else {
+        // the top 64 bits, with every lower bit folded into a sticky bit 0, round as the
+        // full value does (64 bits keep the 53 of the double plus guard and round bits)
+        const int lz = __clzll((long long)a.hi);
+        const unsigned long long top = lz ? (a.hi << lz) | (a.lo >> (64 - lz)) : a.hi;
+        const unsigned long long rest = lz ? a.lo << lz : a.lo;
+        d = __ull2double_rn(top | (rest ? 1ull : 0ull)) * pow2_d(64 - lz);
+    }
+    d *= pow2_d(-R);
+    return neg ? -d : d;
+}
+
+GLS_DI I128 warp_sum_i128(I128 v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        I128 w;
+        w.lo = __shfl_xor_sync(0xffffffffu, v.lo, o);
+        w.hi = __shfl_xor_sync(0xffffffffu, v.hi, o);
+        i128_add(v, w);
+    }
+    return v;
+}
+
+constexpr int kWarps = kThreads / 32;
+
+// One fixed-point column of the block's row: lane 0 of each warp leaves its warp's sum in
+// red[warp][k]; a NaN or infinite pair sets bit k of nan instead of being summed.
+template <int K>
+GLS_DI void fixed_column(const FF& f, int k, I128 (&red)[kWarps][K], unsigned& nan) {
+    const bool bad = !(isfinite(f.hi) && isfinite(f.lo));
+    I128 v{0ull, 0ull};
+    if (!bad) {
+        const int R = fixed_scale(k);
+        v = f32_to_fixed(f.hi, R);
+        i128_add(v, f32_to_fixed(f.lo, R));
+    }
+    v = warp_sum_i128(v);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][k] = v;
+    if (bad) nan |= 1u << k;
+}
+
+// Per-thread accumulator of passes 1 and 3.  Fixed-point record: [0] N, then per channel
+// c at 1+5c: sx, sxx, sy, sxy, syy.  Float record (pass 1): [0..2NC) minimum of (m_c, v_c),
+// [2NC..4NC) maximum.  All threads of the block must call the write functions.
 template <int MC, int NC>
 struct Pass1Acc {
     static constexpr int NM = (MC == 1) ? 1 : NC;
+    static constexpr int K = 1 + 5 * NC;
     FF sx[NM], sxx[NM], sy[NC], sxy[NC], syy[NC];
     float mn[2 * NC], mx[2 * NC];
     int n;
@@ -144,8 +260,8 @@ struct Pass1Acc {
         n = 0;
     }
 
-    GLS_DI void add(const float* m, const float* v, const NlfThresholds& th) {
-        if (!in_range<MC, NC>(m, v, th)) return;
+    // a pixel already known to be selected
+    GLS_DI void add_selected(const float* m, const float* v) {
         n++;
 #pragma unroll
         for (int c = 0; c < NC; c++) {
@@ -164,26 +280,204 @@ struct Pass1Acc {
         }
     }
 
-    GLS_DI void write(double* part_d, float* part_f) {
-        double vals[1 + 5 * NC];
-        vals[0] = (double)n;
+    GLS_DI void add(const float* m, const float* v, const NlfThresholds& th) {
+        if (in_range<MC, NC>(m, v, th)) add_selected(m, v);
+    }
+
+    // The block's fixed-point row (threads < K) and NaN mask (thread 0).
+    GLS_DI void write_fixed(unsigned long long* part_i, unsigned* part_nan) const {
+        __shared__ I128 red[kWarps][K];
+        __shared__ unsigned nanw[kWarps];
+        unsigned nan = 0;
+        {
+            I128 c0{(unsigned long long)n, 0ull};
+            c0 = warp_sum_i128(c0);
+            if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][0] = c0;
+        }
 #pragma unroll
         for (int c = 0; c < NC; c++) {
             const int cm = MC == 1 ? 0 : c;
-            vals[1 + 5 * c + 0] = ff_value(sx[cm]);
-            vals[1 + 5 * c + 1] = ff_value(sxx[cm]);
-            vals[1 + 5 * c + 2] = ff_value(sy[c]);
-            vals[1 + 5 * c + 3] = ff_value(sxy[c]);
-            vals[1 + 5 * c + 4] = ff_value(syy[c]);
+            fixed_column<K>(sx[cm], 1 + 5 * c + 0, red, nan);
+            fixed_column<K>(sxx[cm], 1 + 5 * c + 1, red, nan);
+            fixed_column<K>(sy[c], 1 + 5 * c + 2, red, nan);
+            fixed_column<K>(sxy[c], 1 + 5 * c + 3, red, nan);
+            fixed_column<K>(syy[c], 1 + 5 * c + 4, red, nan);
         }
-        block_reduce_write<1 + 5 * NC>(vals, part_d + (size_t)blockIdx.x * kNlfK);
-        block_minmax_write<2 * NC>(mn, mx, part_f + (size_t)blockIdx.x * kNlfKF);
+        nan = __reduce_or_sync(0xffffffffu, nan);
+        if ((threadIdx.x & 31) == 0) nanw[threadIdx.x >> 5] = nan;
+        __syncthreads();
+        if (threadIdx.x < K) {
+            I128 s = red[0][threadIdx.x];
+#pragma unroll
+            for (int w = 1; w < kWarps; w++) i128_add(s, red[w][threadIdx.x]);
+            unsigned long long* row = part_i + 2 * ((size_t)blockIdx.x * kNlfK + threadIdx.x);
+            row[0] = s.lo;
+            row[1] = s.hi;
+        }
+        if (threadIdx.x == 0) {
+            unsigned m = 0;
+#pragma unroll
+            for (int w = 0; w < kWarps; w++) m |= nanw[w];
+            part_nan[blockIdx.x] = m;
+        }
+        __syncthreads();
     }
+
+    GLS_DI void write_minmax(float* part_f) { block_minmax_write<2 * NC>(mn, mx, part_f + (size_t)blockIdx.x * kNlfKF); }
 };
+
+// Ticket of a pass: true in the one block that finishes last, once every block's row is
+// visible to it.  No block ever waits for another.
+GLS_DI bool last_block(unsigned* ticket) {
+    __shared__ unsigned s_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = (atomicAdd(ticket, 1u) == gridDim.x - 1) ? 1u : 0u;
+    __syncthreads();
+    const bool last = s_last != 0u;
+    if (last) __threadfence();
+    return last;
+}
+
+// std::max(v, a) as gls::max(DVector, double) evaluates it (gls_linalg.hpp:238-243)
+__device__ double refmax(double v, double a) { return (v < a) ? a : v; }
+
+__device__ void neumaier(double& s, double& c, double x) {
+    const double t = s + x;
+    if (fabs(s) >= fabs(x)) c += (s - t) + x;
+    else c += (x - t) + s;
+    s = t;
+}
+
+// The regression step (thread 0) from the column totals.  Stage 1 fits the pass-1 sums and
+// decides whether the explicit passes 2 and 3 are needed: it bounds every pass-1 residual
+// by the extremes of the selected statistics and, when even the largest possible squared
+// residual is below a lower bound of the RMS residual (computed from the sums), pass 3
+// provably keeps every pass-1 pixel and the pass-1 fit is final.  Stage 3 fits the refit sums.
+template <int NC>
+__device__ void fit_totals(const double* tot, const float* fmm, int stage, NlfFit* fit, float* out) {
+    const double N = tot[0];
+    double A[4], B[4];
+    for (int ch = 0; ch < NC; ch++) {
+        const double sx = tot[1 + 5 * ch], sxx = tot[2 + 5 * ch], sy = tot[3 + 5 * ch], sxy = tot[4 + 5 * ch];
+        B[ch] = refmax((N * sxy - sx * sy) / (N * sxx - sx * sx), 1e-8);
+        A[ch] = refmax((sy - B[ch] * sx) / N, 1e-8);
+    }
+    bool done = true;
+    if (stage == 1) {
+        fit->N1 = N;
+        for (int ch = 0; ch < NC; ch++) {
+            fit->A[ch] = A[ch];
+            fit->B[ch] = B[ch];
+            const double sx = tot[1 + 5 * ch], sxx = tot[2 + 5 * ch], sy = tot[3 + 5 * ch];
+            const double sxy = tot[4 + 5 * ch], syy = tot[5 + 5 * ch];
+            const double a = A[ch], b = B[ch];
+            const double t1 = N * a * a, t2 = 2.0 * a * b * sx, t3 = b * b * sxx;
+            const double t4 = -2.0 * a * sy, t5 = -2.0 * b * sxy, t6 = syy;
+            const double e = t1 + t2 + t3 + t4 + t5 + t6;
+            const double mag = fabs(t1) + fabs(t2) + fabs(t3) + fabs(t4) + fabs(t5) + fabs(t6);
+            const double e_lo = e - 1e-12 * mag;
+            bool skip = N > 0 && e_lo > 0 && a == a && b == b;
+            if (skip) {
+                const double rms_lo = sqrt(e_lo / N) * (1.0 - 1e-6);
+                const double mlo = (double)fmm[ch], mhi = (double)fmm[2 * NC + ch];
+                const double vlo = (double)fmm[NC + ch], vhi = (double)fmm[3 * NC + ch];
+                const double dmax = a + b * (b >= 0 ? mhi : mlo) - vlo;
+                const double dmin = a + b * (b >= 0 ? mlo : mhi) - vhi;
+                const double mabs_ = fmax(fabs(dmax), fabs(dmin));
+                skip = mabs_ * mabs_ * (1.0 + 1e-9) <= rms_lo;
+            }
+            if (!skip) done = false;
+        }
+        fit->mode = done ? 0 : 1;
+    } else {
+        fit->mode = 0;
+    }
+    if (done) {
+        for (int ch = 0; ch < NC; ch++) {
+            out[ch] = (float)A[ch];
+            out[NC + ch] = (float)B[ch];
+        }
+    }
+}
+
+// Solve of pass 1 (stage 1) or pass 3 (stage 3), run by the last block of the pass: exact
+// column totals over the nblocks rows (warp w sums columns w, w + 8, ...), NaN masks, the
+// pass-1 extremes, then the fit.  Leaves the ticket at zero for the next pass.
+template <int NC>
+GLS_DI void solve_fixed(const NlfScratch& s, int nblocks, int stage, float* out) {
+    constexpr int K = 1 + 5 * NC;
+    __shared__ double tot[K];
+    __shared__ float fmm[4 * NC];
+    __shared__ unsigned nanw[kWarps];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int k = warp; k < K; k += kWarps) {
+        I128 acc{0ull, 0ull};
+        for (int b = lane; b < nblocks; b += 32) {
+            const unsigned long long* row = s.part_i + 2 * ((size_t)b * kNlfK + k);
+            i128_add(acc, I128{__ldcg(row), __ldcg(row + 1)});
+        }
+        acc = warp_sum_i128(acc);
+        if (lane == 0) tot[k] = fixed_to_f64(acc, fixed_scale(k));
+    }
+    if (stage == 1) {
+        for (int k = warp; k < 4 * NC; k += kWarps) {
+            const bool is_min = k < 2 * NC;
+            float v = is_min ? glsm::inf_() : -glsm::inf_();
+            for (int b = lane; b < nblocks; b += 32) {
+                const float x = __ldcg(s.part_f + (size_t)b * kNlfKF + k);
+                v = is_min ? fminf(v, x) : fmaxf(v, x);
+            }
+            v = is_min ? warp_min_f(v) : warp_max_f(v);
+            if (lane == 0) fmm[k] = v;
+        }
+    }
+    unsigned nan = 0;
+    for (int b = threadIdx.x; b < nblocks; b += kThreads) nan |= __ldcg(s.part_nan + b);
+    nan = __reduce_or_sync(0xffffffffu, nan);
+    if (lane == 0) nanw[warp] = nan;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned m = 0;
+        for (int w = 0; w < kWarps; w++) m |= nanw[w];
+        for (int k = 0; k < K; k++)
+            if (m & (1u << k)) tot[k] = __longlong_as_double(0x7ff8000000000000ll);
+        fit_totals<NC>(tot, fmm, stage, s.fit, out);
+        atomicExch(s.ticket, 0u);
+    }
+}
+
+// Solve of pass 2, run by its last block: RMS of the residuals per channel, evaluated with
+// sqrtf as gls::sqrt(Vector) does.
+template <int NC>
+GLS_DI void solve_pass2(const NlfScratch& s, int nblocks) {
+    __shared__ double tot[NC];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int k = warp; k < NC; k += kWarps) {
+        double sum = 0.0, c = 0.0;
+        for (int b = lane; b < nblocks; b += 32) neumaier(sum, c, __ldcg(s.part_d + (size_t)b * kNlfK + k));
+        const double v = warp_sum_d(sum + c);
+        if (lane == 0) tot[k] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int ch = 0; ch < NC; ch++) s.fit->err2[ch] = (double)sqrtf((float)(tot[ch] / s.fit->N1));
+        s.fit->mode = 2;
+        atomicExch(s.ticket, 0u);
+    }
+}
+
+// End of every pass-1 kernel: the block's rows, then the solve in the last block.
+template <int MC, int NC>
+GLS_DI void pass1_epilogue(Pass1Acc<MC, NC>& acc, const NlfScratch& s, float* out) {
+    acc.write_fixed(s.part_i, s.part_nan);
+    acc.write_minmax(s.part_f);
+    if (last_block(s.ticket)) solve_fixed<NC>(s, gridDim.x, 1, out);
+}
 
 template <int MC, int NC, class Src>
 __global__ void __launch_bounds__(kThreads) nlf_pass1_kernel(Src src, int sw, int sh, NlfThresholds th,
-                                                             double* part_d, float* part_f) {
+                                                             NlfScratch s, float* out) {
     Pass1Acc<MC, NC> acc;
     acc.init();
     const int tiles_x = (sw + kTX - 1) / kTX, tiles_y = (sh + kTY - 1) / kTY;
@@ -195,15 +489,15 @@ __global__ void __launch_bounds__(kThreads) nlf_pass1_kernel(Src src, int sw, in
         src.stats(x, y, m, v);
         acc.add(m, v, th);
     }
-    acc.write(part_d, part_f);
+    pass1_epilogue<MC, NC>(acc, s, out);
 }
 
 // Explicit pass 2 (only when solve 1 could not prove pass 3 trivial): sum of squared
 // residuals per channel, FP64 per pixel as the reference computes it.
 template <int MC, int NC, class Src>
 __global__ void __launch_bounds__(kThreads) nlf_pass2_kernel(Src src, int sw, int sh, NlfThresholds th,
-                                                             const NlfFit* fit, double* part_d) {
-    if (fit->mode != 1) return;
+                                                             NlfScratch s) {
+    if (s.fit->mode != 1) return;
     double acc[NC];
 #pragma unroll
     for (int c = 0; c < NC; c++) acc[c] = 0.0;
@@ -217,21 +511,22 @@ __global__ void __launch_bounds__(kThreads) nlf_pass2_kernel(Src src, int sw, in
         if (!in_range<MC, NC>(m, v, th)) continue;
 #pragma unroll
         for (int c = 0; c < NC; c++) {
-            const double d = (fit->A[c] + fit->B[c] * (double)m[MC == 1 ? 0 : c]) - (double)v[c];
+            const double d = (s.fit->A[c] + s.fit->B[c] * (double)m[MC == 1 ? 0 : c]) - (double)v[c];
             acc[c] += d * d;
         }
     }
-    block_reduce_write<NC>(acc, part_d + (size_t)blockIdx.x * kNlfK);
+    block_reduce_write<NC>(acc, s.part_d + (size_t)blockIdx.x * kNlfK);
+    if (last_block(s.ticket)) solve_pass2<NC>(s, gridDim.x);
 }
 
-// Explicit pass 3: refit on the pixels whose squared residual is <= err2 in every channel.
+// Explicit pass 3: refit on the pixels whose squared residual (FP64) is <= err2 in every
+// channel.
 template <int MC, int NC, class Src>
 __global__ void __launch_bounds__(kThreads) nlf_pass3_kernel(Src src, int sw, int sh, NlfThresholds th,
-                                                             const NlfFit* fit, double* part_d) {
-    if (fit->mode != 2) return;
-    double vals[1 + 5 * NC];
-#pragma unroll
-    for (int k = 0; k < 1 + 5 * NC; k++) vals[k] = 0.0;
+                                                             NlfScratch s, float* out) {
+    if (s.fit->mode != 2) return;
+    Pass1Acc<MC, NC> acc;
+    acc.init();
     const int tiles_x = (sw + kTX - 1) / kTX, tiles_y = (sh + kTY - 1) / kTY;
     const int tx = threadIdx.x % kTX, ty = threadIdx.x / kTX;
     for (int t = blockIdx.x; t < tiles_x * tiles_y; t += gridDim.x) {
@@ -243,138 +538,13 @@ __global__ void __launch_bounds__(kThreads) nlf_pass3_kernel(Src src, int sw, in
         bool ok = true;
 #pragma unroll
         for (int c = 0; c < NC; c++) {
-            const double d = (fit->A[c] + fit->B[c] * (double)m[MC == 1 ? 0 : c]) - (double)v[c];
-            if (!(d * d <= fit->err2[c])) ok = false;
+            const double d = (s.fit->A[c] + s.fit->B[c] * (double)m[MC == 1 ? 0 : c]) - (double)v[c];
+            if (!(d * d <= s.fit->err2[c])) ok = false;
         }
-        if (!ok) continue;
-        vals[0] += 1.0;
-#pragma unroll
-        for (int c = 0; c < NC; c++) {
-            const double mm = (double)m[MC == 1 ? 0 : c], vv = (double)v[c];
-            vals[1 + 5 * c + 0] += mm;
-            vals[1 + 5 * c + 1] += mm * mm;
-            vals[1 + 5 * c + 2] += vv;
-            vals[1 + 5 * c + 3] += mm * vv;
-        }
+        if (ok) acc.add_selected(m, v);
     }
-    block_reduce_write<1 + 5 * NC>(vals, part_d + (size_t)blockIdx.x * kNlfK);
-}
-
-// std::max(v, a) as gls::max(DVector, double) evaluates it (gls_linalg.hpp:238-243)
-__device__ double refmax(double v, double a) { return (v < a) ? a : v; }
-
-__device__ void neumaier(double& s, double& c, double x) {
-    const double t = s + x;
-    if (fabs(s) >= fabs(x)) c += (s - t) + x;
-    else c += (x - t) + s;
-    s = t;
-}
-
-// One block of kSolveThreads: thread t sums (compensated) the partial rows t, t + T, ...;
-// the per-thread sums are then added in a fixed tree, so the result does not depend on
-// scheduling.  Thread 0 runs the FP64 regression step of the given stage.
-constexpr int kSolveThreads = 256;
-
-template <int NC>
-__global__ void __launch_bounds__(kSolveThreads) nlf_solve_kernel(const double* part_d, const float* part_f,
-                                                                  int nblocks, int stage, NlfFit* fit, float* out) {
-    constexpr int K = 1 + 5 * NC;
-    __shared__ double red[kSolveThreads];
-    __shared__ float fred[kSolveThreads];
-    __shared__ double tot[kNlfK];
-    __shared__ float fmm[kNlfKF];
-    if (stage == 2 && fit->mode != 1) return;
-    if (stage == 3 && fit->mode != 2) return;
-    const int nk = stage == 2 ? NC : K;
-    const int t = threadIdx.x;
-    double s[K], c[K];
-#pragma unroll
-    for (int k = 0; k < K; k++) s[k] = c[k] = 0.0;
-    for (int b = t; b < nblocks; b += kSolveThreads) {
-#pragma unroll
-        for (int k = 0; k < K; k++)
-            if (k < nk) neumaier(s[k], c[k], part_d[(size_t)b * kNlfK + k]);
-    }
-#pragma unroll
-    for (int k = 0; k < K; k++) {
-        if (k >= nk) break;
-        red[t] = s[k] + c[k];
-        __syncthreads();
-        for (int o = kSolveThreads / 2; o > 0; o >>= 1) {
-            if (t < o) red[t] += red[t + o];
-            __syncthreads();
-        }
-        if (t == 0) tot[k] = red[0];
-        __syncthreads();
-    }
-    if (stage == 1) {
-        for (int k = 0; k < 4 * NC; k++) {
-            const bool is_min = k < 2 * NC;
-            float v = is_min ? glsm::inf_() : -glsm::inf_();
-            for (int b = t; b < nblocks; b += kSolveThreads) {
-                const float x = part_f[(size_t)b * kNlfKF + k];
-                v = is_min ? fminf(v, x) : fmaxf(v, x);
-            }
-            fred[t] = v;
-            __syncthreads();
-            for (int o = kSolveThreads / 2; o > 0; o >>= 1) {
-                if (t < o) fred[t] = is_min ? fminf(fred[t], fred[t + o]) : fmaxf(fred[t], fred[t + o]);
-                __syncthreads();
-            }
-            if (t == 0) fmm[k] = fred[0];
-            __syncthreads();
-        }
-    }
-    if (threadIdx.x != 0) return;
-
-    if (stage == 1 || stage == 3) {
-        const double N = tot[0];
-        double A[4], B[4];
-        for (int ch = 0; ch < NC; ch++) {
-            const double sx = tot[1 + 5 * ch], sxx = tot[2 + 5 * ch], sy = tot[3 + 5 * ch], sxy = tot[4 + 5 * ch];
-            B[ch] = refmax((N * sxy - sx * sy) / (N * sxx - sx * sx), 1e-8);
-            A[ch] = refmax((sy - B[ch] * sx) / N, 1e-8);
-        }
-        bool done = true;
-        if (stage == 1) {
-            fit->N1 = N;
-            for (int ch = 0; ch < NC; ch++) {
-                fit->A[ch] = A[ch];
-                fit->B[ch] = B[ch];
-                const double sx = tot[1 + 5 * ch], sxx = tot[2 + 5 * ch], sy = tot[3 + 5 * ch];
-                const double sxy = tot[4 + 5 * ch], syy = tot[5 + 5 * ch];
-                const double a = A[ch], b = B[ch];
-                const double t1 = N * a * a, t2 = 2.0 * a * b * sx, t3 = b * b * sxx;
-                const double t4 = -2.0 * a * sy, t5 = -2.0 * b * sxy, t6 = syy;
-                const double e = t1 + t2 + t3 + t4 + t5 + t6;
-                const double mag = fabs(t1) + fabs(t2) + fabs(t3) + fabs(t4) + fabs(t5) + fabs(t6);
-                const double e_lo = e - 1e-12 * mag;
-                bool skip = N > 0 && e_lo > 0 && a == a && b == b;
-                if (skip) {
-                    const double rms_lo = sqrt(e_lo / N) * (1.0 - 1e-6);
-                    const double mlo = (double)fmm[ch], mhi = (double)fmm[2 * NC + ch];
-                    const double vlo = (double)fmm[NC + ch], vhi = (double)fmm[3 * NC + ch];
-                    const double dmax = a + b * (b >= 0 ? mhi : mlo) - vlo;
-                    const double dmin = a + b * (b >= 0 ? mlo : mhi) - vhi;
-                    const double mabs_ = fmax(fabs(dmax), fabs(dmin));
-                    skip = mabs_ * mabs_ * (1.0 + 1e-9) <= rms_lo;
-                }
-                if (!skip) done = false;
-            }
-            fit->mode = done ? 0 : 1;
-        } else {
-            fit->mode = 0;
-        }
-        if (done) {
-            for (int ch = 0; ch < NC; ch++) {
-                out[ch] = (float)A[ch];
-                out[NC + ch] = (float)B[ch];
-            }
-        }
-    } else {  // stage 2: RMS of the residuals, evaluated with sqrtf as gls::sqrt(Vector) does
-        for (int ch = 0; ch < NC; ch++) fit->err2[ch] = (double)sqrtf((float)(tot[ch] / fit->N1));
-        fit->mode = 2;
-    }
+    acc.write_fixed(s.part_i, s.part_nan);
+    if (last_block(s.ticket)) solve_fixed<NC>(s, gridDim.x, 3, out);
 }
 
 int grid_for(gls_ctx* ctx, int sw, int sh) {
@@ -385,28 +555,27 @@ int grid_for(gls_ctx* ctx, int sw, int sh) {
     return (int)(g < 1 ? 1 : g);
 }
 
-// Everything after pass 1: solve, and the explicit error and refit passes (which exit at
-// once unless solve 1 could not prove them redundant).  pass1_blocks partial rows exist.
+// Everything after pass 1 (whose last block already solved it): the explicit error and
+// refit passes, which exit at once unless solve 1 could not prove them redundant.
 template <int MC, int NC, class Src>
-void nlf_finish(gls_ctx* ctx, const Src& src, int sw, int sh, int pass1_blocks, NlfScratch s, float* out_dev) {
+void nlf_finish(gls_ctx* ctx, const Src& src, int sw, int sh, NlfScratch s, float* out_dev) {
     const NlfThresholds th = nlf_thresholds();
     const int grid = grid_for(ctx, sw, sh);
     cudaStream_t st = ctx->stream;
-    nlf_solve_kernel<NC><<<1, kSolveThreads, 0, st>>>(s.part_d, s.part_f, pass1_blocks, 1, s.fit, out_dev);
-    nlf_pass2_kernel<MC, NC, Src><<<grid, kThreads, 0, st>>>(src, sw, sh, th, s.fit, s.part_d);
-    nlf_solve_kernel<NC><<<1, kSolveThreads, 0, st>>>(s.part_d, s.part_f, grid, 2, s.fit, out_dev);
-    nlf_pass3_kernel<MC, NC, Src><<<grid, kThreads, 0, st>>>(src, sw, sh, th, s.fit, s.part_d);
-    nlf_solve_kernel<NC><<<1, kSolveThreads, 0, st>>>(s.part_d, s.part_f, grid, 3, s.fit, out_dev);
-    ctx->launches += 5;
+    nlf_pass2_kernel<MC, NC, Src><<<grid, kThreads, 0, st>>>(src, sw, sh, th, s);
+    nlf_pass3_kernel<MC, NC, Src><<<grid, kThreads, 0, st>>>(src, sw, sh, th, s, out_dev);
+    ctx->launches += 2;
 }
 
 template <int MC, int NC, class Src>
 gls_status run_fit(gls_ctx* ctx, const Src& src, int sw, int sh, NlfScratch s, float* out_dev) {
     const NlfThresholds th = nlf_thresholds();
     const int grid = grid_for(ctx, sw, sh);
-    nlf_pass1_kernel<MC, NC, Src><<<grid, kThreads, 0, ctx->stream>>>(src, sw, sh, th, s.part_d, s.part_f);
+    // the scratch may have held other data (the context's scratch is shared): clear the ticket
+    GLS_CHECK(check_cuda(ctx, cudaMemsetAsync(s.ticket, 0, sizeof(unsigned), ctx->stream), "clear regression ticket"));
+    nlf_pass1_kernel<MC, NC, Src><<<grid, kThreads, 0, ctx->stream>>>(src, sw, sh, th, s, out_dev);
     ctx->launches += 1;
-    nlf_finish<MC, NC, Src>(ctx, src, sw, sh, grid, s, out_dev);
+    nlf_finish<MC, NC, Src>(ctx, src, sw, sh, s, out_dev);
     return check_launch(ctx, "noise model regression");
 }
 

@@ -24,6 +24,7 @@ namespace gls {
 namespace {
 
 constexpr int kT = 256;
+static_assert(kT == kThreads, "the regression epilogue reduces over blocks of kThreads");
 
 // ---- shared-memory accessors (coordinates in image space, origin at (x0, y0)) ----
 struct SAcc1 {
@@ -114,7 +115,7 @@ __global__ void __launch_bounds__(kT) raw_pass1_kernel(RawPass1Args a) {
         }
         __syncthreads();
     }
-    acc.write(a.part_d, a.part_f);
+    pass1_epilogue<4, 4>(acc, a.nlf, a.nlf_out);
 }
 
 // =========================================================================================
@@ -310,7 +311,7 @@ __global__ void __launch_bounds__(kT) level_pass1_kernel(LevelPass1Args a) {
         }
         __syncthreads();
     }
-    acc.write(a.part_d, a.part_f);
+    pass1_epilogue<1, 3>(acc, a.nlf, a.nlf_out);
 }
 
 // =========================================================================================
@@ -465,8 +466,8 @@ struct RawU16SrcS {
 gls_status fused_raw_fit(gls_ctx* ctx, const RawPass1Args& args, bool half, NlfScratch s, float* out_dev) {
     RawPass1Args a = args;
     a.th = nlf_thresholds();
-    a.part_d = s.part_d;
-    a.part_f = s.part_f;
+    a.nlf = s;
+    a.nlf_out = out_dev;
     const int qw = a.w / 2, qh = a.h / 2;
     const long tiles = (long)((qw + RQ - 1) / RQ) * ((qh + RQ - 1) / RQ);
     const int grid = persistent_grid(ctx, tiles, 4);
@@ -474,12 +475,12 @@ gls_status fused_raw_fit(gls_ctx* ctx, const RawPass1Args& args, bool half, NlfS
         raw_pass1_kernel<__half><<<grid, kT, 0, ctx->stream>>>(a);
         RawU16SrcS<__half> src{{a.raw, a.w, a.h, a.pitch}, {a.sm[0], a.sm[1], a.sm[2], a.sm[3]}, a.black, a.bayer};
         ctx->launches++;
-        nlf_finish<4, 4>(ctx, src, qw, qh, grid, s, out_dev);
+        nlf_finish<4, 4>(ctx, src, qw, qh, s, out_dev);
     } else {
         raw_pass1_kernel<float><<<grid, kT, 0, ctx->stream>>>(a);
         RawU16SrcS<float> src{{a.raw, a.w, a.h, a.pitch}, {a.sm[0], a.sm[1], a.sm[2], a.sm[3]}, a.black, a.bayer};
         ctx->launches++;
-        nlf_finish<4, 4>(ctx, src, qw, qh, grid, s, out_dev);
+        nlf_finish<4, 4>(ctx, src, qw, qh, s, out_dev);
     }
     return check_launch(ctx, "raw noise statistics (fused)");
 }
@@ -502,8 +503,8 @@ gls_status fused_level_fit(gls_ctx* ctx, const LevelPass1Args& args, bool in_hal
                            float* out_dev) {
     LevelPass1Args a = args;
     a.th = nlf_thresholds();
-    a.part_d = s.part_d;
-    a.part_f = s.part_f;
+    a.nlf = s;
+    a.nlf_out = out_dev;
     const long tiles = (long)((a.w + LT - 1) / LT) * ((a.h + LT - 1) / LT);
     const int grid = persistent_grid(ctx, tiles, 4);
     if (in_half) {
@@ -511,12 +512,12 @@ gls_status fused_level_fit(gls_ctx* ctx, const LevelPass1Args& args, bool in_hal
         else level_pass1_kernel<__half, float><<<grid, kT, 0, ctx->stream>>>(a);
         LevelSrc<__half> src{{(const half4*)a.in, a.w, a.h, a.pitch}};
         ctx->launches++;
-        nlf_finish<1, 3>(ctx, src, a.w, a.h, grid, s, out_dev);
+        nlf_finish<1, 3>(ctx, src, a.w, a.h, s, out_dev);
     } else {
         level_pass1_kernel<float, float><<<grid, kT, 0, ctx->stream>>>(a);
         LevelSrc<float> src{{(const float4*)a.in, a.w, a.h, a.pitch}};
         ctx->launches++;
-        nlf_finish<1, 3>(ctx, src, a.w, a.h, grid, s, out_dev);
+        nlf_finish<1, 3>(ctx, src, a.w, a.h, s, out_dev);
     }
     return check_launch(ctx, "level statistics (fused)");
 }

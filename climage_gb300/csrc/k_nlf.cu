@@ -6,13 +6,15 @@
 // [0.001, 0.5] x [0, 0.001] (pass 1), measures the RMS residual (pass 2), and refits on the
 // pixels whose squared residual is <= that RMS (pass 3).  Here:
 //   pass 1  every thread accumulates the sums of its pixels in float-float (exact
-//           products, compensated adds), blocks reduce in FP64 to per-block partials;
-//   solve 1 one block reduces the partials (compensated FP64, fixed order) and fits A, B.
-//           It bounds every pass-1 residual by the extremes of the selected statistics; when
+//           products, compensated adds) and converts them to 128-bit fixed point; blocks
+//           reduce those exactly (integer adds) to per-block rows;
+//   solve 1 the last block to finish pass 1 adds the rows (exact again), rounds each total
+//           once to a double, and fits A, B in FP64.  It bounds every pass-1 residual by the extremes of the selected statistics; when
 //           even the largest possible squared residual is below a lower bound of the RMS
 //           (computed from the sums), pass 3 provably keeps every pass-1 pixel and the
 //           pass-1 fit is the answer -- the common case, one pass over the data;
-//   pass 2/3 otherwise run as the reference does, per pixel in FP64.
+//   pass 2/3 otherwise run as the reference does, per pixel in FP64 (the refit sums of
+//           pass 3 travel in fixed point like those of pass 1), each solved by its last block.
 #include "gls_nlf.cuh"
 
 namespace gls {

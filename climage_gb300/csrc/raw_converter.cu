@@ -117,6 +117,8 @@ struct gls_raw_converter {
         GLS_CHECK(alloc(&p, (1 + GLS_MAX_LEVELS) * 8 * sizeof(float)));
         nlf_dev = (float*)p;
         GLS_CHECK(alloc(&nlf_scratch, kNlfScratchBytes));
+        // the regression ticket starts at zero; every pass leaves it at zero
+        GLS_CHECK(check_cuda(ctx, cudaMemsetAsync(nlf_scratch, 0, kNlfHeaderBytes, ctx->stream), "clear regression state"));
         gf_scratch = nullptr;
         gf_scratch_bytes = 0;
         w = width;
