@@ -175,11 +175,6 @@ struct FastDiv {
         const float ax = fabs_(x);
         return ax <= 1.15292150e18f && (ax >= 1.03397577e-25f || ax == 0.0f);
     }
-    // a value whose differences with any other such value stay in_range
-    GLS_HDM static bool operand_ok(float v) {
-        const float av = fabs_(v);
-        return av <= 5.76460752e17f && (av >= 8.67361738e-19f || av == 0.0f);  // [2^-60, 2^59]
-    }
 };
 
 // smoothstep with the interpolation denominator e1 - e0 shared by many evaluations: the

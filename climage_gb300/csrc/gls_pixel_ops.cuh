@@ -420,12 +420,8 @@ __device__ __noinline__ float4 bilateral_literal(const Acc4& im, int px, int py,
     return make_float4(div_(f0, n0), div_(f1, n1), div_(f2, n2), 0.0f);
 }
 
-// CHECK: test every sample difference against the division shortcut's exact range; a
-// caller that has verified every value of the 5x5 window with FastDiv::operand_ok passes
-// CHECK = false and values_ok = true instead.
-template <bool CHECK, class Acc4>
-GLS_DI float4 bilateral_px(const Acc4& im, int px, int py, const Nlf6& n, float chromaBoost, float gradientBoost,
-                           bool values_ok = true) {
+template <class Acc4>
+GLS_DI float4 bilateral_px(const Acc4& im, int px, int py, const Nlf6& n, float chromaBoost, float gradientBoost) {
     const float4 c = im.at(px, py);
     const float sig0 = sqrt_(n.a[0] + n.b[0] * c.x);
     const float sig1 = sqrt_(n.a[1] + n.b[1] * c.x);
@@ -437,11 +433,16 @@ GLS_DI float4 bilateral_px(const Acc4& im, int px, int py, const Nlf6& n, float 
         lumaBoost = gradientBoost -
                     (gradientBoost - 1.0f) * smoothstep_(0.5f, 2.0f, length2_(div_(g.x, sig0), div_(g.y, sig0)));
     }
-    // weight = 1 - step(edge, length(diff)) = !(sqrt_rn(|diff|^2) >= edge), decided on the
-    // squared length; the divisions by sigma share their divisor; the weights are 0 or 1,
-    // so w * s is exact and the multiply-add can be fused without changing a bit.  Any
-    // sample outside the shortcuts' exact range, or too close to an edge to decide
-    // without the square root, sends the pixel to the literal evaluation.
+    // weight = 1 - step(edge, length(diff / sigma)) = !(sqrt_rn(q) >= edge), where
+    // q = RN(RN(d0^2) + RN(d1^2)) + RN(d2^2) with d_k = RN(diff_k / sigma_k).  Each tap is
+    // decided on qa = sum diff_k^2 * RN(1/sigma_k)^2 instead: all terms are non-negative, so
+    // qa and q both lie within about 12 roundings (2^-20.4 relative) of the exact value, and
+    // a tap whose qa clears the square-root band of the edge (2^-20) widened by 2^-18 has the
+    // same weight either way.  The fast path keeps edges below 2^20 and 2^-60 <= sigma <= 2^30,
+    // so an overflowing diff^2 (or product) means d^2 > 2^68 and weight 0 on both sides, and
+    // qa is never NaN for finite samples; a tap that stays undecided, or a sample that is not
+    // finite, sends the pixel to the literal evaluation.  The weights are 0 or 1, so w * s is exact and the multiply-add can
+    // be fused without changing a bit.
     SqrtGe ge0, ge1;
     ge0.init(lumaBoost * GLS_SQRT2_F);
     ge1.init(chromaBoost * GLS_SQRT2_F);
@@ -449,8 +450,12 @@ GLS_DI float4 bilateral_px(const Acc4& im, int px, int py, const Nlf6& n, float 
     dv0.init(sig0);
     dv1.init(sig1);
     dv2.init(sig2);
-    if (!(values_ok && dv0.ok && dv1.ok && dv2.ok && ge0.ok && ge1.ok))
+    if (!(dv0.ok && dv1.ok && dv2.ok && ge0.ok && ge1.ok && ge0.e < 1048576.0f && ge1.e < 1048576.0f))
         return bilateral_literal(im, px, py, sig0, sig1, sig2, ge0.e, ge1.e);
+    constexpr float kWiden = 3.814697265625e-06f;  // 2^-18
+    const float r0 = dv0.y * dv0.y, r1 = dv1.y * dv1.y, r2 = dv2.y * dv2.y;
+    const float lo0 = ge0.lo * (1.0f - kWiden), hi0 = ge0.hi * (1.0f + kWiden);
+    const float lo1 = ge1.lo * (1.0f - kWiden), hi1 = ge1.hi * (1.0f + kWiden);
     float f0 = 0.0f, f1 = 0.0f, f2 = 0.0f, n0 = 0.0f, n1 = 0.0f, n2 = 0.0f;
     bool redo = false;
 #pragma unroll 1
@@ -459,11 +464,10 @@ GLS_DI float4 bilateral_px(const Acc4& im, int px, int py, const Nlf6& n, float 
         for (int x = -2; x <= 2; x++) {
             const float4 s = im.at(px + x, py + y);
             const float x0 = s.x - c.x, x1 = s.y - c.y, x2 = s.z - c.z;
-            if (CHECK) redo |= !(FastDiv::in_range(x0) && FastDiv::in_range(x1) && FastDiv::in_range(x2));
-            const float d0 = dv0.fast(x0), d1 = dv1.fast(x1), d2 = dv2.fast(x2);
-            const float q = d0 * d0 + d1 * d1 + d2 * d2;
-            redo |= ge0.ambiguous(q) || ge1.ambiguous(q);
-            const float w0 = q < ge0.lo ? 1.0f : 0.0f, w1 = q < ge1.lo ? 1.0f : 0.0f;
+            const float qa = glsm::fma_(x0 * x0, r0, glsm::fma_(x1 * x1, r1, (x2 * x2) * r2));
+            const bool in0 = qa < lo0, in1 = qa < lo1;
+            redo |= !(in0 || qa > hi0) || !(in1 || qa > hi1);
+            const float w0 = in0 ? 1.0f : 0.0f, w1 = in1 ? 1.0f : 0.0f;
             f0 = glsm::fma_(w0, s.x, f0);
             n0 = n0 + w0;
             f1 = glsm::fma_(w1, s.y, f1);

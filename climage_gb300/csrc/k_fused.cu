@@ -326,14 +326,11 @@ __global__ void __launch_bounds__(kT) denoise_reasm_kernel(DenoiseArgs a) {
     __shared__ float4 s_in[PW * PH];
     const int x0 = blockIdx.x * DW, y0 = blockIdx.y * DH;
     const GImg4<SIn> gin{(const typename Storage<SIn>::T4*)a.in, a.w, a.h, a.pitch};
-    bool ok = true;
     for (int i = threadIdx.x; i < PW * PH; i += kT) {
         const int r = i / PW, c = i - r * PW;
-        const float4 v = gin.at(x0 - 2 + c, y0 - 2 + r);
-        ok &= FastDiv::operand_ok(v.x) && FastDiv::operand_ok(v.y) && FastDiv::operand_ok(v.z);
-        s_in[i] = v;
+        s_in[i] = gin.at(x0 - 2 + c, y0 - 2 + r);
     }
-    const bool tile_ok = __syncthreads_and(ok);
+    __syncthreads();
     const SAcc4f I{s_in, x0 - 2, y0 - 2, PW};
     Nlf6 n;
 #pragma unroll
@@ -347,7 +344,7 @@ __global__ void __launch_bounds__(kT) denoise_reasm_kernel(DenoiseArgs a) {
     for (int i = threadIdx.x; i < DW * DH; i += kT) {
         const int r = i / DW, c = i - r * DW, x = x0 + c, y = y0 + r;
         if (x >= a.w || y >= a.h) continue;
-        float4 d = ALGO == 0 ? bilateral_px<false>(I, x, y, n, a.chroma_boost, a.gradient_boost, tile_ok)
+        float4 d = ALGO == 0 ? bilateral_px(I, x, y, n, a.chroma_boost, a.gradient_boost)
                              : guided_fast_px(I, x, y, n);
         d = round4<S>(d);
         if (REASM) d = round4<S>(reassemble_px(d, i1, d1, x, y, a.w, a.h, a.cw, a.ch, a.sharpening, n.a[0], n.b[0]));
@@ -371,18 +368,13 @@ __global__ void __launch_bounds__(kT) final_kernel(FinalArgs a) {
     __shared__ float4 s_den[EW * EH];
     const int x0 = blockIdx.x * FW, y0 = blockIdx.y * FH;
     const int w = a.w, h = a.h;
-    bool ok = true;
     for (int i = threadIdx.x; i < PW * PH; i += kT) {
         const int r = i / PW, c = i - r * PW;
         const int gx = clampi(x0 - 3 + c, 0, w - 1), gy = clampi(y0 - 3 + r, 0, h - 1);
         const uint2 u = __ldg(reinterpret_cast<const uint2*>(a.level0 + (size_t)gy * a.l0_pitch + gx));
-        half4 hv;
-        *reinterpret_cast<uint2*>(&hv) = u;
-        const float4 v = Storage<__half>::cvt(hv);
-        ok &= FastDiv::operand_ok(v.x) && FastDiv::operand_ok(v.y) && FastDiv::operand_ok(v.z);
-        s_l0[i] = hv;
+        *reinterpret_cast<uint2*>(&s_l0[i]) = u;
     }
-    const bool tile_ok = __syncthreads_and(ok);
+    __syncthreads();
     const SAcc4h L0{s_l0, x0 - 3, y0 - 3, PW};
     Nlf6 n;
 #pragma unroll
@@ -396,7 +388,7 @@ __global__ void __launch_bounds__(kT) final_kernel(FinalArgs a) {
     for (int i = threadIdx.x; i < EW * EH; i += kT) {
         const int r = i / EW, c = i - r * EW, x = x0 - 1 + c, y = y0 - 1 + r;
         if (x < 0 || x >= w || y < 0 || y >= h) continue;
-        float4 d = ALGO == 0 ? bilateral_px<false>(L0, x, y, n, a.chroma_boost, a.gradient_boost, tile_ok)
+        float4 d = ALGO == 0 ? bilateral_px(L0, x, y, n, a.chroma_boost, a.gradient_boost)
                              : guided_fast_px(L0, x, y, n);
         d = round4<S>(d);
         d = round4<S>(reassemble_px(d, i1, d1, x, y, w, h, a.cw, a.ch, a.sharpening, n.a[0], n.b[0]));

@@ -137,7 +137,7 @@ __global__ void bilateral_kernel(GImg4<S> in, typename Storage<S>::T4* out, int 
                                  float gb) {
     PIXEL_XY
     if (x >= in.w || y >= in.h) return;
-    Storage<S>::st4(out + (size_t)y * opitch + x, bilateral_px<true>(in, x, y, nlf_get(nlf), cb, gb));
+    Storage<S>::st4(out + (size_t)y * opitch + x, bilateral_px(in, x, y, nlf_get(nlf), cb, gb));
 }
 
 template <class S>

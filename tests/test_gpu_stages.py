@@ -171,6 +171,29 @@ def test_denoise(ctx, frame, half, boost):
     assert mismatch(host(out), orc.denoise_guided(l0, va, vb, prec)) == 0
 
 
+@pytest.mark.parametrize("seed", range(4))
+def test_denoise_taps_at_the_edge(ctx, seed):
+    """Sample differences of sigma * sqrt(2) * (1 + t) with |t| of a few ulp put many taps of
+    the bilateral filter on (or next to) the edge of its 0/1 weight, where the kernel's fast
+    decision must hand over to the literal evaluation."""
+    import torch
+    rng = np.random.default_rng(100 + seed)
+    h, w = 32, 48
+    sig = np.float32(0.01)
+    va, vb = [float(sig * sig), 2.5e-5, 4e-5], [0.0, 0.0, 0.0]
+    img = np.zeros((h, w, 4), np.float32)
+    t = rng.uniform(-6e-7, 6e-7, (h, w)).astype(np.float32)
+    delta = (sig * np.float32(np.sqrt(2.0)) * (np.float32(1.0) + t)).astype(np.float32)
+    img[..., 0] = np.float32(0.3) + np.where(rng.random((h, w)) < 0.5, delta, np.float32(0.0))
+    img[..., 1] = np.float32(0.2) + np.where(rng.random((h, w)) < 0.3, np.float32(0.005) * (1 + t), np.float32(0.0))
+    img[..., 2] = np.float32(0.25)
+    out = empty((h, w, 4))
+    for boost in ((1.0, 1.0), (1.0, 2.0)):
+        ctx.denoiseImage(dev(img), va, vb, boost[0], boost[1], out)
+        torch.cuda.synchronize()
+        assert mismatch(host(out), orc.denoise_bilateral(img, va, vb, boost[0], boost[1])) == 0
+
+
 @pytest.mark.parametrize("half", [False, True], ids=["f32", "f16"])
 def test_guided_filter(ctx, frame, half):
     import torch
