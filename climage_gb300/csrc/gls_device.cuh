@@ -129,16 +129,27 @@ struct BilinearTap {
     float w00, w10, w01, w11;
 };
 
-GLS_DI BilinearTap bilinear_tap(float u, float v, int w, int h) {
-    const float fu = u * (float)w - 0.5f;
-    const float fv = v * (float)h - 0.5f;
-    const float i0f = floorf(fu), j0f = floorf(fv);
-    float a = fu - i0f, b = fv - j0f;
+// One axis of the sampler: texel index below the (texel-centred) coordinate u * n - 0.5 and
+// the fraction above it, quantized to 8 bits as the hardware sampler does.
+struct Tap1 {
+    int i0;
+    float a;
+};
+
+GLS_DI Tap1 tap1(float u, int n) {
+    const float fu = u * (float)n - 0.5f;
+    const float f = floorf(fu);
+    float a = fu - f;
     a = floorf(a * 256.0f + 0.5f) * 0.00390625f;
-    b = floorf(b * 256.0f + 0.5f) * 0.00390625f;
+    return Tap1{(int)f, a};
+}
+
+GLS_DI BilinearTap bilinear_tap(float u, float v, int w, int h) {
+    const Tap1 tx = tap1(u, w), ty = tap1(v, h);
+    const float a = tx.a, b = ty.a;
     BilinearTap t;
-    t.i0 = (int)i0f;
-    t.j0 = (int)j0f;
+    t.i0 = tx.i0;
+    t.j0 = ty.i0;
     t.w00 = (1.0f - a) * (1.0f - b);
     t.w10 = a * (1.0f - b);
     t.w01 = (1.0f - a) * b;
@@ -161,6 +172,59 @@ GLS_DI float4 sample4(const Acc& im, const BilinearTap& t) {
 template <class Acc>
 GLS_DI float4 sample4(const Acc& im, float u, float v, int w, int h) {
     return sample4(im, bilinear_tap(u, v, w, h));
+}
+
+// One axis of a tap resolved against a tile staged in shared memory: i0, i1 are the texel
+// positions of the two taps relative to the tile (for a row axis already multiplied by the
+// tile's row length), oma = 1 - a.  sample over the tile then forms the weights and the
+// blend exactly as sample4 does.
+struct TabTap {
+    int i0, i1;
+    float a, oma;
+};
+
+// taps clamped to an image of n texels (clamp-to-edge), then made relative to the tile
+// origin org; cap bounds the result to the tile for memory safety
+GLS_DI TabTap tab_tap(Tap1 t, int n, int org, int cap, int ld) {
+    TabTap r;
+    r.i0 = clampi(clampi(t.i0, 0, n - 1) - org, 0, cap - 1) * ld;
+    r.i1 = clampi(clampi(t.i0 + 1, 0, n - 1) - org, 0, cap - 1) * ld;
+    r.a = t.a;
+    r.oma = 1.0f - t.a;
+    return r;
+}
+
+// taps into a tile that already holds the clamped image around its edges
+GLS_DI TabTap tab_tap_tile(Tap1 t, int org, int cap, int ld) {
+    TabTap r;
+    r.i0 = clampi(t.i0 - org, 0, cap - 1) * ld;
+    r.i1 = clampi(t.i0 + 1 - org, 0, cap - 1) * ld;
+    r.a = t.a;
+    r.oma = 1.0f - t.a;
+    return r;
+}
+
+GLS_DI float4 tab_sample4(const float4* s, const TabTap& tx, const TabTap& ty) {
+    const float w00 = tx.oma * ty.oma, w10 = tx.a * ty.oma, w01 = tx.oma * ty.a, w11 = tx.a * ty.a;
+    const float4 p00 = s[ty.i0 + tx.i0], p10 = s[ty.i0 + tx.i1];
+    const float4 p01 = s[ty.i1 + tx.i0], p11 = s[ty.i1 + tx.i1];
+    float4 r;
+    r.x = w00 * p00.x + w10 * p10.x + w01 * p01.x + w11 * p11.x;
+    r.y = w00 * p00.y + w10 * p10.y + w01 * p01.y + w11 * p11.y;
+    r.z = w00 * p00.z + w10 * p10.z + w01 * p01.z + w11 * p11.z;
+    r.w = w00 * p00.w + w10 * p10.w + w01 * p01.w + w11 * p11.w;
+    return r;
+}
+
+GLS_DI float tab_sample_x(const float4* s, const TabTap& tx, const TabTap& ty) {
+    const float w00 = tx.oma * ty.oma, w10 = tx.a * ty.oma, w01 = tx.oma * ty.a, w11 = tx.a * ty.a;
+    return w00 * s[ty.i0 + tx.i0].x + w10 * s[ty.i0 + tx.i1].x + w01 * s[ty.i1 + tx.i0].x +
+           w11 * s[ty.i1 + tx.i1].x;
+}
+
+GLS_DI float tab_sample1(const float* s, const TabTap& tx, const TabTap& ty) {
+    const float w00 = tx.oma * ty.oma, w10 = tx.a * ty.oma, w01 = tx.oma * ty.a, w11 = tx.a * ty.a;
+    return w00 * s[ty.i0 + tx.i0] + w10 * s[ty.i0 + tx.i1] + w01 * s[ty.i1 + tx.i0] + w11 * s[ty.i1 + tx.i1];
 }
 
 // ---------------------------------------------------------------------------------------

@@ -535,25 +535,21 @@ GLS_DI float4 guided_fast_px(const Acc4& im, int px, int py, const Nlf6& n) {
 // ---- a17: reassembleImage (demosaic.cl:867-896) ----
 // d0: the denoised fine pixel; i1/d1: the coarse level before/after denoise; (w, h) the
 // fine level's size, (w1, h1) the coarse level's.
-template <class AccI, class AccD>
-GLS_DI float4 reassemble_px(float4 d0, const AccI& i1, const AccD& d1, int x, int y, int w, int h, int w1, int h1,
-                            float sharpening, float nlf0, float nlf1) {
-    const float nx = div_(1.0f, (float)w), ny = div_(1.0f, (float)h);
-    const float ipx = ((float)x + 0.5f) * nx, ipy = ((float)y + 0.5f) * ny;
-    const float4 p1 = sample4(i1, ipx, ipy, w1, h1);
-    const float4 pd1 = sample4(d1, ipx, ipy, w1, h1);
+// The arithmetic of reassembleImage once its samples are known: p1, pd1 are the coarse
+// image and its denoised version at the pixel; sharp() returns the .x of the denoised coarse
+// level one fine pixel to the right, left, below and above (asked for only when sharpening).
+template <class SharpF>
+GLS_DI float4 reassemble_from(float4 d0, float4 p1, float4 pd1, const SharpF& sharp, float sharpening, float nlf0,
+                              float nlf1) {
     float4 dp;
     dp.x = d0.x - (p1.x - pd1.x);
     dp.y = d0.y - (p1.y - pd1.y);
     dp.z = d0.z - (p1.z - pd1.z);
     dp.w = d0.w - (p1.w - pd1.w);
     if (sharpening > 1.0f) {
-        const float ax = sample4(d1, ipx + nx, ipy + 0.0f * ny, w1, h1).x;
-        const float bx = sample4(d1, ipx - nx, ipy - 0.0f * ny, w1, h1).x;
-        const float dx = ((ax - bx) * 0.5f);
-        const float ay = sample4(d1, ipx + 0.0f * nx, ipy + ny, w1, h1).x;
-        const float by = sample4(d1, ipx - 0.0f * nx, ipy - ny, w1, h1).x;
-        const float dy = ((ay - by) * 0.5f);
+        const float4 g = sharp();
+        const float dx = ((g.x - g.y) * 0.5f);
+        const float dy = ((g.z - g.w) * 0.5f);
         const float threshold = 0.25f * sqrt_(nlf0 + nlf1 * pd1.x);
         const float detail = smoothstep_(0.25f * threshold, threshold, length2_(dx, dy)) *
                              (1.0f - smoothstep_(0.95f, 1.0f, dp.x)) * (0.6f + 0.4f * smoothstep_(0.0f, 0.1f, dp.x));
@@ -563,30 +559,43 @@ GLS_DI float4 reassemble_px(float4 d0, const AccI& i1, const AccD& d1, int x, in
     return dp;
 }
 
+template <class AccI, class AccD>
+GLS_DI float4 reassemble_px(float4 d0, const AccI& i1, const AccD& d1, int x, int y, int w, int h, int w1, int h1,
+                            float sharpening, float nlf0, float nlf1) {
+    const float nx = div_(1.0f, (float)w), ny = div_(1.0f, (float)h);
+    const float ipx = ((float)x + 0.5f) * nx, ipy = ((float)y + 0.5f) * ny;
+    const float4 p1 = sample4(i1, ipx, ipy, w1, h1);
+    const float4 pd1 = sample4(d1, ipx, ipy, w1, h1);
+    auto sharp = [&]() {
+        return make_float4(sample4(d1, ipx + nx, ipy + 0.0f * ny, w1, h1).x,
+                           sample4(d1, ipx - nx, ipy - 0.0f * ny, w1, h1).x,
+                           sample4(d1, ipx + 0.0f * nx, ipy + ny, w1, h1).x,
+                           sample4(d1, ipx - 0.0f * nx, ipy - ny, w1, h1).x);
+    };
+    return reassemble_from(d0, p1, pd1, sharp, sharpening, nlf0, nlf1);
+}
+
 // ---- a18: localToneMappingMask (demosaic.cl:1026-1107) ----
 struct LtmParams {
     float eps, shadows, highlights, detail;
 };
 
-template <class AccIn, class AccG>
-GLS_DI float ltm_mask_px(const AccIn& in, const AccG& guide, int x, int y, int w, int h, int gw, int gh,
-                         const LtmParams& lp, const Mat3& m) {
+// Guide sample offsets of localToneMappingMask, in fine pixels: sample i sits at
+// (kLtmOff[i % 3], kLtmOff[i / 3]) + 0.5 from the pixel, with weight kLtmW[i].
+#define GLS_LTM_OFFSETS {-1.5f, 0.5f, 2.0f}
+
+// The arithmetic of localToneMappingMask once its samples are known: gs[i] the guide's .x at
+// the nine offsets, inp the denoised image at the pixel.
+GLS_DI float ltm_mask_from(const float (&gs)[9], float4 inp, const LtmParams& lp, const Mat3& m) {
     const float bw[9] = {0.16f, 0.16f, 0.08f, 0.16f, 0.16f, 0.08f, 0.08f, 0.08f, 0.04f};
-    const float bx[9] = {-1.5f, 0.5f, 2.0f, -1.5f, 0.5f, 2.0f, -1.5f, 0.5f, 2.0f};
-    const float by[9] = {-1.5f, -1.5f, -1.5f, 0.5f, 0.5f, 0.5f, 2.0f, 2.0f, 2.0f};
-    const float nx = div_(1.0f, (float)w), ny = div_(1.0f, (float)h);
-    const float px = (float)x * nx, py = (float)y * ny;
-    float gs[9];
     float sum = 0.0f, sumSq = 0.0f;
 #pragma unroll
     for (int i = 0; i < 9; i++) {
-        gs[i] = sample4(guide, px + (bx[i] + 0.5f) * nx, py + (by[i] + 0.5f) * ny, gw, gh).x;
         const float s = bw[i] * gs[i];
         sum = sum + s;
         sumSq = sumSq + s * s;
     }
     const float mean = sum, var = sumSq - sum * sum;
-    const float4 inp = sample4(in, px + 0.5f * nx, py + 0.5f * ny, w, h);
     const float luma = inp.x;
     float filtered = 0.0f, knorm = 0.0f;
     FastDiv dv;
@@ -603,6 +612,20 @@ GLS_DI float ltm_mask_px(const AccIn& in, const AccG& guide, int x, int y, int w
     const float hc = mmin(length3_(sqrt_(2.0f * rgb.x), sqrt_(2.0f * rgb.y), sqrt_(2.0f * rgb.z)), 1.0f);
     const float tc = mix_(lp.shadows, lp.highlights, hc);
     return div_(glsm::pow_(illuminance, div_(1.0f, tc)) * glsm::pow_(reflectance, lp.detail), luma);
+}
+
+template <class AccIn, class AccG>
+GLS_DI float ltm_mask_px(const AccIn& in, const AccG& guide, int x, int y, int w, int h, int gw, int gh,
+                         const LtmParams& lp, const Mat3& m) {
+    const float off[3] = GLS_LTM_OFFSETS;
+    const float nx = div_(1.0f, (float)w), ny = div_(1.0f, (float)h);
+    const float px = (float)x * nx, py = (float)y * ny;
+    float gs[9];
+#pragma unroll
+    for (int i = 0; i < 9; i++)
+        gs[i] = sample4(guide, px + (off[i % 3] + 0.5f) * nx, py + (off[i / 3] + 0.5f) * ny, gw, gh).x;
+    const float4 inp = sample4(in, px + 0.5f * nx, py + 0.5f * ny, w, h);
+    return ltm_mask_from(gs, inp, lp, m);
 }
 
 // ---- a19: convertTosRGB + toneCurve & co (demosaic.cl:1380-1474) ----

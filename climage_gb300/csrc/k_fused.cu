@@ -355,26 +355,146 @@ __global__ void __launch_bounds__(kT) denoise_reasm_kernel(DenoiseArgs a) {
 // =========================================================================================
 // final: level-0 denoise + reassemble over the tile and a one-pixel ring (the local tone
 // mapping samples its input bilinearly), then the LTM mask, YCbCr -> camera and
-// convertTosRGB.  32x16 output tiles.
+// convertTosRGB.  30x14 output tiles: with its ring the denoised tile is 32x16, two
+// positions per thread.
+//
+// Every bilinear sample here splits into an x part that depends only on the column and a y
+// part that depends only on the row (tap1).  The block evaluates those parts once per
+// column and row into tables, and stages the texels they reach -- the two half-resolution
+// levels under the ring and the .x plane of the LTM guide -- in shared memory; a sample is
+// then four table-indexed loads and the weights and blend of sample4, bit for bit.  The
+// coordinates grow monotonically with x and y, so the first and last column (row) bound the
+// texels a tile reaches: with the pyramid's sizes (w >> 1, w >> 3) that is at most
+// FW / 2 + 4 half-resolution and FW / 8 + 5 guide texels across.
 // =========================================================================================
-// 30x14 outputs: the denoised tile with its ring is 32x16 = 2 positions per thread
 constexpr int FW = 30, FH = 14;
+constexpr int EW = FW + 2, EH = FH + 2;        // denoised level 0 with its ring
+constexpr int HTW = EW / 2 + 6, HTH = EH / 2 + 6;  // half-resolution tile capacity
+constexpr int GTW = FW / 8 + 8, GTH = FH / 8 + 8;  // guide tile capacity
+
+// tile origins (texels) and the table slots of one block
+struct FinalTabs {
+    TabTap rx[3][EW], ry[3][EH];  // reassemble: u = ipx, ipx + nx, ipx - nx (rows likewise)
+    TabTap lx[FW], ly[FH];        // LTM input sample on the denoised tile
+    TabTap gx[3][FW], gy[3][FH];  // LTM guide, offsets GLS_LTM_OFFSETS + 0.5
+    int org[8];                   // half-res x0, x1, y0, y1; guide x0, x1, y0, y1
+};
+
+// coordinate of table entry e of the block (the same float operations as the per-pixel
+// samplers); which: 0 reassemble, 1 LTM input, 2 guide
+GLS_DI float final_coord(int which, int k, int pos, float n) {
+    const float off[3] = GLS_LTM_OFFSETS;
+    if (which == 0) {
+        const float ip = ((float)pos + 0.5f) * n;
+        return k == 0 ? ip : (k == 1 ? ip + n : ip - n);
+    }
+    const float p = (float)pos * n;
+    if (which == 1) return p + 0.5f * n;
+    return p + (off[k] + 0.5f) * n;
+}
 
 template <class S, int ALGO, bool LTM, bool OUT_F32>
 __global__ void __launch_bounds__(kT) final_kernel(FinalArgs a) {
     constexpr int PW = FW + 6, PH = FH + 6;  // level 0 (binary16), origin (x0 - 3, y0 - 3)
-    constexpr int EW = FW + 2, EH = FH + 2;  // denoised level 0, origin (x0 - 1, y0 - 1)
     __shared__ half4 s_l0[PW * PH];
-    __shared__ float4 s_den[EW * EH];
+    __shared__ float4 s_den[EW * EH];            // origin (x0 - 1, y0 - 1)
+    __shared__ float4 s_i1[HTW * HTH], s_d1[HTW * HTH];
+    __shared__ float s_g[GTW * GTH];
+    __shared__ Tap1 s_raw[3 * EW + 3 * EH + FW + FH + 3 * FW + 3 * FH];
+    __shared__ FinalTabs T;
     const int x0 = blockIdx.x * FW, y0 = blockIdx.y * FH;
     const int w = a.w, h = a.h;
+    const float nx = div_(1.0f, (float)w), ny = div_(1.0f, (float)h);
+
+    // ---- phase 1: level-0 tile, raw table entries, tile origins ----
     for (int i = threadIdx.x; i < PW * PH; i += kT) {
         const int r = i / PW, c = i - r * PW;
         const int gx = clampi(x0 - 3 + c, 0, w - 1), gy = clampi(y0 - 3 + r, 0, h - 1);
         const uint2 u = __ldg(reinterpret_cast<const uint2*>(a.level0 + (size_t)gy * a.l0_pitch + gx));
         *reinterpret_cast<uint2*>(&s_l0[i]) = u;
     }
+    // entry layout: rx[3][EW], ry[3][EH], lx[FW], ly[FH], gx[3][FW], gy[3][FH]
+    constexpr int NRX = 3 * EW, NRY = 3 * EH, NLX = FW, NLY = FH, NGX = 3 * FW, NGY = 3 * FH;
+    constexpr int NT = NRX + NRY + NLX + NLY + NGX + NGY;
+    for (int e = threadIdx.x; e < NT; e += kT) {
+        int q = e;
+        Tap1 t;
+        if (q < NRX) {
+            t = tap1(final_coord(0, q / EW, x0 - 1 + q % EW, nx), a.cw);
+        } else if ((q -= NRX) < NRY) {
+            t = tap1(final_coord(0, q / EH, y0 - 1 + q % EH, ny), a.ch);
+        } else if ((q -= NRY) < NLX) {
+            t = tap1(final_coord(1, 0, x0 + q, nx), w);
+        } else if ((q -= NLX) < NLY) {
+            t = tap1(final_coord(1, 0, y0 + q, ny), h);
+        } else if ((q -= NLY) < NGX) {
+            t = tap1(final_coord(2, q / FW, x0 + q % FW, nx), a.gw);
+        } else {
+            q -= NGX;
+            t = tap1(final_coord(2, q / FH, y0 + q % FH, ny), a.gh);
+        }
+        s_raw[e] = t;
+    }
+    if (threadIdx.x < 8) {
+        // extremes: the smallest index sits at the first column (row) and smallest offset,
+        // the largest at the last one and the largest offset; clamped to the image
+        const int j = threadIdx.x;
+        const bool guide = j >= 4, is_y = (j & 2) != 0, hi = (j & 1) != 0;
+        const int n = guide ? (is_y ? a.gh : a.gw) : (is_y ? a.ch : a.cw);
+        const float step = is_y ? ny : nx;
+        const int pos = guide ? (is_y ? (hi ? y0 + FH - 1 : y0) : (hi ? x0 + FW - 1 : x0))
+                              : (is_y ? (hi ? y0 + EH - 2 : y0 - 1) : (hi ? x0 + EW - 2 : x0 - 1));
+        int v = hi ? -2147483647 : 2147483647;
+        for (int k = 0; k < 3; k++) {
+            const int i0 = tap1(final_coord(guide ? 2 : 0, k, pos, step), n).i0;
+            v = hi ? max(v, i0 + 1) : min(v, i0);
+        }
+        T.org[j] = clampi(v, 0, n - 1);
+    }
     __syncthreads();
+
+    // ---- phase 2: tables against the tile origins, half-resolution and guide tiles ----
+    const int hx0 = T.org[0], hy0 = T.org[2], gx0 = T.org[4], gy0 = T.org[6];
+    const int htw = min(T.org[1] - hx0 + 1, HTW), hth = min(T.org[3] - hy0 + 1, HTH);
+    const int gtw = min(T.org[5] - gx0 + 1, GTW), gth = min(T.org[7] - gy0 + 1, GTH);
+    for (int e = threadIdx.x; e < NT; e += kT) {
+        const Tap1 t = s_raw[e];
+        int q = e;
+        if (q < NRX) {
+            T.rx[q / EW][q % EW] = tab_tap(t, a.cw, hx0, HTW, 1);
+        } else if ((q -= NRX) < NRY) {
+            T.ry[q / EH][q % EH] = tab_tap(t, a.ch, hy0, HTH, HTW);
+        } else if ((q -= NRY) < NLX) {
+            T.lx[q] = tab_tap_tile(t, x0 - 1, EW, 1);
+        } else if ((q -= NLX) < NLY) {
+            T.ly[q] = tab_tap_tile(t, y0 - 1, EH, EW);
+        } else if ((q -= NLY) < NGX) {
+            T.gx[q / FW][q % FW] = tab_tap(t, a.gw, gx0, GTW, 1);
+        } else {
+            q -= NGX;
+            T.gy[q / FH][q % FH] = tab_tap(t, a.gh, gy0, GTH, GTW);
+        }
+    }
+    typedef typename Storage<S>::T4 T4;
+    {
+        const GImg4<S> i1{(const T4*)a.pyr0, a.cw, a.ch, a.cpitch};
+        const GImg4<S> d1{(const T4*)a.den1, a.cw, a.ch, a.cpitch};
+        for (int i = threadIdx.x; i < htw * hth; i += kT) {
+            const int r = i / htw, c = i - r * htw;
+            s_i1[r * HTW + c] = i1.at(hx0 + c, hy0 + r);
+            s_d1[r * HTW + c] = d1.at(hx0 + c, hy0 + r);
+        }
+        if (LTM) {
+            const GImg4<S> guide{(const T4*)a.guide, a.gw, a.gh, a.gpitch};
+            for (int i = threadIdx.x; i < gtw * gth; i += kT) {
+                const int r = i / gtw, c = i - r * gtw;
+                s_g[r * GTW + c] = guide.at(gx0 + c, gy0 + r).x;
+            }
+        }
+    }
+    __syncthreads();
+
+    // ---- phase 3: denoise + reassemble over the tile and its ring ----
     const SAcc4h L0{s_l0, x0 - 3, y0 - 3, PW};
     Nlf6 n;
 #pragma unroll
@@ -382,16 +502,19 @@ __global__ void __launch_bounds__(kT) final_kernel(FinalArgs a) {
         n.a[k] = a.nlf_dev[k] * a.mul[k];
         n.b[k] = a.nlf_dev[3 + k] * a.mul[3 + k];
     }
-    typedef typename Storage<S>::T4 T4;
-    const GImg4<S> i1{(const T4*)a.pyr0, a.cw, a.ch, a.cpitch};
-    const GImg4<S> d1{(const T4*)a.den1, a.cw, a.ch, a.cpitch};
     for (int i = threadIdx.x; i < EW * EH; i += kT) {
         const int r = i / EW, c = i - r * EW, x = x0 - 1 + c, y = y0 - 1 + r;
         if (x < 0 || x >= w || y < 0 || y >= h) continue;
         float4 d = ALGO == 0 ? bilateral_px(L0, x, y, n, a.chroma_boost, a.gradient_boost)
                              : guided_fast_px(L0, x, y, n);
         d = round4<S>(d);
-        d = round4<S>(reassemble_px(d, i1, d1, x, y, w, h, a.cw, a.ch, a.sharpening, n.a[0], n.b[0]));
+        const float4 p1 = tab_sample4(s_i1, T.rx[0][c], T.ry[0][r]);
+        const float4 pd1 = tab_sample4(s_d1, T.rx[0][c], T.ry[0][r]);
+        auto sharp = [&]() {
+            return make_float4(tab_sample_x(s_d1, T.rx[1][c], T.ry[0][r]), tab_sample_x(s_d1, T.rx[2][c], T.ry[0][r]),
+                               tab_sample_x(s_d1, T.rx[0][c], T.ry[1][r]), tab_sample_x(s_d1, T.rx[0][c], T.ry[2][r]));
+        };
+        d = round4<S>(reassemble_from(d, p1, pd1, sharp, a.sharpening, n.a[0], n.b[0]));
         s_den[i] = d;
     }
     __syncthreads();
@@ -404,16 +527,20 @@ __global__ void __launch_bounds__(kT) final_kernel(FinalArgs a) {
         }
         __syncthreads();
     }
-    const SAcc4f D{s_den, x0 - 1, y0 - 1, EW};
-    const GImg4<S> guide{(const T4*)a.guide, a.gw, a.gh, a.gpitch};
+
+    // ---- phase 4: LTM mask, YCbCr -> camera, sRGB ----
     for (int i = threadIdx.x; i < FW * FH; i += kT) {
         const int r = i / FW, c = i - r * FW, x = x0 + c, y = y0 + r;
         if (x >= w || y >= h) continue;
-        const float4 den = D.at(x, y);
+        const float4 den = s_den[(r + 1) * EW + c + 1];
         if (a.tap_den) reinterpret_cast<float4*>(a.tap_den)[(size_t)y * a.tap_pitch + x] = den;
         float mask = 0.0f;
         if (LTM) {
-            mask = Storage<S>::round(ltm_mask_px(D, guide, x, y, w, h, a.gw, a.gh, a.ltm, a.icy));
+            float gs[9];
+#pragma unroll
+            for (int k = 0; k < 9; k++) gs[k] = tab_sample1(s_g, T.gx[k % 3][c], T.gy[k / 3][r]);
+            const float4 inp = tab_sample4(s_den, T.lx[c], T.ly[r]);
+            mask = Storage<S>::round(ltm_mask_from(gs, inp, a.ltm, a.icy));
             if (a.tap_mask) a.tap_mask[(size_t)y * a.tap_pitch + x] = mask;
         }
         const float3 cam = round3<S>(transform_px(a.icy, make_float3(den.x, den.y, den.z)));
@@ -534,6 +661,9 @@ gls_status fused_denoise(gls_ctx* ctx, const DenoiseArgs& a, bool in_half, bool 
 }
 
 gls_status fused_final(gls_ctx* ctx, const FinalArgs& a, bool half, int algo, bool ltm, bool out_f32) {
+    // the staged tiles are sized for the pyramid's levels 1 and 3
+    if (a.cw != a.w >> 1 || a.ch != a.h >> 1 || (ltm && (a.gw != a.w >> 3 || a.gh != a.h >> 3)))
+        return set_error(ctx, GLS_ERR_INVALID_SIZE, "final stage: levels 1 and 3 must be the pyramid's");
     const dim3 grid((a.w + FW - 1) / FW, (a.h + FH - 1) / FH);
     cudaStream_t st = ctx->stream;
 #define GLS_FIN(SS, AL) \
