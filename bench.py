@@ -61,9 +61,11 @@ def make_frames(cfg, rank):
 
 
 def algorithmic_bytes_per_px(S, O, L):
-    """Compulsory bytes per pixel of the reference dataflow: raw in (2) + level 0 written
-    and read (2 x 3), 5 full-resolution single-channel planes of S bytes, output O, and
-    7 S-byte RGBA accesses per pixel on each coarser level (G = sum of 4^-l)."""
+    """Compulsory bytes per pixel of the reference dataflow, every global sync point
+    materialised once: raw noise fit 3 passes x 2 B; demosaic 2 B in + level 0 S out;
+    level-0 fit 3 passes x S; final pass level 0 S in + output O; each coarser level 7 S-byte
+    accesses per pixel of its own (write, 3 fit passes, denoise read and write, parent read),
+    G = sum of 4^-l over the coarser levels.  Total 8 + 5S + O + 7S*G."""
     G = sum(4.0 ** -l for l in range(1, L))
     return 8 + 5 * S + O + 7 * S * G
 
