@@ -3,13 +3,14 @@
 Workload (default): the phone-resolution plain pipeline -- three 4032x3024 RGGB 12-bit
 synthetic frames at read-noise/gain {2/1, 6/4, 12/16} (the last one takes the high-noise
 raw branch), 5-level pyramid, fp32 intermediates, local tone mapping on, RGBA8 output.
-One step = those three frames through RawConverter::demosaicImage.
+One step = those three frames as one burst (gls_raw_batch: demosaicImage per frame, each
+frame on its own stream).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
 value: MPix/s with the raw frames already in HBM, CUDA-event timed per step with an L2
 flush (a 256 MB write) between steps, max over ranks.  e2e: the same frames through the
-host-buffer entry point (pinned uint16 in, RGBA8 out, copies inside the timed region).
+host-buffer burst entry point (pinned uint16 in, RGBA8 out, copies inside the timed region).
 --impl reference times the CPU restatement of the reference pipeline (the oracle; the
 reference's OpenCL kernels cannot run on this machine) with every host thread.
 """
@@ -228,9 +229,13 @@ def main():
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream(dev)
 
+    # the frames of a step are a burst: one lane (converter on its own stream) per frame
+    lanes = len(frames)
+    batch = gls.RawBatch(ctx, lanes)
+    batch.reserve(w, h, cfg["levels"], cfg["storage"])
+
     def step():
-        for r, p, o in zip(raws, params, outs):
-            conv.demosaicImage(r, p, o, defer_noise_model=True)
+        batch.demosaic(raws, params, outs)
 
     for _ in range(args.warmup):
         step()
@@ -264,7 +269,8 @@ def main():
     # ---- per-stage profile (separate pass) and roofline of the dominant kernel ----
     conv.profile(True)
     for _ in range(2):
-        step()
+        for r, p, o in zip(raws, params, outs):
+            conv.demosaicImage(r, p, o, defer_noise_model=True)
     torch.cuda.synchronize()
     prof = conv.profileReport()
     conv.profile(False)
@@ -283,17 +289,21 @@ def main():
     if not args.no_e2e and not args.profile_only:
         hosts = [torch.from_numpy(f[0]).pin_memory() for f in frames]
         houts = [torch.empty((h, w, 4), dtype=torch.uint8).pin_memory() for _ in frames]
-        for hr, ho, p in zip(hosts, houts, params):
-            conv.demosaicImageHostPtr(hr.data_ptr(), w, h, p, ho.data_ptr(), 4)
+
+        def host_step():
+            batch.demosaic_host_ptr([t.data_ptr() for t in hosts], [(w, h)] * len(frames), params,
+                                    [t.data_ptr() for t in houts], 4)
+
+        for _ in range(args.warmup):
+            host_step()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            for hr, ho, p in zip(hosts, houts, params):
-                conv.demosaicImageHostPtr(hr.data_ptr(), w, h, p, ho.data_ptr(), 4)
+            host_step()
         e2e_s = time.perf_counter() - t0
         e2e = {"value": round(world * mpix_per_step * args.steps / e2e_s, 3), "unit": "MPix/s",
                "h2d_bytes_per_step": int(sum(f[0].nbytes for f in frames)),
-               "d2h_bytes_per_step": int(len(frames) * w * h * 4 + len(frames) * 9 * 8 * 4)}
+               "d2h_bytes_per_step": int(len(frames) * w * h * 4)}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu and not args.profile_only:
@@ -307,7 +317,8 @@ def main():
             "config": {"workload": cfg["name"], "frames_per_step": len(frames), "width": w, "height": h,
                        "levels": cfg["levels"], "storage": "fp32", "output": "rgba8", "local_tone_mapping": True,
                        "noise": cfg["noise"], "l2": "flushed between steps (256 MB write)",
-                       "parallelism": "replicas" if world > 1 else "single"},
+                       "parallelism": "replicas" if world > 1 else "single",
+                       "schedule": "the step's frames as one burst over %d streams (gls_raw_batch)" % lanes},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
                          "traffic": NCU_TRAFFIC[dom][0] if dom in NCU_TRAFFIC else None, "traffic_unit": "B/launch",

@@ -5,8 +5,11 @@
 // reference exactly; the differences are in how the work is scheduled:
 //   * the noise-model regressions run on the device (k_nlf.cu), so one frame is a single
 //     stream of kernel launches with no host round trip;
-//   * working images are reallocated when the frame size, pyramid depth or storage
-//     precision changes (the reference sizes them once, by the first frame).
+//   * working images are allocated for the largest frame and deepest pyramid seen so far
+//     and smaller frames run in views of them (the reference sizes them once, by the first
+//     frame, and cannot take a larger one);
+//   * gls_raw_batch spreads the frames of a burst over converters on their own streams.
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -80,6 +83,7 @@ struct gls_raw_converter {
             if (b.p) cudaFree(b.p);
         owned.clear();
         w = h = L = 0;
+        cap_w = cap_h = cap_L = 0;
     }
 
     gls_status alloc(void** p, size_t bytes) {
@@ -100,51 +104,90 @@ struct gls_raw_converter {
     ImgRef level0{};
     bool staged_alloc = false, high_noise_alloc = false;
 
+    // Working images are allocated for a capacity (the largest frame, deepest pyramid seen so
+    // far) with the capacity's pitch; a frame that fits is processed in views of them, so a
+    // converter that alternates frame sizes neither reallocates nor synchronises.
+    int cap_w = 0, cap_h = 0, cap_L = 0;
+
+    void set_views() {
+        auto view = [](ImgRef& r, int iw, int ih) {
+            if (r.ptr) {
+                r.w = iw;
+                r.h = ih;
+            }
+        };
+        view(level0, w, h);
+        for (int i = 0; i < cap_L - 1; i++) view(pyr[i], w >> (i + 1), h >> (i + 1));
+        for (int i = 0; i < cap_L; i++) view(den[i], w >> i, h >> i);
+        view(green, w, h);
+        view(linA, w, h);
+        view(linB, w, h);
+        view(mask, w, h);
+        view(scaled, w, h);
+        view(hnA, w / 2, h / 2);
+        view(hnB, w / 2, h / 2);
+    }
+
     gls_status ensure(int width, int height, int levels, bool half_storage) {
-        if (width == w && height == h && levels == L && half_storage == half) return GLS_OK;
-        cudaStreamSynchronize(ctx->stream);
-        release();
-        staged_alloc = high_noise_alloc = false;
-        half = half_storage;
-        {
+        const bool fits = cap_w >= width && cap_h >= height && cap_L >= levels && half_storage == half;
+        if (!fits) {
+            const bool keep = half_storage == half && cap_w > 0;
+            const int nw = keep ? std::max(cap_w, width) : width, nh = keep ? std::max(cap_h, height) : height;
+            const int nL = keep ? std::max(cap_L, levels) : levels;
+            cudaStreamSynchronize(ctx->stream);
+            release();
+            for (int i = 0; i < GLS_MAX_LEVELS; i++) pyr[i] = den[i] = ImgRef{};
+            green = linA = linB = mask = scaled = hnA = hnB = ImgRef{};
+            staged_alloc = high_noise_alloc = false;
+            half = half_storage;
+            {
+                void* p = nullptr;
+                GLS_CHECK(alloc(&p, (size_t)nw * nh * 8));
+                level0 = ImgRef{p, nw, nh, nw, true};
+            }
+            for (int i = 0; i < nL - 1; i++) GLS_CHECK(img(pyr[i], nw >> (i + 1), nh >> (i + 1), 4));
+            for (int i = 1; i < nL; i++) GLS_CHECK(img(den[i], nw >> i, nh >> i, 4));
             void* p = nullptr;
-            GLS_CHECK(alloc(&p, (size_t)width * height * 8));
-            level0 = ImgRef{p, width, height, width, true};
+            GLS_CHECK(alloc(&p, (1 + GLS_MAX_LEVELS) * 8 * sizeof(float)));
+            nlf_dev = (float*)p;
+            GLS_CHECK(alloc(&nlf_scratch, kNlfScratchBytes));
+            // the regression ticket starts at zero; every pass leaves it at zero
+            GLS_CHECK(check_cuda(ctx, cudaMemsetAsync(nlf_scratch, 0, kNlfHeaderBytes, ctx->stream),
+                                 "clear regression state"));
+            gf_scratch = nullptr;
+            gf_scratch_bytes = 0;
+            cap_w = nw;
+            cap_h = nh;
+            cap_L = nL;
         }
-        for (int i = 0; i < levels - 1; i++) GLS_CHECK(img(pyr[i], width >> (i + 1), height >> (i + 1), 4));
-        for (int i = 1; i < levels; i++) GLS_CHECK(img(den[i], width >> i, height >> i, 4));
-        void* p = nullptr;
-        GLS_CHECK(alloc(&p, (1 + GLS_MAX_LEVELS) * 8 * sizeof(float)));
-        nlf_dev = (float*)p;
-        GLS_CHECK(alloc(&nlf_scratch, kNlfScratchBytes));
-        // the regression ticket starts at zero; every pass leaves it at zero
-        GLS_CHECK(check_cuda(ctx, cudaMemsetAsync(nlf_scratch, 0, kNlfHeaderBytes, ctx->stream), "clear regression state"));
-        gf_scratch = nullptr;
-        gf_scratch_bytes = 0;
         w = width;
         h = height;
         L = levels;
+        set_views();
         return GLS_OK;
     }
 
     // working images of the single-stage pipeline, allocated on first use
     gls_status ensure_staged() {
         if (staged_alloc) return GLS_OK;
-        GLS_CHECK(img(green, w, h, 1));
-        GLS_CHECK(img(linA, w, h, 4));
-        GLS_CHECK(img(linB, w, h, 4));
-        GLS_CHECK(img(mask, w, h, 1));
-        GLS_CHECK(img(den[0], w, h, 4));
+        GLS_CHECK(img(green, cap_w, cap_h, 1));
+        GLS_CHECK(img(linA, cap_w, cap_h, 4));
+        GLS_CHECK(img(linB, cap_w, cap_h, 4));
+        GLS_CHECK(img(mask, cap_w, cap_h, 1));
+        GLS_CHECK(img(den[0], cap_w, cap_h, 4));
         staged_alloc = true;
-        return ensure_high_noise();
+        GLS_CHECK(ensure_high_noise());
+        set_views();
+        return GLS_OK;
     }
 
     gls_status ensure_high_noise() {
         if (high_noise_alloc) return GLS_OK;
-        GLS_CHECK(img(scaled, w, h, 1));
-        GLS_CHECK(img(hnA, w / 2, h / 2, 4));
-        GLS_CHECK(img(hnB, w / 2, h / 2, 4));
+        GLS_CHECK(img(scaled, cap_w, cap_h, 1));
+        GLS_CHECK(img(hnA, cap_w / 2, cap_h / 2, 4));
+        GLS_CHECK(img(hnB, cap_w / 2, cap_h / 2, 4));
         high_noise_alloc = true;
+        set_views();
         return GLS_OK;
     }
 
@@ -474,6 +517,46 @@ struct gls_raw_converter {
         return check_launch(ctx, "RawConverter::demosaicImage");
     }
 
+    // device staging of the host-buffer entry points: raw frame, RGBA8 output and its RGB8 copy
+    gls_status ensure_staging(int fw, int fh) {
+        const size_t rb = (size_t)fw * fh * 2, ob = (size_t)fw * fh * 4 + (size_t)fw * fh * 3;
+        if (raw_dev_bytes < rb) {
+            if (raw_dev) cudaFree(raw_dev);
+            raw_dev = nullptr;
+            raw_dev_bytes = 0;
+            GLS_CHECK(check_cuda(ctx, cudaMalloc(&raw_dev, rb), "cudaMalloc(raw)"));
+            raw_dev_bytes = rb;
+        }
+        if (out_dev_bytes < ob) {
+            if (out_dev) cudaFree(out_dev);
+            out_dev = nullptr;
+            out_dev_bytes = 0;
+            GLS_CHECK(check_cuda(ctx, cudaMalloc(&out_dev, ob), "cudaMalloc(output)"));
+            out_dev_bytes = ob;
+        }
+        return GLS_OK;
+    }
+
+    // host raw in, host RGBA8/RGB8 out, all on this converter's stream (no synchronisation)
+    gls_status run_host(const uint16_t* raw, int fw, int fh, int stride, gls_demosaic_params* p, uint8_t* out,
+                        int out_channels) {
+        GLS_CHECK(ensure_staging(fw, fh));
+        GLS_CHECK(check_cuda(ctx, cudaMemcpy2DAsync(raw_dev, (size_t)fw * 2, raw, (size_t)stride * 2, (size_t)fw * 2,
+                                                    fh, cudaMemcpyHostToDevice, ctx->stream), "copy raw frame"));
+        GLS_CHECK(ensure(fw, fh, p->pyramid_levels, p->storage == GLS_STORAGE_F16));
+        GLS_CHECK(run(raw_dev, fw, p, out_dev, false, fw));
+        const void* src = out_dev;
+        if (out_channels == 3) {
+            uint8_t* rgb = out_dev + (size_t)fw * fh * 4;
+            rgba8_to_rgb8_kernel<<<dim3((fw + 31) / 32, (fh + 7) / 8), dim3(32, 8), 0, ctx->stream>>>(
+                (const uchar4*)out_dev, fw, fh, rgb);
+            ctx->launches++;
+            src = rgb;
+        }
+        return check_cuda(ctx, cudaMemcpyAsync(out, src, (size_t)fw * fh * out_channels, cudaMemcpyDeviceToHost,
+                                               ctx->stream), "copy output");
+    }
+
     gls_status fetch_noise_model(gls_demosaic_params* p) {
         const size_t n = (1 + GLS_MAX_LEVELS) * 8;
         GLS_CHECK(check_cuda(ctx, cudaMemcpyAsync(nlf_host, nlf_dev, n * sizeof(float), cudaMemcpyDeviceToHost,
@@ -607,35 +690,7 @@ gls_status gls_raw_converter_demosaic_host(gls_raw_converter* c, const uint16_t*
         return set_error(ctx, GLS_ERR_INVALID_ARGUMENT, "out_channels must be 3 or 4");
     if (stride < w) return set_error(ctx, GLS_ERR_INVALID_SIZE, "raw stride smaller than width");
     GLS_CHECK(validate_params(ctx, p, w, h));
-    const size_t rb = (size_t)w * h * 2, ob = (size_t)w * h * 4 + (size_t)w * h * 3;
-    if (c->raw_dev_bytes < rb) {
-        if (c->raw_dev) cudaFree(c->raw_dev);
-        c->raw_dev = nullptr;
-        c->raw_dev_bytes = 0;
-        GLS_CHECK(check_cuda(ctx, cudaMalloc(&c->raw_dev, rb), "cudaMalloc(raw)"));
-        c->raw_dev_bytes = rb;
-    }
-    if (c->out_dev_bytes < ob) {
-        if (c->out_dev) cudaFree(c->out_dev);
-        c->out_dev = nullptr;
-        c->out_dev_bytes = 0;
-        GLS_CHECK(check_cuda(ctx, cudaMalloc(&c->out_dev, ob), "cudaMalloc(output)"));
-        c->out_dev_bytes = ob;
-    }
-    GLS_CHECK(check_cuda(ctx, cudaMemcpy2DAsync(c->raw_dev, (size_t)w * 2, raw, (size_t)stride * 2, (size_t)w * 2, h,
-                                                cudaMemcpyHostToDevice, ctx->stream), "copy raw frame"));
-    GLS_CHECK(c->ensure(w, h, p->pyramid_levels, p->storage == GLS_STORAGE_F16));
-    GLS_CHECK(c->run(c->raw_dev, w, p, c->out_dev, false, w));
-    const void* src = c->out_dev;
-    if (out_channels == 3) {
-        uint8_t* rgb = c->out_dev + (size_t)w * h * 4;
-        rgba8_to_rgb8_kernel<<<dim3((w + 31) / 32, (h + 7) / 8), dim3(32, 8), 0, ctx->stream>>>(
-            (const uchar4*)c->out_dev, w, h, rgb);
-        ctx->launches++;
-        src = rgb;
-    }
-    GLS_CHECK(check_cuda(ctx, cudaMemcpyAsync(out, src, (size_t)w * h * out_channels, cudaMemcpyDeviceToHost,
-                                              ctx->stream), "copy output"));
+    GLS_CHECK(c->run_host(raw, w, h, stride, p, out, out_channels));
     return c->fetch_noise_model(p);
 }
 
@@ -663,6 +718,219 @@ gls_status gls_raw_converter_fast_demosaic(gls_raw_converter* c, const gls_image
     const RgbParams rp = rgb_params_init(rc.contrast, rc.saturation, rc.toneCurveSlope, rc.exposureBias, rc.blacks, 0);
     launch_srgb(ctx, half_rgb, nullptr, out->ptr, out->format == GLS_RGBA_F32, pitch_elems(out), p->rgb_cam, rp);
     return check_launch(ctx, "RawConverter::fastDemosaicImage");
+}
+
+}  // extern "C"
+
+// =========================================================================================
+// gls_raw_batch: a burst of frames spread over converters ("lanes") on their own streams.
+// The work of one frame stays a serial chain (raw fit -> demosaic -> level fits -> denoise
+// -> final); frames are independent, so lanes overlap one frame's latency-bound parts (the
+// small pyramid levels, the regression solves) with another's full-frame kernels.
+// =========================================================================================
+struct gls_raw_batch {
+    gls_ctx* ctx = nullptr;  // the caller's context: its stream forks and joins the lanes
+    std::vector<gls_ctx*> lane_ctx;
+    std::vector<cudaStream_t> lane_stream;
+    std::vector<gls_raw_converter*> lane;
+    cudaEvent_t fork = nullptr;
+    std::vector<cudaEvent_t> join;
+    std::vector<int> lane_of;
+};
+
+namespace {
+
+// Longest processing time first: frames by pixel count, largest first, each to the lane with
+// the fewest pixels so far (ties: the lower frame index, the lower lane).
+void plan_lanes(int n, const int* widths, const int* heights, int lanes, int* lane_of) {
+    std::vector<int> order(n);
+    for (int i = 0; i < n; i++) order[i] = i;
+    auto px = [&](int i) { return (long long)widths[i] * heights[i]; };
+    for (int i = 1; i < n; i++) {  // stable insertion sort by decreasing pixel count
+        const int v = order[i];
+        int j = i - 1;
+        while (j >= 0 && px(order[j]) < px(v)) {
+            order[j + 1] = order[j];
+            j--;
+        }
+        order[j + 1] = v;
+    }
+    std::vector<long long> load(lanes, 0);
+    for (int k = 0; k < n; k++) {
+        const int i = order[k];
+        int best = 0;
+        for (int l = 1; l < lanes; l++)
+            if (load[l] < load[best]) best = l;
+        lane_of[i] = best;
+        load[best] += px(i);
+    }
+}
+
+gls_status batch_error(gls_raw_batch* b, int l, gls_status s) {
+    if (s != GLS_OK && l >= 0) set_error(b->ctx, s, "lane %d: %s", l, b->lane_ctx[l]->last_error.c_str());
+    return s;
+}
+
+// fork: every lane waits for the work already on the caller's stream
+gls_status batch_fork(gls_raw_batch* b) {
+    GLS_CHECK(check_cuda(b->ctx, cudaEventRecord(b->fork, b->ctx->stream), "cudaEventRecord(fork)"));
+    for (size_t l = 0; l < b->lane.size(); l++)
+        GLS_CHECK(check_cuda(b->ctx, cudaStreamWaitEvent(b->lane_stream[l], b->fork, 0), "cudaStreamWaitEvent(fork)"));
+    return GLS_OK;
+}
+
+// join: the caller's stream waits for every lane; the lanes' launches count on the context
+gls_status batch_join(gls_raw_batch* b, const std::vector<uint64_t>& launches0) {
+    for (size_t l = 0; l < b->lane.size(); l++) {
+        GLS_CHECK(check_cuda(b->ctx, cudaEventRecord(b->join[l], b->lane_stream[l]), "cudaEventRecord(join)"));
+        GLS_CHECK(check_cuda(b->ctx, cudaStreamWaitEvent(b->ctx->stream, b->join[l], 0), "cudaStreamWaitEvent(join)"));
+        b->ctx->launches += b->lane_ctx[l]->launches - launches0[l];
+    }
+    return GLS_OK;
+}
+
+std::vector<uint64_t> lane_launches(gls_raw_batch* b) {
+    std::vector<uint64_t> v;
+    for (auto* c : b->lane_ctx) v.push_back(c->launches);
+    return v;
+}
+
+}  // namespace
+
+extern "C" {
+
+gls_status gls_raw_batch_plan(int n, const int* widths, const int* heights, int lanes, int* lane_of) {
+    if (n < 0 || lanes < 1 || (n > 0 && (!widths || !heights || !lane_of))) return GLS_ERR_INVALID_ARGUMENT;
+    plan_lanes(n, widths, heights, lanes, lane_of);
+    return GLS_OK;
+}
+
+gls_status gls_raw_batch_destroy(gls_raw_batch* b) {
+    if (!b) return GLS_ERR_INVALID_ARGUMENT;
+    cudaStreamSynchronize(b->ctx->stream);
+    for (size_t l = 0; l < b->lane.size(); l++) {
+        if (b->lane[l]) gls_raw_converter_destroy(b->lane[l]);
+        if (b->lane_ctx[l]) gls_ctx_destroy(b->lane_ctx[l]);
+        if (b->lane_stream[l]) cudaStreamDestroy(b->lane_stream[l]);
+        if (b->join[l]) cudaEventDestroy(b->join[l]);
+    }
+    if (b->fork) cudaEventDestroy(b->fork);
+    delete b;
+    return GLS_OK;
+}
+
+gls_status gls_raw_batch_create(gls_ctx* ctx, int lanes, gls_raw_batch** out) {
+    if (!ctx || !out) return GLS_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    if (lanes < 1 || lanes > 16) return set_error(ctx, GLS_ERR_INVALID_ARGUMENT, "lanes must be in [1, 16]");
+    gls_raw_batch* b = new gls_raw_batch();
+    b->ctx = ctx;
+    b->lane_ctx.assign(lanes, nullptr);
+    b->lane_stream.assign(lanes, nullptr);
+    b->lane.assign(lanes, nullptr);
+    b->join.assign(lanes, nullptr);
+    gls_status s = check_cuda(ctx, cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming), "cudaEventCreate");
+    for (int l = 0; l < lanes && s == GLS_OK; l++) {
+        s = gls_ctx_create(ctx->device, &b->lane_ctx[l]);
+        if (s != GLS_OK) {
+            set_error(ctx, s, "lane %d: context", l);
+            break;
+        }
+        s = check_cuda(ctx, cudaStreamCreateWithFlags(&b->lane_stream[l], cudaStreamNonBlocking), "cudaStreamCreate");
+        if (s != GLS_OK) break;
+        b->lane_ctx[l]->stream = b->lane_stream[l];
+        s = check_cuda(ctx, cudaEventCreateWithFlags(&b->join[l], cudaEventDisableTiming), "cudaEventCreate");
+        if (s != GLS_OK) break;
+        s = gls_raw_converter_create(b->lane_ctx[l], &b->lane[l]);
+        if (s != GLS_OK) batch_error(b, l, s);
+    }
+    if (s != GLS_OK) {
+        gls_raw_batch_destroy(b);
+        return s;
+    }
+    *out = b;
+    return GLS_OK;
+}
+
+gls_status gls_raw_batch_reserve(gls_raw_batch* b, int width, int height, int levels, int storage) {
+    if (!b) return GLS_ERR_INVALID_ARGUMENT;
+    if (width <= 0 || height <= 0 || (width & 1) || (height & 1) || levels < 4 || levels > GLS_MAX_LEVELS ||
+        (storage != GLS_STORAGE_F32 && storage != GLS_STORAGE_F16))
+        return set_error(b->ctx, GLS_ERR_INVALID_ARGUMENT, "reserve: bad frame size, levels or storage");
+    for (size_t l = 0; l < b->lane.size(); l++) {
+        gls_raw_converter* c = b->lane[l];
+        gls_status s = c->ensure(width, height, levels, storage == GLS_STORAGE_F16);
+        if (s == GLS_OK) s = c->ensure_high_noise();
+        if (s == GLS_OK) s = c->ensure_staging(width, height);
+        if (s != GLS_OK) return batch_error(b, (int)l, s);
+    }
+    for (size_t l = 0; l < b->lane.size(); l++)
+        GLS_CHECK(check_cuda(b->ctx, cudaStreamSynchronize(b->lane_stream[l]), "synchronize lanes"));
+    return GLS_OK;
+}
+
+gls_status gls_raw_batch_demosaic(gls_raw_batch* b, int n, const gls_image_desc* raws,
+                                  const gls_demosaic_params* params, const gls_image_desc* outs) {
+    if (!b) return GLS_ERR_INVALID_ARGUMENT;
+    gls_ctx* ctx = b->ctx;
+    if (n < 0 || (n > 0 && (!raws || !params || !outs))) return set_error(ctx, GLS_ERR_INVALID_ARGUMENT, "batch arrays");
+    std::vector<int> ws(n), hs(n);
+    for (int i = 0; i < n; i++) {
+        GLS_CHECK(check_desc(ctx, &raws[i], "raw", GLS_R16_UNORM));
+        GLS_CHECK(check_desc(ctx, &outs[i], "out", GLS_RGBA8_UNORM, GLS_RGBA_F32));
+        if (outs[i].width != raws[i].width || outs[i].height != raws[i].height)
+            return set_error(ctx, GLS_ERR_INVALID_SIZE, "frame %d: output size differs from the raw frame", i);
+        GLS_CHECK(validate_params(ctx, &params[i], raws[i].width, raws[i].height));
+        ws[i] = raws[i].width;
+        hs[i] = raws[i].height;
+    }
+    b->lane_of.assign(n, 0);
+    const int lanes = (int)b->lane.size();
+    plan_lanes(n, ws.data(), hs.data(), lanes, b->lane_of.data());
+    const std::vector<uint64_t> l0 = lane_launches(b);
+    GLS_CHECK(batch_fork(b));
+    // frames in index order, so the lanes' work is enqueued interleaved
+    for (int i = 0; i < n; i++) {
+        const int l = b->lane_of[i];
+        gls_raw_converter* c = b->lane[l];
+        gls_demosaic_params p = params[i];
+        gls_status s = c->ensure(ws[i], hs[i], p.pyramid_levels, p.storage == GLS_STORAGE_F16);
+        if (s == GLS_OK)
+            s = c->run((const uint16_t*)raws[i].ptr, pitch_elems(&raws[i]), &p, outs[i].ptr,
+                       outs[i].format == GLS_RGBA_F32, pitch_elems(&outs[i]));
+        if (s != GLS_OK) return batch_error(b, l, s);
+    }
+    return batch_join(b, l0);
+}
+
+gls_status gls_raw_batch_demosaic_host(gls_raw_batch* b, int n, const uint16_t* const* raws, const int* widths,
+                                       const int* heights, const int* raw_strides, const gls_demosaic_params* params,
+                                       uint8_t* const* outs, int out_channels) {
+    if (!b) return GLS_ERR_INVALID_ARGUMENT;
+    gls_ctx* ctx = b->ctx;
+    if (n < 0 || (n > 0 && (!raws || !widths || !heights || !raw_strides || !params || !outs)))
+        return set_error(ctx, GLS_ERR_INVALID_ARGUMENT, "batch arrays");
+    if (out_channels != 3 && out_channels != 4)
+        return set_error(ctx, GLS_ERR_INVALID_ARGUMENT, "out_channels must be 3 or 4");
+    for (int i = 0; i < n; i++) {
+        if (!raws[i] || !outs[i]) return set_error(ctx, GLS_ERR_INVALID_ARGUMENT, "frame %d: null buffer", i);
+        if (raw_strides[i] < widths[i]) return set_error(ctx, GLS_ERR_INVALID_SIZE, "frame %d: stride < width", i);
+        GLS_CHECK(validate_params(ctx, &params[i], widths[i], heights[i]));
+    }
+    b->lane_of.assign(n, 0);
+    const int lanes = (int)b->lane.size();
+    plan_lanes(n, widths, heights, lanes, b->lane_of.data());
+    const std::vector<uint64_t> l0 = lane_launches(b);
+    GLS_CHECK(batch_fork(b));
+    for (int i = 0; i < n; i++) {
+        const int l = b->lane_of[i];
+        gls_demosaic_params p = params[i];
+        const gls_status s =
+            b->lane[l]->run_host(raws[i], widths[i], heights[i], raw_strides[i], &p, outs[i], out_channels);
+        if (s != GLS_OK) return batch_error(b, l, s);
+    }
+    GLS_CHECK(batch_join(b, l0));
+    return check_cuda(ctx, cudaStreamSynchronize(ctx->stream), "synchronize");
 }
 
 }  // extern "C"

@@ -8,6 +8,7 @@ kernels of libgls_cuda.  There is no CPU fallback: without the built library eve
 raises.
 """
 import ctypes
+import weakref
 import os
 
 import numpy as np
@@ -129,6 +130,15 @@ SIGNATURES = [
     ("gls_raw_converter_set_mode", _I, [_P, _I]),
     ("gls_raw_converter_profile", _I, [_P, _I]),
     ("gls_raw_converter_profile_report", _I, [_P, ctypes.c_char_p, ctypes.c_size_t]),
+    ("gls_raw_batch_create", _I, [_P, _I, ctypes.POINTER(_P)]),
+    ("gls_raw_batch_destroy", _I, [_P]),
+    ("gls_raw_batch_reserve", _I, [_P, _I, _I, _I, _I]),
+    ("gls_raw_batch_demosaic", _I, [_P, _I, _D, ctypes.POINTER(DemosaicParams), _D]),
+    ("gls_raw_batch_demosaic_host", _I, [_P, _I, ctypes.POINTER(_P), ctypes.POINTER(ctypes.c_int),
+                                         ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                         ctypes.POINTER(DemosaicParams), ctypes.POINTER(_P), _I]),
+    ("gls_raw_batch_plan", _I, [_I, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int), _I,
+                                ctypes.POINTER(ctypes.c_int)]),
 ]
 
 
@@ -222,6 +232,9 @@ class Context:
         s = self._lib.gls_ctx_create(device, ctypes.byref(self.handle))
         if s != GLS_OK:
             raise GlsError(s, "gls_ctx_create")
+        # converters and batches made on this context: closed before it, whatever the order
+        # in which Python finalises them
+        self._children = weakref.WeakSet()
         self.set_stream(stream if stream is not None else torch.cuda.current_stream(device))
 
     def set_stream(self, stream):
@@ -245,6 +258,8 @@ class Context:
 
     def close(self):
         if self.handle:
+            for child in list(getattr(self, "_children", ())):
+                child.close()
             self._lib.gls_ctx_destroy(self.handle)
             self.handle = ctypes.c_void_p()
 
@@ -358,6 +373,7 @@ class RawConverter:
         self.ctx = ctx
         self.handle = ctypes.c_void_p()
         ctx.check(lib().gls_raw_converter_create(ctx.handle, ctypes.byref(self.handle)), "RawConverter")
+        ctx._children.add(self)
 
     def demosaicImage(self, raw, params, out, defer_noise_model=False):
         """raw: (H, W) uint16 CUDA tensor; out: (H, W, 4) uint8 (RGBA8) or float32 CUDA tensor."""
@@ -406,6 +422,64 @@ class RawConverter:
     def close(self):
         if self.handle:
             lib().gls_raw_converter_destroy(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def batch_plan(sizes, lanes):
+    """The lane of each (width, height) frame as gls_raw_batch assigns them."""
+    n = len(sizes)
+    ws = (ctypes.c_int * max(n, 1))(*[w for w, _ in sizes])
+    hs = (ctypes.c_int * max(n, 1))(*[h for _, h in sizes])
+    out = (ctypes.c_int * max(n, 1))()
+    s = lib().gls_raw_batch_plan(n, ws, hs, int(lanes), out)
+    if s != GLS_OK:
+        raise GlsError(s, "gls_raw_batch_plan")
+    return [int(out[i]) for i in range(n)]
+
+
+class RawBatch:
+    """gls_raw_batch: a burst of frames over `lanes` converters on their own streams, forked
+    from and joined back to the context's stream."""
+
+    def __init__(self, ctx, lanes=3):
+        self.ctx = ctx
+        self.handle = ctypes.c_void_p()
+        ctx.check(lib().gls_raw_batch_create(ctx.handle, int(lanes), ctypes.byref(self.handle)), "RawBatch")
+        ctx._children.add(self)
+
+    def reserve(self, width, height, levels, storage=STORAGE_F32):
+        self.ctx.check(lib().gls_raw_batch_reserve(self.handle, int(width), int(height), int(levels), int(storage)),
+                       "RawBatch.reserve")
+
+    def demosaic(self, raws, params, outs):
+        """raws: (H, W) uint16 CUDA tensors; params: DemosaicParams; outs: (H, W, 4) uint8 or float32."""
+        n = len(raws)
+        rd = (ImageDesc * max(n, 1))(*[desc(r) for r in raws])
+        od = (ImageDesc * max(n, 1))(*[desc(o) for o in outs])
+        pa = (DemosaicParams * max(n, 1))(*params)
+        self.ctx.check(lib().gls_raw_batch_demosaic(self.handle, n, rd, pa, od), "RawBatch.demosaic")
+        return outs
+
+    def demosaic_host_ptr(self, raw_ptrs, sizes, params, out_ptrs, channels=4):
+        """Host frames by address (pinned for overlapped copies); sizes: (width, height)."""
+        n = len(raw_ptrs)
+        rp = (ctypes.c_void_p * max(n, 1))(*raw_ptrs)
+        op = (ctypes.c_void_p * max(n, 1))(*out_ptrs)
+        ws = (ctypes.c_int * max(n, 1))(*[w for w, _ in sizes])
+        hs = (ctypes.c_int * max(n, 1))(*[h for _, h in sizes])
+        pa = (DemosaicParams * max(n, 1))(*params)
+        self.ctx.check(lib().gls_raw_batch_demosaic_host(self.handle, n, rp, ws, hs, ws, pa, op, int(channels)),
+                       "RawBatch.demosaic_host")
+
+    def close(self):
+        if self.handle:
+            lib().gls_raw_batch_destroy(self.handle)
             self.handle = ctypes.c_void_p()
 
     def __del__(self):

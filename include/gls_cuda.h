@@ -108,6 +108,7 @@ typedef struct gls_raw_converter gls_raw_converter;
 
 /* ---- context ---- */
 GLS_API gls_status gls_ctx_create(int device, gls_ctx** out);
+/* Destroy the converters and batches made on a context before the context itself. */
 GLS_API gls_status gls_ctx_destroy(gls_ctx* ctx);
 GLS_API gls_status gls_ctx_set_stream(gls_ctx* ctx, void* cuda_stream);
 GLS_API gls_status gls_ctx_synchronize(gls_ctx* ctx);
@@ -252,6 +253,35 @@ GLS_API gls_status gls_raw_converter_set_mode(gls_raw_converter* conv, int mode)
  * {"stage": [total_ms, calls], ...} accumulated since profiling was enabled. */
 GLS_API gls_status gls_raw_converter_profile(gls_raw_converter* conv, int enable);
 GLS_API gls_status gls_raw_converter_profile_report(gls_raw_converter* conv, char* buf, size_t buf_len);
+
+/* ---- bursts: demosaicImage over many frames at once ----
+ * No counterpart in the reference, where a burst is a loop of demosaicImage calls.  The
+ * frames (any sizes, CFA phases, bit depths and parameters) are spread over `lanes`
+ * converters, each on its own stream, largest frame first to the least-loaded lane; one
+ * frame's stages stay in order while different frames overlap.  gls_raw_batch_demosaic
+ * forks the lanes from the context's stream and joins them back with events, so it returns
+ * at once, later work on that stream sees every output, and the whole call can be captured
+ * in a CUDA graph from that stream once gls_raw_batch_reserve has sized the lanes (nothing
+ * is allocated for frames that fit; the single-stage schedule of GuidedPrecise may still
+ * allocate on first use).  Noise models are not returned (as with defer_noise_model).  On an
+ * error, outputs of the call are undefined. */
+typedef struct gls_raw_batch gls_raw_batch;
+GLS_API gls_status gls_raw_batch_create(gls_ctx* ctx, int lanes, gls_raw_batch** out);
+GLS_API gls_status gls_raw_batch_destroy(gls_raw_batch* batch);
+/* Sizes every lane for frames up to width x height, `levels` pyramid levels and `storage`. */
+GLS_API gls_status gls_raw_batch_reserve(gls_raw_batch* batch, int width, int height, int levels, int storage);
+/* n device frames: raws[i] R16_UNORM, outs[i] RGBA8_UNORM or RGBA_F32 of the same size. */
+GLS_API gls_status gls_raw_batch_demosaic(gls_raw_batch* batch, int n, const gls_image_desc* raws,
+                                          const gls_demosaic_params* params, const gls_image_desc* outs);
+/* n host frames (as gls_raw_converter_demosaic_host); returns when every output is written.
+ * Copies run on the lanes' streams, so with pinned host buffers they overlap other frames. */
+GLS_API gls_status gls_raw_batch_demosaic_host(gls_raw_batch* batch, int n, const uint16_t* const* raws,
+                                               const int* widths, const int* heights, const int* raw_strides_px,
+                                               const gls_demosaic_params* params, uint8_t* const* outs,
+                                               int out_channels);
+/* The lane of each frame, as the batch assigns them (frames by decreasing pixel count, each
+ * to the lane with the fewest pixels so far; ties to the lower frame index and lane). */
+GLS_API gls_status gls_raw_batch_plan(int n, const int* widths, const int* heights, int lanes, int* lane_of);
 
 #ifdef __cplusplus
 }
