@@ -148,19 +148,54 @@ GLS_DI float2 sobel_signed(const Acc& im, int x, int y) {
 }
 
 // sob(i, j) returns the SobelVal at offset (i, j) from the centre.
+// The literal evaluation (rare: sigma outside the ranges the fast forms cover).
 template <class SobF>
-GLS_DI float2 bilateral_sobel(const SobF& sob, float sigma) {
+__device__ __noinline__ float2 bilateral_sobel_literal(const SobF& sob, float e0, float e1) {
     const SobelVal c = sob(0, 0);
     float sx = 0.0f, sy = 0.0f, ws = 0.0f;
+    for (int j = -2; j <= 2; j++) {
+        for (int i = -2; i <= 2; i++) {
+            const SobelVal g = sob(i, j);
+            const float w = 1.0f - glsm::smoothstep_ref(e0, e1, 0.05f * mabs(g.len - c.len));
+            sx = sx + w * g.gx;
+            sy = sy + w * g.gy;
+            ws = ws + w;
+        }
+    }
+    return make_float2(div_(sx, ws), div_(sy, ws));
+}
+
+// The weight 1 - smoothstep(e0, e1, x) of every tap is evaluated in one of two exact forms,
+// chosen once per pixel:
+//  - e0 >= 2^-36 and e1 - e0 in the shortcut's divisor range: x and e0 are floats, so a
+//    positive x - e0 is at least 2^-60 and the shared-divisor division is exact for it;
+//  - sigma = 0 (a black neighbourhood): e0 = e1 = 0 and x >= 0, so (x - 0) / 0 clamps to
+//    1 for x > 0 and 0/0 to 0 (the clamp returns the bound for NaN): the weight is x == 0.
+// Any other sigma (NaN, subnormal) takes the literal evaluation.
+template <class SobF>
+GLS_DI float2 bilateral_sobel(const SobF& sob, float sigma) {
     const float e0 = 4.0f * sigma, e1 = 16.0f * sigma;
     FastDiv den;
     den.init(e1 - e0);
+    const bool fast = den.ok && den.d > 0.0f && e0 >= 1.4551915228366852e-11f;  // 2^-36
+    const bool zero = e0 == 0.0f && e1 == 0.0f;
+    if (!(fast || zero)) return bilateral_sobel_literal(sob, e0, e1);
+    const SobelVal c = sob(0, 0);
+    float sx = 0.0f, sy = 0.0f, ws = 0.0f;
 #pragma unroll
     for (int j = -2; j <= 2; j++) {
 #pragma unroll
         for (int i = -2; i <= 2; i++) {
             const SobelVal g = sob(i, j);
-            const float w = 1.0f - glsm::smoothstep_den(e0, den, 0.05f * mabs(g.len - c.len));
+            const float x = 0.05f * mabs(g.len - c.len);
+            float w;
+            if (fast) {
+                const float num = x - e0;
+                const float t = !(num > 0.0f) ? 0.0f : (num >= den.d ? 1.0f : den.fast(num));
+                w = 1.0f - t * t * (3.0f - 2.0f * t);
+            } else {
+                w = x > 0.0f ? 0.0f : 1.0f;
+            }
             sx = sx + w * g.gx;
             sy = sy + w * g.gy;
             ws = ws + w;
@@ -308,7 +343,9 @@ GLS_DI void cswap(float& a, float& b) {
     b = mmax(t, b);
 }
 
-template <class Acc4>
+// HALF_EXACT: the accessor returns binary16 values already (a half4 tile), so the
+// rounding of every read to binary16 is the identity and is skipped.
+template <bool HALF_EXACT = false, class Acc4>
 GLS_DI float4 despeckle_px(const Acc4& im, int px, int py, float va0, float vb0) {
     using glsm::round_half;
     float sample = 0.0f, firstMax = 0.0f, secMax = 0.0f;
@@ -317,9 +354,9 @@ GLS_DI float4 despeckle_px(const Acc4& im, int px, int py, float va0, float vb0)
     float acb[6], acr[6];
     auto rd = [&](int dx, int dy, float& cb, float& cr) {
         const float4 p = im.at(px + dx, py + dy);
-        const float v = round_half(p.x);
-        cb = round_half(p.y);
-        cr = round_half(p.z);
+        const float v = HALF_EXACT ? p.x : round_half(p.x);
+        cb = HALF_EXACT ? p.y : round_half(p.y);
+        cr = HALF_EXACT ? p.z : round_half(p.z);
         secMax = (v <= firstMax && v > secMax) ? v : secMax;
         secMax = v > firstMax ? firstMax : secMax;
         firstMax = v > firstMax ? v : firstMax;

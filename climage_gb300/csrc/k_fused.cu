@@ -46,15 +46,14 @@ struct SAcc4f {
 };
 
 struct SobelMap {
-    const float* base;
-    int plane;  // elements per plane (gx | gy | len)
+    const float4* base;  // {|gx|, |gy|, length, -}
     int x0, y0, ld, x, y;
     GLS_DI SobelVal operator()(int i, int j) const {
-        const int k = (y + j - y0) * ld + (x + i - x0);
+        const float4 q = base[(y + j - y0) * ld + (x + i - x0)];
         SobelVal v;
-        v.gx = base[k];
-        v.gy = base[plane + k];
-        v.len = base[2 * plane + k];
+        v.gx = q.x;
+        v.gy = q.y;
+        v.len = q.z;
         return v;
     }
 };
@@ -127,12 +126,12 @@ __global__ void __launch_bounds__(kT) demosaic_kernel(DemosaicArgs a) {
     constexpr int SW = TW + 8, SH = TH + 8;    // Sobel map, origin (x0 - 4, y0 - 4)
     constexpr int GW = TW + 4, GH = TH + 4;    // green, origin (x0 - 2, y0 - 2)
     constexpr int CW = TW + 2, CH = TH + 2;    // YCbCr (binary16), origin (x0 - 1, y0 - 1)
-    static_assert(CW * CH * 8 <= 3 * SW * SH * 4, "YCbCr tile must fit in the Sobel map space");
+    static_assert(CW * CH * 8 <= SW * SH * 16, "YCbCr tile must fit in the Sobel map space");
     static_assert(GW % 2 == 0, "green region pairs");
     __shared__ float s_raw[RH * RW];
     __shared__ float s_green[GH * GW];
-    __shared__ __align__(16) float s_u[3 * SH * SW];
-    half4* s_ycc = reinterpret_cast<half4*>(s_u);
+    __shared__ float4 s_sob[SH * SW];
+    half4* s_ycc = reinterpret_cast<half4*>(s_sob);
 
     const int x0 = blockIdx.x * TW, y0 = blockIdx.y * TH;
     const int w = a.w, h = a.h, bayer = a.bayer;
@@ -159,9 +158,7 @@ __global__ void __launch_bounds__(kT) demosaic_kernel(DemosaicArgs a) {
     for (int i = tid; i < SH * SW; i += kT) {
         const int r = i / SW, c = i - r * SW;
         const SobelVal sv = sobel_abs(R, x0 - 4 + c, y0 - 4 + r);
-        s_u[i] = sv.gx;
-        s_u[SH * SW + i] = sv.gy;
-        s_u[2 * SH * SW + i] = sv.len;
+        s_sob[i] = make_float4(sv.gx, sv.gy, sv.len, 0.0f);
     }
     if (a.tap_scaled) {
         for (int i = tid; i < TW * TH; i += kT) {
@@ -184,7 +181,7 @@ __global__ void __launch_bounds__(kT) demosaic_kernel(DemosaicArgs a) {
             const int xr = xa + e_rb, xg = xa + (1 - e_rb);
             const bool yin = y >= 0 && y < h;
             if (yin && xr >= 0 && xr < w) {
-                const SobelMap sob{s_u, SH * SW, x0 - 4, y0 - 4, SW, xr, y};
+                const SobelMap sob{s_sob, x0 - 4, y0 - 4, SW, xr, y};
                 s_green[r * GW + 2 * k + e_rb] = Storage<S>::round(green_at(R, xr, y, lv, sob));
             }
             if (yin && xg >= 0 && xg < w) s_green[r * GW + 2 * k + 1 - e_rb] = Storage<S>::round(R.at(xg, y));
@@ -236,7 +233,7 @@ __global__ void __launch_bounds__(kT) demosaic_kernel(DemosaicArgs a) {
     for (int i = tid; i < TW * TH; i += kT) {
         const int r = i / TW, c = i - r * TW, x = x0 + c, y = y0 + r;
         if (x >= w || y >= h) continue;
-        a.level0[(size_t)y * a.l0_pitch + x] = to_half4(despeckle_px(Y, x, y, a.va0, a.vb0));
+        a.level0[(size_t)y * a.l0_pitch + x] = to_half4(despeckle_px<true>(Y, x, y, a.va0, a.vb0));
     }
 }
 
