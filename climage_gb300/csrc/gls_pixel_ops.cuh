@@ -772,29 +772,19 @@ GLS_DI float4 despeckle_rgba_px(const Acc4& im, int px, int py) {
                        clamp_(s[3], smn[3], smx[3]));
 }
 
+// The literal evaluation of denoiseRawRGBA (divisions and the square root per tap).
 template <class Acc4>
-GLS_DI float4 denoise_rgba_px(const Acc4& im, int px, int py, const float rv[4]) {
+__device__ __noinline__ float4 denoise_rgba_literal(const Acc4& im, int px, int py, const float sg[4]) {
     const float4 c = im.at(px, py);
     const float in[4] = {c.x, c.y, c.z, c.w};
-    float sg[4], f[4] = {0, 0, 0, 0}, nrm[4] = {0, 0, 0, 0};
-#pragma unroll
-    for (int k = 0; k < 4; k++) sg[k] = sqrt_(rv[k] * in[k]);
-    FastDiv dv[4];
-#pragma unroll
-    for (int k = 0; k < 4; k++) dv[k].init(sg[k]);
-    SqrtGe ge;
-    ge.init(1.0f);
-#pragma unroll
+    float f[4] = {0, 0, 0, 0}, nrm[4] = {0, 0, 0, 0};
     for (int y = -2; y <= 2; y++) {
-#pragma unroll
         for (int x = -2; x <= 2; x++) {
             const float4 s4 = im.at(px + x, py + y);
             const float s[4] = {s4.x, s4.y, s4.z, s4.w};
             float d[4];
-#pragma unroll
-            for (int k = 0; k < 4; k++) d[k] = dv[k](s[k] - in[k]);
-            const float w = ge(d[0] * d[0] + d[1] * d[1] + d[2] * d[2] + d[3] * d[3]) ? 0.0f : 1.0f;
-#pragma unroll
+            for (int k = 0; k < 4; k++) d[k] = div_(s[k] - in[k], sg[k]);
+            const float w = 1.0f - step_(1.0f, length4_(d[0], d[1], d[2], d[3]));
             for (int k = 0; k < 4; k++) {
                 f[k] = f[k] + w * s[k];
                 nrm[k] = nrm[k] + w;
@@ -802,6 +792,69 @@ GLS_DI float4 denoise_rgba_px(const Acc4& im, int px, int py, const float rv[4])
         }
     }
     return make_float4(div_(f[0], nrm[0]), div_(f[1], nrm[1]), div_(f[2], nrm[2]), div_(f[3], nrm[3]));
+}
+
+// denoiseRawRGBA: weight = 1 - step(1, length(diff / sigma)).  Channels with sigma > 0 enter
+// qa = sum diff_k^2 * RN(1/sigma_k)^2, decided against 1 +- 2^-20 widened by 2^-18 as in
+// bilateral_px.  A channel with sigma = 0 (a zero plane value) has diff / 0 = NaN for
+// diff == 0 and +-inf otherwise, and NaN outranks inf in the sum: when such channels exist
+// the weight is 1 exactly if one of them has diff == 0.  Non-finite samples, sigma outside
+// the shortcut's range and taps inside the band take the literal evaluation.
+template <class Acc4>
+GLS_DI float4 denoise_rgba_px(const Acc4& im, int px, int py, const float rv[4]) {
+    const float4 c = im.at(px, py);
+    const float in[4] = {c.x, c.y, c.z, c.w};
+    float sg[4], r[4];
+    unsigned zmask = 0;
+    bool lit = false;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        sg[k] = sqrt_(rv[k] * in[k]);
+        FastDiv d;
+        d.init(sg[k]);
+        if (sg[k] == 0.0f) zmask |= 1u << k;
+        else if (!d.ok) lit = true;
+        r[k] = sg[k] == 0.0f ? 0.0f : d.y * d.y;
+    }
+    if (lit) return denoise_rgba_literal(im, px, py, sg);
+    SqrtGe ge;
+    ge.init(1.0f);
+    constexpr float kWiden = 3.814697265625e-06f;  // 2^-18
+    const float lo = ge.lo * (1.0f - kWiden), hi = ge.hi * (1.0f + kWiden);
+    float f[4] = {0, 0, 0, 0}, n = 0.0f;
+    bool redo = false;
+#pragma unroll 1
+    for (int y = -2; y <= 2; y++) {
+#pragma unroll
+        for (int x = -2; x <= 2; x++) {
+            const float4 s4 = im.at(px + x, py + y);
+            const float s[4] = {s4.x, s4.y, s4.z, s4.w};
+            float xs[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) xs[k] = s[k] - in[k];
+            float w;
+            if (zmask) {
+                bool nan = false;
+#pragma unroll
+                for (int k = 0; k < 4; k++)
+                    if (zmask & (1u << k)) nan |= xs[k] == 0.0f;
+                redo |= !(fabsf(xs[0]) + fabsf(xs[1]) + fabsf(xs[2]) + fabsf(xs[3]) <= 3.402823466e38f);
+                w = nan ? 1.0f : 0.0f;
+            } else {
+                const float qa = glsm::fma_(xs[0] * xs[0], r[0],
+                                            glsm::fma_(xs[1] * xs[1], r[1],
+                                                       glsm::fma_(xs[2] * xs[2], r[2], (xs[3] * xs[3]) * r[3])));
+                const bool in1 = qa < lo;
+                redo |= !(in1 || qa > hi);
+                w = in1 ? 1.0f : 0.0f;
+            }
+#pragma unroll
+            for (int k = 0; k < 4; k++) f[k] = glsm::fma_(w, s[k], f[k]);
+            n = n + w;
+        }
+    }
+    if (redo) return denoise_rgba_literal(im, px, py, sg);
+    return make_float4(div_(f[0], n), div_(f[1], n), div_(f[2], n), div_(f[3], n));
 }
 
 }  // namespace gls

@@ -194,6 +194,28 @@ def test_denoise_taps_at_the_edge(ctx, seed):
         assert mismatch(host(out), orc.denoise_bilateral(img, va, vb, boost[0], boost[1])) == 0
 
 
+@pytest.mark.parametrize("seed", range(3))
+def test_denoise_raw_rgba_zeros_and_edges(ctx, seed):
+    """denoiseRawRGBA where planes are zero (sigma = 0: the tap weight comes from NaN or
+    infinite quotients) and where sample differences sit on the weight's edge."""
+    import torch
+    rng = np.random.default_rng(200 + seed)
+    h, w = 24, 40
+    rv = [1e-4, 2e-4, 1.5e-4, 3e-4]
+    img = np.zeros((h, w, 4), np.float32)
+    base = np.float32(0.25)
+    sig0 = np.sqrt(np.float32(rv[0]) * base).astype(np.float32)
+    t = rng.uniform(-8e-7, 8e-7, (h, w)).astype(np.float32)
+    img[..., 0] = base + np.where(rng.random((h, w)) < 0.5, sig0 * (np.float32(1) + t), np.float32(0))
+    img[..., 1] = np.where(rng.random((h, w)) < 0.4, np.float32(0), rng.uniform(0, 0.3, (h, w)).astype(np.float32))
+    img[..., 2] = np.where(rng.random((h, w)) < 0.7, np.float32(0), np.float32(0.125))
+    img[..., 3] = np.float32(0.3)
+    out = empty((h, w, 4))
+    ctx.denoiseRawRGBAImage(dev(img), rv, out)
+    torch.cuda.synchronize()
+    assert mismatch(host(out), orc.denoise_rgba(img, rv)) == 0
+
+
 @pytest.mark.parametrize("half", [False, True], ids=["f32", "f16"])
 def test_guided_filter(ctx, frame, half):
     import torch
