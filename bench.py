@@ -38,6 +38,7 @@ def parse():
     ap.add_argument("--impl", default="gls", choices=["gls", "reference"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-psnr", action="store_true")
     ap.add_argument("--profile-only", action="store_true", help="a short run for ncu: no clocks, no cpu leg")
     return ap.parse_args()
 
@@ -171,6 +172,28 @@ def cpu_leg(frames, max_seconds=30.0):
     return {"value": round(mpix / dt, 3), "unit": "MPix/s", "cores": threads, "kind": "port",
             "sample": "%d frame(s) of %dx%d (read sigma %.0f DN, gain %.0f), oracle fp32, %d threads, %.2f s/frame"
                       % (n, raw.shape[1], raw.shape[0], 2.0, 1.0, threads, dt)}
+
+
+def psnr_leg(conv, frames, dev):
+    """Error of the GPU output against the FP64 run of the oracle (the error oracle): float
+    RGB of the first frame, PSNR over [0, 1] and the largest absolute difference."""
+    import torch
+    from climage_gb300 import configs
+    from oracle import oracle as orc
+    from tests.helpers import oracle_params
+    raw, _, spec = frames[0]
+    h, w = raw.shape
+    out = torch.empty((h, w, 4), dtype=torch.float32, device=dev)
+    conv.demosaicImage(torch.from_numpy(raw).to(dev), configs.to_gls_params(spec), out, defer_noise_model=True)
+    torch.cuda.synchronize()
+    got = out.cpu().numpy()[..., :3].astype(np.float64)
+    ref = orc.demosaic(raw, oracle_params(spec), orc.F64, want=("rgbaf",))["rgbaf"][..., :3].astype(np.float64)
+    err = np.abs(got - ref)
+    mse = float(np.mean(err ** 2))
+    return {"db": round(10 * np.log10(1.0 / mse), 2) if mse > 0 else None, "max_abs": round(float(err.max()), 6),
+            "p99_99_abs": round(float(np.quantile(err, 0.9999)), 6),
+            "frac_over_half_lsb": float(np.mean(err > 0.5 / 255)),
+            "frame": "%dx%d, read sigma 2 DN, gain 1" % (w, h), "output": "RGB float (before UNORM8)"}
 
 
 def run_reference(args, cfg):
@@ -308,6 +331,9 @@ def main():
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu and not args.profile_only:
         cpu = cpu_leg(frames)
+    psnr = None
+    if rank == 0 and not args.no_psnr and not args.profile_only:
+        psnr = psnr_leg(conv, frames, dev)
 
     if rank == 0:
         line = {
@@ -332,6 +358,7 @@ def main():
             "clocks": sampler.summary(),
             "e2e": e2e,
             "cpu_baseline": cpu,
+            "psnr_vs_fp64": psnr,
         }
         print(json.dumps(line), flush=True)
     conv.close()
