@@ -154,11 +154,23 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
-def cpu_leg(frames, max_seconds=30.0):
-    """The oracle on the host cores over a bounded sample: the first frame, full size."""
+def cpu_leg(frames, max_seconds=30.0, gpu_rgb=None):
+    """The oracle on the host cores over a bounded sample: the first frame, full size.  With
+    gpu_rgb (the GPU's float RGB output of that frame) it also runs the oracle's FP64
+    pipeline once, untimed, as the error checker: PSNR and error tail of the GPU output."""
     from oracle import oracle as orc
     from tests.helpers import oracle_params
     raw, _, spec = frames[0]
+    psnr = None
+    if gpu_rgb is not None:
+        ref = orc.demosaic(raw, oracle_params(spec), orc.F64, want=("rgbaf",))["rgbaf"][..., :3].astype(np.float64)
+        err = np.abs(gpu_rgb.astype(np.float64) - ref)
+        mse = float(np.mean(err ** 2))
+        psnr = {"db": round(10 * np.log10(1.0 / mse), 2) if mse > 0 else None, "max_abs": round(float(err.max()), 6),
+                "p99_99_abs": round(float(np.quantile(err, 0.9999)), 6),
+                "frac_over_half_lsb": float(np.mean(err > 0.5 / 255)),
+                "frame": "%dx%d, read sigma 2 DN, gain 1" % (raw.shape[1], raw.shape[0]),
+                "output": "RGB float (before UNORM8)"}
     threads = orc.threads()
     t0 = time.perf_counter()
     n = 0
@@ -171,29 +183,7 @@ def cpu_leg(frames, max_seconds=30.0):
     mpix = raw.size / 1e6
     return {"value": round(mpix / dt, 3), "unit": "MPix/s", "cores": threads, "kind": "port",
             "sample": "%d frame(s) of %dx%d (read sigma %.0f DN, gain %.0f), oracle fp32, %d threads, %.2f s/frame"
-                      % (n, raw.shape[1], raw.shape[0], 2.0, 1.0, threads, dt)}
-
-
-def psnr_leg(conv, frames, dev):
-    """Error of the GPU output against the FP64 run of the oracle (the error oracle): float
-    RGB of the first frame, PSNR over [0, 1] and the largest absolute difference."""
-    import torch
-    from climage_gb300 import configs
-    from oracle import oracle as orc
-    from tests.helpers import oracle_params
-    raw, _, spec = frames[0]
-    h, w = raw.shape
-    out = torch.empty((h, w, 4), dtype=torch.float32, device=dev)
-    conv.demosaicImage(torch.from_numpy(raw).to(dev), configs.to_gls_params(spec), out, defer_noise_model=True)
-    torch.cuda.synchronize()
-    got = out.cpu().numpy()[..., :3].astype(np.float64)
-    ref = orc.demosaic(raw, oracle_params(spec), orc.F64, want=("rgbaf",))["rgbaf"][..., :3].astype(np.float64)
-    err = np.abs(got - ref)
-    mse = float(np.mean(err ** 2))
-    return {"db": round(10 * np.log10(1.0 / mse), 2) if mse > 0 else None, "max_abs": round(float(err.max()), 6),
-            "p99_99_abs": round(float(np.quantile(err, 0.9999)), 6),
-            "frac_over_half_lsb": float(np.mean(err > 0.5 / 255)),
-            "frame": "%dx%d, read sigma 2 DN, gain 1" % (w, h), "output": "RGB float (before UNORM8)"}
+                      % (n, raw.shape[1], raw.shape[0], 2.0, 1.0, threads, dt)}, psnr
 
 
 def run_reference(args, cfg):
@@ -328,12 +318,15 @@ def main():
                "h2d_bytes_per_step": int(sum(f[0].nbytes for f in frames)),
                "d2h_bytes_per_step": int(len(frames) * w * h * 4)}
 
-    cpu = None
+    cpu = psnr = None
     if rank == 0 and world == 1 and not args.no_cpu and not args.profile_only:
-        cpu = cpu_leg(frames)
-    psnr = None
-    if rank == 0 and not args.no_psnr and not args.profile_only:
-        psnr = psnr_leg(conv, frames, dev)
+        gpu_rgb = None
+        if not args.no_psnr:
+            fo = torch.empty((h, w, 4), dtype=torch.float32, device=dev)
+            conv.demosaicImage(raws[0], configs.to_gls_params(frames[0][2]), fo, defer_noise_model=True)
+            torch.cuda.synchronize()
+            gpu_rgb = fo.cpu().numpy()[..., :3]
+        cpu, psnr = cpu_leg(frames, gpu_rgb=gpu_rgb)
 
     if rank == 0:
         line = {
