@@ -137,6 +137,14 @@ SIGNATURES = [
     ("gls_raw_batch_demosaic_host", _I, [_P, _I, ctypes.POINTER(_P), ctypes.POINTER(ctypes.c_int),
                                          ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
                                          ctypes.POINTER(DemosaicParams), ctypes.POINTER(_P), _I]),
+    ("gls_cnn_create", _I, [_P, ctypes.POINTER(_P)]),
+    ("gls_cnn_destroy", _I, [_P]),
+    ("gls_cnn_param_count", _I, []),
+    ("gls_cnn_set_params", _I, [_P, _FP, _I]),
+    ("gls_cnn_get_params", _I, [_P, _FP, _I]),
+    ("gls_cnn_get_grads", _I, [_P, _FP, _I]),
+    ("gls_cnn_forward", _I, [_P, _P, _I, _I, _I, _P]),
+    ("gls_cnn_train_step", _I, [_P, _P, _P, _I, _I, _I, _F, _FP]),
     ("gls_raw_batch_plan", _I, [_I, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int), _I,
                                 ctypes.POINTER(ctypes.c_int)]),
 ]
@@ -487,3 +495,80 @@ class RawBatch:
             self.close()
         except Exception:
             pass
+
+
+# layer shapes of the learned stage: (cin, cout)
+CNN_LAYERS = [(4, 32), (32, 32), (32, 32), (32, 32), (32, 4)]
+
+
+class Cnn:
+    """gls_cnn: the learned stage's 5-layer BF16 CNN (forward, training on the GPU)."""
+
+    def __init__(self, ctx):
+        self.ctx = ctx
+        self.handle = ctypes.c_void_p()
+        ctx.check(lib().gls_cnn_create(ctx.handle, ctypes.byref(self.handle)), "Cnn")
+        ctx._children.add(self)
+        self.nparam = int(lib().gls_cnn_param_count())
+
+    def set_params(self, params):
+        p = np.ascontiguousarray(params, np.float32).ravel()
+        self.ctx.check(lib().gls_cnn_set_params(self.handle, p.ctypes.data_as(_FP), p.size), "Cnn.set_params")
+
+    def params(self):
+        p = np.zeros(self.nparam, np.float32)
+        self.ctx.check(lib().gls_cnn_get_params(self.handle, p.ctypes.data_as(_FP), p.size), "Cnn.params")
+        return p
+
+    def grads(self):
+        g = np.zeros(self.nparam, np.float32)
+        self.ctx.check(lib().gls_cnn_get_grads(self.handle, g.ctypes.data_as(_FP), g.size), "Cnn.grads")
+        return g
+
+    def forward(self, inp, out):
+        """inp: (n, h, w, 4) float32 CUDA tensor; out: same shape, filled with (strength logit, residual)."""
+        n, h, w, _ = inp.shape
+        self.ctx.check(lib().gls_cnn_forward(self.handle, ctypes.c_void_p(inp.data_ptr()), w, h, n,
+                                             ctypes.c_void_p(out.data_ptr())), "Cnn.forward")
+        return out
+
+    def train_step(self, inp, gt, lr):
+        n, h, w, _ = inp.shape
+        loss = (ctypes.c_float * 2)()
+        self.ctx.check(lib().gls_cnn_train_step(self.handle, ctypes.c_void_p(inp.data_ptr()),
+                                                ctypes.c_void_p(gt.data_ptr()), w, h, n, float(lr), loss),
+                       "Cnn.train_step")
+        return float(loss[0]), float(loss[1])
+
+    def close(self):
+        if self.handle:
+            lib().gls_cnn_destroy(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def cnn_split(params):
+    """Flat parameter array -> [(W (cout, 3, 3, cin), b (cout,)) per layer]."""
+    out, o = [], 0
+    for cin, cout in CNN_LAYERS:
+        W = np.asarray(params[o:o + cout * 9 * cin], np.float32).reshape(cout, 3, 3, cin)
+        o += cout * 9 * cin
+        out.append((W, np.asarray(params[o:o + cout], np.float32)))
+        o += cout
+    return out
+
+
+def cnn_init(seed=0):
+    """He-initialised parameters (zero biases; the head starts near zero residual and logit)."""
+    rng = np.random.default_rng(seed)
+    parts = []
+    for l, (cin, cout) in enumerate(CNN_LAYERS):
+        std = np.sqrt(2.0 / (9 * cin)) * (0.1 if l == len(CNN_LAYERS) - 1 else 1.0)
+        parts.append(rng.normal(0.0, std, cout * 9 * cin).astype(np.float32))
+        parts.append(np.zeros(cout, np.float32))
+    return np.concatenate(parts)

@@ -279,6 +279,26 @@ GLS_API gls_status gls_raw_batch_demosaic_host(gls_raw_batch* batch, int n, cons
                                                const int* widths, const int* heights, const int* raw_strides_px,
                                                const gls_demosaic_params* params, uint8_t* const* outs,
                                                int out_channels);
+/* ---- the learned stage: a 5-layer 3x3 BF16 CNN ----
+ * No counterpart in the reference.  4 -> 32 -> 32 -> 32 -> 32 -> 4 channels, ReLU between
+ * layers, zero-padded borders.  Input per pixel: demosaiced linear R, G, B and the noise
+ * sigma; output per pixel: a denoise-strength logit and an RGB residual.  Parameters are a
+ * flat FP32 array, per layer W[cout][3][3][cin] then b[cout] (gls_cnn_param_count() in all).
+ * All tensors are device NHWC fp32: in [n][h][w][4], out [n][h][w][4], gt [n][h][w][3]. */
+typedef struct gls_cnn gls_cnn;
+GLS_API gls_status gls_cnn_create(gls_ctx* ctx, gls_cnn** out);
+GLS_API gls_status gls_cnn_destroy(gls_cnn* cnn);
+GLS_API int gls_cnn_param_count(void);
+GLS_API gls_status gls_cnn_set_params(gls_cnn* cnn, const float* params, int n);
+GLS_API gls_status gls_cnn_get_params(gls_cnn* cnn, float* params, int n);
+/* the gradients of the last training step (of the mean losses below) */
+GLS_API gls_status gls_cnn_get_grads(gls_cnn* cnn, float* grads, int n);
+GLS_API gls_status gls_cnn_forward(gls_cnn* cnn, const float* in, int width, int height, int n, float* out);
+/* One Adam step (lr > 0; lr = 0 only computes the gradients) on a batch against the clean
+ * RGB gt; loss[0] = mean squared error of (input RGB + residual), loss[1] = strength loss. */
+GLS_API gls_status gls_cnn_train_step(gls_cnn* cnn, const float* in, const float* gt, int width, int height, int n,
+                                      float lr, float loss[2]);
+
 /* The lane of each frame, as the batch assigns them (frames by decreasing pixel count, each
  * to the lane with the fewest pixels so far; ties to the lower frame index and lane). */
 GLS_API gls_status gls_raw_batch_plan(int n, const int* widths, const int* heights, int lanes, int* lane_of);
