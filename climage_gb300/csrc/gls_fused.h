@@ -33,6 +33,25 @@ struct DemosaicArgs {
     float* tap_scaled;
     float* tap_green;
     int tap_pitch;
+    // learned stage: with cnn_in set, the kernel stops after interpolateRedBlue and writes
+    // the network input [h][w][4] = (R, G, B, sigma), sigma = sqrt(A1 + B1 * G) from the
+    // fitted raw noise model (rawA_dev = A[0..3])
+    float* cnn_in;
+    const float* rawA_dev;
+};
+
+// After the learned stage: linear RGB + the network's residual, blendHighlights,
+// cam -> YCbCr, despeckle -> level 0, and the level-0 noise-model multiplier
+// 2 sigmoid(logit) per pixel.
+struct PostCnnArgs {
+    const float* cnn_in;  // [h][w][4]
+    const float* head;    // [h][w][4]: strength logit, residual RGB
+    int w, h;
+    Mat3 cam_ycbcr;
+    float va0, vb0;
+    half4* level0;
+    int l0_pitch;
+    float* strength;      // [h][w]
 };
 
 struct LevelPass1Args {
@@ -78,10 +97,12 @@ struct FinalArgs {
     float* tap_den;
     float* tap_mask;
     int tap_pitch;
+    const float* strength;  // learned stage: level-0 noise-model multiplier per pixel (or null)
 };
 
 gls_status fused_raw_fit(gls_ctx* ctx, const RawPass1Args& a, bool half, NlfScratch s, float* out_dev);
 gls_status fused_demosaic(gls_ctx* ctx, const DemosaicArgs& a, bool raw_u16, bool half);
+gls_status fused_post_cnn(gls_ctx* ctx, const PostCnnArgs& a, bool half);
 gls_status fused_level_fit(gls_ctx* ctx, const LevelPass1Args& a, bool in_half, bool half, NlfScratch s,
                            float* out_dev);
 gls_status fused_denoise(gls_ctx* ctx, const DenoiseArgs& a, bool in_half, bool half, int algo, bool reasm);

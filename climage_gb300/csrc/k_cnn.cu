@@ -341,8 +341,10 @@ __global__ void reduce_rows_kernel(const float* part, int rows, int cols, float*
 // Loss of a batch and its gradient at the head.  in: [img][h][w][4] fp32 (R, G, B, sigma);
 // head: [img][h][w][4] fp32 (strength logit, residual RGB); gt: [img][h][w][3] fp32.
 //   residual loss  mean over pixels and channels of (in_rgb + r - gt)^2
-//   strength loss  lambda * mean over pixels of (sigmoid(s) - tgt)^2, tgt = min(1, e2 / sigma^2)
-//                  with e2 the mean squared residual error of the pixel (no gradient through tgt)
+//   strength loss  lambda * mean over pixels of (sigmoid(s) - tgt)^2, tgt = min(1, e2 / sigma^2) / 2
+//                  with e2 the mean squared residual error of the pixel (no gradient through tgt);
+//                  the pipeline scales the level-0 noise model by 2 sigmoid(s) (<= 1 after
+//                  training; exactly 1 for a zero logit)
 // The per-block sums of both losses go to part[block][2].
 // ---------------------------------------------------------------------------------------
 constexpr float kStrengthWeight = 0.1f;
@@ -356,7 +358,7 @@ __global__ void loss_grad_kernel(const float* in, const float* head, const float
         const float4 o = reinterpret_cast<const float4*>(head)[p];
         const float e0 = x.x + o.y - gt[3 * p + 0], e1 = x.y + o.z - gt[3 * p + 1], e2 = x.z + o.w - gt[3 * p + 2];
         const float mse = (e0 * e0 + e1 * e1 + e2 * e2) * (1.0f / 3.0f);
-        const float tgt = fminf(1.0f, mse / fmaxf(x.w * x.w, 1e-8f));
+        const float tgt = 0.5f * fminf(1.0f, mse / fmaxf(x.w * x.w, 1e-8f));
         const float s = 1.0f / (1.0f + expf(-o.x));
         l0 += 3.0f * mse;
         l1 += (s - tgt) * (s - tgt);

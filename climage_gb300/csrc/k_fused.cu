@@ -120,7 +120,7 @@ __global__ void __launch_bounds__(kT) raw_pass1_kernel(RawPass1Args a) {
 // =========================================================================================
 // demosaic: TW x TH output tile, 256 threads.
 // =========================================================================================
-template <int TW, int TH, bool RAW_U16, class S>
+template <int TW, int TH, bool RAW_U16, class S, bool CNNIN>
 __global__ void __launch_bounds__(kT) demosaic_kernel(DemosaicArgs a) {
     constexpr int RW = TW + 10, RH = TH + 10;  // scaled raw, origin (x0 - 5, y0 - 5)
     constexpr int SW = TW + 8, SH = TH + 8;    // Sobel map, origin (x0 - 4, y0 - 4)
@@ -199,6 +199,18 @@ __global__ void __launch_bounds__(kT) demosaic_kernel(DemosaicArgs a) {
     }
     const SAcc1 G{s_green, x0 - 2, y0 - 2, GW};
 
+    if (CNNIN) {  // the learned stage's input: red/blue at the tile, and the noise sigma
+        const float cv = mmax(a.rawB_dev ? div_(a.rawB_dev[0] + a.rawB_dev[2], 2.0f) : a.cv_host, 1e-6f);
+        for (int i = tid; i < TW * TH; i += kT) {
+            const int r = i / TW, c = i - r * TW, x = x0 + c, y = y0 + r;
+            if (x >= w || y >= h) continue;
+            const float3 p = round3<S>(red_blue_at(R, G, x, y, bayer, cv));
+            const float sig = sqrt_(mmax(a.rawA_dev[1] + a.rawB_dev[1] * p.y, 1e-8f));
+            reinterpret_cast<float4*>(a.cnn_in)[(size_t)y * w + x] = make_float4(p.x, p.y, p.z, sig);
+        }
+        return;
+    }
+
     // 4. red/blue, highlight recovery, camera -> YCbCr (the Sobel map is dead: reuse it)
     {
         const float cv = mmax(a.rawB_dev ? div_(a.rawB_dev[0] + a.rawB_dev[2], 2.0f) : a.cv_host, 1e-6f);
@@ -234,6 +246,44 @@ __global__ void __launch_bounds__(kT) demosaic_kernel(DemosaicArgs a) {
         const int r = i / TW, c = i - r * TW, x = x0 + c, y = y0 + r;
         if (x >= w || y >= h) continue;
         a.level0[(size_t)y * a.l0_pitch + x] = to_half4(despeckle_px<true>(Y, x, y, a.va0, a.vb0));
+    }
+}
+
+// =========================================================================================
+// post_cnn: the learned stage's residual added to the linear RGB, then blendHighlights,
+// cam -> YCbCr over the tile and a one-pixel ring (clamped reads: the same values the
+// fused kernel's border replication gives), despeckle -> level 0, and the level-0
+// noise-model multiplier.  A residual that is exactly zero leaves the value as it is (also
+// a -0), so a network with all-zero parameters reproduces the plain pipeline bit for bit.
+// =========================================================================================
+constexpr int PCW = 32, PCH = 8;
+
+template <class S>
+__global__ void __launch_bounds__(kT) post_cnn_kernel(PostCnnArgs a) {
+    constexpr int CW = PCW + 2, CH = PCH + 2;
+    __shared__ half4 s_ycc[CW * CH];
+    const int x0 = blockIdx.x * PCW, y0 = blockIdx.y * PCH;
+    for (int i = threadIdx.x; i < CW * CH; i += kT) {
+        const int r = i / CW, c = i - r * CW;
+        const int x = clampi(x0 - 1 + c, 0, a.w - 1), y = clampi(y0 - 1 + r, 0, a.h - 1);
+        const size_t px = (size_t)y * a.w + x;
+        const float4 lin = reinterpret_cast<const float4*>(a.cnn_in)[px];
+        const float4 o = reinterpret_cast<const float4*>(a.head)[px];
+        float3 p = make_float3(o.y == 0.0f ? lin.x : lin.x + o.y, o.z == 0.0f ? lin.y : lin.y + o.z,
+                               o.w == 0.0f ? lin.z : lin.z + o.w);
+        p = round3<S>(p);
+        p = round3<S>(blend_highlights_px(p, 1.0f));
+        p = round3<S>(transform_px(a.cam_ycbcr, p));
+        s_ycc[i] = to_half4(make_float4(p.x, p.y, p.z, 0.0f));
+    }
+    __syncthreads();
+    const SAcc4h Y{s_ycc, x0 - 1, y0 - 1, CW};
+    for (int i = threadIdx.x; i < PCW * PCH; i += kT) {
+        const int r = i / PCW, c = i - r * PCW, x = x0 + c, y = y0 + r;
+        if (x >= a.w || y >= a.h) continue;
+        a.level0[(size_t)y * a.l0_pitch + x] = to_half4(despeckle_px<true>(Y, x, y, a.va0, a.vb0));
+        const float lg = a.head[((size_t)y * a.w + x) * 4];
+        a.strength[(size_t)y * a.w + x] = 2.0f * div_(1.0f, 1.0f + glsm::exp2_(-lg * 1.44269504f));
     }
 }
 
@@ -502,8 +552,17 @@ __global__ void __launch_bounds__(kT) final_kernel(FinalArgs a) {
     for (int i = threadIdx.x; i < EW * EH; i += kT) {
         const int r = i / EW, c = i - r * EW, x = x0 - 1 + c, y = y0 - 1 + r;
         if (x < 0 || x >= w || y < 0 || y >= h) continue;
-        float4 d = ALGO == 0 ? bilateral_px(L0, x, y, n, a.chroma_boost, a.gradient_boost)
-                             : guided_fast_px(L0, x, y, n);
+        Nlf6 nm = n;
+        if (a.strength) {  // the learned stage's per-pixel multiplier of the noise model
+            const float m = a.strength[(size_t)y * w + x];
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                nm.a[k] = n.a[k] * m;
+                nm.b[k] = n.b[k] * m;
+            }
+        }
+        float4 d = ALGO == 0 ? bilateral_px(L0, x, y, nm, a.chroma_boost, a.gradient_boost)
+                             : guided_fast_px(L0, x, y, nm);
         d = round4<S>(d);
         const float4 p1 = tab_sample4(s_i1, T.rx[0][c], T.ry[0][r]);
         const float4 pd1 = tab_sample4(s_d1, T.rx[0][c], T.ry[0][r]);
@@ -604,15 +663,26 @@ gls_status fused_raw_fit(gls_ctx* ctx, const RawPass1Args& args, bool half, NlfS
 gls_status fused_demosaic(gls_ctx* ctx, const DemosaicArgs& a, bool raw_u16, bool half) {
     constexpr int TW = 28, TH = 28;
     const dim3 grid((a.w + TW - 1) / TW, (a.h + TH - 1) / TH);
+    cudaStream_t st = ctx->stream;
+#define GLS_DEM(U16, SS)                                                               \
+    if (a.cnn_in) demosaic_kernel<TW, TH, U16, SS, true><<<grid, kT, 0, st>>>(a);     \
+    else demosaic_kernel<TW, TH, U16, SS, false><<<grid, kT, 0, st>>>(a);
     if (raw_u16) {
-        if (half) demosaic_kernel<TW, TH, true, __half><<<grid, kT, 0, ctx->stream>>>(a);
-        else demosaic_kernel<TW, TH, true, float><<<grid, kT, 0, ctx->stream>>>(a);
+        if (half) { GLS_DEM(true, __half) } else { GLS_DEM(true, float) }
     } else {
-        if (half) demosaic_kernel<TW, TH, false, __half><<<grid, kT, 0, ctx->stream>>>(a);
-        else demosaic_kernel<TW, TH, false, float><<<grid, kT, 0, ctx->stream>>>(a);
+        if (half) { GLS_DEM(false, __half) } else { GLS_DEM(false, float) }
     }
+#undef GLS_DEM
     ctx->launches++;
     return check_launch(ctx, "demosaic (fused)");
+}
+
+gls_status fused_post_cnn(gls_ctx* ctx, const PostCnnArgs& a, bool half) {
+    const dim3 grid((a.w + PCW - 1) / PCW, (a.h + PCH - 1) / PCH);
+    if (half) post_cnn_kernel<__half><<<grid, kT, 0, ctx->stream>>>(a);
+    else post_cnn_kernel<float><<<grid, kT, 0, ctx->stream>>>(a);
+    ctx->launches++;
+    return check_launch(ctx, "after the learned stage");
 }
 
 gls_status fused_level_fit(gls_ctx* ctx, const LevelPass1Args& args, bool in_half, bool half, NlfScratch s,

@@ -75,6 +75,13 @@ struct gls_raw_converter {
     // parity taps
     gls_image_desc taps[5]{};
     bool tap_set[5]{};
+    // learned stage: this converter's own copy of the network (on its stream), its input,
+    // its output and the level-0 noise-model multiplier, all dense [h][w]
+    gls_cnn* cnn = nullptr;
+    float* cnn_in = nullptr;
+    float* cnn_head = nullptr;
+    float* strength = nullptr;
+    bool learned_alloc = false;
 
     ~gls_raw_converter() { release(); }
 
@@ -138,7 +145,7 @@ struct gls_raw_converter {
             release();
             for (int i = 0; i < GLS_MAX_LEVELS; i++) pyr[i] = den[i] = ImgRef{};
             green = linA = linB = mask = scaled = hnA = hnB = ImgRef{};
-            staged_alloc = high_noise_alloc = false;
+            staged_alloc = high_noise_alloc = learned_alloc = false;
             half = half_storage;
             {
                 void* p = nullptr;
@@ -188,6 +195,16 @@ struct gls_raw_converter {
         GLS_CHECK(img(hnB, cap_w / 2, cap_h / 2, 4));
         high_noise_alloc = true;
         set_views();
+        return GLS_OK;
+    }
+
+    gls_status ensure_learned() {
+        if (learned_alloc) return GLS_OK;
+        const size_t n = (size_t)cap_w * cap_h;
+        GLS_CHECK(alloc((void**)&cnn_in, n * 16));
+        GLS_CHECK(alloc((void**)&cnn_head, n * 16));
+        GLS_CHECK(alloc((void**)&strength, n * 4));
+        learned_alloc = true;
         return GLS_OK;
     }
 
@@ -264,13 +281,17 @@ struct gls_raw_converter {
     gls_status run(const uint16_t* raw, int rpitch, gls_demosaic_params* p, void* out, bool out_float, int opitch) {
         if (mode == 0 && p->denoise_algorithm != GLS_DENOISE_GUIDED_PRECISE)
             return run_fused(raw, rpitch, p, out, out_float, opitch);
+        if (cnn)
+            return set_error(ctx, GLS_ERR_UNSUPPORTED,
+                             "the learned stage runs in the fused schedule only (not with GuidedPrecise)");
         return run_staged(raw, rpitch, p, out, out_float, opitch);
     }
 
     float* tap_ptr(int stage) { return tap_set[stage] ? (float*)taps[stage].ptr : nullptr; }
 
+    // cnn_input_only: stop after interpolateRedBlue, writing the learned stage's input there
     gls_status run_fused(const uint16_t* raw, int rpitch, gls_demosaic_params* p, void* out, bool out_float,
-                         int opitch) {
+                         int opitch, float* cnn_input_only = nullptr) {
         const int Lv = L;
         const int bayer = p->bayer_pattern;
         const bool high_noise = p->noise_level > 0.6f;
@@ -310,6 +331,10 @@ struct gls_raw_converter {
         da.tap_scaled = tap_ptr(0);
         da.tap_green = tap_ptr(1);
         da.tap_pitch = w;
+        da.rawA_dev = nlf_dev;
+        const bool learned = cnn != nullptr && !cnn_input_only;
+        if (learned) GLS_CHECK(ensure_learned());
+        da.cnn_in = cnn_input_only ? cnn_input_only : (learned ? cnn_in : nullptr);
         if (high_noise) {
             // raw-domain despeckle and bilateral on the quarter-resolution CFA planes
             GLS_CHECK(ensure_high_noise());
@@ -328,6 +353,27 @@ struct gls_raw_converter {
             GLS_CHECK(fused_demosaic(ctx, da, true, half));
         }
         mark("demosaic");
+        if (cnn_input_only) {
+            collect();
+            return check_launch(ctx, "learned stage input");
+        }
+        if (learned) {
+            GLS_CHECK(gls_cnn_forward(cnn, cnn_in, w, h, 1, cnn_head));
+            mark("learned stage");
+            PostCnnArgs pa{};
+            pa.cnn_in = cnn_in;
+            pa.head = cnn_head;
+            pa.w = w;
+            pa.h = h;
+            pa.cam_ycbcr = da.cam_ycbcr;
+            pa.va0 = da.va0;
+            pa.vb0 = da.vb0;
+            pa.level0 = (half4*)level0.ptr;
+            pa.l0_pitch = level0.pitch;
+            pa.strength = strength;
+            GLS_CHECK(fused_post_cnn(ctx, pa, half));
+            mark("residual+highlights+despeckle");
+        }
         tap(2, level0, 4);
 
         // pyramid: noise model of every level, downsampled levels
@@ -417,6 +463,7 @@ struct gls_raw_converter {
         f.tap_den = tap_ptr(3);
         f.tap_mask = tap_ptr(4);
         f.tap_pitch = w;
+        f.strength = learned ? strength : nullptr;
         const int algo0 = (algo == GLS_DENOISE_GUIDED_FAST) ? 1 : 0;
         GLS_CHECK(fused_final(ctx, f, half, algo0, rc.localToneMapping != 0, out_float));
         mark("denoise L0+LTM+sRGB");
@@ -607,8 +654,44 @@ gls_status gls_raw_converter_destroy(gls_raw_converter* c) {
     if (c->nlf_host) cudaFreeHost(c->nlf_host);
     if (c->raw_dev) cudaFree(c->raw_dev);
     if (c->out_dev) cudaFree(c->out_dev);
+    if (c->cnn) gls_cnn_destroy(c->cnn);
     delete c;
     return GLS_OK;
+}
+
+gls_status gls_raw_converter_set_cnn(gls_raw_converter* c, gls_cnn* src) {
+    if (!c) return GLS_ERR_INVALID_ARGUMENT;
+    if (c->cnn) {
+        cudaStreamSynchronize(c->ctx->stream);
+        gls_cnn_destroy(c->cnn);
+        c->cnn = nullptr;
+    }
+    if (!src) return GLS_OK;
+    const int n = gls_cnn_param_count();
+    std::vector<float> prm(n);
+    gls_status s = gls_cnn_get_params(src, prm.data(), n);
+    if (s != GLS_OK) return set_error(c->ctx, s, "learned stage: reading the network's parameters");
+    GLS_CHECK(gls_cnn_create(c->ctx, &c->cnn));
+    s = gls_cnn_set_params(c->cnn, prm.data(), n);
+    if (s != GLS_OK) {
+        gls_cnn_destroy(c->cnn);
+        c->cnn = nullptr;
+    }
+    return s;
+}
+
+gls_status gls_raw_converter_cnn_input(gls_raw_converter* c, const gls_image_desc* raw,
+                                       const gls_demosaic_params* params, const gls_image_desc* out) {
+    if (!c) return GLS_ERR_INVALID_ARGUMENT;
+    gls_ctx* ctx = c->ctx;
+    GLS_CHECK(check_desc(ctx, raw, "raw", GLS_R16_UNORM));
+    GLS_CHECK(check_desc(ctx, out, "out", GLS_RGBA_F32));
+    if (out->width != raw->width || out->height != raw->height || out->stride_bytes != out->width * 16)
+        return set_error(ctx, GLS_ERR_INVALID_SIZE, "learned stage input: dense RGBA_F32 of the raw frame's size");
+    GLS_CHECK(validate_params(ctx, params, raw->width, raw->height));
+    GLS_CHECK(c->ensure(raw->width, raw->height, params->pyramid_levels, params->storage == GLS_STORAGE_F16));
+    gls_demosaic_params p = *params;
+    return c->run_fused((const uint16_t*)raw->ptr, pitch_elems(raw), &p, nullptr, false, 0, (float*)out->ptr);
 }
 
 gls_status gls_raw_converter_set_mode(gls_raw_converter* c, int mode) {
@@ -798,6 +881,15 @@ std::vector<uint64_t> lane_launches(gls_raw_batch* b) {
 }  // namespace
 
 extern "C" {
+
+gls_status gls_raw_batch_set_cnn(gls_raw_batch* b, gls_cnn* cnn) {
+    if (!b) return GLS_ERR_INVALID_ARGUMENT;
+    for (size_t l = 0; l < b->lane.size(); l++) {
+        const gls_status s = gls_raw_converter_set_cnn(b->lane[l], cnn);
+        if (s != GLS_OK) return batch_error(b, (int)l, s);
+    }
+    return GLS_OK;
+}
 
 gls_status gls_raw_batch_plan(int n, const int* widths, const int* heights, int lanes, int* lane_of) {
     if (n < 0 || lanes < 1 || (n > 0 && (!widths || !heights || !lane_of))) return GLS_ERR_INVALID_ARGUMENT;

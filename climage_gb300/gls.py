@@ -130,6 +130,9 @@ SIGNATURES = [
     ("gls_raw_converter_set_mode", _I, [_P, _I]),
     ("gls_raw_converter_profile", _I, [_P, _I]),
     ("gls_raw_converter_profile_report", _I, [_P, ctypes.c_char_p, ctypes.c_size_t]),
+    ("gls_raw_converter_set_cnn", _I, [_P, _P]),
+    ("gls_raw_converter_cnn_input", _I, [_P, _D, ctypes.POINTER(DemosaicParams), _D]),
+    ("gls_raw_batch_set_cnn", _I, [_P, _P]),
     ("gls_raw_batch_create", _I, [_P, _I, ctypes.POINTER(_P)]),
     ("gls_raw_batch_destroy", _I, [_P]),
     ("gls_raw_batch_reserve", _I, [_P, _I, _I, _I, _I]),
@@ -424,6 +427,17 @@ class RawConverter:
         self.ctx.check(lib().gls_raw_converter_profile_report(self.handle, buf, len(buf)), "profile report")
         return json.loads(buf.value.decode())
 
+    def setCnn(self, cnn):
+        """Run the learned stage with (a copy of) this Cnn; None returns to the plain pipeline."""
+        self.ctx.check(lib().gls_raw_converter_set_cnn(self.handle, cnn.handle if cnn is not None else None),
+                       "RawConverter.setCnn")
+
+    def cnnInput(self, raw, params, out):
+        """The learned stage's input (R, G, B, sigma) of a raw frame into out (H, W, 4) float32."""
+        self.ctx.check(lib().gls_raw_converter_cnn_input(self.handle, desc(raw), ctypes.byref(params), desc(out)),
+                       "RawConverter.cnnInput")
+        return out
+
     def setTap(self, stage, tensor):
         self.ctx.check(lib().gls_raw_converter_set_tap(self.handle, int(stage), desc(tensor)), "setTap")
 
@@ -460,6 +474,10 @@ class RawBatch:
         self.handle = ctypes.c_void_p()
         ctx.check(lib().gls_raw_batch_create(ctx.handle, int(lanes), ctypes.byref(self.handle)), "RawBatch")
         ctx._children.add(self)
+
+    def set_cnn(self, cnn):
+        self.ctx.check(lib().gls_raw_batch_set_cnn(self.handle, cnn.handle if cnn is not None else None),
+                       "RawBatch.set_cnn")
 
     def reserve(self, width, height, levels, storage=STORAGE_F32):
         self.ctx.check(lib().gls_raw_batch_reserve(self.handle, int(width), int(height), int(levels), int(storage)),

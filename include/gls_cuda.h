@@ -254,6 +254,19 @@ GLS_API gls_status gls_raw_converter_set_mode(gls_raw_converter* conv, int mode)
 GLS_API gls_status gls_raw_converter_profile(gls_raw_converter* conv, int enable);
 GLS_API gls_status gls_raw_converter_profile_report(gls_raw_converter* conv, char* buf, size_t buf_len);
 
+/* ---- the learned stage in the pipeline (see gls_cnn below; no counterpart in the reference) ----
+ * With a network set (the converter keeps its own copy), demosaicImage runs it after
+ * interpolateRedBlue: its residual is added to the linear RGB before blendHighlights and
+ * transformImage, and 2 sigmoid(strength logit) multiplies the level-0 denoise noise model
+ * per pixel.  An all-zero network reproduces the plain pipeline exactly.  Fused schedule
+ * only (not with GuidedPrecise).  cnn = NULL returns to the plain pipeline. */
+typedef struct gls_cnn gls_cnn;
+GLS_API gls_status gls_raw_converter_set_cnn(gls_raw_converter* conv, gls_cnn* cnn);
+/* The network's input for a raw frame (the pipeline up to interpolateRedBlue): dense
+ * RGBA_F32 out = (R, G, B, sigma), sigma = sqrt(A1 + B1 * G) of the fitted raw noise model. */
+GLS_API gls_status gls_raw_converter_cnn_input(gls_raw_converter* conv, const gls_image_desc* raw,
+                                               const gls_demosaic_params* params, const gls_image_desc* out);
+
 /* ---- bursts: demosaicImage over many frames at once ----
  * No counterpart in the reference, where a burst is a loop of demosaicImage calls.  The
  * frames (any sizes, CFA phases, bit depths and parameters) are spread over `lanes`
@@ -285,7 +298,6 @@ GLS_API gls_status gls_raw_batch_demosaic_host(gls_raw_batch* batch, int n, cons
  * sigma; output per pixel: a denoise-strength logit and an RGB residual.  Parameters are a
  * flat FP32 array, per layer W[cout][3][3][cin] then b[cout] (gls_cnn_param_count() in all).
  * All tensors are device NHWC fp32: in [n][h][w][4], out [n][h][w][4], gt [n][h][w][3]. */
-typedef struct gls_cnn gls_cnn;
 GLS_API gls_status gls_cnn_create(gls_ctx* ctx, gls_cnn** out);
 GLS_API gls_status gls_cnn_destroy(gls_cnn* cnn);
 GLS_API int gls_cnn_param_count(void);
@@ -299,6 +311,8 @@ GLS_API gls_status gls_cnn_forward(gls_cnn* cnn, const float* in, int width, int
 GLS_API gls_status gls_cnn_train_step(gls_cnn* cnn, const float* in, const float* gt, int width, int height, int n,
                                       float lr, float loss[2]);
 
+/* every lane runs the learned stage with (its own copy of) this network; NULL: plain */
+GLS_API gls_status gls_raw_batch_set_cnn(gls_raw_batch* batch, gls_cnn* cnn);
 /* The lane of each frame, as the batch assigns them (frames by decreasing pixel count, each
  * to the lane with the fewest pixels so far; ties to the lower frame index and lane). */
 GLS_API gls_status gls_raw_batch_plan(int n, const int* widths, const int* heights, int lanes, int* lane_of);

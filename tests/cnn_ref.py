@@ -59,7 +59,7 @@ def forward(params, inp, exact=False):
 def strength_target(inp, head, gt):
     x = np.asarray(inp, np.float64)
     e = x[..., :3] + head[..., 1:4] - np.asarray(gt, np.float64)
-    return np.minimum(1.0, np.mean(e * e, axis=-1) / np.maximum(x[..., 3] ** 2, 1e-8))
+    return 0.5 * np.minimum(1.0, np.mean(e * e, axis=-1) / np.maximum(x[..., 3] ** 2, 1e-8))
 
 
 def loss_grad(inp, head, gt, exact=False, tgt=None):
