@@ -45,7 +45,7 @@ struct DemosaicArgs {
 // 2 sigmoid(logit) per pixel.
 struct PostCnnArgs {
     const float* cnn_in;  // [h][w][4]
-    const float* head;    // [h][w][4]: strength logit, residual RGB
+    const float* head;    // [h][w][4]: strength logit, residual RGB in units of sigma
     int w, h;
     Mat3 cam_ycbcr;
     float va0, vb0;

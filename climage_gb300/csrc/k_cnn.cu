@@ -1,7 +1,7 @@
 // k_cnn.cu -- the learned stage: a 5-layer 3x3 BF16 CNN (4 -> 32 -> 32 -> 32 -> 32 -> 4
 // channels, ReLU between layers) that reads the demosaiced linear RGB plus a per-pixel noise
 // sigma map and predicts a per-pixel denoise strength (channel 0, a logit) and an RGB
-// residual (channels 1..3).  No counterpart in the reference: it is inserted after
+// residual in units of that sigma (channels 1..3).  No counterpart in the reference: it is inserted after
 // interpolateRedBlue (raw_converter.cpp:127 of the reference), where the residual is added
 // before transformImage and the strength scales the level-0 denoise.
 //
@@ -25,6 +25,8 @@ namespace gls {
 namespace {
 
 constexpr int kLayers = 5;
+// the noise sigma enters the network scaled to the range of the image values
+constexpr float kSigmaScale = 64.0f;
 constexpr int kCin[kLayers] = {4, 32, 32, 32, 32};     // real input channels
 constexpr int kCout[kLayers] = {32, 32, 32, 32, 4};    // real output channels
 
@@ -66,7 +68,8 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], 
 
 // ---------------------------------------------------------------------------------------
 // Activation loader: a (TR + 2) x (TC + 2) halo tile of an NHWC tensor with `csrc` channels
-// (bf16, or fp32 for the network input) into shared memory with CIN channels per pixel
+// (bf16, or fp32 for the network input, whose sigma channel 3 is scaled by kSigmaScale) into
+// shared memory with CIN channels per pixel
 // (zero-filled beyond csrc and outside the image) and a pixel stride of CIN + 8 elements,
 // which keeps ldmatrix rows on distinct banks.
 // ---------------------------------------------------------------------------------------
@@ -86,7 +89,7 @@ __device__ __forceinline__ void load_halo(__nv_bfloat16* s, const void* src, int
                 const float* f = static_cast<const float*>(src) + base;
 #pragma unroll
                 for (int k = 0; k < 8; k++)
-                    if (q * 8 + k < csrc) v[k] = __float2bfloat16_rn(f[q * 8 + k]);
+                    if (q * 8 + k < csrc) v[k] = __float2bfloat16_rn(q * 8 + k == 3 ? f[3] * kSigmaScale : f[q * 8 + k]);
             } else {
                 const __nv_bfloat16* b = static_cast<const __nv_bfloat16*>(src) + base;
                 if (csrc % 8 == 0 && q * 8 + 8 <= csrc) {
@@ -339,8 +342,9 @@ __global__ void reduce_rows_kernel(const float* part, int rows, int cols, float*
 
 // ---------------------------------------------------------------------------------------
 // Loss of a batch and its gradient at the head.  in: [img][h][w][4] fp32 (R, G, B, sigma);
-// head: [img][h][w][4] fp32 (strength logit, residual RGB); gt: [img][h][w][3] fp32.
-//   residual loss  mean over pixels and channels of (in_rgb + r - gt)^2
+// head: [img][h][w][4] fp32 (strength logit, residual RGB in units of sigma); gt:
+// [img][h][w][3] fp32.
+//   residual loss  mean over pixels and channels of (in_rgb + sigma * r - gt)^2
 //   strength loss  lambda * mean over pixels of (sigmoid(s) - tgt)^2, tgt = min(1, e2 / sigma^2) / 2
 //                  with e2 the mean squared residual error of the pixel (no gradient through tgt);
 //                  the pipeline scales the level-0 noise model by 2 sigmoid(s) (<= 1 after
@@ -356,13 +360,14 @@ __global__ void loss_grad_kernel(const float* in, const float* head, const float
     for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < npx; p += (size_t)gridDim.x * blockDim.x) {
         const float4 x = reinterpret_cast<const float4*>(in)[p];
         const float4 o = reinterpret_cast<const float4*>(head)[p];
-        const float e0 = x.x + o.y - gt[3 * p + 0], e1 = x.y + o.z - gt[3 * p + 1], e2 = x.z + o.w - gt[3 * p + 2];
+        const float e0 = x.x + x.w * o.y - gt[3 * p + 0], e1 = x.y + x.w * o.z - gt[3 * p + 1],
+                    e2 = x.z + x.w * o.w - gt[3 * p + 2];
         const float mse = (e0 * e0 + e1 * e1 + e2 * e2) * (1.0f / 3.0f);
         const float tgt = 0.5f * fminf(1.0f, mse / fmaxf(x.w * x.w, 1e-8f));
         const float s = 1.0f / (1.0f + expf(-o.x));
         l0 += 3.0f * mse;
         l1 += (s - tgt) * (s - tgt);
-        const float gr = 2.0f * inv_n * (1.0f / 3.0f);
+        const float gr = 2.0f * inv_n * (1.0f / 3.0f) * x.w;
         const float gs = kStrengthWeight * 2.0f * inv_n * (s - tgt) * s * (1.0f - s);
         __nv_bfloat16* d = dhead + 4 * p;
         d[0] = __float2bfloat16_rn(gs);

@@ -250,7 +250,8 @@ __global__ void __launch_bounds__(kT) demosaic_kernel(DemosaicArgs a) {
 }
 
 // =========================================================================================
-// post_cnn: the learned stage's residual added to the linear RGB, then blendHighlights,
+// post_cnn: the learned stage's residual (its RGB output times the pixel's sigma) added to
+// the linear RGB, then blendHighlights,
 // cam -> YCbCr over the tile and a one-pixel ring (clamped reads: the same values the
 // fused kernel's border replication gives), despeckle -> level 0, and the level-0
 // noise-model multiplier.  A residual that is exactly zero leaves the value as it is (also
@@ -269,8 +270,9 @@ __global__ void __launch_bounds__(kT) post_cnn_kernel(PostCnnArgs a) {
         const size_t px = (size_t)y * a.w + x;
         const float4 lin = reinterpret_cast<const float4*>(a.cnn_in)[px];
         const float4 o = reinterpret_cast<const float4*>(a.head)[px];
-        float3 p = make_float3(o.y == 0.0f ? lin.x : lin.x + o.y, o.z == 0.0f ? lin.y : lin.y + o.z,
-                               o.w == 0.0f ? lin.z : lin.z + o.w);
+        const float rx = lin.w * o.y, ry = lin.w * o.z, rz = lin.w * o.w;  // residual = sigma * output
+        float3 p = make_float3(rx == 0.0f ? lin.x : lin.x + rx, ry == 0.0f ? lin.y : lin.y + ry,
+                               rz == 0.0f ? lin.z : lin.z + rz);
         p = round3<S>(p);
         p = round3<S>(blend_highlights_px(p, 1.0f));
         p = round3<S>(transform_px(a.cam_ycbcr, p));

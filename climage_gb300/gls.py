@@ -581,12 +581,14 @@ def cnn_split(params):
     return out
 
 
-def cnn_init(seed=0):
-    """He-initialised parameters (zero biases; the head starts near zero residual and logit)."""
+def cnn_init(seed=0, head_std=0.0):
+    """He-initialised hidden layers, zero biases; the head starts at zero (head_std = 0), so
+    the untrained network is the plain pipeline exactly (residual 0, multiplier 1)."""
     rng = np.random.default_rng(seed)
     parts = []
     for l, (cin, cout) in enumerate(CNN_LAYERS):
-        std = np.sqrt(2.0 / (9 * cin)) * (0.1 if l == len(CNN_LAYERS) - 1 else 1.0)
-        parts.append(rng.normal(0.0, std, cout * 9 * cin).astype(np.float32))
+        std = head_std if l == len(CNN_LAYERS) - 1 else np.sqrt(2.0 / (9 * cin))
+        parts.append(rng.normal(0.0, std, cout * 9 * cin).astype(np.float32) if std > 0
+                     else np.zeros(cout * 9 * cin, np.float32))
         parts.append(np.zeros(cout, np.float32))
     return np.concatenate(parts)

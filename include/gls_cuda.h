@@ -256,7 +256,7 @@ GLS_API gls_status gls_raw_converter_profile_report(gls_raw_converter* conv, cha
 
 /* ---- the learned stage in the pipeline (see gls_cnn below; no counterpart in the reference) ----
  * With a network set (the converter keeps its own copy), demosaicImage runs it after
- * interpolateRedBlue: its residual is added to the linear RGB before blendHighlights and
+ * interpolateRedBlue: its residual (sigma times its RGB output) is added to the linear RGB before blendHighlights and
  * transformImage, and 2 sigmoid(strength logit) multiplies the level-0 denoise noise model
  * per pixel.  An all-zero network reproduces the plain pipeline exactly.  Fused schedule
  * only (not with GuidedPrecise).  cnn = NULL returns to the plain pipeline. */
@@ -295,7 +295,7 @@ GLS_API gls_status gls_raw_batch_demosaic_host(gls_raw_batch* batch, int n, cons
 /* ---- the learned stage: a 5-layer 3x3 BF16 CNN ----
  * No counterpart in the reference.  4 -> 32 -> 32 -> 32 -> 32 -> 4 channels, ReLU between
  * layers, zero-padded borders.  Input per pixel: demosaiced linear R, G, B and the noise
- * sigma; output per pixel: a denoise-strength logit and an RGB residual.  Parameters are a
+ * sigma; output per pixel: a denoise-strength logit and an RGB residual in units of sigma.  Parameters are a
  * flat FP32 array, per layer W[cout][3][3][cin] then b[cout] (gls_cnn_param_count() in all).
  * All tensors are device NHWC fp32: in [n][h][w][4], out [n][h][w][4], gt [n][h][w][3]. */
 GLS_API gls_status gls_cnn_create(gls_ctx* ctx, gls_cnn** out);

@@ -7,6 +7,7 @@ import numpy as np
 from climage_gb300.gls import CNN_LAYERS
 
 STRENGTH_WEIGHT = 0.1
+SIGMA_SCALE = 64.0  # the network sees the sigma channel scaled by this
 
 
 def cnn_split(params):
@@ -46,7 +47,9 @@ def forward(params, inp, exact=False):
     """Returns (activations [input, a0..a3], head (n, h, w, 4))."""
     r = (lambda v: np.asarray(v, np.float64)) if exact else bf16
     layers = cnn_split(params)
-    acts = [r(inp)]
+    x = np.array(inp, np.float64)
+    x[..., 3] = (np.asarray(inp, np.float32)[..., 3] * np.float32(SIGMA_SCALE)).astype(np.float64)
+    acts = [r(x)]
     a = acts[0]
     for l, (W, b) in enumerate(layers):
         z = conv3x3(a, r(W), np.asarray(b, np.float64))
@@ -56,9 +59,15 @@ def forward(params, inp, exact=False):
         acts.append(a)
 
 
+def corrected(inp, head):
+    """The network's RGB output applied: input RGB + sigma * residual."""
+    x = np.asarray(inp, np.float64)
+    return x[..., :3] + x[..., 3:4] * head[..., 1:4]
+
+
 def strength_target(inp, head, gt):
     x = np.asarray(inp, np.float64)
-    e = x[..., :3] + head[..., 1:4] - np.asarray(gt, np.float64)
+    e = corrected(inp, head) - np.asarray(gt, np.float64)
     return 0.5 * np.minimum(1.0, np.mean(e * e, axis=-1) / np.maximum(x[..., 3] ** 2, 1e-8))
 
 
@@ -67,7 +76,7 @@ def loss_grad(inp, head, gt, exact=False, tgt=None):
     l0 + STRENGTH_WEIGHT * l1, the strength target held fixed (given, or from this head)."""
     r = (lambda v: np.asarray(v, np.float64)) if exact else bf16
     x = np.asarray(inp, np.float64)
-    e = x[..., :3] + head[..., 1:4] - np.asarray(gt, np.float64)
+    e = corrected(inp, head) - np.asarray(gt, np.float64)
     npx = e.shape[0] * e.shape[1] * e.shape[2]
     if tgt is None:
         tgt = strength_target(inp, head, gt)
@@ -75,7 +84,7 @@ def loss_grad(inp, head, gt, exact=False, tgt=None):
     l0 = float(np.sum(e * e) / (3 * npx))
     l1 = float(np.sum((s - tgt) ** 2) / npx)
     d = np.zeros(head.shape)
-    d[..., 1:4] = 2.0 * e / (3 * npx)
+    d[..., 1:4] = 2.0 * e * x[..., 3:4] / (3 * npx)
     d[..., 0] = STRENGTH_WEIGHT * 2.0 * (s - tgt) * s * (1 - s) / npx
     return l0, l1, r(d)
 

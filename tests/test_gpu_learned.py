@@ -66,7 +66,7 @@ def test_nonzero_network_changes_the_output(ctx):
     raw, _, meta = synthetic.make_frame(128, 96, bayer=2, gain=4.0, read_sigma=6.0, seed=8)
     spec = configs.make_spec(meta, levels=4)
     cnn = gls.Cnn(ctx)
-    cnn.set_params(gls.cnn_init(2) * 5.0)
+    cnn.set_params(gls.cnn_init(2, head_std=0.05))
     plain, lrn = gls.RawConverter(ctx), gls.RawConverter(ctx)
     lrn.setCnn(cnn)
     a, b = run(plain, raw, spec, True), run(lrn, raw, spec, True)
