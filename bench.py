@@ -39,6 +39,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-psnr", action="store_true")
+    ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--profile-only", action="store_true", help="a short run for ncu: no clocks, no cpu leg")
     return ap.parse_args()
 
@@ -318,6 +319,37 @@ def main():
                "h2d_bytes_per_step": int(sum(f[0].nbytes for f in frames)),
                "d2h_bytes_per_step": int(len(frames) * w * h * 4)}
 
+    # ---- the learned form: the same burst with the learned stage (shipped parameters) ----
+    learned_line = None
+    if not args.no_learned and not args.profile_only:
+        from climage_gb300 import learned
+        prm = learned.load_params()
+        if prm is not None:
+            cnn = gls.Cnn(ctx)
+            cnn.set_params(prm)
+            lb = gls.RawBatch(ctx, lanes)
+            lb.reserve(w, h, cfg["levels"], cfg["storage"])
+            lb.set_cnn(cnn)
+            for _ in range(args.warmup):
+                lb.demosaic(raws, params, outs)
+            torch.cuda.synchronize()
+            ls = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+            le = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+            for k in range(args.steps):
+                flush.fill_(k & 0xFF)
+                ls[k].record(stream)
+                lb.demosaic(raws, params, outs)
+                le[k].record(stream)
+            torch.cuda.synchronize()
+            lms = float(sum(a.elapsed_time(b) for a, b in zip(ls, le)))
+            verdict = learned.judge(ctx, cnn, range(10**6, 10**6 + 2))
+            learned_line = {"value": round(world * mpix_per_step * args.steps / (lms / 1e3), 3), "unit": "MPix/s",
+                            "ms_per_step": round(lms / args.steps, 4),
+                            "judge": {k: verdict[k] for k in ("plain", "learned", "linear_input", "linear_corrected")},
+                            "judge_frames": "2 held-out 1024x768 scenes, read sigma 4-16 DN, gain 0.25-4"}
+            lb.close()
+            cnn.close()
+
     cpu = psnr = None
     if rank == 0 and world == 1 and not args.no_cpu and not args.profile_only:
         gpu_rgb = None
@@ -352,6 +384,7 @@ def main():
             "e2e": e2e,
             "cpu_baseline": cpu,
             "psnr_vs_fp64": psnr,
+            "learned_form": learned_line,
         }
         print(json.dumps(line), flush=True)
     conv.close()
