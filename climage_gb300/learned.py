@@ -206,6 +206,30 @@ def load_params(path=PARAMS_PATH):
     return np.load(path).astype(np.float32) if os.path.exists(path) else None
 
 
+def time_forward(w, h, warmup=3, reps=5):
+    """CUDA-event time of one forward pass of the shipped network over a w x h frame."""
+    import torch
+    ctx = gls.Context(0)
+    cnn = gls.Cnn(ctx)
+    cnn.set_params(load_params())
+    x = torch.rand((1, h, w, 4), device="cuda")
+    out = torch.empty_like(x)
+    for _ in range(warmup):
+        cnn.forward(x, out)
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    for _ in range(reps):
+        cnn.forward(x, out)
+    e.record()
+    torch.cuda.synchronize()
+    ms = s.elapsed_time(e) / reps
+    flop = 2 * 9 * sum(cin * cout for cin, cout in gls.CNN_LAYERS) * w * h
+    print(json.dumps({"forward_ms": round(ms, 4), "pixels": w * h, "tflops": round(flop / ms / 1e9, 1)}))
+    cnn.close()
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--crops", type=int, default=20000)
@@ -217,7 +241,12 @@ def main():
     ap.add_argument("--judge-only", default=None, help="judge these saved parameters, no training")
     ap.add_argument("--gain", type=float, nargs=2, default=None, help="gain range (e-/DN) of the frames")
     ap.add_argument("--sigma", type=float, nargs=2, default=None, help="read noise range (DN) of the frames")
+    ap.add_argument("--time-forward", type=int, nargs=2, default=None, metavar=("W", "H"),
+                    help="only time the network's forward pass over a W x H frame (shipped parameters)")
     args = ap.parse_args()
+    if args.time_forward:
+        time_forward(*args.time_forward)
+        return
     if args.gain:
         NOISE["gain"] = tuple(args.gain)
     if args.sigma:
