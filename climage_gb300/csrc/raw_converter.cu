@@ -673,6 +673,7 @@ gls_status gls_raw_converter_set_cnn(gls_raw_converter* c, gls_cnn* src) {
     if (s != GLS_OK) return set_error(c->ctx, s, "learned stage: reading the network's parameters");
     GLS_CHECK(gls_cnn_create(c->ctx, &c->cnn));
     s = gls_cnn_set_params(c->cnn, prm.data(), n);
+    if (s == GLS_OK) s = gls_cnn_set_backend(c->cnn, gls_cnn_get_backend(src));
     if (s != GLS_OK) {
         gls_cnn_destroy(c->cnn);
         c->cnn = nullptr;

@@ -147,6 +147,9 @@ SIGNATURES = [
     ("gls_cnn_get_params", _I, [_P, _FP, _I]),
     ("gls_cnn_get_grads", _I, [_P, _FP, _I]),
     ("gls_cnn_forward", _I, [_P, _P, _I, _I, _I, _P]),
+    ("gls_cnn_set_backend", _I, [_P, _I]),
+    ("gls_cnn_get_backend", _I, [_P]),
+    ("gls_cnn_status", _I, [_P]),
     ("gls_cnn_train_step", _I, [_P, _P, _P, _I, _I, _I, _F, _FP]),
     ("gls_raw_batch_plan", _I, [_I, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int), _I,
                                 ctypes.POINTER(ctypes.c_int)]),
@@ -549,6 +552,13 @@ class Cnn:
         self.ctx.check(lib().gls_cnn_forward(self.handle, ctypes.c_void_p(inp.data_ptr()), w, h, n,
                                              ctypes.c_void_p(out.data_ptr())), "Cnn.forward")
         return out
+
+    def set_backend(self, backend):
+        """1: tcgen05 (default) for the hidden layers' forward pass; 0: mma.sync."""
+        self.ctx.check(lib().gls_cnn_set_backend(self.handle, int(backend)), "Cnn.set_backend")
+
+    def status(self):
+        self.ctx.check(lib().gls_cnn_status(self.handle), "Cnn.status")
 
     def train_step(self, inp, gt, lr):
         n, h, w, _ = inp.shape

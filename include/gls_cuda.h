@@ -306,6 +306,13 @@ GLS_API gls_status gls_cnn_get_params(gls_cnn* cnn, float* params, int n);
 /* the gradients of the last training step (of the mean losses below) */
 GLS_API gls_status gls_cnn_get_grads(gls_cnn* cnn, float* grads, int n);
 GLS_API gls_status gls_cnn_forward(gls_cnn* cnn, const float* in, int width, int height, int n, float* out);
+/* Tensor-core path of the hidden layers' forward pass (inference and training): 1 (default)
+ * 5th-generation tcgen05.mma with tensor-memory accumulators, 0 warp-level mma.sync; the
+ * backward pass always uses mma.sync.  A converter given this network copies the choice. */
+GLS_API gls_status gls_cnn_set_backend(gls_cnn* cnn, int backend);
+GLS_API int gls_cnn_get_backend(gls_cnn* cnn);
+/* Synchronises; GLS_ERR_TIMEOUT when a tcgen05 block gave up waiting for its MMAs. */
+GLS_API gls_status gls_cnn_status(gls_cnn* cnn);
 /* One Adam step (lr > 0; lr = 0 only computes the gradients) on a batch against the clean
  * RGB gt; loss[0] = mean squared error of (input RGB + residual), loss[1] = strength loss. */
 GLS_API gls_status gls_cnn_train_step(gls_cnn* cnn, const float* in, const float* gt, int width, int height, int n,
