@@ -239,13 +239,15 @@ __global__ void __launch_bounds__(CT) conv3x3_kernel(ConvArgs a) {
 // address with the same strides: SBO = one halo row (160 B), LBO = one channel block
 // (2880 B).  For B, SBO = 8 output channels (128 B), LBO = one channel block (512 B).
 // One thread issues the MMAs and commits them to an mbarrier; every thread waits on it
-// (bounded: after kWaitLimit polls it records an error and skips the result), then each
-// warp reads its 32 lanes of the accumulator (tcgen05.ld 32x32b) for the epilogue.  Warp 0
-// allocates the 32 TMEM columns and frees them on every path.
+// (bounded: after kWaitLimit polls the block records an error, drains its copies and
+// stops), then each warp reads its 32 lanes of the accumulator (tcgen05.ld 32x32b) for the
+// epilogue.  Warp 0 allocates the 32 TMEM columns and frees them on every path.
 // ---------------------------------------------------------------------------------------
 constexpr int TC5_R = 16, TC5_C = 8;  // output tile rows x columns
 constexpr int TC5_HR = TC5_R + 2, TC5_HC = TC5_C + 2;
 constexpr uint32_t kWaitLimit = 1u << 24;
+
+__device__ __forceinline__ int cdiv_d(int a, int b) { return (a + b - 1) / b; }
 
 __device__ __forceinline__ uint64_t tc5_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
     return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
@@ -255,15 +257,23 @@ __device__ __forceinline__ uint64_t tc5_desc(uint32_t saddr, uint32_t lbo, uint3
 // kind::f16, BF16 A and B (K-major), FP32 D, M = 128, N = 32
 constexpr uint32_t kIdescBf16M128N32 = (1u << 4) | (1u << 7) | (1u << 10) | ((32u >> 3) << 17) | ((128u >> 4) << 24);
 
-__global__ void __launch_bounds__(CT) conv3x3_tc05_kernel(ConvArgs a, int* err) {
-    constexpr int HALO_B = 4 * TC5_HR * TC5_HC * 16, W_B = 9 * 4 * 32 * 16;
-    __shared__ __align__(128) unsigned char s_a[HALO_B];
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, bool valid) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(valid ? 16 : 0) : "memory");
+}
+
+// Persistent: each block stages the weights once and walks tiles blockIdx.x, + gridDim.x,
+// ...; the halo of the next tile streams in (cp.async, zero-filled outside the image) into
+// the other of two buffers while the current tile's MMAs and epilogue run.
+__global__ void __launch_bounds__(CT) conv3x3_tc05_kernel(ConvArgs a, int nimg, int* err) {
+    constexpr int HALO_N = 4 * TC5_HR * TC5_HC, HALO_B = HALO_N * 16, W_B = 9 * 4 * 32 * 16;
+    __shared__ __align__(128) unsigned char s_a[2][HALO_B];
     __shared__ __align__(128) unsigned char s_b[W_B];
     __shared__ __align__(8) uint64_t s_bar;
     __shared__ uint32_t s_taddr;
-    const int x0 = blockIdx.x * TC5_C, y0 = blockIdx.y * TC5_R, img = blockIdx.z;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t bar = smem_u32(&s_bar);
+    const int tiles_x = cdiv_d(a.w, TC5_C), tiles_y = cdiv_d(a.h, TC5_R);
+    const int tiles_img = tiles_x * tiles_y, ntiles = tiles_img * nimg;
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 32;\n" ::"r"(smem_u32(&s_taddr)));
@@ -273,83 +283,104 @@ __global__ void __launch_bounds__(CT) conv3x3_tc05_kernel(ConvArgs a, int* err) 
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar));
         asm volatile("fence.mbarrier_init.release.cluster;\n");
     }
-    // halo tile: 16 bytes = 8 channels of one pixel per (cb, row, col)
-    const __nv_bfloat16* in = (const __nv_bfloat16*)a.in + img * a.in_stride;
-    for (int i = threadIdx.x; i < 4 * TC5_HR * TC5_HC; i += CT) {
-        const int cb = i / (TC5_HR * TC5_HC), p = i - cb * (TC5_HR * TC5_HC);
-        const int r = p / TC5_HC, c = p - r * TC5_HC;
-        const int x = x0 - 1 + c, y = y0 - 1 + r;
-        uint4 v = make_uint4(0u, 0u, 0u, 0u);
-        if (x >= 0 && x < a.w && y >= 0 && y < a.h)
-            v = *reinterpret_cast<const uint4*>(in + ((size_t)y * a.w + x) * 32 + cb * 8);
-        *reinterpret_cast<uint4*>(s_a + (size_t)i * 16) = v;
-    }
-    // weights: global [n][tap][ci] -> shared [tap][cb][n][8]
     for (int i = threadIdx.x; i < 9 * 4 * 32; i += CT) {
         const int tap = i / 128, r = i - tap * 128, cb = r / 32, n = r - cb * 32;
         *reinterpret_cast<uint4*>(s_b + (size_t)i * 16) =
             *reinterpret_cast<const uint4*>(a.wt + (size_t)n * 288 + tap * 32 + cb * 8);
     }
-    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    auto prefetch = [&](int t, int buf) {
+        const int img = t / tiles_img, tt = t - img * tiles_img;
+        const int x0 = (tt % tiles_x) * TC5_C, y0 = (tt / tiles_x) * TC5_R;
+        const __nv_bfloat16* in = (const __nv_bfloat16*)a.in + img * a.in_stride;
+        const uint32_t base = smem_u32(s_a[buf]);
+        for (int i = threadIdx.x; i < HALO_N; i += CT) {
+            const int cb = i / (TC5_HR * TC5_HC), p = i - cb * (TC5_HR * TC5_HC);
+            const int r = p / TC5_HC, c = p - r * TC5_HC;
+            const int x = x0 - 1 + c, y = y0 - 1 + r;
+            const bool ok = x >= 0 && x < a.w && y >= 0 && y < a.h;
+            cp_async16(base + i * 16, ok ? (const void*)(in + ((size_t)y * a.w + x) * 32 + cb * 8) : (const void*)in, ok);
+        }
+    };
+    int t = blockIdx.x;
+    if (t < ntiles) prefetch(t, 0);
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     const uint32_t taddr = s_taddr;
-
-    if (threadIdx.x == 0) {
-        const uint32_t abase = smem_u32(s_a), bbase = smem_u32(s_b);
+    for (int it = 0; t < ntiles; t += gridDim.x, it++) {
+        const int buf = it & 1;
+        if (t + (int)gridDim.x < ntiles) prefetch(t + gridDim.x, buf ^ 1);
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+        asm volatile("cp.async.wait_group 1;\n" ::: "memory");  // this tile's halo has landed
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        if (threadIdx.x == 0) {
+            const uint32_t abase = smem_u32(s_a[buf]), bbase = smem_u32(s_b);
 #pragma unroll 1
-        for (int tap = 0; tap < 9; tap++) {
-            const int dy = tap / 3, dx = tap % 3;
+            for (int tap = 0; tap < 9; tap++) {
+                const int dy = tap / 3, dx = tap % 3;
 #pragma unroll
-            for (int kc = 0; kc < 2; kc++) {
-                const uint64_t ad = tc5_desc(abase + (uint32_t)(((2 * kc * TC5_HR + dy) * TC5_HC + dx) * 16),
-                                             TC5_HR * TC5_HC * 16, TC5_HC * 16);
-                const uint64_t bd = tc5_desc(bbase + (uint32_t)((tap * 4 + 2 * kc) * 32 * 16), 32 * 16, 8 * 16);
-                const uint32_t acc = (tap | kc) ? 1u : 0u;
-                asm volatile(
-                    "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(taddr),
-                    "l"(ad), "l"(bd), "r"(kIdescBf16M128N32), "r"(acc));
+                for (int kc = 0; kc < 2; kc++) {
+                    const uint64_t ad = tc5_desc(abase + (uint32_t)(((2 * kc * TC5_HR + dy) * TC5_HC + dx) * 16),
+                                                 TC5_HR * TC5_HC * 16, TC5_HC * 16);
+                    const uint64_t bd = tc5_desc(bbase + (uint32_t)((tap * 4 + 2 * kc) * 32 * 16), 32 * 16, 8 * 16);
+                    const uint32_t acc = (tap | kc) ? 1u : 0u;
+                    asm volatile(
+                        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(taddr),
+                        "l"(ad), "l"(bd), "r"(kIdescBf16M128N32), "r"(acc));
+                }
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar)
+                         : "memory");
+        }
+        // this tile's MMAs complete phase `it` of the barrier (bounded wait, block-uniform verdict)
+        uint32_t done = 0;
+        for (uint32_t k = 0; k < kWaitLimit && !done; k++) {
+            asm volatile(
+                "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+                : "=r"(done)
+                : "r"(bar), "r"((uint32_t)(it & 1))
+                : "memory");
+        }
+        if (!__syncthreads_and(done)) {  // stop; drain the copies and free TMEM below
+            if (threadIdx.x == 0) atomicExch(err, 1);
+            break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        {
+            uint32_t v[32];
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+                "%14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];\n"
+                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                  "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
+                  "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]),
+                  "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+                : "r"(taddr + ((uint32_t)(warp * 32) << 16)));
+            asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+            const int img = t / tiles_img, tt = t - img * tiles_img;
+            const int m = warp * 32 + lane;
+            const int x = (tt % tiles_x) * TC5_C + (m & 7), y = (tt / tiles_x) * TC5_R + (m >> 3);
+            if (x < a.w && y < a.h) {
+                __nv_bfloat16 o[32];
+#pragma unroll
+                for (int n = 0; n < 32; n++)
+                    o[n] = __float2bfloat16_rn(fmaxf(__uint_as_float(v[n]) + a.bias[n], 0.0f));
+                uint4* dst =
+                    reinterpret_cast<uint4*>((__nv_bfloat16*)a.out + img * a.out_stride + ((size_t)y * a.w + x) * 32);
+#pragma unroll
+                for (int q = 0; q < 4; q++) dst[q] = reinterpret_cast<const uint4*>(o)[q];
             }
         }
-        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar)
-                     : "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+        __syncthreads();
     }
-    // wait for the MMAs (phase 0 of the barrier), bounded
-    uint32_t done = 0;
-    for (uint32_t it = 0; it < kWaitLimit && !done; it++) {
-        asm volatile(
-            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
-            : "=r"(done)
-            : "r"(bar), "r"(0u)
-            : "memory");
-    }
-    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-    if (done) {
-        uint32_t v[32];
-        asm volatile(
-            "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
-            "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];\n"
-            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-              "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
-              "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
-              "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
-            : "r"(taddr + ((uint32_t)(warp * 32) << 16)));
-        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-        // accumulator row m = 32 * warp + lane: pixel (m / 8, m % 8) of the tile
-        const int m = warp * 32 + lane, x = x0 + (m & 7), y = y0 + (m >> 3);
-        if (x < a.w && y < a.h) {
-            __nv_bfloat16 o[32];
-#pragma unroll
-            for (int n = 0; n < 32; n++) o[n] = __float2bfloat16_rn(fmaxf(__uint_as_float(v[n]) + a.bias[n], 0.0f));
-            uint4* dst = reinterpret_cast<uint4*>((__nv_bfloat16*)a.out + img * a.out_stride + ((size_t)y * a.w + x) * 32);
-#pragma unroll
-            for (int q = 0; q < 4; q++) dst[q] = reinterpret_cast<const uint4*>(o)[q];
-        }
-    } else if (threadIdx.x == 0) {
-        atomicExch(err, 1);
-    }
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 32;\n" ::"r"(taddr));
@@ -699,7 +730,9 @@ struct gls_cnn {
             if (backend == 1) {
                 ConvArgs a{act[l - 1], 32, wfwd[l], b + off[l] + 32 * 9 * 32, act[l], 32, nullptr, w, h,
                            px * 32, px * 32, 0};
-                conv3x3_tc05_kernel<<<dim3(cdiv(w, TC5_C), cdiv(h, TC5_R), n), CT, 0, ctx->stream>>>(a, err_dev);
+                const int tiles = cdiv(w, TC5_C) * cdiv(h, TC5_R) * n;
+                const int per = 4 * (ctx->num_sms > 0 ? ctx->num_sms : 148);
+                conv3x3_tc05_kernel<<<tiles < per ? tiles : per, CT, 0, ctx->stream>>>(a, n, err_dev);
                 ctx->launches++;
             } else {
                 conv<32, 32, 0, false>(act[l - 1], 32, px * 32, wfwd[l], b + off[l] + 32 * 9 * 32, act[l], 32,

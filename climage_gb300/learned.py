@@ -206,12 +206,15 @@ def load_params(path=PARAMS_PATH):
     return np.load(path).astype(np.float32) if os.path.exists(path) else None
 
 
-def time_forward(w, h, warmup=3, reps=5):
-    """CUDA-event time of one forward pass of the shipped network over a w x h frame."""
+def time_forward(w, h, warmup=3, reps=5, backend=None):
+    """CUDA-event time of one forward pass of the shipped network over a w x h frame
+    (hidden layers on `backend`: 0 warp-level MMA, 1 tcgen05; None keeps the default)."""
     import torch
     ctx = gls.Context(0)
     cnn = gls.Cnn(ctx)
     cnn.set_params(load_params())
+    if backend is not None:
+        cnn.set_backend(backend)
     x = torch.rand((1, h, w, 4), device="cuda")
     out = torch.empty_like(x)
     for _ in range(warmup):
@@ -225,7 +228,8 @@ def time_forward(w, h, warmup=3, reps=5):
     torch.cuda.synchronize()
     ms = s.elapsed_time(e) / reps
     flop = 2 * 9 * sum(cin * cout for cin, cout in gls.CNN_LAYERS) * w * h
-    print(json.dumps({"forward_ms": round(ms, 4), "pixels": w * h, "tflops": round(flop / ms / 1e9, 1)}))
+    cnn.status()
+    print(json.dumps({"backend": backend, "forward_ms": round(ms, 4), "pixels": w * h, "tflops": round(flop / ms / 1e9, 1)}))
     cnn.close()
     ctx.close()
 
@@ -241,11 +245,13 @@ def main():
     ap.add_argument("--judge-only", default=None, help="judge these saved parameters, no training")
     ap.add_argument("--gain", type=float, nargs=2, default=None, help="gain range (e-/DN) of the frames")
     ap.add_argument("--sigma", type=float, nargs=2, default=None, help="read noise range (DN) of the frames")
+    ap.add_argument("--backend", type=int, default=None, choices=(0, 1),
+                    help="hidden-layer forward backend for --time-forward (0 mma.sync, 1 tcgen05)")
     ap.add_argument("--time-forward", type=int, nargs=2, default=None, metavar=("W", "H"),
                     help="only time the network's forward pass over a W x H frame (shipped parameters)")
     args = ap.parse_args()
     if args.time_forward:
-        time_forward(*args.time_forward)
+        time_forward(*args.time_forward, backend=args.backend)
         return
     if args.gain:
         NOISE["gain"] = tuple(args.gain)
