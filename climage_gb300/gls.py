@@ -116,6 +116,7 @@ SIGNATURES = [
     ("gls_despeckle_raw_rgba", _I, [_P, _D, _D]),
     ("gls_denoise_raw_rgba", _I, [_P, _D, _FP, _D]),
     ("gls_unpack_raw_bits", _I, [_P, _P, ctypes.c_size_t, _I, _P, ctypes.c_size_t]),
+    ("gls_auto_white_balance", _I, [_P, _D, _FP, _FP, _F, _F, _I, _FP, _FP]),
     ("gls_selftest", _I, [_P, ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)]),
     ("gls_cam_xyz_coeff", _I, [_FP, _FP, _FP]),
     ("gls_cam_ycbcr", _I, [_FP, _FP]),
@@ -297,6 +298,16 @@ class Context:
         self.check(self._lib.gls_compute_raw_noise_statistics(self.handle, desc(scaled), bayer, out),
                    "computeRawNoiseStatistics")
         return np.array(out[:], np.float32)
+
+    def autoWhiteBalance(self, raw, rgb_ycbcr, scale_mul, white, black, bayer):
+        """autoWhiteBalance over a raw uint16 device tensor: (gains (3,) with green 1,
+        highlight fraction)."""
+        wb = (ctypes.c_float * 3)()
+        hl = ctypes.c_float()
+        self.check(self._lib.gls_auto_white_balance(self.handle, desc(raw), farr(rgb_ycbcr, 9),
+                                                    farr(scale_mul, 4), float(white), float(black), int(bayer), wb,
+                                                    ctypes.byref(hl)), "autoWhiteBalance")
+        return np.array(wb[:], np.float32), np.float32(hl.value)
 
     def interpolateGreen(self, scaled, green, bayer, luma_variance):
         self.check(self._lib.gls_interpolate_green(self.handle, desc(scaled), desc(green), bayer, float(luma_variance)),

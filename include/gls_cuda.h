@@ -215,6 +215,17 @@ GLS_API gls_status gls_unpack_raw_bits(gls_ctx* ctx, const void* packed, size_t 
  * sqrt-then-compare, [3] hardware float->half rounding vs the portable conversion. */
 GLS_API gls_status gls_selftest(gls_ctx* ctx, uint64_t n, uint64_t seed, uint64_t mismatches[4]);
 
+/* autoWhiteBalance (demosaic_utils.cpp:976-1026): the white-balance gains of a raw
+ * R16_UNORM frame (device) -- rgb_ycbcr is cam_ycbcr(rgb_cam), scale_mul the four channel
+ * multipliers (normalised to green inside), white and black the raw levels.  Writes the
+ * gains {r, g, b} (g = 1) to wb_out and, when not null, the fraction of 2x2 quads with a
+ * channel in (0.5, 1] to *highlights; both host memory (the call synchronizes the context's
+ * stream).  Bit-identical to the reference's fp32 computation, which runs on 4x4 tiles and
+ * keeps its sums in quad order. */
+GLS_API gls_status gls_auto_white_balance(gls_ctx* ctx, const gls_image_desc* raw, const float rgb_ycbcr[9],
+                                          const float scale_mul[4], float white_level, float black_level,
+                                          int bayer_pattern, float wb_out[3], float* highlights);
+
 /* ---- host colour math (demosaic_utils.cpp:25-52, 809-822; gls_linalg.hpp:545-556) ---- */
 GLS_API gls_status gls_cam_xyz_coeff(const float cam_xyz[9], float pre_mul[3], float rgb_cam[9]);
 GLS_API gls_status gls_cam_ycbcr(const float rgb_cam[9], float out[9]);

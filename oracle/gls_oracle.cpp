@@ -1406,6 +1406,160 @@ int dispatch(int prec, F&& f) {
 
 }  // namespace
 
+// ---------------------------------------------------------------------------------------
+// autoWhiteBalance (demosaic_utils.cpp:857-1026), restated in the reference's operation
+// order: 4x4 tiles of even size; per tile, over its 2x2 quads in raster order, the fp32
+// running sums of the YCbCr image (M), of the absolute deviations from the mean (D) and,
+// per luma bin of the near-white quads, of their normalised camera RGB.  Host CFA table
+// (demosaic.hpp:83-88): {red, green, blue, green2} as (x, y).
+// ---------------------------------------------------------------------------------------
+namespace awb {
+
+const int kHostBayer[4][4][2] = {
+    {{1, 0}, {0, 0}, {0, 1}, {1, 1}},  // grbg
+    {{0, 1}, {0, 0}, {1, 0}, {1, 1}},  // gbrg
+    {{0, 0}, {1, 0}, {1, 1}, {0, 1}},  // rggb
+    {{1, 1}, {1, 0}, {0, 0}, {0, 1}},  // bggr
+};
+constexpr int kBins = 128;
+
+// readQuad (demosaic_utils.cpp:836-849): {red, (green + green2) / 2, blue}
+inline void read_quad(const uint16_t* tile, int stride, int x, int y, int bayer, float q[3]) {
+    const int (*o)[2] = kHostBayer[bayer];
+    auto at = [&](int c) { return (float)tile[(size_t)(y + o[c][1]) * stride + x + o[c][0]]; };
+    q[0] = at(0);
+    q[1] = (at(1) + at(3)) / 2.0f;
+    q[2] = at(2);
+}
+
+// rgb_ycbcr * v, each row accumulated from 0 (gls_linalg.hpp:353-372)
+inline void mat_vec(const float m[9], const float v[3], float out[3]) {
+    for (int j = 0; j < 3; j++) {
+        float acc = 0;
+        for (int k = 0; k < 3; k++) acc += m[3 * j + k] * v[k];
+        out[j] = acc;
+    }
+}
+
+// The camera RGB of a quad scaled by scale_mul and clipped at 1 (its YCbCr), and whether
+// a channel sits in (0.5, 1] (demosaic_utils.cpp:861-881).
+inline bool quad_ycbcr(const uint16_t* tile, int stride, int x, int y, int bayer, const float m[9],
+                       const float smul[3], float black, float out[3]) {
+    float q[3], rgb[3];
+    read_quad(tile, stride, x, y, bayer, q);
+    bool highlights = false;
+    for (int c = 0; c < 3; c++) {
+        rgb[c] = (smul[c] * (q[c] - black)) / (float)0xffff;
+        if (rgb[c] > 1.0f) rgb[c] = 1.0f;
+        else if (rgb[c] > 0.5f) highlights = true;
+    }
+    mat_vec(m, rgb, out);
+    return highlights;
+}
+
+// Luma bin of (kBins - 1) * Y rounded half away from zero, clamped to [0, kBins - 1].  A
+// negative rounded value lands in the top bin: the reference converts it to size_t before
+// clamping, which on x86-64 wraps it to a huge value.
+inline int luma_bin(float Y) {
+    const float r = std::round((float)(kBins - 1) * Y);
+    if (r < 0.0f || r > (float)(kBins - 1)) return kBins - 1;
+    return (int)r;
+}
+
+struct TileResult {
+    float gain[3];
+    int highlights;
+};
+
+// autoWhiteBalanceKernel (demosaic_utils.cpp:851-966) over one tile of tw x th pixels.
+TileResult tile(const uint16_t* t, int stride, int tw, int th, const float m[9], const float smul[3], float white,
+                float black, int bayer, float fraction) {
+    const int qw = tw / 2, qh = th / 2;
+    int highlight_px = 0;
+    float M[3] = {0, 0, 0};
+    for (int y = 0; y < th; y += 2)
+        for (int x = 0; x < tw; x += 2) {
+            float p[3];
+            if (quad_ycbcr(t, stride, x, y, bayer, m, smul, black, p)) highlight_px++;
+            for (int c = 0; c < 3; c++) M[c] = M[c] + p[c];
+        }
+    const float n_quads = (float)th * tw / 4;
+    for (int c = 0; c < 3; c++) M[c] = M[c] / n_quads;
+
+    float D[3] = {0, 0, 0};
+    for (int y = 0; y < qh; y++)
+        for (int x = 0; x < qw; x++) {
+            float p[3];
+            quad_ycbcr(t, stride, 2 * x, 2 * y, bayer, m, smul, black, p);
+            for (int c = 0; c < 3; c++) D[c] = D[c] + std::fabs(p[c] - M[c]);
+        }
+    const float n_yuv = (float)qh * qw;
+    for (int c = 0; c < 3; c++) D[c] = D[c] / n_yuv;
+
+    float bin_sum[kBins][3] = {};
+    int bin_n[kBins] = {};
+    const float Wr = 1.5f, WCr = 1.5f;
+    int white_n = 0;
+    float YMax = 0;
+    for (int y = 0; y < qh; y++)
+        for (int x = 0; x < qw; x++) {
+            float p[3];
+            quad_ycbcr(t, stride, 2 * x, 2 * y, bayer, m, smul, black, p);
+            if (std::fabs(p[1] - (M[1] + std::copysign(D[1], M[1]))) < Wr * D[1] &&
+                std::fabs(p[2] - (WCr * M[2] + std::copysign(D[2], M[2]))) < Wr * D[2]) {
+                float q[3];
+                read_quad(t, stride, 2 * x, 2 * y, bayer, q);
+                const float Y = p[0];
+                if (Y > YMax) YMax = Y;
+                const int b = luma_bin(Y);
+                for (int c = 0; c < 3; c++) bin_sum[b][c] = bin_sum[b][c] + (q[c] - black) / white;
+                bin_n[b]++;
+                white_n++;
+            }
+        }
+    const int top = luma_bin(YMax);
+    if (top == 0) return {{1, 1, 1}, 0};
+    int n90 = 0;
+    float avg[3] = {0, 0, 0};
+    for (int i = top; i >= 0; i--) {
+        for (int c = 0; c < 3; c++) avg[c] = avg[c] + bin_sum[i][c];
+        n90 += bin_n[i];
+        if ((float)n90 > fraction * (float)white_n) break;
+    }
+    TileResult r;
+    float g[3];
+    for (int c = 0; c < 3; c++) avg[c] = avg[c] / (float)n90;
+    for (int c = 0; c < 3; c++) g[c] = YMax / avg[c];
+    const float g1 = g[1];
+    for (int c = 0; c < 3; c++) r.gain[c] = g[c] / g1;
+    r.highlights = highlight_px;
+    return r;
+}
+
+// autoWhiteBalance (demosaic_utils.cpp:976-1026): the mean of the 16 tiles' gains,
+// normalised to green, and the fraction of quads with a channel in (0.5, 1].
+void auto_white_balance(const uint16_t* raw, int w, int h, int stride, const float m[9], const float smul4[4],
+                        float white, float black, int bayer, float wb[3], float* highlights) {
+    const float s1 = smul4[1];
+    const float smul[3] = {smul4[0] / s1, smul4[1] / s1, smul4[2] / s1};
+    const int tw = 2 * ((w / 4) / 2), th = 2 * ((h / 4) / 2);
+    float g[3] = {0, 0, 0};
+    float hl = 0;
+    for (int ty = 0; ty < 4; ty++)
+        for (int tx = 0; tx < 4; tx++) {
+            const TileResult r =
+                tile(raw + (size_t)ty * th * stride + tx * tw, stride, tw, th, m, smul, white, black, bayer, 0.01f);
+            for (int c = 0; c < 3; c++) g[c] = g[c] + r.gain[c];
+            hl = hl + (float)r.highlights;
+        }
+    for (int c = 0; c < 3; c++) g[c] = g[c] / 16.0f;
+    const float g1 = g[1];
+    for (int c = 0; c < 3; c++) wb[c] = g[c] / g1;
+    if (highlights) *highlights = hl / (float)(w * h / 4);
+}
+
+}  // namespace awb
+
 extern "C" {
 
 int oracle_threads(void) { return num_threads(); }
@@ -1651,6 +1805,14 @@ long oracle_unpack_bits(const uint8_t* packed, long n_bytes, int bits, uint16_t*
         out[k] = (uint16_t)v;
     }
     return k;
+}
+
+int oracle_auto_white_balance(const uint16_t* raw, int w, int h, int stride, const float rgb_ycbcr[9],
+                               const float scale_mul[4], float white, float black, int bayer, float wb[3],
+                               float* highlights) {
+    if (w < 0 || h < 0 || stride < w || bayer < 0 || bayer > 3) return -1;
+    awb::auto_white_balance(raw, w, h, stride, rgb_ycbcr, scale_mul, white, black, bayer, wb, highlights);
+    return 0;
 }
 
 float oracle_atan2pi(float y, float x) { return glsm::atan2pi_(y, x); }

@@ -131,6 +131,12 @@ void oracle_matmul3x3(const float a[9], const float b[9], float out[9]);
 // project's extension (4 samples in 5 bytes, big-endian bit order).
 long oracle_unpack_bits(const uint8_t* packed, long n_bytes, int bits, uint16_t* out, long max_out);
 
+/* autoWhiteBalance (demosaic_utils.cpp:976-1026): raw uint16 -> wb gains {r, g, b}
+ * (green = 1) and the highlight fraction. */
+int oracle_auto_white_balance(const uint16_t* raw, int w, int h, int stride, const float rgb_ycbcr[9],
+                              const float scale_mul[4], float white, float black, int bayer, float wb[3],
+                              float* highlights);
+
 // OpenCL built-ins, exported for tests/test_clmath.py
 float oracle_atan2pi(float y, float x);
 float oracle_tanh(float x);

@@ -357,6 +357,25 @@ def unpack_bits(packed, bits):
     return out[:k]
 
 
+def auto_white_balance(raw, rgb_ycbcr, scale_mul, white, black, bayer, reference=False):
+    """autoWhiteBalance (demosaic_utils.cpp:976-1026) over a uint16 raw frame: (wb gains
+    (3,) with green 1, highlight fraction).  reference=True runs the reference's own code
+    (oracle/_ref/libref_host.so) instead of the restatement."""
+    raw = np.ascontiguousarray(raw, np.uint16)
+    h, w = raw.shape
+    wb = (ctypes.c_float * 3)()
+    hl = ctypes.c_float()
+    args = (_p(raw), w, h, w, _arr(np.ravel(rgb_ycbcr), 9), _arr(scale_mul, 4), ctypes.c_float(white),
+            ctypes.c_float(black), int(bayer), wb, ctypes.byref(hl))
+    if reference:
+        if ref_lib() is None:
+            raise FileNotFoundError(REF_PATH)
+        ref_lib().ref_auto_white_balance(*args)
+    elif lib().oracle_auto_white_balance(*args) != 0:
+        raise ValueError("autoWhiteBalance: invalid arguments")
+    return np.array(wb[:], np.float32), np.float32(hl.value)
+
+
 # ---- host colour math ----
 
 def _m9(fn, *mats):

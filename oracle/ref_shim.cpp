@@ -65,4 +65,18 @@ void ref_unpack14(const uint16_t* in_words, long n_words, uint16_t* out) {
     gls::unpack14BitsInto16Bits(out, in_words, (size_t)n_words);
 }
 
+// autoWhiteBalance over a raw uint16 frame (row stride in pixels); the reference prints
+// its result on stdout.
+void ref_auto_white_balance(const uint16_t* raw, int w, int h, int stride, const float rgb_ycbcr[9],
+                            const float scale_mul[4], float white, float black, int bayer, float wb[3],
+                            float* highlights) {
+    auto* px = reinterpret_cast<gls::luma_pixel_16*>(const_cast<uint16_t*>(raw));
+    const gls::image<gls::luma_pixel_16> img(w, h, stride, std::span<gls::luma_pixel_16>(px, (size_t)stride * h));
+    gls::Matrix<3, 3> m;
+    for (int i = 0; i < 9; i++) m[i / 3][i % 3] = rgb_ycbcr[i];
+    const gls::Vector<4> sm = {scale_mul[0], scale_mul[1], scale_mul[2], scale_mul[3]};
+    const auto r = autoWhiteBalance(img, m, sm, white, black, (BayerPattern)bayer, highlights);
+    for (int i = 0; i < 3; i++) wb[i] = r[i];
+}
+
 }  // extern "C"

@@ -2,9 +2,9 @@
 
 The reference's colour math (cam_xyz_coeff, cam_ycbcr, gls::inverse, matrix products from
 CLImage/app/src/main/cpp/demosaic_utils.cpp and src/gls_linalg.hpp) and its packed-raw
-unpack routines (src/gls_image_tiff.cpp:53-87) are compiled from the reference sources
-into oracle/_ref/libref_host.so (make -C oracle ref); this script runs them on fixed
-inputs and stores the results bit-exactly.  It also records hashes of the oracle's own
+unpack routines (src/gls_image_tiff.cpp:53-87) and autoWhiteBalance (demosaic_utils.cpp:
+976-1026) are compiled from the reference sources into oracle/_ref/libref_host.so (make -C
+oracle ref); this script runs them on fixed inputs and stores the results bit-exactly.  It also records hashes of the oracle's own
 pipeline outputs on small seeded frames, which pin the oracle across machines.
 
     make -C oracle ref && python tests/golden/make_golden.py
@@ -73,6 +73,23 @@ def unpack_fixture(ref):
     return res
 
 
+def awb_fixture():
+    """autoWhiteBalance of the reference (demosaic_utils.cpp:976-1026) on the seeded frames
+    of tests/awb_frames.py.  The reference keeps its luma-bin sums in gls::Vector<3>, whose
+    default constructor leaves the elements unset, so its histogram starts from whatever
+    the stack held; oracle/Makefile builds it with -ftrivial-auto-var-init=zero, which gives
+    the zeroed bins the code means."""
+    from tests import awb_frames
+    out = {}
+    for case in awb_frames.CASES:
+        raw, m, sm, white, black, bayer = awb_frames.make(case, orc.cam_ycbcr)
+        wb, hl = orc.auto_white_balance(raw, m, sm, white, black, bayer, reference=True)
+        out[case[0]] = {"raw_sha256": hashlib.sha256(raw.tobytes()).hexdigest(), "rgb_ycbcr": bits(m),
+                        "scale_mul": bits(sm), "white": bits([white])[0], "black": bits([black])[0],
+                        "bayer": bayer, "wb": bits(wb), "highlights": bits([hl])[0]}
+    return out
+
+
 def oracle_pins():
     pins = {}
     for name, (w, h, bayer, prec, levels) in {
@@ -99,6 +116,8 @@ def main():
     with open(os.path.join(HERE, "ref_colour.json"), "w") as f:
         json.dump(colour_fixture(ref), f, indent=1)
     np.savez_compressed(os.path.join(HERE, "ref_unpack.npz"), **unpack_fixture(ref))
+    with open(os.path.join(HERE, "ref_awb.json"), "w") as f:
+        json.dump(awb_fixture(), f, indent=1)
     with open(os.path.join(HERE, "oracle_pins.json"), "w") as f:
         json.dump(oracle_pins(), f, indent=1)
     print("golden fixtures written to", HERE)

@@ -2,7 +2,8 @@
 reference's own compiled code (tests/golden, written by make_golden.py from
 oracle/_ref), the noise-model regression meets known answers, and the stencils satisfy
 the properties the reference's algorithms imply (constant images, CFA phase shifts).
-The reference has no tests or golden vectors of its own for this path."""
+autoWhiteBalance equals the reference's compiled code on seeded frames.  The reference has
+no tests or golden vectors of its own for this path."""
 import hashlib
 import json
 import os
@@ -49,6 +50,34 @@ def test_unpack_equals_reference():
         np.testing.assert_array_equal(orc.unpack_bits(packed, nbits), fx["unpacked%d" % nbits])
 
 
+@pytest.fixture(scope="module")
+def awb_golden():
+    with open(os.path.join(GOLDEN, "ref_awb.json")) as f:
+        return json.load(f)
+
+
+def awb_inputs(case, fx):
+    """The case's frame (regenerated from its seed and checked against the fixture's hash)
+    and the fixture's stored parameters."""
+    from tests import awb_frames
+    raw = awb_frames.make(case, orc.cam_ycbcr)[0]
+    assert hashlib.sha256(raw.tobytes()).hexdigest() == fx["raw_sha256"], case[0]
+    return raw, f32(fx["rgb_ycbcr"]), f32(fx["scale_mul"]), f32([fx["white"]])[0], f32([fx["black"]])[0], fx["bayer"]
+
+
+def test_auto_white_balance_equals_reference(awb_golden):
+    """Bit for bit, including crafted frames with clipped highlights and with dark quads
+    whose negative luma bin the reference maps to the top bin (crafted_dark, crafted_mixed)."""
+    from tests import awb_frames
+    assert set(awb_golden) == {c[0] for c in awb_frames.CASES}
+    for case in awb_frames.CASES:
+        fx = awb_golden[case[0]]
+        raw, m, sm, white, black, bayer = awb_inputs(case, fx)
+        wb, hl = orc.auto_white_balance(raw, m, sm, white, black, bayer)
+        np.testing.assert_array_equal(wb.view(np.uint32), np.array(fx["wb"], np.uint32), err_msg=case[0])
+        assert int(np.float32(hl).view(np.uint32)) == fx["highlights"], case[0]
+
+
 def test_unpack_round_trip_all_depths():
     rng = np.random.default_rng(9)
     for nbits in (10, 12, 14, 16):
@@ -57,7 +86,7 @@ def test_unpack_round_trip_all_depths():
 
 
 def test_oracle_self_pins():
-    """The oracle gives the same bits on every machine (x86-64 here, aarch64 on the GPU machine)."""
+    """The oracle gives the same bits on every machine (x86-64 and aarch64)."""
     with open(os.path.join(GOLDEN, "oracle_pins.json")) as f:
         pins = json.load(f)
     for name, (w, h, bayer, prec, levels) in {
