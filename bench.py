@@ -40,6 +40,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-psnr", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--no-awb", action="store_true")
     ap.add_argument("--profile-only", action="store_true", help="a short run for ncu: no clocks, no cpu leg")
     return ap.parse_args()
 
@@ -350,6 +351,34 @@ def main():
             lb.close()
             cnn.close()
 
+    # ---- autoWhiteBalance of the first frame (its own entry point, bit-exact) ----
+    awb_line = None
+    if rank == 0 and not args.no_awb and not args.profile_only:
+        sp = frames[0][2]
+        awb_args = (gls.cam_ycbcr(np.array(sp["rgb_cam"], np.float32).reshape(3, 3)), sp["scale_mul"],
+                    sp["white_level"], sp["black_level"], cfg["bayer"])
+        for _ in range(3):
+            wb, hl = ctx.autoWhiteBalance(raws[0], *awb_args)
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record(stream)
+        for _ in range(5):
+            wb, hl = ctx.autoWhiteBalance(raws[0], *awb_args)
+        a1.record(stream)
+        torch.cuda.synchronize()
+        awb_ms = a0.elapsed_time(a1) / 5
+        awb_line = {"ms_per_frame": round(awb_ms, 4), "mpix_s": round(w * h / 1e3 / awb_ms, 1),
+                    "gains": [float(v) for v in wb], "highlights": float(hl),
+                    "note": "one call per frame, synchronous (16-byte result read back); the reference's fp32 "
+                            "sums are kept in quad order, one block per tile"}
+        if world == 1 and not args.no_cpu:
+            from oracle import oracle as orc
+            t0 = time.perf_counter()
+            owb, ohl = orc.auto_white_balance(frames[0][0], *awb_args)
+            awb_line["cpu_baseline"] = {"ms_per_frame": round((time.perf_counter() - t0) * 1e3, 1), "cores": 1,
+                                        "kind": "port"}
+            awb_line["bit_exact_vs_oracle"] = bool(np.array_equal(owb.view(np.uint32), wb.view(np.uint32))
+                                                   and np.float32(ohl).view(np.uint32) == np.float32(hl).view(np.uint32))
+
     cpu = psnr = None
     if rank == 0 and world == 1 and not args.no_cpu and not args.profile_only:
         gpu_rgb = None
@@ -385,6 +414,7 @@ def main():
             "cpu_baseline": cpu,
             "psnr_vs_fp64": psnr,
             "learned_form": learned_line,
+            "auto_white_balance": awb_line,
         }
         print(json.dumps(line), flush=True)
     conv.close()

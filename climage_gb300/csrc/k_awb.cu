@@ -12,11 +12,12 @@
 // frame's gain is the mean of the 16 tiles' gains.
 //
 // fp32 sums in a fixed order are not associative, so the kernel keeps the reference's order:
-// one block per tile; in each pass the block's other warps compute the per-quad terms of a
-// chunk in parallel while three lanes of warp 0 add up the previous chunk, one lane per
+// one block per tile; in passes 1 and 2 the block's other warps compute the per-quad terms
+// of a chunk in parallel while three lanes of warp 0 add up the previous chunk, one lane per
 // component, in quad order (the adds form the critical path: one dependent add per quad and
-// pass).  In pass 3 the selected quads of a chunk are compacted in quad order and 128
-// threads, one per bin, add their own bin's entries in that order.  Counts, the luma
+// pass).  In pass 3 the selected quads of a chunk are sorted by bin, stably (warp match
+// ranks plus per-bin offsets), and 128 threads, one per bin, add their own bin's entries in
+// quad order.  Counts, the luma
 // maximum and the highlight count are exact in any order.  The 16 tile results are combined
 // in tile order by the last block to finish (a ticket, no waiting).
 #include "gls_internal.h"
@@ -53,20 +54,32 @@ struct AwbTile {
     int highlights;
 };
 
-// readQuad (demosaic_utils.cpp:836-849)
-__device__ __forceinline__ void awb_read_quad(const AwbArgs& a, const uint16_t* tile, int qx, int qy, float q[3]) {
+// The four raw values of quad (qx, qy): red, green, blue, green2 (readQuad,
+// demosaic_utils.cpp:836-849, before its conversion).
+struct RawQuad {
+    uint16_t v[4];
+};
+
+__device__ __forceinline__ RawQuad awb_load(const AwbArgs& a, const uint16_t* tile, int qx, int qy) {
     const int(*o)[2] = c_awb_cfa[a.bayer];
     const uint16_t* p = tile + (size_t)(2 * qy) * a.stride + 2 * qx;
-    q[0] = (float)p[o[0][1] * a.stride + o[0][0]];
-    q[1] = ((float)p[o[1][1] * a.stride + o[1][0]] + (float)p[o[3][1] * a.stride + o[3][0]]) / 2.0f;
-    q[2] = (float)p[o[2][1] * a.stride + o[2][0]];
+    RawQuad r;
+#pragma unroll
+    for (int c = 0; c < 4; c++) r.v[c] = __ldg(p + o[c][1] * a.stride + o[c][0]);
+    return r;
+}
+
+// readQuad's value: {red, (green + green2) / 2, blue}
+__device__ __forceinline__ void awb_quad(const RawQuad& r, float q[3]) {
+    q[0] = (float)r.v[0];
+    q[1] = ((float)r.v[1] + (float)r.v[3]) / 2.0f;
+    q[2] = (float)r.v[2];
 }
 
 // The YCbCr of a quad (rows accumulated from 0, as gls::Matrix * gls::Vector does) and
 // whether a channel of its clipped RGB lies in (0.5, 1] (demosaic_utils.cpp:861-881).
-__device__ __forceinline__ bool awb_ycbcr(const AwbArgs& a, const uint16_t* tile, int qx, int qy, float p[3]) {
-    float q[3], rgb[3];
-    awb_read_quad(a, tile, qx, qy, q);
+__device__ __forceinline__ bool awb_ycbcr(const AwbArgs& a, const float q[3], float p[3]) {
+    float rgb[3];
     bool hl = false;
 #pragma unroll
     for (int c = 0; c < 3; c++) {
@@ -92,31 +105,52 @@ __device__ __forceinline__ int awb_bin(float Y) {
     return (int)r;
 }
 
-// acc += v[0] + ... + v[n-1], one add at a time in index order
+// acc += v[0] + ... + v[n-1], one add at a time in index order.  v holds kAwbChunk floats;
+// the next 16 are loaded while the current 16 are added (reads stay inside the buffer).
 __device__ __forceinline__ float serial_sum(float acc, const float* v, int n) {
     int i = 0;
-    for (; i + 16 <= n; i += 16) {
-        float4 x[4];
+    float4 cur[4];
 #pragma unroll
-        for (int j = 0; j < 4; j++) x[j] = reinterpret_cast<const float4*>(v + i)[j];
+    for (int j = 0; j < 4; j++) cur[j] = reinterpret_cast<const float4*>(v)[j];
+    for (; i + 16 <= n; i += 16) {
+        const int nx = min(i + 16, kAwbChunk - 16);
+        float4 nxt[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) nxt[j] = reinterpret_cast<const float4*>(v + nx)[j];
 #pragma unroll
         for (int j = 0; j < 4; j++) {
-            acc = acc + x[j].x;
-            acc = acc + x[j].y;
-            acc = acc + x[j].z;
-            acc = acc + x[j].w;
+            acc = acc + cur[j].x;
+            acc = acc + cur[j].y;
+            acc = acc + cur[j].z;
+            acc = acc + cur[j].w;
         }
+#pragma unroll
+        for (int j = 0; j < 4; j++) cur[j] = nxt[j];
     }
     for (; i < n; i++) acc = acc + v[i];
     return acc;
 }
 
+constexpr int kProducers = kAwbThreads - 32;
+constexpr int kPerProducer = (kAwbChunk + kProducers - 1) / kProducers;
+constexpr int kRounds = kAwbChunk / kAwbThreads;  // pass 3: quads per thread and chunk
+constexpr int kWarps = kAwbThreads / 32;
+
+union AwbSmem {
+    float v[2][3][kAwbChunk];  // passes 1 and 2: double-buffered per-quad terms
+    struct {
+        int off[kWarps][kAwbBins];  // per (warp, bin): count, then offset
+        float4 sorted[kAwbChunk];   // the chunk's near-white entries, by bin then quad
+    } p3;
+};
+
 // Passes 1 and 2: the quad-order fp32 sums of the three YCbCr components (MODE 0) or of
-// their absolute deviations from mean[] (MODE 1); returns the count of highlight quads
-// (MODE 0, per thread) and leaves the sums in out[] (all threads).
+// their absolute deviations from mean[] (MODE 1).  Warps 1.. compute chunk k while lanes
+// 0-2 of warp 0 add up chunk k - 1.  Returns the thread's count of highlight quads
+// (MODE 0) and leaves the sums in out[] (all threads).
 template <int MODE>
-__device__ int awb_sum_pass(const AwbArgs& a, const uint16_t* tile, int qw, int n, const float* mean,
-                            float (*s_v)[3][kAwbChunk], float* out) {
+__device__ int awb_sum_pass(const AwbArgs& a, const uint16_t* tile, int qw, int n, const float* mean, AwbSmem& sm,
+                            float* out) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nchunks = (n + kAwbChunk - 1) / kAwbChunk;
     int hl = 0;
@@ -124,24 +158,33 @@ __device__ int awb_sum_pass(const AwbArgs& a, const uint16_t* tile, int qw, int 
     for (int k = 0; k <= nchunks; k++) {
         if (warp != 0) {
             if (k < nchunks) {
-                for (int i = threadIdx.x - 32; i < kAwbChunk; i += kAwbThreads - 32) {
-                    const int q = k * kAwbChunk + i;
-                    if (q >= n) break;
-                    float p[3];
-                    const bool h = awb_ycbcr(a, tile, q % qw, q / qw, p);
-                    if (MODE == 0) {
-                        hl += h;
-                    } else {
+                RawQuad r[kPerProducer];
 #pragma unroll
-                        for (int c = 0; c < 3; c++) p[c] = fabsf(p[c] - mean[c]);
+                for (int j = 0; j < kPerProducer; j++) {  // every load first, then the arithmetic
+                    const int i = threadIdx.x - 32 + j * kProducers, q = k * kAwbChunk + i;
+                    if (i < kAwbChunk && q < n) r[j] = awb_load(a, tile, q % qw, q / qw);
+                }
+#pragma unroll
+                for (int j = 0; j < kPerProducer; j++) {
+                    const int i = threadIdx.x - 32 + j * kProducers, q = k * kAwbChunk + i;
+                    if (i < kAwbChunk && q < n) {
+                        float qv[3], p[3];
+                        awb_quad(r[j], qv);
+                        const bool h = awb_ycbcr(a, qv, p);
+                        if (MODE == 0) {
+                            hl += h;
+                        } else {
+#pragma unroll
+                            for (int c = 0; c < 3; c++) p[c] = fabsf(p[c] - mean[c]);
+                        }
+#pragma unroll
+                        for (int c = 0; c < 3; c++) sm.v[k & 1][c][i] = p[c];
                     }
-#pragma unroll
-                    for (int c = 0; c < 3; c++) s_v[k & 1][c][i] = p[c];
                 }
             }
         } else if (k > 0 && lane < 3) {
             const int base = (k - 1) * kAwbChunk;
-            acc = serial_sum(acc, s_v[(k - 1) & 1][lane], min(kAwbChunk, n - base));
+            acc = serial_sum(acc, sm.v[(k - 1) & 1][lane], min(kAwbChunk, n - base));
         }
         __syncthreads();
     }
@@ -158,19 +201,19 @@ __device__ __forceinline__ int block_sum_int(int v, int* s_red) {
     if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = v;
     __syncthreads();
     int t = 0;
-    for (int w = 0; w < kAwbThreads / 32; w++) t += s_red[w];
+    for (int w = 0; w < kWarps; w++) t += s_red[w];
     __syncthreads();
     return t;
 }
 
 __global__ void __launch_bounds__(kAwbThreads) awb_tile_kernel(AwbArgs a, AwbTile* tiles, unsigned* ticket,
                                                                float* out) {
-    __shared__ __align__(16) float s_v[2][3][kAwbChunk];
-    __shared__ __align__(16) float4 s_list[kAwbChunk];
+    __shared__ __align__(16) AwbSmem sm;
     __shared__ float s_bin[kAwbBins][3];
     __shared__ int s_bin_n[kAwbBins];
-    __shared__ int s_red[kAwbThreads / 32];
-    __shared__ float s_fmax[kAwbThreads / 32];
+    __shared__ int s_base[kAwbBins], s_count[kAwbBins];
+    __shared__ int s_red[kWarps];
+    __shared__ float s_fmax[kWarps];
     __shared__ bool s_last;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -180,71 +223,111 @@ __global__ void __launch_bounds__(kAwbThreads) awb_tile_kernel(AwbArgs a, AwbTil
 
     // pass 1: M (demosaic_utils.cpp:859-882)
     float M[3], D[3];
-    const int hl = block_sum_int(awb_sum_pass<0>(a, tile, qw, n, nullptr, s_v, M), s_red);
+    const int hl = block_sum_int(awb_sum_pass<0>(a, tile, qw, n, nullptr, sm, M), s_red);
     const float n_quads = (float)a.th * (float)a.tw / 4.0f;
     for (int c = 0; c < 3; c++) M[c] = M[c] / n_quads;
     // pass 2: D (demosaic_utils.cpp:899-906)
-    awb_sum_pass<1>(a, tile, qw, n, M, s_v, D);
+    awb_sum_pass<1>(a, tile, qw, n, M, sm, D);
     const float n_yuv = (float)qh * (float)qw;
     for (int c = 0; c < 3; c++) D[c] = D[c] / n_yuv;
 
-    // pass 3: near-white quads by luma bin (demosaic_utils.cpp:908-940)
+    // pass 3: near-white quads by luma bin (demosaic_utils.cpp:908-940).  Per chunk, warp w
+    // holds quads base + 128 w + 32 r + lane (r = 0..3), so (warp, r, lane) is quad order;
+    // the entries of a bin are placed in that order (warp offsets, then ranks over rounds),
+    // a stable sort by bin, and thread b < 128 adds bin b's entries in quad order.
     const float Wr = 1.5f, WCr = 1.5f;
     const float c1 = M[1] + copysignf(D[1], M[1]), c2 = WCr * M[2] + copysignf(D[2], M[2]);
     const float w1 = Wr * D[1], w2 = Wr * D[2];
+    const unsigned lanes_below = (1u << lane) - 1u;
     float bin_acc[3] = {0.0f, 0.0f, 0.0f};
     int bin_n = 0, white_n = 0;
     float ymax = 0.0f;
-    constexpr int kPer = kAwbChunk / kAwbThreads;  // quads per thread and chunk
-    for (int base = 0; base < n; base += kAwbChunk) {
-        float4 e[kPer];
-        int cnt = 0;
+    int* off_flat = &sm.p3.off[0][0];
+    RawQuad rq[kRounds];
 #pragma unroll
-        for (int j = 0; j < kPer; j++) {
-            const int q = base + tid * kPer + j;
+    for (int r = 0; r < kRounds; r++) {
+        const int q = warp * (kRounds * 32) + r * 32 + lane;
+        if (q < n) rq[r] = awb_load(a, tile, q % qw, q / qw);
+    }
+    for (int base = 0; base < n; base += kAwbChunk) {
+        for (int i = tid; i < kWarps * kAwbBins; i += kAwbThreads) off_flat[i] = 0;
+        int bin[kRounds];
+        float4 e[kRounds];
+#pragma unroll
+        for (int r = 0; r < kRounds; r++) {
+            bin[r] = -1;
+            const int q = base + warp * (kRounds * 32) + r * 32 + lane;
             if (q < n) {
-                float p[3];
-                const int qx = q % qw, qy = q / qw;
-                awb_ycbcr(a, tile, qx, qy, p);
+                float qv[3], p[3];
+                awb_quad(rq[r], qv);
+                awb_ycbcr(a, qv, p);
                 if (fabsf(p[1] - c1) < w1 && fabsf(p[2] - c2) < w2) {
-                    float rq[3];
-                    awb_read_quad(a, tile, qx, qy, rq);
                     const float Y = p[0];
                     ymax = Y > ymax ? Y : ymax;
-                    e[cnt++] = make_float4((rq[0] - a.black) / a.white, (rq[1] - a.black) / a.white,
-                                           (rq[2] - a.black) / a.white, __int_as_float(awb_bin(Y)));
+                    bin[r] = awb_bin(Y);
+                    e[r] = make_float4((qv[0] - a.black) / a.white, (qv[1] - a.black) / a.white,
+                                       (qv[2] - a.black) / a.white, 0.0f);
+                    white_n++;
                 }
             }
-        }
-        white_n += cnt;
-        // stable compaction: entries keep quad order
-        int incl = cnt;
-        for (int o = 1; o < 32; o <<= 1) {
-            const int v = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += v;
-        }
-        if (lane == 31) s_red[warp] = incl;
-        __syncthreads();
-        int off = incl - cnt, total = 0;
-        for (int w = 0; w < kAwbThreads / 32; w++) {
-            const int t = s_red[w];
-            if (w < warp) off += t;
-            total += t;
         }
 #pragma unroll
-        for (int j = 0; j < kPer; j++)
-            if (j < cnt) s_list[off + j] = e[j];
+        for (int r = 0; r < kRounds; r++) {  // the next chunk's quads load during the sort
+            const int q = base + kAwbChunk + warp * (kRounds * 32) + r * 32 + lane;
+            if (q < n) rq[r] = awb_load(a, tile, q % qw, q / qw);
+        }
+        __syncthreads();  // counts cleared
+        // rank of each entry among the same bin's entries of this warp, rounds in order:
+        // the lowest lane of a match group reads and advances the warp's count of the bin
+        int rank[kRounds];
+#pragma unroll
+        for (int r = 0; r < kRounds; r++) {
+            const unsigned same = __match_any_sync(0xffffffffu, bin[r]);
+            const int leader = __ffs(same) - 1;
+            int prior = 0;
+            if (bin[r] >= 0 && lane == leader) {
+                prior = sm.p3.off[warp][bin[r]];
+                sm.p3.off[warp][bin[r]] = prior + __popc(same);
+            }
+            prior = __shfl_sync(0xffffffffu, prior, leader);
+            rank[r] = prior + __popc(same & lanes_below);
+            __syncwarp();
+        }
+        __syncthreads();
+        if (tid < kAwbBins) {  // per bin: offsets over warps, then over bins
+            int total = 0;
+#pragma unroll
+            for (int w = 0; w < kWarps; w++) {
+                const int c = sm.p3.off[w][tid];
+                sm.p3.off[w][tid] = total;
+                total += c;
+            }
+            int incl = total;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int v = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += v;
+            }
+            if (lane == 31) s_red[warp] = incl;
+            s_count[tid] = total;
+            s_base[tid] = incl - total;
+        }
+        __syncthreads();
+        if (tid < kAwbBins)
+            for (int w = 0; w < (tid >> 5); w++) s_base[tid] += s_red[w];
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < kRounds; r++)
+            if (bin[r] >= 0) sm.p3.sorted[s_base[bin[r]] + sm.p3.off[warp][bin[r]] + rank[r]] = e[r];
         __syncthreads();
         if (tid < kAwbBins) {
-            for (int i = 0; i < total; i++) {
-                const float4 v = s_list[i];
-                if (__float_as_int(v.w) == tid) {
-                    bin_acc[0] = bin_acc[0] + v.x;
-                    bin_acc[1] = bin_acc[1] + v.y;
-                    bin_acc[2] = bin_acc[2] + v.z;
-                    bin_n++;
-                }
+            const int b0 = s_base[tid], b1 = b0 + s_count[tid];
+            for (int i = b0; i < b1; i++) {
+                const float4 v = sm.p3.sorted[i];
+                bin_acc[0] = bin_acc[0] + v.x;
+                bin_acc[1] = bin_acc[1] + v.y;
+                bin_acc[2] = bin_acc[2] + v.z;
             }
+            bin_n += b1 - b0;
         }
         __syncthreads();
     }
@@ -263,7 +346,7 @@ __global__ void __launch_bounds__(kAwbThreads) awb_tile_kernel(AwbArgs a, AwbTil
     // the tile's gain (demosaic_utils.cpp:942-965)
     if (tid == 0) {
         float YMax = 0.0f;
-        for (int w = 0; w < kAwbThreads / 32; w++) YMax = s_fmax[w] > YMax ? s_fmax[w] : YMax;
+        for (int w = 0; w < kWarps; w++) YMax = s_fmax[w] > YMax ? s_fmax[w] : YMax;
         AwbTile r;
         const int top = awb_bin(YMax);
         if (top == 0) {
