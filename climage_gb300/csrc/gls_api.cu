@@ -213,6 +213,7 @@ const char* gls_status_string(gls_status s) {
         case GLS_ERR_OUT_OF_MEMORY: return "out of memory";
         case GLS_ERR_TIMEOUT: return "timeout";
         case GLS_ERR_FORMAT: return "unsupported pixel format";
+        case GLS_ERR_BAD_STREAM: return "malformed compressed stream";
     }
     return "unknown status";
 }

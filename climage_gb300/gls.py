@@ -18,10 +18,11 @@ LIB_PATH = os.path.join(HERE, "libgls_cuda.so")
 
 GLS_OK = 0
 GLS_ERR_INVALID_SIZE = 2
+GLS_ERR_BAD_STREAM = 8
 # image size limit of Context.guidedFilterNoAlloc (gls_cuda.h)
 GUIDED_FILTER_NOALLOC_MAX_PIXELS = 116490
 STATUS = {0: "ok", 1: "invalid argument", 2: "invalid size", 3: "unsupported", 4: "CUDA error",
-          5: "out of memory", 6: "timeout", 7: "unsupported pixel format"}
+          5: "out of memory", 6: "timeout", 7: "unsupported pixel format", 8: "malformed compressed stream"}
 
 R16_UNORM, R_F32, R_F16, RGBA_F32, RGBA_F16, RGBA8_UNORM, RGB8_UNORM = range(7)
 GRBG, GBRG, RGGB, BGGR = range(4)
@@ -117,6 +118,8 @@ SIGNATURES = [
     ("gls_denoise_raw_rgba", _I, [_P, _D, _FP, _D]),
     ("gls_unpack_raw_bits", _I, [_P, _P, ctypes.c_size_t, _I, _P, ctypes.c_size_t]),
     ("gls_auto_white_balance", _I, [_P, _D, _FP, _FP, _F, _F, _I, _FP, _FP]),
+    ("gls_dng_decode_lossless_jpeg", _I, [_P, _P, ctypes.c_size_t, _I, ctypes.POINTER(ctypes.c_uint64),
+                                          ctypes.POINTER(ctypes.c_uint64), _I, _I, _D]),
     ("gls_selftest", _I, [_P, ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)]),
     ("gls_cam_xyz_coeff", _I, [_FP, _FP, _FP]),
     ("gls_cam_ycbcr", _I, [_FP, _FP]),
@@ -308,6 +311,18 @@ class Context:
                                                     farr(scale_mul, 4), float(white), float(black), int(bayer), wb,
                                                     ctypes.byref(hl)), "autoWhiteBalance")
         return np.array(wb[:], np.float32), np.float32(hl.value)
+
+    def decodeLosslessJPEG(self, data, offsets, sizes, tile_width, tile_height, out):
+        """Lossless-JPEG tiles (or one strip) of a DNG image: data is a host uint8 array (or
+        bytes) holding the streams at offsets/sizes; out is the (H, W) uint16 device image."""
+        buf = np.ascontiguousarray(np.frombuffer(data, np.uint8) if isinstance(data, (bytes, bytearray))
+                                   else data, np.uint8)
+        n = len(offsets)
+        offs = (ctypes.c_uint64 * n)(*[int(o) for o in offsets])
+        lens = (ctypes.c_uint64 * n)(*[int(v) for v in sizes])
+        self.check(self._lib.gls_dng_decode_lossless_jpeg(self.handle, ctypes.c_void_p(buf.ctypes.data), buf.size, n,
+                                                          offs, lens, int(tile_width), int(tile_height), desc(out)),
+                   "decodeLosslessJPEG")
 
     def interpolateGreen(self, scaled, green, bayer, luma_variance):
         self.check(self._lib.gls_interpolate_green(self.handle, desc(scaled), desc(green), bayer, float(luma_variance)),

@@ -37,6 +37,7 @@ typedef enum {
     GLS_ERR_OUT_OF_MEMORY = 5,
     GLS_ERR_TIMEOUT = 6,
     GLS_ERR_FORMAT = 7,
+    GLS_ERR_BAD_STREAM = 8, /* a compressed stream the reference decoder rejects */
 } gls_status;
 
 /* Pixel formats (gls_cl_image.hpp:232-292 maps the same pixel types to OpenCL formats). */
@@ -225,6 +226,19 @@ GLS_API gls_status gls_selftest(gls_ctx* ctx, uint64_t n, uint64_t seed, uint64_
 GLS_API gls_status gls_auto_white_balance(gls_ctx* ctx, const gls_image_desc* raw, const float rgb_ycbcr[9],
                                           const float scale_mul[4], float white_level, float black_level,
                                           int bayer_pattern, float wb_out[3], float* highlights);
+
+/* DecodeLosslessJPEG (src/gls_dng_lossless_jpeg.cpp:3253-3275) over the tiles or the strip of
+ * a DNG image, as the DNG reader calls it (src/gls_image_tiff.cpp:369-440): data is host
+ * memory holding the n_streams lossless-JPEG streams (stream i at offsets[i], sizes[i] bytes:
+ * TileOffsets/TileByteCounts, or one StripOffsets/StripByteCounts entry); each stream decodes
+ * to tile_width x tile_height samples (for a strip: the image size), placed at tile
+ * (i mod tiles_across, i div tiles_across), tiles_across = ceil(out->width / tile_width), and
+ * clipped at the image border.  out is the R16_UNORM device image.  The span of data that
+ * holds the streams is copied to the device once; the call synchronizes the context's
+ * stream.  GLS_ERR_BAD_STREAM for a stream the reference decoder rejects. */
+GLS_API gls_status gls_dng_decode_lossless_jpeg(gls_ctx* ctx, const uint8_t* data, size_t data_size, int n_streams,
+                                                const uint64_t* offsets, const uint64_t* sizes, int tile_width,
+                                                int tile_height, const gls_image_desc* out);
 
 /* ---- host colour math (demosaic_utils.cpp:25-52, 809-822; gls_linalg.hpp:545-556) ---- */
 GLS_API gls_status gls_cam_xyz_coeff(const float cam_xyz[9], float pre_mul[3], float rgb_cam[9]);

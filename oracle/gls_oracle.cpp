@@ -1560,6 +1560,513 @@ void auto_white_balance(const uint16_t* raw, int w, int h, int stride, const flo
 
 }  // namespace awb
 
+// ---------------------------------------------------------------------------------------
+// Lossless JPEG (ITU-T T.81 process 14, SOF3) as DNG stores raw tiles and strips: the
+// decoder restates DecodeLosslessJPEG (src/gls_dng_lossless_jpeg.cpp:540-2142) -- marker
+// parsing, Huffman decoding with its 8-bit lookup and its rules for invalid codes (17 bits
+// consumed, category 0) and category 16 (-32768, no extra bits), predictors 0-7, restart
+// intervals (bits dropped to the byte boundary, predictors reset); the encoder is test
+// infrastructure of its own (any predictor, optional restart interval, length-limited
+// Huffman tables built from the symbol counts) for streams the reference's encoder, which
+// always writes predictor 1 without restarts, does not produce.
+// ---------------------------------------------------------------------------------------
+namespace lj92 {
+
+struct Table {
+    uint8_t bits[17] = {};
+    uint8_t val[256] = {};
+    int mincode[17] = {}, maxcode[18] = {}, valptr[17] = {};
+    int look_n[256] = {}, look_v[256] = {};
+    bool present = false;
+};
+
+// Figures C.1, C.2 and F.15 of T.81: canonical codes, decoding bounds, 8-bit lookup
+void derive(Table& t) {
+    int size[257], code[257], n = 0;
+    for (int l = 1; l <= 16; l++)
+        for (int i = 0; i < t.bits[l]; i++) size[n++] = l;
+    size[n] = 0;
+    int c = 0, si = size[0], p = 0;
+    while (size[p]) {
+        while (size[p] == si) code[p++] = c++;
+        c <<= 1;
+        si++;
+    }
+    p = 0;
+    for (int l = 1; l <= 16; l++) {
+        if (t.bits[l]) {
+            t.valptr[l] = p;
+            t.mincode[l] = code[p];
+            p += t.bits[l];
+            t.maxcode[l] = code[p - 1];
+        } else {
+            t.maxcode[l] = -1;
+        }
+    }
+    t.maxcode[17] = 0xFFFFF;
+    for (int k = 0; k < 256; k++) t.look_n[k] = 0;
+    for (int q = 0; q < n; q++)
+        if (size[q] <= 8) {
+            const int lo = code[q] << (8 - size[q]), hi = lo | ((1 << (8 - size[q])) - 1);
+            for (int k = lo; k <= hi; k++) {
+                t.look_n[k] = size[q];
+                t.look_v[k] = t.val[q];
+            }
+        }
+}
+
+// The bit reader of the reference (FillBitBuffer, gls_dng_lossless_jpeg.cpp:1315-1353):
+// FF 00 is a data byte FF; FF followed by anything else is a marker, at which the reader
+// steps back and supplies zero bytes; past the end of the buffer every byte reads as FF.
+struct Reader {
+    const uint8_t* d;
+    size_t n, pos;
+    uint64_t buf = 0;
+    int left = 0;
+    int get() { return pos < n ? d[pos++] : 0xFF; }
+    void unget() {
+        if (pos == 0) throw 1;
+        pos--;
+    }
+    void fill(int need) {
+        while (left < 25) {
+            int c = get();
+            if (c == 0xFF) {
+                const int c2 = get();
+                if (c2 != 0) {
+                    unget();
+                    unget();
+                    if (left >= need) break;
+                    c = 0;
+                }
+            }
+            buf = (buf << 8) | (uint64_t)c;
+            left += 8;
+        }
+    }
+    int show8() {
+        if (left < 8) fill(8);
+        return (int)((buf >> (left - 8)) & 0xFF);
+    }
+    int bits(int k) {
+        if (left < k) fill(k);
+        left -= k;
+        return (int)((buf >> left) & (0xFFFFu >> (16 - k)));
+    }
+    int bit() {
+        if (!left) fill(1);
+        left--;
+        return (int)((buf >> left) & 1);
+    }
+};
+
+int huff_decode(Reader& r, const Table& t) {
+    int code = r.show8();
+    if (t.look_n[code]) {
+        r.left -= t.look_n[code];
+        return t.look_v[code];
+    }
+    r.left -= 8;
+    int l = 8;
+    while (code > t.maxcode[l]) {
+        code = (code << 1) | r.bit();
+        l++;
+    }
+    if (l > 16) return 0;
+    return t.val[t.valptr[l] + (code - t.mincode[l])];
+}
+
+int diff(Reader& r, const Table& t) {
+    const int s = huff_decode(r, t);
+    if (!s) return 0;
+    if (s == 16) return -32768;
+    if (s > 16) throw 1;
+    int x = r.bits(s);
+    if (x < (0x8000 >> (16 - s))) x += (-1 << s) + 1;
+    return x;
+}
+
+struct Header {
+    int precision = 0, width = 0, height = 0, ncomp = 0, ns = 0, ss = 0, pt = 0, restart = 0;
+    int comp_id[4] = {}, scan_table[4] = {};
+    size_t scan_pos = 0;
+    Table tab[4];
+};
+
+struct Bytes {
+    const uint8_t* d;
+    size_t n, pos = 0;
+    int get() {
+        if (pos >= n) throw 1;
+        return d[pos++];
+    }
+    int get2() {
+        const int a = get();
+        return (a << 8) | get();
+    }
+    void skip(size_t k) {
+        if (pos + k >= n) throw 1;
+        pos += k;
+    }
+    int marker() {
+        int c;
+        do {
+            do c = get(); while (c != 0xFF);
+            do c = get(); while (c == 0xFF);
+        } while (c == 0);
+        return c;
+    }
+};
+
+// the marker segments up to the next frame, scan or image marker (ProcessTables)
+int tables(Bytes& b, Header& h) {
+    for (;;) {
+        const int c = b.marker();
+        if ((c >= 0xC0 && c <= 0xCF && c != 0xC4 && c != 0xCC) || c == 0xD8 || c == 0xD9 || c == 0xDA) return c;
+        if (c == 0xC4) {  // DHT
+            int len = b.get2() - 2;
+            while (len > 0) {
+                const int idx = b.get();
+                if (idx < 0 || idx >= 4) throw 1;
+                Table& t = h.tab[idx];
+                t.present = true;
+                int count = 0;
+                t.bits[0] = 0;
+                for (int i = 1; i <= 16; i++) count += (t.bits[i] = (uint8_t)b.get());
+                if (count > 256) throw 1;
+                for (int j = 0; j < count; j++) t.val[j] = (uint8_t)b.get();
+                len -= 1 + 16 + count;
+            }
+        } else if (c == 0xDB || (c >= 0xD0 && c <= 0xD7) || c == 0x01) {
+        } else if (c == 0xDD) {  // DRI
+            if (b.get2() != 4) throw 1;
+            h.restart = b.get2();
+        } else {
+            const int len = b.get2() - 2;
+            b.skip((size_t)len);
+        }
+    }
+}
+
+Header parse(const uint8_t* d, size_t n) {
+    Header h;
+    Bytes b{d, n};
+    if (b.get() != 0xFF || b.get() != 0xD8) throw 1;
+    int c = tables(b, h);
+    if (c != 0xC0 && c != 0xC1 && c != 0xC3) throw 1;
+    const int len = b.get2();
+    h.precision = b.get();
+    h.height = b.get2();
+    h.width = b.get2();
+    h.ncomp = b.get();
+    if (h.height <= 0 || h.width <= 0 || h.ncomp <= 0 || h.precision < 2 || h.precision > 16) throw 1;
+    if (len != h.ncomp * 3 + 8) throw 1;
+    int sampling[256];
+    for (int i = 0; i < h.ncomp; i++) {
+        const int id = b.get(), hv = b.get();
+        b.get();
+        if (i < 4) h.comp_id[i] = id;
+        sampling[i] = hv;
+    }
+    for (int i = 0; i < h.ncomp; i++)
+        if (sampling[i] != 0x11) throw 1;
+    c = tables(b, h);
+    if (c != 0xDA) throw 1;
+    const int slen = b.get2() - 3;
+    h.ns = b.get();
+    if (slen != h.ns * 2 + 3 || h.ns < 1 || h.ns > 4) throw 1;
+    for (int i = 0; i < h.ns; i++) {
+        const int cc = b.get(), tt = b.get();
+        int ci = 0;
+        while (ci < h.ncomp && ci < 4 && h.comp_id[ci] != cc) ci++;
+        if (ci >= h.ncomp || ci >= 4) throw 1;
+        h.scan_table[i] = (tt >> 4) & 15;
+    }
+    h.ss = b.get();
+    b.get();
+    h.pt = b.get() & 0x0F;
+    for (int i = 0; i < h.ns; i++) {
+        const int t = h.scan_table[i];
+        if (t > 3 || !h.tab[t].present) throw 1;
+        derive(h.tab[t]);
+    }
+    h.scan_pos = b.pos;
+    return h;
+}
+
+int predict(int ss, int left, int upper, int diag) {
+    switch (ss) {
+        case 0: return 0;
+        case 1: return left;
+        case 2: return upper;
+        case 3: return diag;
+        case 4: return left + upper - diag;
+        case 5: return left + ((upper - diag) >> 1);
+        case 6: return upper + ((left - diag) >> 1);
+        case 7: return (left + upper) >> 1;
+    }
+    throw 1;
+}
+
+// DecodeImage: samples row by row, components interleaved; returns the sample count
+long decode(const uint8_t* d, size_t n, uint16_t* out, long max_out, int info[8]) {
+    Header h = parse(d, n);
+    const int W = h.width, H = h.height, C = h.ns;
+    const long total = (long)W * H * C;
+    if (info) {
+        info[0] = W, info[1] = H, info[2] = C, info[3] = h.precision;
+        info[4] = h.ss, info[5] = h.pt, info[6] = h.restart, info[7] = h.ncomp;
+    }
+    if (total > max_out) return -2;
+    Reader r{d, n, h.scan_pos};
+    const int rows_per_restart = h.restart / W;
+    int to_go = rows_per_restart, next_rst = 0;
+    std::vector<uint16_t> prev((size_t)W * C), cur((size_t)W * C);
+    auto first_row = [&](std::vector<uint16_t>& row) {
+        for (int k = 0; k < C; k++)
+            row[k] = (uint16_t)(diff(r, h.tab[h.scan_table[k]]) + (1 << (h.precision - h.pt - 1)));
+        for (int x = 1; x < W; x++)
+            for (int k = 0; k < C; k++)
+                row[(size_t)x * C + k] = (uint16_t)(diff(r, h.tab[h.scan_table[k]]) + row[(size_t)(x - 1) * C + k]);
+        if (rows_per_restart) to_go--;
+    };
+    first_row(prev);
+    std::copy(prev.begin(), prev.end(), out);
+    for (int y = 1; y < H; y++) {
+        if (rows_per_restart) {
+            if (to_go == 0) {  // ProcessRestart: drop the buffered bits, find RSTn
+                r.pos -= r.left / 8;
+                r.left = 0;
+                r.buf = 0;
+                int c;
+                do {
+                    do {
+                        if (r.pos >= r.n) throw 1;
+                        c = r.get();
+                    } while (c != 0xFF);
+                    do {
+                        if (r.pos >= r.n) throw 1;
+                        c = r.get();
+                    } while (c == 0xFF);
+                } while (c == 0);
+                if (c != 0xD0 + next_rst) throw 1;
+                next_rst = (next_rst + 1) & 7;
+                to_go = rows_per_restart;
+                first_row(cur);
+                std::copy(cur.begin(), cur.end(), out + (size_t)y * W * C);
+                std::swap(prev, cur);
+                continue;
+            }
+            to_go--;
+        }
+        for (int k = 0; k < C; k++) cur[k] = (uint16_t)(diff(r, h.tab[h.scan_table[k]]) + prev[k]);
+        for (int x = 1; x < W; x++)
+            for (int k = 0; k < C; k++) {
+                const size_t i = (size_t)x * C + k;
+                const int p = predict(h.ss, cur[i - C], prev[i], prev[i - C]);
+                cur[i] = (uint16_t)(diff(r, h.tab[h.scan_table[k]]) + p);
+            }
+        std::copy(cur.begin(), cur.end(), out + (size_t)y * W * C);
+        std::swap(prev, cur);
+    }
+    return total;
+}
+
+// ---- test encoder ----
+struct Writer {
+    std::vector<uint8_t> out;
+    uint64_t acc = 0;
+    int nacc = 0;
+    void put(int code, int len) {
+        for (int i = len - 1; i >= 0; i--) {
+            acc = (acc << 1) | ((code >> i) & 1);
+            if (++nacc == 8) {
+                const uint8_t b = (uint8_t)acc;
+                out.push_back(b);
+                if (b == 0xFF) out.push_back(0);
+                acc = 0;
+                nacc = 0;
+            }
+        }
+    }
+    void align() {  // pad with 1 bits
+        while (nacc) put(1, 1);
+    }
+};
+
+int category(int d) {
+    int a = d < 0 ? -d : d, s = 0;
+    while (a) {
+        s++;
+        a >>= 1;
+    }
+    return s;
+}
+
+// code lengths <= 16 for the used categories: Huffman lengths, then Annex K.3's
+// adjustment; a reserved symbol of count 1 keeps the all-ones code out of use
+void lengths(const long freq[17], uint8_t bits[17], uint8_t val[256], int* nval) {
+    std::vector<std::pair<long, int>> sym;
+    for (int s = 0; s <= 16; s++)
+        if (freq[s]) sym.push_back({freq[s], s});
+    sym.push_back({1, 256});
+    const int n = (int)sym.size();
+    std::vector<long> w(2 * n);
+    std::vector<int> parent(2 * n, -1);
+    std::vector<int> alive;
+    for (int i = 0; i < n; i++) {
+        w[i] = sym[i].first;
+        alive.push_back(i);
+    }
+    int next = n;
+    while (alive.size() > 1) {
+        std::sort(alive.begin(), alive.end(), [&](int a, int b) { return w[a] != w[b] ? w[a] > w[b] : a > b; });
+        const int a = alive.back();
+        alive.pop_back();
+        const int b = alive.back();
+        alive.pop_back();
+        w[next] = w[a] + w[b];
+        parent[a] = parent[b] = next;
+        alive.push_back(next++);
+    }
+    int count[40] = {};
+    std::vector<int> len(n);
+    for (int i = 0; i < n; i++) {
+        int l = 0;
+        for (int p = i; parent[p] >= 0; p = parent[p]) l++;
+        len[i] = n == 1 ? 1 : l;
+        count[len[i]]++;
+    }
+    for (int l = 39; l > 16; l--)  // K.3: move pairs up
+        while (count[l] > 0) {
+            int j = l - 2;
+            while (count[j] == 0) j--;
+            count[l] -= 2;
+            count[l - 1]++;
+            count[j + 1] += 2;
+            count[j]--;
+        }
+    int l = 16;
+    while (count[l] == 0) l--;
+    count[l]--;  // drop the reserved symbol (one of the longest codes)
+    std::vector<int> order(n);
+    for (int i = 0; i < n; i++) order[i] = i;
+    std::sort(order.begin(), order.end(), [&](int a, int b) {
+        const bool ra = sym[a].second == 256, rb = sym[b].second == 256;
+        if (ra != rb) return rb;
+        return sym[a].first != sym[b].first ? sym[a].first > sym[b].first : sym[a].second < sym[b].second;
+    });
+    int k = 0;
+    bits[0] = 0;
+    for (int q = 1; q <= 16; q++) {
+        bits[q] = (uint8_t)count[q];
+        for (int m = 0; m < count[q]; m++, k++) val[k] = (uint8_t)sym[order[k]].second;
+    }
+    *nval = k;
+}
+
+long encode(const uint16_t* src, int rows, int cols, int comps, int precision, int ss, int restart_rows,
+            uint8_t* out, long cap) {
+    if (comps < 1 || comps > 4 || ss < 1 || ss > 7 || precision < 2 || precision > 16) return -1;
+    auto sample = [&](int y, int x, int k) { return (int)src[((size_t)y * cols + x) * comps + k]; };
+    // the differences, as the decoder will predict them
+    std::vector<int> dif((size_t)rows * cols * comps);
+    for (int y = 0; y < rows; y++) {
+        const bool first = y == 0 || (restart_rows && y % restart_rows == 0);
+        for (int x = 0; x < cols; x++)
+            for (int k = 0; k < comps; k++) {
+                int p;
+                if (first) p = x == 0 ? 1 << (precision - 1) : sample(y, x - 1, k);
+                else if (x == 0) p = sample(y - 1, 0, k);
+                else p = predict(ss, sample(y, x - 1, k), sample(y - 1, x, k), sample(y - 1, x - 1, k));
+                int d = (sample(y, x, k) - p) & 0xFFFF;
+                if (d >= 0x8000) d -= 0x10000;
+                dif[((size_t)y * cols + x) * comps + k] = d;
+            }
+    }
+    long freq[4][17] = {};
+    for (size_t i = 0; i < dif.size(); i++) freq[i % comps][category(dif[i]) > 16 ? 16 : category(dif[i])]++;
+    uint8_t bits[4][17], val[4][256];
+    int nval[4], code[4][17] = {}, size[4][17] = {};
+    for (int k = 0; k < comps; k++) {
+        lengths(freq[k], bits[k], val[k], &nval[k]);
+        int c = 0, p = 0;
+        for (int l = 1; l <= 16; l++) {
+            for (int m = 0; m < bits[k][l]; m++, p++) {
+                code[k][val[k][p]] = c++;
+                size[k][val[k][p]] = l;
+            }
+            c <<= 1;
+        }
+    }
+    Writer w;
+    auto put2 = [&](int v) {
+        w.out.push_back((uint8_t)(v >> 8));
+        w.out.push_back((uint8_t)v);
+    };
+    w.out = {0xFF, 0xD8};
+    for (int k = 0; k < comps; k++) {
+        w.out.push_back(0xFF);
+        w.out.push_back(0xC4);
+        put2(2 + 1 + 16 + nval[k]);
+        w.out.push_back((uint8_t)k);
+        for (int l = 1; l <= 16; l++) w.out.push_back(bits[k][l]);
+        for (int m = 0; m < nval[k]; m++) w.out.push_back(val[k][m]);
+    }
+    if (restart_rows) {
+        w.out.push_back(0xFF);
+        w.out.push_back(0xDD);
+        put2(4);
+        put2(restart_rows * cols);
+    }
+    w.out.push_back(0xFF);
+    w.out.push_back(0xC3);
+    put2(8 + 3 * comps);
+    w.out.push_back((uint8_t)precision);
+    put2(rows);
+    put2(cols);
+    w.out.push_back((uint8_t)comps);
+    for (int k = 0; k < comps; k++) {
+        w.out.push_back((uint8_t)k);
+        w.out.push_back(0x11);
+        w.out.push_back(0);
+    }
+    w.out.push_back(0xFF);
+    w.out.push_back(0xDA);
+    put2(6 + 2 * comps);
+    w.out.push_back((uint8_t)comps);
+    for (int k = 0; k < comps; k++) {
+        w.out.push_back((uint8_t)k);
+        w.out.push_back((uint8_t)(k << 4));
+    }
+    w.out.push_back((uint8_t)ss);
+    w.out.push_back(0);
+    w.out.push_back(0);
+    int rst = 0;
+    for (int y = 0; y < rows; y++) {
+        if (restart_rows && y > 0 && y % restart_rows == 0) {
+            w.align();
+            w.out.push_back(0xFF);
+            w.out.push_back((uint8_t)(0xD0 + (rst++ & 7)));
+        }
+        for (int x = 0; x < cols; x++)
+            for (int k = 0; k < comps; k++) {
+                const int d = dif[((size_t)y * cols + x) * comps + k];
+                const int s = category(d) > 16 ? 16 : category(d);
+                w.put(code[k][s], size[k][s]);
+                if (s && s < 16) w.put(d < 0 ? d + (1 << s) - 1 : d, s);
+            }
+    }
+    w.align();
+    w.out.push_back(0xFF);
+    w.out.push_back(0xD9);
+    if ((long)w.out.size() > cap) return -2;
+    std::copy(w.out.begin(), w.out.end(), out);
+    return (long)w.out.size();
+}
+
+}  // namespace lj92
+
 extern "C" {
 
 int oracle_threads(void) { return num_threads(); }
@@ -1813,6 +2320,19 @@ int oracle_auto_white_balance(const uint16_t* raw, int w, int h, int stride, con
     if (w < 0 || h < 0 || stride < w || bayer < 0 || bayer > 3) return -1;
     awb::auto_white_balance(raw, w, h, stride, rgb_ycbcr, scale_mul, white, black, bayer, wb, highlights);
     return 0;
+}
+
+long oracle_lj92_decode(const uint8_t* data, long size, uint16_t* out, long max_out, int info[8]) {
+    try {
+        return lj92::decode(data, (size_t)size, out, max_out, info);
+    } catch (...) {
+        return -1;
+    }
+}
+
+long oracle_lj92_encode(const uint16_t* src, int rows, int cols, int comps, int precision, int predictor,
+                        int restart_rows, uint8_t* out, long cap) {
+    return lj92::encode(src, rows, cols, comps, precision, predictor, restart_rows, out, cap);
 }
 
 float oracle_atan2pi(float y, float x) { return glsm::atan2pi_(y, x); }

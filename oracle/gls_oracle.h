@@ -131,6 +131,15 @@ void oracle_matmul3x3(const float a[9], const float b[9], float out[9]);
 // project's extension (4 samples in 5 bytes, big-endian bit order).
 long oracle_unpack_bits(const uint8_t* packed, long n_bytes, int bits, uint16_t* out, long max_out);
 
+/* DecodeLosslessJPEG (src/gls_dng_lossless_jpeg.cpp:3253-3275): one stream -> its samples
+ * (rows x cols x components); info = {width, height, components, precision, predictor,
+ * point transform, restart interval, frame components}.  Returns the sample count, -1 for a
+ * stream the reference rejects, -2 when max_out is too small. */
+long oracle_lj92_decode(const uint8_t* data, long size, uint16_t* out, long max_out, int info[8]);
+/* Test encoder: any predictor 1-7, restart every restart_rows rows (0: none). */
+long oracle_lj92_encode(const uint16_t* src, int rows, int cols, int comps, int precision, int predictor,
+                        int restart_rows, uint8_t* out, long cap);
+
 /* autoWhiteBalance (demosaic_utils.cpp:976-1026): raw uint16 -> wb gains {r, g, b}
  * (green = 1) and the highlight fraction. */
 int oracle_auto_white_balance(const uint16_t* raw, int w, int h, int stride, const float rgb_ycbcr[9],

@@ -376,6 +376,60 @@ def auto_white_balance(raw, rgb_ycbcr, scale_mul, white, black, bayer, reference
     return np.array(wb[:], np.float32), np.float32(hl.value)
 
 
+def lj92_decode(stream, reference=False):
+    """A lossless-JPEG stream (bytes) -> (samples uint16 (height, width * components), info
+    dict); reference=True runs the reference's DecodeLosslessJPEG (oracle/_ref)."""
+    b = np.frombuffer(bytes(stream), np.uint8)
+    info = (ctypes.c_int * 8)()
+    if reference:
+        if ref_lib() is None:
+            raise FileNotFoundError(REF_PATH)
+        fn = ref_lib().ref_lj92_decode
+        fn.restype = ctypes.c_long
+        probe = lib().oracle_lj92_decode
+        probe.restype = ctypes.c_long
+        probe(_p(b), b.size, None, 0, info)  # header only: the geometry
+        cap = max(info[0] * info[1] * info[2], 1)
+        out = np.zeros(cap, np.uint16)
+        n = fn(_p(b), ctypes.c_long(b.size), _p(out), ctypes.c_long(cap))
+    else:
+        fn = lib().oracle_lj92_decode
+        fn.restype = ctypes.c_long
+        fn(_p(b), b.size, None, 0, info)
+        cap = max(info[0] * info[1] * info[2], 1)
+        out = np.zeros(cap, np.uint16)
+        n = fn(_p(b), ctypes.c_long(b.size), _p(out), ctypes.c_long(cap), info)
+    if n < 0:
+        raise ValueError("lossless JPEG stream rejected (%d)" % n)
+    keys = ("width", "height", "components", "precision", "predictor", "point_transform", "restart_interval",
+            "frame_components")
+    meta = dict(zip(keys, info[:8]))
+    return out[:n].reshape(meta["height"], meta["width"] * meta["components"]), meta
+
+
+def lj92_encode(samples, components, precision, predictor=1, restart_rows=0, reference=False):
+    """(height, width * components) uint16 samples -> lossless-JPEG bytes.  reference=True
+    uses the reference's EncodeLosslessJPEG (predictor 1, no restarts)."""
+    s = np.ascontiguousarray(samples, np.uint16)
+    rows, n = s.shape
+    cols = n // components
+    cap = s.size * 4 + 4096
+    out = np.zeros(cap, np.uint8)
+    if reference:
+        if predictor != 1 or restart_rows:
+            raise ValueError("the reference encoder writes predictor 1 without restarts")
+        fn = ref_lib().ref_lj92_encode
+        fn.restype = ctypes.c_long
+        k = fn(_p(s), rows, cols, components, precision, _p(out), ctypes.c_long(cap))
+    else:
+        fn = lib().oracle_lj92_encode
+        fn.restype = ctypes.c_long
+        k = fn(_p(s), rows, cols, components, precision, predictor, restart_rows, _p(out), ctypes.c_long(cap))
+    if k < 0:
+        raise ValueError("encoding failed (%d)" % k)
+    return out[:k].tobytes()
+
+
 # ---- host colour math ----
 
 def _m9(fn, *mats):

@@ -4,6 +4,7 @@
 // raw unpack; never shipped, never built on a machine without the reference sources.
 #include <cstdint>
 #include <cstring>
+#include <vector>
 
 #include "demosaic.hpp"
 
@@ -77,6 +78,38 @@ void ref_auto_white_balance(const uint16_t* raw, int w, int h, int stride, const
     const gls::Vector<4> sm = {scale_mul[0], scale_mul[1], scale_mul[2], scale_mul[3]};
     const auto r = autoWhiteBalance(img, m, sm, white, black, (BayerPattern)bayer, highlights);
     for (int i = 0; i < 3; i++) wb[i] = r[i];
+}
+
+// DecodeLosslessJPEG (gls_dng_lossless_jpeg.cpp:3253-3275) over one stream: writes the
+// decoded 16-bit samples (at most max_samples) and returns their count, -1 when the
+// reference rejects the stream, -2 when out is too small.
+long ref_lj92_decode(const uint8_t* data, long size, uint16_t* out, long max_samples) {
+    try {
+        std::vector<uint8_t> copy(data, data + size);
+        gls::dng_stream stream(copy.data(), copy.size());
+        gls::dng_spooler spooler;
+        gls::DecodeLosslessJPEG(stream, spooler, 0, 0xFFFFFFFFu, false, (uint64_t)size);
+        const long n = (long)(spooler.size() / 2);
+        if (n > max_samples) return -2;
+        memcpy(out, spooler.data(), n * 2);
+        return n;
+    } catch (...) {
+        return -1;
+    }
+}
+
+// EncodeLosslessJPEG (gls_dng_lossless_jpeg.cpp:3280-3287): predictor 1, one Huffman table
+// per channel.  Returns the stream's length, or -1.
+long ref_lj92_encode(const uint16_t* src, int rows, int cols, int channels, int bit_depth, uint8_t* out,
+                     long capacity) {
+    try {
+        gls::dng_stream stream(out, (size_t)capacity);
+        gls::EncodeLosslessJPEG(src, (uint32_t)rows, (uint32_t)cols, (uint32_t)channels, (uint32_t)bit_depth,
+                                cols * channels, channels, stream);
+        return (long)stream.Position();
+    } catch (...) {
+        return -1;
+    }
 }
 
 }  // extern "C"

@@ -3,8 +3,9 @@
 The reference's colour math (cam_xyz_coeff, cam_ycbcr, gls::inverse, matrix products from
 CLImage/app/src/main/cpp/demosaic_utils.cpp and src/gls_linalg.hpp) and its packed-raw
 unpack routines (src/gls_image_tiff.cpp:53-87) and autoWhiteBalance (demosaic_utils.cpp:
-976-1026) are compiled from the reference sources into oracle/_ref/libref_host.so (make -C
-oracle ref); this script runs them on fixed inputs and stores the results bit-exactly.  It also records hashes of the oracle's own
+976-1026) and the lossless-JPEG codec (src/gls_dng_lossless_jpeg.cpp) are compiled from the
+reference sources into oracle/_ref/libref_host.so (make -C oracle ref); this script runs them
+on fixed inputs and stores the results bit-exactly.  It also records hashes of the oracle's own
 pipeline outputs on small seeded frames, which pin the oracle across machines.
 
     make -C oracle ref && python tests/golden/make_golden.py
@@ -90,6 +91,24 @@ def awb_fixture():
     return out
 
 
+def lj92_fixture():
+    """Lossless-JPEG streams and the reference decoder's output (DecodeLosslessJPEG,
+    gls_dng_lossless_jpeg.cpp:3253-3275): the "ref_" cases are written by the reference's
+    EncodeLosslessJPEG, the "own_" cases (predictors 2-7, restart intervals, which that
+    encoder never writes) by the oracle's test encoder."""
+    from tests import lj92_cases
+    streams, meta = {}, {}
+    for name, rows, cols, comps, prec, pred, rst, kind, seed in lj92_cases.CASES:
+        x = lj92_cases.samples(rows, cols, comps, prec, kind, seed)
+        st = orc.lj92_encode(x, comps, prec, pred, rst, reference=name.startswith("ref_"))
+        dec, info = orc.lj92_decode(st, reference=True)
+        assert np.array_equal(dec, x), name
+        streams[name] = np.frombuffer(st, np.uint8)
+        meta[name] = {"rows": rows, "cols": cols, "components": comps, "precision": prec, "predictor": pred,
+                      "restart_rows": rst, "samples_sha256": hashlib.sha256(dec.tobytes()).hexdigest()}
+    return streams, meta
+
+
 def oracle_pins():
     pins = {}
     for name, (w, h, bayer, prec, levels) in {
@@ -118,6 +137,10 @@ def main():
     np.savez_compressed(os.path.join(HERE, "ref_unpack.npz"), **unpack_fixture(ref))
     with open(os.path.join(HERE, "ref_awb.json"), "w") as f:
         json.dump(awb_fixture(), f, indent=1)
+    streams, meta = lj92_fixture()
+    np.savez_compressed(os.path.join(HERE, "ref_lj92.npz"), **streams)
+    with open(os.path.join(HERE, "ref_lj92.json"), "w") as f:
+        json.dump(meta, f, indent=1)
     with open(os.path.join(HERE, "oracle_pins.json"), "w") as f:
         json.dump(oracle_pins(), f, indent=1)
     print("golden fixtures written to", HERE)

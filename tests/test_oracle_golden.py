@@ -78,6 +78,31 @@ def test_auto_white_balance_equals_reference(awb_golden):
         assert int(np.float32(hl).view(np.uint32)) == fx["highlights"], case[0]
 
 
+def lj92_fixture():
+    with open(os.path.join(GOLDEN, "ref_lj92.json")) as f:
+        meta = json.load(f)
+    return np.load(os.path.join(GOLDEN, "ref_lj92.npz")), meta
+
+
+def test_lj92_decode_equals_reference():
+    """The oracle's lossless-JPEG decoder gives the reference decoder's samples on streams
+    written by the reference's encoder and by the oracle's (predictors 2-7, restarts)."""
+    streams, meta = lj92_fixture()
+    for name, m in meta.items():
+        dec, info = orc.lj92_decode(streams[name].tobytes())
+        assert hashlib.sha256(dec.tobytes()).hexdigest() == m["samples_sha256"], name
+        assert (info["height"], info["width"], info["components"]) == (m["rows"], m["cols"], m["components"])
+        assert info["predictor"] == m["predictor"], name
+
+
+def test_lj92_round_trip():
+    from tests import lj92_cases
+    for name, rows, cols, comps, prec, pred, rst, kind, seed in lj92_cases.CASES:
+        x = lj92_cases.samples(rows, cols, comps, prec, kind, seed + 100)
+        dec, _ = orc.lj92_decode(orc.lj92_encode(x, comps, prec, pred, rst))
+        np.testing.assert_array_equal(dec, x, err_msg=name)
+
+
 def test_unpack_round_trip_all_depths():
     rng = np.random.default_rng(9)
     for nbits in (10, 12, 14, 16):
