@@ -41,6 +41,7 @@ def parse():
     ap.add_argument("--no-psnr", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--no-awb", action="store_true")
+    ap.add_argument("--no-dng", action="store_true")
     ap.add_argument("--profile-only", action="store_true", help="a short run for ncu: no clocks, no cpu leg")
     return ap.parse_args()
 
@@ -379,6 +380,33 @@ def main():
             awb_line["bit_exact_vs_oracle"] = bool(np.array_equal(owb.view(np.uint32), wb.view(np.uint32))
                                                    and np.float32(ohl).view(np.uint32) == np.float32(hl).view(np.uint32))
 
+    # ---- DNG ingest: the first frame as one lossless-JPEG strip (the layout the reference's
+    # DNG writer uses), decoded from pinned host memory into the device frame ----
+    dng_line = None
+    if rank == 0 and world == 1 and not args.no_cpu and not args.no_dng and not args.profile_only:
+        from oracle import oracle as orc
+        raw0 = frames[0][0]
+        stream = orc.lj92_encode(raw0, 1, cfg["bits"], 1, 0)  # the input (test encoder)
+        pinned = torch.from_numpy(np.frombuffer(stream, np.uint8).copy()).pin_memory()
+        dec = torch.empty((h, w), dtype=torch.int32, device=dev).to(torch.uint16)
+        for _ in range(3):
+            ctx.decodeLosslessJPEG(pinned.numpy(), [0], [len(stream)], w, h, dec)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(5):
+            ctx.decodeLosslessJPEG(pinned.numpy(), [0], [len(stream)], w, h, dec)
+        torch.cuda.synchronize()
+        dms = (time.perf_counter() - t0) / 5 * 1e3
+        exact = bool(np.array_equal(dec.cpu().numpy(), raw0))
+        t0 = time.perf_counter()
+        orc.lj92_decode(stream)
+        cms = (time.perf_counter() - t0) * 1e3
+        dng_line = {"ms_per_frame": round(dms, 3), "mpix_s": round(w * h / 1e3 / dms, 1),
+                    "stream_bytes": len(stream), "bit_exact": exact,
+                    "layout": "one strip, one component, predictor 1, %d-bit" % cfg["bits"],
+                    "timed": "host pinned stream in, decoded frame in HBM, synchronous call",
+                    "cpu_baseline": {"ms_per_frame": round(cms, 1), "cores": 1, "kind": "port"}}
+
     cpu = psnr = None
     if rank == 0 and world == 1 and not args.no_cpu and not args.profile_only:
         gpu_rgb = None
@@ -415,6 +443,7 @@ def main():
             "psnr_vs_fp64": psnr,
             "learned_form": learned_line,
             "auto_white_balance": awb_line,
+            "dng_decode": dng_line,
         }
         print(json.dumps(line), flush=True)
     conv.close()
