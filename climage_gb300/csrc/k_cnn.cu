@@ -270,9 +270,11 @@ __global__ void __launch_bounds__(CT) conv3x3_tc05_kernel(ConvArgs a, int nimg, 
     __shared__ __align__(128) unsigned char s_b[W_B];
     __shared__ __align__(8) uint64_t s_bar;
     __shared__ uint32_t s_taddr;
+    __shared__ float s_bias[32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t bar = smem_u32(&s_bar);
     const int tiles_x = cdiv_d(a.w, TC5_C), tiles_y = cdiv_d(a.h, TC5_R);
+    if (threadIdx.x < 32) s_bias[threadIdx.x] = a.bias[threadIdx.x];
     const int tiles_img = tiles_x * tiles_y, ntiles = tiles_img * nimg;
 
     if (warp == 0) {
@@ -294,11 +296,13 @@ __global__ void __launch_bounds__(CT) conv3x3_tc05_kernel(ConvArgs a, int nimg, 
         const __nv_bfloat16* in = (const __nv_bfloat16*)a.in + img * a.in_stride;
         const uint32_t base = smem_u32(s_a[buf]);
         for (int i = threadIdx.x; i < HALO_N; i += CT) {
-            const int cb = i / (TC5_HR * TC5_HC), p = i - cb * (TC5_HR * TC5_HC);
+            // consecutive threads take consecutive 16-byte pieces of a pixel's 64 bytes
+            const int p = i >> 2, cb = i & 3;
             const int r = p / TC5_HC, c = p - r * TC5_HC;
             const int x = x0 - 1 + c, y = y0 - 1 + r;
             const bool ok = x >= 0 && x < a.w && y >= 0 && y < a.h;
-            cp_async16(base + i * 16, ok ? (const void*)(in + ((size_t)y * a.w + x) * 32 + cb * 8) : (const void*)in, ok);
+            cp_async16(base + (uint32_t)(cb * TC5_HR * TC5_HC + p) * 16,
+                       ok ? (const void*)(in + ((size_t)y * a.w + x) * 32 + cb * 8) : (const void*)in, ok);
         }
     };
     int t = blockIdx.x;
@@ -370,7 +374,7 @@ __global__ void __launch_bounds__(CT) conv3x3_tc05_kernel(ConvArgs a, int nimg, 
                 __nv_bfloat16 o[32];
 #pragma unroll
                 for (int n = 0; n < 32; n++)
-                    o[n] = __float2bfloat16_rn(fmaxf(__uint_as_float(v[n]) + a.bias[n], 0.0f));
+                    o[n] = __float2bfloat16_rn(fmaxf(__uint_as_float(v[n]) + s_bias[n], 0.0f));
                 uint4* dst =
                     reinterpret_cast<uint4*>((__nv_bfloat16*)a.out + img * a.out_stride + ((size_t)y * a.w + x) * 32);
 #pragma unroll
