@@ -391,6 +391,293 @@ __global__ void __launch_bounds__(CT) conv3x3_tc05_kernel(ConvArgs a, int nimg, 
 }
 
 // ---------------------------------------------------------------------------------------
+// The whole forward pass in one kernel (inference): per 24x24-pixel output tile, the five
+// layers run out of shared memory and TMEM; HBM sees only the fp32 input and output.
+//   buffers: two 34x34-pixel activation buffers, [8-channel block][row][col][8 channels]
+//            bf16 (the canonical no-swizzle K-major layout of the tc05 kernel), ping-pong;
+//            the network input (4 channels) is a single 8-channel plane in the second one
+//   layers:  each layer computes positions [1, 33) of the buffer (eight 16x8 MMA tiles, one
+//            32-column TMEM accumulator each); the valid area shrinks by one pixel per layer
+//            from [0, 34) to the tile [5, 29), so what lies outside it never reaches a valid
+//            output.  Positions outside the image are stored as zero after every layer (the
+//            per-layer zero padding of the layer-by-layer path)
+//   layer 1: K = 16 of which 4 input channels; the second K core matrix is read 16 bytes on
+//            (the next pixel, always finite) against zero weights
+//   head:    N = 16 (4 real outputs), fp32 out for the tile's valid, in-image pixels
+// Weights of all layers (72 KB) are staged once per persistent block.  One thread issues
+// each layer's 72 (layer 1, head: 72) or 144 MMAs and commits them to an mbarrier; every wait is
+// bounded (an error flag, then the block drains and frees TMEM).
+// ---------------------------------------------------------------------------------------
+constexpr int FU_O = 24, FU_G = FU_O + 10;
+constexpr int FU_PLANE = FU_G * FU_G * 16;  // one 8-channel plane, bytes
+constexpr int FU_ACT = 4 * FU_PLANE;        // 32 channels
+constexpr int FU_W1 = 9 * 2 * 32 * 16, FU_WH = 9 * 4 * 32 * 16, FU_W5 = 9 * 4 * 16 * 16;
+constexpr int FU_SMEM = 2 * FU_ACT + FU_W1 + 3 * FU_WH + FU_W5 + 5 * 32 * 4 + 64;  // + 2 mbarriers, TMEM address
+constexpr uint32_t kIdescBf16M128N16 = (1u << 4) | (1u << 7) | (1u << 10) | ((16u >> 3) << 17) | ((128u >> 4) << 24);
+
+struct FusedArgs {
+    const float* in;  // [n][h][w][4]
+    float* out;       // [n][h][w][4]
+    int w, h, nimg;
+    const __nv_bfloat16* wt[5];  // packed forward weights [nout_p][9][cin_p]
+    const float* bias[5];
+};
+
+// bounded wait on phase `parity` of an mbarrier: non-blocking polls (test_wait), so the
+// block resumes as soon as the MMAs complete; the verdict is block-uniform
+__device__ __forceinline__ bool fu_wait(uint32_t bar, uint32_t parity) {
+    uint32_t done = 0;
+    for (uint32_t k = 0; k < 4 * kWaitLimit && !done; k++) {
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(bar), "r"(parity)
+            : "memory");
+    }
+    return __syncthreads_and(done) != 0;
+}
+
+__device__ __forceinline__ void fu_sync_for_mma() {
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+}
+
+// One layer's MMAs (thread 0): tiles 0-3 committed to bar0, tiles 4-7 to bar1, so the
+// epilogue of the first half runs while the second half computes.  Descriptors are the
+// base descriptors plus the (16-byte unit) offsets of the tap, K step and tile.
+template <int KCS, int NB>
+__device__ __forceinline__ void fu_issue(uint32_t taddr, uint32_t abase, uint32_t lbo_a, uint32_t wbase,
+                                         uint32_t idesc, uint32_t bar0, uint32_t bar1) {
+    const uint64_t a0 = tc5_desc(abase, lbo_a, FU_G * 16), b0 = tc5_desc(wbase, NB * 16, 8 * 16);
+#pragma unroll 1
+    for (int t = 0; t < 8; t++) {
+        const int rb = t >> 2, cbk = t & 3;
+        const uint64_t at = a0 + (uint64_t)((16 * rb * FU_G + 8 * cbk) * 16 >> 4);
+#pragma unroll
+        for (int tap = 0; tap < 9; tap++) {
+#pragma unroll
+            for (int kc = 0; kc < KCS; kc++) {
+                const uint64_t ad = at + (uint64_t)((2 * kc * FU_PLANE + ((tap / 3) * FU_G + tap % 3) * 16) >> 4);
+                const uint64_t bd = b0 + (uint64_t)(((tap * 2 * KCS + 2 * kc) * NB * 16) >> 4);
+                asm volatile(
+                    "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(taddr + 32u * t),
+                    "l"(ad), "l"(bd), "r"(idesc), "r"((tap | kc) ? 1u : 0u));
+            }
+        }
+        if (t == 3)
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar0)
+                         : "memory");
+    }
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar1)
+                 : "memory");
+}
+
+// a 32-lane x 32-column accumulator read (no wait: tcgen05.wait::ld follows the batch)
+__device__ __forceinline__ void fu_ld32_nowait(uint32_t addr, uint32_t (&v)[32]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+        "%14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];\n"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+          "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
+          "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]),
+          "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]),
+          "=r"(v[30]), "=r"(v[31])
+        : "r"(addr));
+}
+
+__device__ __forceinline__ void fu_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory"); }
+
+__device__ __forceinline__ void fu_ld32(uint32_t addr, uint32_t (&v)[32]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+        "%14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];\n"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+          "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
+          "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]),
+          "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]),
+          "=r"(v[30]), "=r"(v[31])
+        : "r"(addr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+}
+
+// hidden-layer epilogue of four tiles (t0..t0+3): bias, ReLU, zero outside the image,
+// bf16 into the next buffer; the four accumulator reads share one wait
+__device__ __forceinline__ void fu_epilogue(uint32_t taddr, unsigned char* obuf, const float* bias, int y0, int x0,
+                                            int w, int h, int t0) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, m = warp * 32 + lane;
+    uint32_t v[4][32];
+    const uint32_t base = taddr + ((uint32_t)(warp * 32) << 16) + 32u * t0;
+#pragma unroll
+    for (int q = 0; q < 4; q++) fu_ld32_nowait(base + 32u * q, v[q]);
+    fu_ld_wait();
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const int t = t0 + q;
+        const int r = 1 + 16 * (t >> 2) + (m >> 3), c = 1 + 8 * (t & 3) + (m & 7);
+        const int y = y0 - 5 + r, x = x0 - 5 + c;
+        const bool in = x >= 0 && x < w && y >= 0 && y < h;
+        uint32_t o[16];
+#pragma unroll
+        for (int n = 0; n < 16; n++) {
+            const float lo = in ? fmaxf(__uint_as_float(v[q][2 * n]) + bias[2 * n], 0.0f) : 0.0f;
+            const float hi = in ? fmaxf(__uint_as_float(v[q][2 * n + 1]) + bias[2 * n + 1], 0.0f) : 0.0f;
+            const __nv_bfloat162 p2 = __floats2bfloat162_rn(lo, hi);
+            o[n] = *reinterpret_cast<const uint32_t*>(&p2);
+        }
+        unsigned char* dst = obuf + (size_t)(r * FU_G + c) * 16;
+#pragma unroll
+        for (int cb = 0; cb < 4; cb++)
+            *reinterpret_cast<uint4*>(dst + cb * FU_PLANE) = make_uint4(o[4 * cb], o[4 * cb + 1], o[4 * cb + 2], o[4 * cb + 3]);
+    }
+}
+
+__global__ void __launch_bounds__(CT, 1) cnn_fused_kernel(FusedArgs a, int* err) {
+    extern __shared__ __align__(1024) unsigned char fu_smem[];
+    unsigned char* bufA = fu_smem;
+    unsigned char* bufB = bufA + FU_ACT;
+    unsigned char* w1 = bufB + FU_ACT;
+    unsigned char* wh = w1 + FU_W1;  // layers 2..4
+    unsigned char* w5 = wh + 3 * FU_WH;
+    float* s_bias = reinterpret_cast<float*>(w5 + FU_W5);  // [5][32]
+    uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_bias + 5 * 32);  // two
+    uint32_t* s_taddr = reinterpret_cast<uint32_t*>(s_bar + 2);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t bar = smem_u32(s_bar), bar1 = smem_u32(s_bar + 1);
+
+    // everything the tensor cores may read stays finite: clear the buffers once
+    for (int i = threadIdx.x; i < 2 * FU_ACT / 16; i += CT) reinterpret_cast<uint4*>(fu_smem)[i] = make_uint4(0, 0, 0, 0);
+    // weights: [tap][8-channel block][n][8]
+    for (int i = threadIdx.x; i < 9 * 2 * 32; i += CT) {
+        const int tap = i / 64, r = i - tap * 64, cb = r / 32, n = r - cb * 32;
+        *reinterpret_cast<uint4*>(w1 + (size_t)i * 16) =
+            *reinterpret_cast<const uint4*>(a.wt[0] + (size_t)n * 144 + tap * 16 + cb * 8);
+    }
+    for (int l = 0; l < 3; l++)
+        for (int i = threadIdx.x; i < 9 * 4 * 32; i += CT) {
+            const int tap = i / 128, r = i - tap * 128, cb = r / 32, n = r - cb * 32;
+            *reinterpret_cast<uint4*>(wh + (size_t)l * FU_WH + (size_t)i * 16) =
+                *reinterpret_cast<const uint4*>(a.wt[1 + l] + (size_t)n * 288 + tap * 32 + cb * 8);
+        }
+    for (int i = threadIdx.x; i < 9 * 4 * 16; i += CT) {
+        const int tap = i / 64, r = i - tap * 64, cb = r / 16, n = r - cb * 16;
+        uint4 v = make_uint4(0, 0, 0, 0);
+        if (n < 8) v = *reinterpret_cast<const uint4*>(a.wt[4] + (size_t)n * 288 + tap * 32 + cb * 8);
+        *reinterpret_cast<uint4*>(w5 + (size_t)i * 16) = v;
+    }
+    for (int i = threadIdx.x; i < 5 * 32; i += CT) {
+        const int l = i / 32, n = i - l * 32;
+        s_bias[i] = (l < 4 || n < 4) ? a.bias[l][n] : 0.0f;
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;\n" ::"r"(smem_u32(s_taddr)));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+    }
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar1));
+        asm volatile("fence.mbarrier_init.release.cluster;\n");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t taddr = *s_taddr;
+    const int tiles_x = cdiv_d(a.w, FU_O), tiles_y = cdiv_d(a.h, FU_O);
+    const int tiles_img = tiles_x * tiles_y, ntiles = tiles_img * a.nimg;
+    const long long img_px = (long long)a.w * a.h;
+    uint32_t phase = 0;
+    bool ok = true;
+    for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+        const int img = t / tiles_img, tt = t - img * tiles_img;
+        const int x0 = (tt % tiles_x) * FU_O, y0 = (tt / tiles_x) * FU_O;
+        const float* in = a.in + (size_t)img * img_px * 4;
+        // the network input: 34x34 pixels, 4 channels (sigma scaled) + 4 zero, bf16, into bufB
+        constexpr int kPx = (FU_G * FU_G + CT - 1) / CT;  // pixels per thread; all loads first
+        float4 f[kPx];
+#pragma unroll
+        for (int j = 0; j < kPx; j++) {
+            const int p = threadIdx.x + j * CT, r = p / FU_G, c = p - r * FU_G;
+            const int y = y0 - 5 + r, x = x0 - 5 + c;
+            f[j] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (p < FU_G * FU_G && x >= 0 && x < a.w && y >= 0 && y < a.h)
+                f[j] = __ldg(reinterpret_cast<const float4*>(in + ((size_t)y * a.w + x) * 4));
+        }
+#pragma unroll
+        for (int j = 0; j < kPx; j++) {
+            const int p = threadIdx.x + j * CT;
+            if (p < FU_G * FU_G) {
+                __nv_bfloat16 v[8];
+                v[0] = __float2bfloat16_rn(f[j].x);
+                v[1] = __float2bfloat16_rn(f[j].y);
+                v[2] = __float2bfloat16_rn(f[j].z);
+                v[3] = __float2bfloat16_rn(f[j].w * kSigmaScale);
+#pragma unroll
+                for (int k = 4; k < 8; k++) v[k] = __float2bfloat16_rn(0.0f);
+                *reinterpret_cast<uint4*>(bufB + (size_t)p * 16) = *reinterpret_cast<const uint4*>(v);
+            }
+        }
+        // layers 1-4: B -> A -> B -> A -> B ... then the head from B
+        unsigned char* src = bufB;
+        unsigned char* dst = bufA;
+        for (int l = 0; l < 4 && ok; l++) {
+            fu_sync_for_mma();
+            if (threadIdx.x == 0) {
+                if (l == 0)
+                    fu_issue<1, 32>(taddr, smem_u32(src), 16, smem_u32(w1), kIdescBf16M128N32, bar, bar1);
+                else
+                    fu_issue<2, 32>(taddr, smem_u32(src), FU_PLANE, smem_u32(wh + (size_t)(l - 1) * FU_WH),
+                                    kIdescBf16M128N32, bar, bar1);
+            }
+            for (int half = 0; half < 2 && ok; half++) {
+                ok = fu_wait(half ? bar1 : bar, phase);
+                if (!ok) break;
+                asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                fu_epilogue(taddr, dst, s_bias + 32 * l, y0, x0, a.w, a.h, 4 * half);
+            }
+            phase ^= 1u;
+            if (!ok) break;
+            asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+            unsigned char* tmp = src;
+            src = dst;
+            dst = tmp;
+        }
+        if (!ok) break;
+        // head: 32 -> 4 (N = 16), fp32 out for the tile's pixels inside the image
+        fu_sync_for_mma();
+        if (threadIdx.x == 0)
+            fu_issue<2, 16>(taddr, smem_u32(src), FU_PLANE, smem_u32(w5), kIdescBf16M128N16, bar, bar1);
+        ok = fu_wait(bar, phase) && fu_wait(bar1, phase);
+        phase ^= 1u;
+        if (!ok) break;
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        {
+            const int m = warp * 32 + lane;
+            float* out = a.out + (size_t)img * img_px * 4;
+            for (int tl = 0; tl < 8; tl++) {
+                uint32_t v[32];
+                fu_ld32(taddr + ((uint32_t)(warp * 32) << 16) + 32u * tl, v);
+                const int r = 1 + 16 * (tl >> 2) + (m >> 3), c = 1 + 8 * (tl & 3) + (m & 7);
+                const int y = y0 - 5 + r, x = x0 - 5 + c;
+                if (r >= 5 && r < 5 + FU_O && c >= 5 && c < 5 + FU_O && x < a.w && y < a.h) {
+                    const float* b = s_bias + 32 * 4;
+                    *reinterpret_cast<float4*>(out + ((size_t)y * a.w + x) * 4) =
+                        make_float4(__uint_as_float(v[0]) + b[0], __uint_as_float(v[1]) + b[1],
+                                    __uint_as_float(v[2]) + b[2], __uint_as_float(v[3]) + b[3]);
+                }
+            }
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+        __syncthreads();
+    }
+    if (!ok && threadIdx.x == 0) atomicExch(err, 1);
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;\n" ::"r"(taddr));
+}
+
+// ---------------------------------------------------------------------------------------
 // Weight gradient of one layer over one 8x16 pixel tile: dW[co][tap][ci] += sum_p
 // dZ[p][co] * A[p + tap][ci] (A zero-padded), as an MMA with M = co, N = (tap, ci),
 // K = the 16 pixels of a tile row.  Both operands are pixel-major in shared memory and
@@ -649,7 +936,9 @@ struct gls_cnn {
     size_t part_floats = 0;
     float* loss_dev = nullptr;
     float* loss_host = nullptr;
-    // hidden layers' forward pass: 1 tcgen05 (default), 0 mma.sync; the backward pass is mma.sync
+    // forward pass: 2 one fused tcgen05 kernel for inference (training keeps the per-layer
+    // path, whose activations the backward pass reads), 1 tcgen05 hidden layers (default),
+    // 0 mma.sync; the backward pass is mma.sync
     int backend = 1;
     int* err_dev = nullptr;  // set by a tcgen05 block whose wait ran out
 
@@ -727,6 +1016,30 @@ struct gls_cnn {
     // forward over n images [n][h][w][4] fp32 -> head [n][h][w][4] fp32 (out or this->head)
     gls_status forward(const float* in, int w, int h, int n, float* out) {
         const size_t px = (size_t)w * h;
+        if (backend == 2 && out) {  // inference: the fused kernel, no activations kept
+            static bool attr_set = false;
+            if (!attr_set) {
+                GLS_CHECK(check_cuda(ctx, cudaFuncSetAttribute(cnn_fused_kernel,
+                                                               cudaFuncAttributeMaxDynamicSharedMemorySize, FU_SMEM),
+                                     "cudaFuncSetAttribute(CNN fused)"));
+                attr_set = true;
+            }
+            FusedArgs fa;
+            fa.in = in;
+            fa.out = out;
+            fa.w = w;
+            fa.h = h;
+            fa.nimg = n;
+            for (int l = 0; l < kLayers; l++) {
+                fa.wt[l] = wfwd[l];
+                fa.bias[l] = master + off[l] + kCout[l] * 9 * kCin[l];
+            }
+            const int tiles = cdiv(w, FU_O) * cdiv(h, FU_O) * n;
+            const int sms = ctx->num_sms > 0 ? ctx->num_sms : 148;
+            cnn_fused_kernel<<<tiles < sms ? tiles : sms, CT, FU_SMEM, ctx->stream>>>(fa, err_dev);
+            ctx->launches++;
+            return check_launch(ctx, "CNN forward (fused)");
+        }
         GLS_CHECK(ensure_batch((int)(px * n)));
         const float* b = master;
         conv<16, 32, 0, true>(in, 4, px * 4, wfwd[0], b + off[0] + 32 * 9 * 4, act[0], 32, px * 32, nullptr, 0, w, h, n);
@@ -801,7 +1114,7 @@ int gls_cnn_param_count(void) {
 }
 
 gls_status gls_cnn_set_backend(gls_cnn* c, int backend) {
-    if (!c || (backend != 0 && backend != 1)) return GLS_ERR_INVALID_ARGUMENT;
+    if (!c || backend < 0 || backend > 2) return GLS_ERR_INVALID_ARGUMENT;
     c->backend = backend;
     return GLS_OK;
 }

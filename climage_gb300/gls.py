@@ -580,7 +580,8 @@ class Cnn:
         return out
 
     def set_backend(self, backend):
-        """1: tcgen05 (default) for the hidden layers' forward pass; 0: mma.sync."""
+        """Forward pass: 1 tcgen05 hidden layers (default), 0 mma.sync, 2 all five layers in one
+        fused tcgen05 kernel (inference; training uses the per-layer path)."""
         self.ctx.check(lib().gls_cnn_set_backend(self.handle, int(backend)), "Cnn.set_backend")
 
     def status(self):

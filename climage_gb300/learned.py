@@ -245,8 +245,8 @@ def main():
     ap.add_argument("--judge-only", default=None, help="judge these saved parameters, no training")
     ap.add_argument("--gain", type=float, nargs=2, default=None, help="gain range (e-/DN) of the frames")
     ap.add_argument("--sigma", type=float, nargs=2, default=None, help="read noise range (DN) of the frames")
-    ap.add_argument("--backend", type=int, default=None, choices=(0, 1),
-                    help="hidden-layer forward backend for --time-forward (0 mma.sync, 1 tcgen05)")
+    ap.add_argument("--backend", type=int, default=None, choices=(0, 1, 2),
+                    help="forward backend for --time-forward (0 mma.sync, 1 tcgen05 layers, 2 fused tcgen05)")
     ap.add_argument("--time-forward", type=int, nargs=2, default=None, metavar=("W", "H"),
                     help="only time the network's forward pass over a W x H frame (shipped parameters)")
     args = ap.parse_args()

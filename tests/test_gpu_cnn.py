@@ -44,7 +44,7 @@ def cnn(ctx):
     c.close()
 
 
-@pytest.mark.parametrize("backend", [0, 1], ids=["mma_sync", "tcgen05"])
+@pytest.mark.parametrize("backend", [0, 1, 2], ids=["mma_sync", "tcgen05", "fused"])
 def test_forward_matches_reference(cnn, backend):
     import torch
     cnn.set_backend(backend)
@@ -64,22 +64,43 @@ def test_forward_matches_reference(cnn, backend):
 
 
 def test_backends_agree(cnn):
-    """tcgen05 and mma.sync accumulate the same products in FP32 in different orders: the
-    hidden activations can differ by one bfloat16 step where a value sits on a rounding
-    boundary, nothing more."""
+    """tcgen05 (per layer or all five layers fused in one kernel) and mma.sync accumulate the
+    same products in FP32 in different orders: the hidden activations can differ by one
+    bfloat16 step where a value sits on a rounding boundary, nothing more."""
     import torch
     rng = np.random.default_rng(11)
     cnn.set_params(gls.cnn_init(3, head_std=0.05))
     inp, _ = batch(rng, 3, 50, 70)
     x = torch.from_numpy(inp).cuda()
     outs = []
-    for backend in (0, 1):
+    for backend in (0, 1, 2):
         cnn.set_backend(backend)
         o = torch.empty_like(x)
         cnn.forward(x, o)
         torch.cuda.synchronize()
         outs.append(o.cpu().numpy())
     cnn.status()
+    assert rel_l2(outs[1], outs[0]) < 2e-3, rel_l2(outs[1], outs[0])
+    assert rel_l2(outs[2], outs[0]) < 2e-3, rel_l2(outs[2], outs[0])
+
+
+@pytest.mark.parametrize("w,h,n", [(24, 24, 1), (1, 1, 1), (25, 47, 2), (200, 9, 1), (300, 230, 1)])
+def test_fused_forward_sizes(cnn, w, h, n):
+    """Tile edges, images smaller than a tile, several images: the fused kernel against the
+    per-layer tcgen05 path."""
+    import torch
+    cnn.set_params(gls.cnn_init(4, head_std=0.05))
+    rng = np.random.default_rng(w * 1000 + h)
+    x = torch.from_numpy(rng.uniform(0, 1, (n, h, w, 4)).astype(np.float32)).cuda()
+    outs = []
+    for backend in (1, 2):
+        cnn.set_backend(backend)
+        o = torch.full_like(x, 123.0)
+        cnn.forward(x, o)
+        torch.cuda.synchronize()
+        outs.append(o.cpu().numpy())
+    cnn.status()
+    assert np.all(np.isfinite(outs[1]))
     assert rel_l2(outs[1], outs[0]) < 2e-3, rel_l2(outs[1], outs[0])
 
 
