@@ -356,6 +356,26 @@ def main():
         e2e = {"value": round(world * mpix_per_step * args.steps / e2e_s, 3), "unit": "MPix/s",
                "h2d_bytes_per_step": int(sum(f[0].nbytes for f in frames)),
                "d2h_bytes_per_step": int(len(frames) * w * h * 4)}
+        # the same burst from packed 12-bit host frames (an uncompressed DNG strip's layout):
+        # the packed bytes cross to the device and are unpacked there
+        from climage_gb300 import synthetic
+        packed = [torch.from_numpy(np.frombuffer(synthetic.pack_bits(f[0], cfg["bits"]), np.uint8).copy()).pin_memory()
+                  for f in frames]
+
+        def packed_step():
+            batch.demosaic_packed_host_ptr([t.data_ptr() for t in packed], [t.numel() for t in packed],
+                                           [cfg["bits"]] * len(frames), [(w, h)] * len(frames), params,
+                                           [t.data_ptr() for t in houts], 4)
+
+        for _ in range(args.warmup):
+            packed_step()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            packed_step()
+        pk_s = time.perf_counter() - t0
+        e2e["packed_input"] = {"value": round(world * mpix_per_step * args.steps / pk_s, 3), "unit": "MPix/s",
+                               "h2d_bytes_per_step": int(sum(t.numel() for t in packed)), "bits": cfg["bits"]}
 
     # ---- the learned form: the same burst with the learned stage (shipped parameters) ----
     learned_line = None

@@ -72,6 +72,8 @@ struct gls_raw_converter {
     size_t raw_dev_bytes = 0;
     uint8_t* out_dev = nullptr;
     size_t out_dev_bytes = 0;
+    uint8_t* packed_dev = nullptr;  // packed 10/12/14-bit raw bytes of the packed host entry point
+    size_t packed_dev_bytes = 0;
     // parity taps
     gls_image_desc taps[5]{};
     bool tap_set[5]{};
@@ -590,6 +592,31 @@ struct gls_raw_converter {
         GLS_CHECK(ensure_staging(fw, fh));
         GLS_CHECK(check_cuda(ctx, cudaMemcpy2DAsync(raw_dev, (size_t)fw * 2, raw, (size_t)stride * 2, (size_t)fw * 2,
                                                     fh, cudaMemcpyHostToDevice, ctx->stream), "copy raw frame"));
+        return finish_host(fw, fh, p, out, out_channels);
+    }
+
+    // packed host raw in (the frame's samples as one MSB-first bit stream, as a DNG strip of
+    // 10/12/14-bit samples stores them): the packed bytes cross to the device and are
+    // unpacked there into the staging frame (unpack12BitsInto16Bits and
+    // unpack14BitsInto16Bits, src/gls_image_tiff.cpp:53-87)
+    gls_status run_packed_host(const uint8_t* packed, size_t n_bytes, int bits, int fw, int fh,
+                               gls_demosaic_params* p, uint8_t* out, int out_channels) {
+        GLS_CHECK(ensure_staging(fw, fh));
+        if (packed_dev_bytes < n_bytes) {
+            if (packed_dev) cudaFree(packed_dev);
+            packed_dev = nullptr;
+            packed_dev_bytes = 0;
+            GLS_CHECK(check_cuda(ctx, cudaMalloc(&packed_dev, n_bytes), "cudaMalloc(packed raw)"));
+            packed_dev_bytes = n_bytes;
+        }
+        GLS_CHECK(check_cuda(ctx, cudaMemcpyAsync(packed_dev, packed, n_bytes, cudaMemcpyHostToDevice, ctx->stream),
+                             "copy packed raw frame"));
+        launch_unpack(ctx, packed_dev, n_bytes, bits, raw_dev, (size_t)fw * fh);
+        return finish_host(fw, fh, p, out, out_channels);
+    }
+
+    // the staged raw frame through the pipeline, RGBA8 (or RGB8) back to the host
+    gls_status finish_host(int fw, int fh, gls_demosaic_params* p, uint8_t* out, int out_channels) {
         GLS_CHECK(ensure(fw, fh, p->pyramid_levels, p->storage == GLS_STORAGE_F16));
         GLS_CHECK(run(raw_dev, fw, p, out_dev, false, fw));
         const void* src = out_dev;
@@ -654,6 +681,7 @@ gls_status gls_raw_converter_destroy(gls_raw_converter* c) {
     if (c->nlf_host) cudaFreeHost(c->nlf_host);
     if (c->raw_dev) cudaFree(c->raw_dev);
     if (c->out_dev) cudaFree(c->out_dev);
+    if (c->packed_dev) cudaFree(c->packed_dev);
     if (c->cnn) gls_cnn_destroy(c->cnn);
     delete c;
     return GLS_OK;
@@ -775,6 +803,29 @@ gls_status gls_raw_converter_demosaic_host(gls_raw_converter* c, const uint16_t*
     if (stride < w) return set_error(ctx, GLS_ERR_INVALID_SIZE, "raw stride smaller than width");
     GLS_CHECK(validate_params(ctx, p, w, h));
     GLS_CHECK(c->run_host(raw, w, h, stride, p, out, out_channels));
+    return c->fetch_noise_model(p);
+}
+
+static gls_status check_packed(gls_ctx* ctx, const void* packed, size_t n_bytes, int bits, int w, int h) {
+    if (!packed) return set_error(ctx, GLS_ERR_INVALID_ARGUMENT, "packed raw is null");
+    if (bits != 10 && bits != 12 && bits != 14 && bits != 16)
+        return set_error(ctx, GLS_ERR_UNSUPPORTED, "unsupported bit depth %d", bits);
+    if ((unsigned long long)w * h > (unsigned long long)(n_bytes * 8 / (size_t)bits))
+        return set_error(ctx, GLS_ERR_INVALID_SIZE, "packed raw holds %zu samples, the frame needs %lld",
+                         n_bytes * 8 / (size_t)bits, (long long)w * h);
+    return GLS_OK;
+}
+
+gls_status gls_raw_converter_demosaic_packed_host(gls_raw_converter* c, const uint8_t* packed, size_t n_bytes,
+                                                  int bits, int w, int h, gls_demosaic_params* p, uint8_t* out,
+                                                  int out_channels) {
+    if (!c || !out) return GLS_ERR_INVALID_ARGUMENT;
+    gls_ctx* ctx = c->ctx;
+    if (out_channels != 3 && out_channels != 4)
+        return set_error(ctx, GLS_ERR_INVALID_ARGUMENT, "out_channels must be 3 or 4");
+    GLS_CHECK(validate_params(ctx, p, w, h));
+    GLS_CHECK(check_packed(ctx, packed, n_bytes, bits, w, h));
+    GLS_CHECK(c->run_packed_host(packed, n_bytes, bits, w, h, p, out, out_channels));
     return c->fetch_noise_model(p);
 }
 
@@ -1020,6 +1071,37 @@ gls_status gls_raw_batch_demosaic_host(gls_raw_batch* b, int n, const uint16_t* 
         gls_demosaic_params p = params[i];
         const gls_status s =
             b->lane[l]->run_host(raws[i], widths[i], heights[i], raw_strides[i], &p, outs[i], out_channels);
+        if (s != GLS_OK) return batch_error(b, l, s);
+    }
+    GLS_CHECK(batch_join(b, l0));
+    return check_cuda(ctx, cudaStreamSynchronize(ctx->stream), "synchronize");
+}
+
+gls_status gls_raw_batch_demosaic_packed_host(gls_raw_batch* b, int n, const uint8_t* const* packed,
+                                              const size_t* n_bytes, const int* bits, const int* widths,
+                                              const int* heights, const gls_demosaic_params* params,
+                                              uint8_t* const* outs, int out_channels) {
+    if (!b) return GLS_ERR_INVALID_ARGUMENT;
+    gls_ctx* ctx = b->ctx;
+    if (n < 0 || (n > 0 && (!packed || !n_bytes || !bits || !widths || !heights || !params || !outs)))
+        return set_error(ctx, GLS_ERR_INVALID_ARGUMENT, "batch arrays");
+    if (out_channels != 3 && out_channels != 4)
+        return set_error(ctx, GLS_ERR_INVALID_ARGUMENT, "out_channels must be 3 or 4");
+    for (int i = 0; i < n; i++) {
+        if (!outs[i]) return set_error(ctx, GLS_ERR_INVALID_ARGUMENT, "frame %d: null buffer", i);
+        GLS_CHECK(validate_params(ctx, &params[i], widths[i], heights[i]));
+        GLS_CHECK(check_packed(ctx, packed[i], n_bytes[i], bits[i], widths[i], heights[i]));
+    }
+    b->lane_of.assign(n, 0);
+    const int lanes = (int)b->lane.size();
+    plan_lanes(n, widths, heights, lanes, b->lane_of.data());
+    const std::vector<uint64_t> l0 = lane_launches(b);
+    GLS_CHECK(batch_fork(b));
+    for (int i = 0; i < n; i++) {
+        const int l = b->lane_of[i];
+        gls_demosaic_params p = params[i];
+        const gls_status s = b->lane[l]->run_packed_host(packed[i], n_bytes[i], bits[i], widths[i], heights[i], &p,
+                                                         outs[i], out_channels);
         if (s != GLS_OK) return batch_error(b, l, s);
     }
     GLS_CHECK(batch_join(b, l0));

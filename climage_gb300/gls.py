@@ -129,6 +129,12 @@ SIGNATURES = [
     ("gls_raw_converter_demosaic", _I, [_P, _D, ctypes.POINTER(DemosaicParams), _D, _I]),
     ("gls_raw_converter_noise_model", _I, [_P, ctypes.POINTER(DemosaicParams)]),
     ("gls_raw_converter_demosaic_host", _I, [_P, _P, _I, _I, _I, ctypes.POINTER(DemosaicParams), _P, _I]),
+    ("gls_raw_converter_demosaic_packed_host", _I, [_P, _P, ctypes.c_size_t, _I, _I, _I,
+                                                    ctypes.POINTER(DemosaicParams), _P, _I]),
+    ("gls_raw_batch_demosaic_packed_host", _I, [_P, _I, ctypes.POINTER(_P), ctypes.POINTER(ctypes.c_size_t),
+                                                ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                                ctypes.POINTER(ctypes.c_int), ctypes.POINTER(DemosaicParams),
+                                                ctypes.POINTER(_P), _I]),
     ("gls_raw_converter_fast_demosaic", _I, [_P, _D, ctypes.POINTER(DemosaicParams), _D]),
     ("gls_raw_converter_set_tap", _I, [_P, _I, _D]),
     ("gls_raw_converter_set_mode", _I, [_P, _I]),
@@ -433,6 +439,16 @@ class RawConverter:
             ctypes.c_void_p(out.ctypes.data), ch), "demosaicImage (host buffers)")
         return out
 
+    def demosaicImagePackedHost(self, packed, bits, w, h, params, out):
+        """packed: uint8 numpy array (ideally pinned) holding the w x h samples as one MSB-first
+        stream of `bits`-bit samples; out: (H, W, 3|4) uint8 numpy array."""
+        packed = np.frombuffer(packed, np.uint8) if isinstance(packed, (bytes, bytearray)) else packed
+        ch = out.shape[2]
+        self.ctx.check(lib().gls_raw_converter_demosaic_packed_host(
+            self.handle, ctypes.c_void_p(packed.ctypes.data), packed.size, int(bits), int(w), int(h),
+            ctypes.byref(params), ctypes.c_void_p(out.ctypes.data), ch), "demosaicImage (packed host buffers)")
+        return out
+
     def demosaicImageHostPtr(self, raw_ptr, w, h, params, out_ptr, channels):
         self.ctx.check(lib().gls_raw_converter_demosaic_host(self.handle, ctypes.c_void_p(raw_ptr), w, h, w,
                                                              ctypes.byref(params), ctypes.c_void_p(out_ptr), channels),
@@ -531,6 +547,19 @@ class RawBatch:
         pa = (DemosaicParams * max(n, 1))(*params)
         self.ctx.check(lib().gls_raw_batch_demosaic_host(self.handle, n, rp, ws, hs, ws, pa, op, int(channels)),
                        "RawBatch.demosaic_host")
+
+    def demosaic_packed_host_ptr(self, packed_ptrs, n_bytes, bits, sizes, params, out_ptrs, channels=4):
+        """Packed host frames by address (see RawConverter.demosaicImagePackedHost)."""
+        n = len(packed_ptrs)
+        pp = (ctypes.c_void_p * max(n, 1))(*packed_ptrs)
+        nb = (ctypes.c_size_t * max(n, 1))(*n_bytes)
+        bb = (ctypes.c_int * max(n, 1))(*bits)
+        op = (ctypes.c_void_p * max(n, 1))(*out_ptrs)
+        ws = (ctypes.c_int * max(n, 1))(*[w for w, _ in sizes])
+        hs = (ctypes.c_int * max(n, 1))(*[h for _, h in sizes])
+        pa = (DemosaicParams * max(n, 1))(*params)
+        self.ctx.check(lib().gls_raw_batch_demosaic_packed_host(self.handle, n, pp, nb, bb, ws, hs, pa, op,
+                                                                int(channels)), "RawBatch.demosaic_packed_host")
 
     def close(self):
         if self.handle:

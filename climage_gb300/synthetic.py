@@ -135,6 +135,18 @@ def pack_bits(samples, bits):
     unpack12BitsInto16Bits / unpack14BitsInto16Bits, src/gls_image_tiff.cpp:53-87)."""
     s = np.ascontiguousarray(samples, dtype=np.uint32).ravel()
     n = s.size
+    g = 8 // np.gcd(bits, 8)  # samples per whole number of bytes
+    if n % g == 0 and g * bits <= 64:
+        # groups of g samples fill g * bits / 8 bytes exactly: assemble each group in a uint64
+        grp = s.reshape(-1, g).astype(np.uint64)
+        acc = np.zeros(grp.shape[0], np.uint64)
+        for j in range(g):
+            acc = (acc << np.uint64(bits)) | grp[:, j]
+        nb = g * bits // 8
+        out = np.empty((grp.shape[0], nb), np.uint8)
+        for k in range(nb):
+            out[:, k] = ((acc >> np.uint64(8 * (nb - 1 - k))) & np.uint64(0xFF)).astype(np.uint8)
+        return out.tobytes()
     total_bits = n * bits
     out = np.zeros((total_bits + 7) // 8, np.uint8)
     bitpos = np.arange(n, dtype=np.int64) * bits

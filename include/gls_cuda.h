@@ -261,6 +261,14 @@ GLS_API gls_status gls_raw_converter_noise_model(gls_raw_converter* conv, gls_de
 GLS_API gls_status gls_raw_converter_demosaic_host(gls_raw_converter* conv, const uint16_t* raw, int width, int height,
                                                    int raw_stride_px, gls_demosaic_params* params, uint8_t* out,
                                                    int out_channels);
+/* As gls_raw_converter_demosaic_host with a packed raw frame: the width x height samples as
+ * one MSB-first stream of `bits`-bit samples (10/12/14/16), the layout of an uncompressed
+ * DNG strip that unpack12BitsInto16Bits / unpack14BitsInto16Bits (src/gls_image_tiff.cpp:
+ * 53-87) read; the packed bytes cross to the device and are unpacked there. */
+GLS_API gls_status gls_raw_converter_demosaic_packed_host(gls_raw_converter* conv, const uint8_t* packed,
+                                                          size_t n_bytes, int bits, int width, int height,
+                                                          gls_demosaic_params* params, uint8_t* out,
+                                                          int out_channels);
 /* RawConverter::fastDemosaicImage (raw_converter.cpp:188-224): half-resolution preview */
 GLS_API gls_status gls_raw_converter_fast_demosaic(gls_raw_converter* conv, const gls_image_desc* raw,
                                                    const gls_demosaic_params* params, const gls_image_desc* out);
@@ -317,6 +325,11 @@ GLS_API gls_status gls_raw_batch_demosaic_host(gls_raw_batch* batch, int n, cons
                                                const int* widths, const int* heights, const int* raw_strides_px,
                                                const gls_demosaic_params* params, uint8_t* const* outs,
                                                int out_channels);
+/* n packed host frames (as gls_raw_converter_demosaic_packed_host) over the batch's lanes. */
+GLS_API gls_status gls_raw_batch_demosaic_packed_host(gls_raw_batch* batch, int n, const uint8_t* const* packed,
+                                                      const size_t* n_bytes, const int* bits, const int* widths,
+                                                      const int* heights, const gls_demosaic_params* params,
+                                                      uint8_t* const* outs, int out_channels);
 /* ---- the learned stage: a 5-layer 3x3 BF16 CNN ----
  * No counterpart in the reference.  4 -> 32 -> 32 -> 32 -> 32 -> 4 channels, ReLU between
  * layers, zero-padded borders.  Input per pixel: demosaiced linear R, G, B and the noise

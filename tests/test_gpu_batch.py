@@ -134,6 +134,40 @@ def test_host_buffers(ctx):
     batch.close()
 
 
+def test_packed_host_frames(ctx):
+    """Packed 10/12/14-bit host frames (one MSB-first bit stream, as an uncompressed DNG strip)
+    give exactly the unpacked frames' output, through a converter and through a batch."""
+    import torch
+    fr = frames(BURST[:4], seed0=4000)
+    bits = [12, 14, 10, 12]  # the bit depths of BURST[:4]
+    want, packed = [], []
+    for f, b in zip(fr, bits):
+        conv = gls.RawConverter(ctx)
+        o = np.zeros((f["h"], f["w"], 4), np.uint8)
+        conv.demosaicImageHost(np.ascontiguousarray(f["raw_np"]), gls.DemosaicParams.from_buffer_copy(f["params"]), o)
+        want.append(o)
+        pk = np.frombuffer(synthetic.pack_bits(f["raw_np"], b), np.uint8).copy()
+        packed.append(pk)
+        o2 = np.zeros_like(o)
+        conv.demosaicImagePackedHost(pk, b, f["w"], f["h"], gls.DemosaicParams.from_buffer_copy(f["params"]), o2)
+        assert np.array_equal(o2, o)
+        conv.close()
+    pinned = [torch.from_numpy(pk).pin_memory() for pk in packed]
+    ho = [torch.zeros((f["h"], f["w"], 4), dtype=torch.uint8).pin_memory() for f in fr]
+    batch = gls.RawBatch(ctx, 2)
+    batch.demosaic_packed_host_ptr([t.data_ptr() for t in pinned], [pk.size for pk in packed], bits,
+                                   [(f["w"], f["h"]) for f in fr], [f["params"] for f in fr],
+                                   [t.data_ptr() for t in ho], 4)
+    for k, (o, w) in enumerate(zip(ho, want)):
+        assert np.array_equal(o.numpy(), w), "frame %d" % k
+    batch.close()
+    conv = gls.RawConverter(ctx)
+    with pytest.raises(gls.GlsError):  # too few bytes for the frame
+        conv.demosaicImagePackedHost(packed[0][:-2], 12, fr[0]["w"], fr[0]["h"], fr[0]["params"],
+                                     np.zeros((fr[0]["h"], fr[0]["w"], 4), np.uint8))
+    conv.close()
+
+
 def test_rejects_bad_frame(ctx):
     import torch
     fr = frames(BURST[:2])
