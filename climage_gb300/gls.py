@@ -120,6 +120,8 @@ SIGNATURES = [
     ("gls_auto_white_balance", _I, [_P, _D, _FP, _FP, _F, _F, _I, _FP, _FP]),
     ("gls_dng_decode_lossless_jpeg", _I, [_P, _P, ctypes.c_size_t, _I, ctypes.POINTER(ctypes.c_uint64),
                                           ctypes.POINTER(ctypes.c_uint64), _I, _I, _D]),
+    ("gls_color_checker_raw_stats", _I, [_P, _D, _F, _F, _I, ctypes.POINTER(ctypes.c_int), _I, _FP, _FP]),
+    ("gls_estimate_raw_parameters", _I, [_P, _D, _F, _F, _I, ctypes.POINTER(ctypes.c_int), _I, _FP, _FP, _FP]),
     ("gls_selftest", _I, [_P, ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)]),
     ("gls_cam_xyz_coeff", _I, [_FP, _FP, _FP]),
     ("gls_cam_ycbcr", _I, [_FP, _FP]),
@@ -329,6 +331,22 @@ class Context:
         self.check(self._lib.gls_dng_decode_lossless_jpeg(self.handle, ctypes.c_void_p(buf.ctypes.data), buf.size, n,
                                                           offs, lens, int(tile_width), int(tile_height), desc(out)),
                    "decodeLosslessJPEG")
+
+    def colorCheckerRawStats(self, raw, black, white, bayer, gmb, rotate_180=False):
+        """(mean (24, 4), var (24, 4)) of the CFA channels per chart patch; gmb = (x, y, w, h)."""
+        mean, var = (ctypes.c_float * 96)(), (ctypes.c_float * 96)()
+        self.check(self._lib.gls_color_checker_raw_stats(self.handle, desc(raw), float(black), float(white), int(bayer),
+                                                         (ctypes.c_int * 4)(*gmb), int(rotate_180), mean, var),
+                   "colorCheckerRawStats")
+        return np.array(mean[:], np.float32).reshape(24, 4), np.array(var[:], np.float32).reshape(24, 4)
+
+    def estimateRawParameters(self, raw, black, white, bayer, gmb, rotate_180=False):
+        """(cam_xyz (3, 3), pre_mul (3,), raw NLF slopes (4,)) from a ColorChecker chart."""
+        cx, pm, nlf = (ctypes.c_float * 9)(), (ctypes.c_float * 3)(), (ctypes.c_float * 4)()
+        self.check(self._lib.gls_estimate_raw_parameters(self.handle, desc(raw), float(black), float(white), int(bayer),
+                                                         (ctypes.c_int * 4)(*gmb), int(rotate_180), cx, pm, nlf),
+                   "estimateRawParameters")
+        return np.array(cx[:], np.float32).reshape(3, 3), np.array(pm[:], np.float32), np.array(nlf[:], np.float32)
 
     def interpolateGreen(self, scaled, green, bayer, luma_variance):
         self.check(self._lib.gls_interpolate_green(self.handle, desc(scaled), desc(green), bayer, float(luma_variance)),

@@ -227,6 +227,21 @@ GLS_API gls_status gls_auto_white_balance(gls_ctx* ctx, const gls_image_desc* ra
                                           const float scale_mul[4], float white_level, float black_level,
                                           int bayer_pattern, float wb_out[3], float* highlights);
 
+/* colorCheckerRawStats (demosaic_utils.cpp:411-533): the mean and variance of the CFA channels
+ * {r, g, b, g2} over the inner half of each patch of a 6x4 ColorChecker chart at gmb_rect =
+ * {x, y, width, height} of a raw R16_UNORM frame (device); mean[24 * 4], var[24 * 4] host
+ * outputs, patch order reversed when rotate_180; the call synchronizes the stream. */
+GLS_API gls_status gls_color_checker_raw_stats(gls_ctx* ctx, const gls_image_desc* raw, float black_level,
+                                               float white_level, int bayer_pattern, const int gmb_rect[4],
+                                               int rotate_180, float mean[96], float var[96]);
+/* estimateRawParameters (demosaic_utils.cpp:686-785): from the chart's patches, the camera
+ * matrix cam_xyz (normalised, row-major 3x3), the white point pre_mul (green 1) and the raw
+ * noise slopes {r, g, b, g2} of the six neutral patches; host outputs, bit-identical to the
+ * reference's fp32/fp64 arithmetic. */
+GLS_API gls_status gls_estimate_raw_parameters(gls_ctx* ctx, const gls_image_desc* raw, float black_level,
+                                               float white_level, int bayer_pattern, const int gmb_rect[4],
+                                               int rotate_180, float cam_xyz[9], float pre_mul[3], float raw_nlf[4]);
+
 /* DecodeLosslessJPEG (src/gls_dng_lossless_jpeg.cpp:3253-3275) over the tiles or the strip of
  * a DNG image, as the DNG reader calls it (src/gls_image_tiff.cpp:369-440): data is host
  * memory holding the n_streams lossless-JPEG streams (stream i at offsets[i], sizes[i] bytes:

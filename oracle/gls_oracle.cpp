@@ -1561,6 +1561,174 @@ void auto_white_balance(const uint16_t* raw, int w, int h, int stride, const flo
 }  // namespace awb
 
 // ---------------------------------------------------------------------------------------
+// Colour-checker calibration (estimateRawParameters, demosaic_utils.cpp:686-785): per patch
+// of a 6x4 ColorChecker chart, the fp32 mean and variance of each CFA channel over the
+// patch's quads in raster order (colorCheckerRawStats, 411-533); the camera matrix and white
+// point from the patch means (matrixFromColorChecker, 83-129, with dcraw's pseudoinverse,
+// gls_linalg.hpp:559-590) and the raw noise slopes from the six neutral patches
+// (linear_regression, 604-621: double sums of fp32 products).
+// ---------------------------------------------------------------------------------------
+namespace calib {
+
+struct Rect {
+    int x, y, w, h;
+};
+
+// alignToQuad (demosaic_utils.cpp:54-71)
+Rect align_to_quad(Rect r) {
+    if (r.y & 1) {
+        r.y += 1;
+        r.h -= 1;
+    }
+    if (r.h & 1) r.h -= 1;
+    if (r.x & 1) {
+        r.x += 1;
+        r.w -= 1;
+    }
+    if (r.w & 1) r.w -= 1;
+    return r;
+}
+
+Rect patch_rect(const Rect& gmb, int row, int col) {
+    const int pw = gmb.w / 6, ph = gmb.h / 4;
+    return align_to_quad({gmb.x + col * pw + (int)(0.25 * pw), gmb.y + row * ph + (int)(0.25 * ph), (int)(0.5 * pw),
+                          (int)(0.5 * ph)});
+}
+
+void patch_stats(const uint16_t* raw, int stride, float black, float white, int bayer, const Rect& gmb, int rotate,
+                 float mean[24][4], float var[24][4]) {
+    const int (*o)[2] = awb::kHostBayer[bayer];
+    for (int row = 0; row < 4; row++)
+        for (int col = 0; col < 6; col++) {
+            const int idx = row * 6 + col;
+            const Rect pr = patch_rect(gmb, row, col);
+            const int samples = pr.w * pr.h / 4;
+            auto px = [&](int y, int x, int c) {
+                const float v = ((float)raw[(size_t)(y + o[c][1]) * stride + x + o[c][0]] - black) / white;
+                return std::min(std::max(v, 0.0f), 1.0f);
+            };
+            float avg[4] = {0, 0, 0, 0};
+            for (int y = 0; y < pr.h; y += 2)
+                for (int x = 0; x < pr.w; x += 2)
+                    for (int c = 0; c < 4; c++) avg[c] = avg[c] + px(pr.y + y, pr.x + x, c);
+            for (int c = 0; c < 4; c++) avg[c] = avg[c] / (float)samples;
+            float v[4] = {0, 0, 0, 0};
+            for (int y = 0; y < pr.h; y += 2)
+                for (int x = 0; x < pr.w; x += 2)
+                    for (int c = 0; c < 4; c++) {
+                        const float d = px(pr.y + y, pr.x + x, c) - avg[c];
+                        v[c] = v[c] + d * d;
+                    }
+            for (int c = 0; c < 4; c++) {
+                mean[idx][c] = avg[c];
+                var[idx][c] = v[c] / (float)samples;
+            }
+        }
+    if (rotate)
+        for (int a = 0, b = 23; a < b; a++, b--)
+            for (int c = 0; c < 4; c++) {
+                std::swap(mean[a][c], mean[b][c]);
+                std::swap(var[a][c], var[b][c]);
+            }
+}
+
+// ColorChecker chart under D65 (xyY), matrixFromColorChecker
+const float kGmbxyY[24][3] = {
+    {0.400f, 0.350f, 10.1f}, {0.377f, 0.345f, 35.8f}, {0.247f, 0.251f, 19.3f}, {0.337f, 0.422f, 13.3f},
+    {0.265f, 0.240f, 24.3f}, {0.261f, 0.343f, 43.1f}, {0.506f, 0.407f, 30.1f}, {0.211f, 0.175f, 12.0f},
+    {0.453f, 0.306f, 19.8f}, {0.285f, 0.202f, 6.6f},  {0.380f, 0.489f, 44.3f}, {0.473f, 0.438f, 43.1f},
+    {0.187f, 0.129f, 6.1f},  {0.305f, 0.478f, 23.4f}, {0.539f, 0.313f, 12.0f}, {0.448f, 0.470f, 59.1f},
+    {0.364f, 0.233f, 19.8f}, {0.196f, 0.252f, 19.8f}, {0.310f, 0.316f, 90.0f}, {0.310f, 0.316f, 59.1f},
+    {0.310f, 0.316f, 36.2f}, {0.310f, 0.316f, 19.8f}, {0.310f, 0.316f, 9.0f},  {0.310f, 0.316f, 3.1f}};
+
+// pseudoinverse of a 24x3 matrix (gls_linalg.hpp:559-590, after dcraw)
+void pseudoinverse(const float in[24][3], float out[24][3]) {
+    float work[3][6];
+    for (int i = 0; i < 3; i++) {
+        for (int j = 0; j < 6; j++) work[i][j] = j == i + 3 ? 1.0f : 0.0f;
+        for (int j = 0; j < 3; j++)
+            for (int k = 0; k < 24; k++) work[i][j] += in[k][i] * in[k][j];
+    }
+    for (int i = 0; i < 3; i++) {
+        float num = work[i][i];
+        for (int j = 0; j < 6; j++) work[i][j] /= num;
+        for (int k = 0; k < 3; k++) {
+            if (k == i) continue;
+            num = work[k][i];
+            for (int j = 0; j < 6; j++) work[k][j] -= work[i][j] * num;
+        }
+    }
+    for (int i = 0; i < 24; i++)
+        for (int j = 0; j < 3; j++) {
+            float acc = 0;
+            for (int k = 0; k < 3; k++) acc += work[j][k + 3] * in[i][k];
+            out[i][j] = acc;
+        }
+}
+
+// {a, b} of the least-squares line through (x, y), six points
+void regress6(const float x[6], const float y[6], float* a, float* b) {
+    double sx = 0.0, sy = 0.0, sxx = 0.0, sxy = 0.0;
+    for (int i = 0; i < 6; i++) sx = sx + x[i];
+    for (int i = 0; i < 6; i++) sy = sy + y[i];
+    for (int i = 0; i < 6; i++) sxx = sxx + (double)(x[i] * x[i]);
+    for (int i = 0; i < 6; i++) sxy = sxy + (double)(x[i] * y[i]);
+    const double n = 6.0;
+    const double bb = (n * sxy - sx * sy) / (n * sxx - sx * sx);
+    const double aa = (sy - bb * sx) / n;
+    *a = (float)aa;
+    *b = (float)bb;
+}
+
+// estimateRawParameters: cam_xyz (3x3), pre_mul (3), raw NLF slopes {r, g, b, g2}; false when
+// cam_xyz_coeff rejects the matrix (a camera white at or below 1e-5)
+bool estimate(const float mean[24][4], const float var[24][4], float cam_xyz[9], float pre_mul[3], float nlf[4]) {
+    float xyz[24][3], inv[24][3];
+    for (int q = 0; q < 24; q++) {
+        const float x = kGmbxyY[q][0], y = kGmbxyY[q][1], Y = kGmbxyY[q][2];
+        xyz[q][0] = Y * x / y;
+        xyz[q][1] = Y;
+        xyz[q][2] = Y * (1 - x - y) / y;
+    }
+    pseudoinverse(xyz, inv);
+    float cx[9];
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+            float acc = 0;
+            for (int k = 0; k < 24; k++) acc += mean[k][i] * inv[k][j];
+            cx[3 * i + j] = acc;
+        }
+    // cam_xyz_coeff's white point (its matrix is dropped); it rejects a white <= 1e-5
+    {
+        M3 m, rgb_cam;
+        memcpy(m, cx, sizeof(M3));
+        mat_mul(m, kXyzRgb, rgb_cam);
+        for (int i = 0; i < 3; i++) {
+            float s = 0;
+            for (int k = 0; k < 3; k++) s += rgb_cam[i][k] * 1.0f;
+            if (!((double)s > 0.00001)) return false;
+            pre_mul[i] = 1 / s;
+        }
+    }
+    const float norm = cx[3] + cx[4] + cx[5];
+    for (int k = 0; k < 9; k++) cam_xyz[k] = cx[k] / norm;
+    const float p1 = pre_mul[1];
+    for (int k = 0; k < 3; k++) pre_mul[k] = pre_mul[k] / p1;
+    const int order[6] = {23, 22, 21, 20, 19, 18};  // Black, Neutral 3.5, 5, 6.5, 8, White
+    for (int c = 0; c < 4; c++) {
+        float x[6], y[6], a;
+        for (int i = 0; i < 6; i++) {
+            x[i] = mean[order[i]][c];
+            y[i] = var[order[i]][c];
+        }
+        regress6(x, y, &a, &nlf[c]);
+    }
+    return true;
+}
+
+}  // namespace calib
+
+// ---------------------------------------------------------------------------------------
 // Lossless JPEG (ITU-T T.81 process 14, SOF3) as DNG stores raw tiles and strips: the
 // decoder restates DecodeLosslessJPEG (src/gls_dng_lossless_jpeg.cpp:540-2142) -- marker
 // parsing, Huffman decoding with its 8-bit lookup and its rules for invalid codes (17 bits
@@ -2333,6 +2501,26 @@ long oracle_lj92_decode(const uint8_t* data, long size, uint16_t* out, long max_
 long oracle_lj92_encode(const uint16_t* src, int rows, int cols, int comps, int precision, int predictor,
                         int restart_rows, uint8_t* out, long cap) {
     return lj92::encode(src, rows, cols, comps, precision, predictor, restart_rows, out, cap);
+}
+
+int oracle_color_checker_raw_stats(const uint16_t* raw, int w, int h, int stride, float black, float white,
+                                   int bayer, const int gmb[4], int rotate_180, float mean[96], float var[96]) {
+    if (bayer < 0 || bayer > 3 || !gmb) return -1;
+    (void)w;
+    (void)h;
+    calib::patch_stats(raw, stride, black, white, bayer, {gmb[0], gmb[1], gmb[2], gmb[3]}, rotate_180,
+                       reinterpret_cast<float(*)[4]>(mean), reinterpret_cast<float(*)[4]>(var));
+    return 0;
+}
+
+int oracle_estimate_raw_parameters(const uint16_t* raw, int w, int h, int stride, float black, float white, int bayer,
+                                   const int gmb[4], int rotate_180, float cam_xyz[9], float pre_mul[3],
+                                   float raw_nlf[4]) {
+    float mean[24][4], var[24][4];
+    if (oracle_color_checker_raw_stats(raw, w, h, stride, black, white, bayer, gmb, rotate_180, &mean[0][0],
+                                       &var[0][0]) != 0)
+        return -1;
+    return calib::estimate(mean, var, cam_xyz, pre_mul, raw_nlf) ? 0 : -2;
 }
 
 float oracle_atan2pi(float y, float x) { return glsm::atan2pi_(y, x); }

@@ -131,6 +131,16 @@ void oracle_matmul3x3(const float a[9], const float b[9], float out[9]);
 // project's extension (4 samples in 5 bytes, big-endian bit order).
 long oracle_unpack_bits(const uint8_t* packed, long n_bytes, int bits, uint16_t* out, long max_out);
 
+/* colorCheckerRawStats (demosaic_utils.cpp:411-533): per patch of the 6x4 chart at gmb =
+ * {x, y, width, height}, mean[24][4] and var[24][4] of the CFA channels {r, g, b, g2}. */
+int oracle_color_checker_raw_stats(const uint16_t* raw, int w, int h, int stride, float black, float white,
+                                   int bayer, const int gmb[4], int rotate_180, float mean[96], float var[96]);
+/* estimateRawParameters (demosaic_utils.cpp:686-785): cam_xyz, pre_mul (green 1) and the raw
+ * NLF slopes; -2 when the fitted matrix gives a camera white <= 1e-5 (the reference throws). */
+int oracle_estimate_raw_parameters(const uint16_t* raw, int w, int h, int stride, float black, float white, int bayer,
+                                   const int gmb[4], int rotate_180, float cam_xyz[9], float pre_mul[3],
+                                   float raw_nlf[4]);
+
 /* DecodeLosslessJPEG (src/gls_dng_lossless_jpeg.cpp:3253-3275): one stream -> its samples
  * (rows x cols x components); info = {width, height, components, precision, predictor,
  * point transform, restart interval, frame components}.  Returns the sample count, -1 for a

@@ -430,6 +430,38 @@ def lj92_encode(samples, components, precision, predictor=1, restart_rows=0, ref
     return out[:k].tobytes()
 
 
+def color_checker_raw_stats(raw, black, white, bayer, gmb, rotate_180=False):
+    """colorCheckerRawStats: (mean (24, 4), var (24, 4)) of the CFA channels per patch."""
+    raw = np.ascontiguousarray(raw, np.uint16)
+    h, w = raw.shape
+    mean = np.zeros(96, np.float32)
+    var = np.zeros(96, np.float32)
+    g = (ctypes.c_int * 4)(*gmb)
+    if lib().oracle_color_checker_raw_stats(_p(raw), w, h, w, ctypes.c_float(black), ctypes.c_float(white),
+                                            int(bayer), g, int(rotate_180), _p(mean), _p(var)) != 0:
+        raise ValueError("colorCheckerRawStats: invalid arguments")
+    return mean.reshape(24, 4), var.reshape(24, 4)
+
+
+def estimate_raw_parameters(raw, black, white, bayer, gmb, rotate_180=False, reference=False):
+    """estimateRawParameters: (cam_xyz (3, 3), pre_mul (3,), raw NLF slopes (4,)); reference=True
+    runs the reference's own code (oracle/_ref)."""
+    raw = np.ascontiguousarray(raw, np.uint16)
+    h, w = raw.shape
+    cx, pm, nlf = (ctypes.c_float * 9)(), (ctypes.c_float * 3)(), (ctypes.c_float * 4)()
+    g = (ctypes.c_int * 4)(*gmb)
+    args = (_p(raw), w, h, w, ctypes.c_float(black), ctypes.c_float(white), int(bayer), g, int(rotate_180), cx, pm, nlf)
+    if reference:
+        if ref_lib() is None:
+            raise FileNotFoundError(REF_PATH)
+        rc = ref_lib().ref_estimate_raw_parameters(*args)
+    else:
+        rc = lib().oracle_estimate_raw_parameters(*args)
+    if rc != 0:
+        raise ValueError("estimateRawParameters failed (%d)" % rc)
+    return np.array(cx[:], np.float32).reshape(3, 3), np.array(pm[:], np.float32), np.array(nlf[:], np.float32)
+
+
 # ---- host colour math ----
 
 def _m9(fn, *mats):

@@ -15,6 +15,12 @@ const char* BayerPatternName[4] = {"GRBG", "GBRG", "RGGB", "BGGR"};
 // never called from this shim.
 #include "gls_image_tiff.cpp"
 
+// colorCheckerRawStats dumps its channels as PNG files (demosaic_utils.cpp:528-531); the
+// PNG writer is not part of the path, so the shim gives it an empty body.
+namespace gls {
+void write_png_file(const std::string&, int, int, int, int, bool, int, std::function<uint8_t*(int row)>) {}
+}  // namespace gls
+
 extern "C" {
 
 void ref_cam_xyz_coeff(const float cam_xyz[9], float pre_mul[3], float rgb_cam[9]) {
@@ -107,6 +113,26 @@ long ref_lj92_encode(const uint16_t* src, int rows, int cols, int channels, int 
         gls::EncodeLosslessJPEG(src, (uint32_t)rows, (uint32_t)cols, (uint32_t)channels, (uint32_t)bit_depth,
                                 cols * channels, channels, stream);
         return (long)stream.Position();
+    } catch (...) {
+        return -1;
+    }
+}
+
+// estimateRawParameters: returns 0, or -1 when the reference throws
+int ref_estimate_raw_parameters(const uint16_t* raw, int w, int h, int stride, float black, float white, int bayer,
+                                const int gmb[4], int rotate_180, float cam_xyz[9], float pre_mul[3],
+                                float raw_nlf[4]) {
+    try {
+        auto* px = reinterpret_cast<gls::luma_pixel_16*>(const_cast<uint16_t*>(raw));
+        const gls::image<gls::luma_pixel_16> img(w, h, stride, std::span<gls::luma_pixel_16>(px, (size_t)stride * h));
+        gls::Matrix<3, 3> cx;
+        gls::Vector<3> pm;
+        const gls::rectangle r = {gmb[0], gmb[1], gmb[2], gmb[3]};
+        const auto nlf = estimateRawParameters(img, &cx, &pm, black, white, (BayerPattern)bayer, r, rotate_180 != 0);
+        for (int i = 0; i < 9; i++) cam_xyz[i] = cx[i / 3][i % 3];
+        for (int i = 0; i < 3; i++) pre_mul[i] = pm[i];
+        for (int i = 0; i < 4; i++) raw_nlf[i] = nlf[i];
+        return 0;
     } catch (...) {
         return -1;
     }

@@ -3,7 +3,7 @@
 The reference's colour math (cam_xyz_coeff, cam_ycbcr, gls::inverse, matrix products from
 CLImage/app/src/main/cpp/demosaic_utils.cpp and src/gls_linalg.hpp) and its packed-raw
 unpack routines (src/gls_image_tiff.cpp:53-87) and autoWhiteBalance (demosaic_utils.cpp:
-976-1026) and the lossless-JPEG codec (src/gls_dng_lossless_jpeg.cpp) are compiled from the
+976-1026), estimateRawParameters (686-785) and the lossless-JPEG codec (src/gls_dng_lossless_jpeg.cpp) are compiled from the
 reference sources into oracle/_ref/libref_host.so (make -C oracle ref); this script runs them
 on fixed inputs and stores the results bit-exactly.  It also records hashes of the oracle's own
 pipeline outputs on small seeded frames, which pin the oracle across machines.
@@ -109,6 +109,20 @@ def lj92_fixture():
     return streams, meta
 
 
+def calib_fixture():
+    """estimateRawParameters of the reference (demosaic_utils.cpp:686-785) on the seeded chart
+    frames of tests/calib_frames.py; its colorCheckerRawStats writes debug PNGs through a
+    writer the shim leaves empty."""
+    from tests import calib_frames
+    out = {}
+    for case in calib_frames.CASES:
+        raw, black, white, bayer, gmb, rot = calib_frames.make(case)
+        cx, pm, nlf = orc.estimate_raw_parameters(raw, black, white, bayer, gmb, rot, reference=True)
+        out[case[0]] = {"raw_sha256": hashlib.sha256(raw.tobytes()).hexdigest(), "cam_xyz": bits(cx),
+                        "pre_mul": bits(pm), "raw_nlf": bits(nlf)}
+    return out
+
+
 def oracle_pins():
     pins = {}
     for name, (w, h, bayer, prec, levels) in {
@@ -141,6 +155,8 @@ def main():
     np.savez_compressed(os.path.join(HERE, "ref_lj92.npz"), **streams)
     with open(os.path.join(HERE, "ref_lj92.json"), "w") as f:
         json.dump(meta, f, indent=1)
+    with open(os.path.join(HERE, "ref_calib.json"), "w") as f:
+        json.dump(calib_fixture(), f, indent=1)
     with open(os.path.join(HERE, "oracle_pins.json"), "w") as f:
         json.dump(oracle_pins(), f, indent=1)
     print("golden fixtures written to", HERE)

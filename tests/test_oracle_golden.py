@@ -103,6 +103,23 @@ def test_lj92_round_trip():
         np.testing.assert_array_equal(dec, x, err_msg=name)
 
 
+def test_estimate_raw_parameters_equals_reference():
+    """The oracle's colour-checker calibration gives the reference's matrix, white point and
+    noise slopes bit for bit (one chart rotated by 180 degrees, one at odd coordinates)."""
+    from tests import calib_frames
+    with open(os.path.join(GOLDEN, "ref_calib.json")) as f:
+        golden = json.load(f)
+    assert set(golden) == {c[0] for c in calib_frames.CASES}
+    for case in calib_frames.CASES:
+        fx = golden[case[0]]
+        raw, black, white, bayer, gmb, rot = calib_frames.make(case)
+        assert hashlib.sha256(raw.tobytes()).hexdigest() == fx["raw_sha256"], case[0]
+        cx, pm, nlf = orc.estimate_raw_parameters(raw, black, white, bayer, gmb, rot)
+        for got, key in ((cx, "cam_xyz"), (pm, "pre_mul"), (nlf, "raw_nlf")):
+            np.testing.assert_array_equal(np.ravel(got).view(np.uint32), np.array(fx[key], np.uint32),
+                                          err_msg=case[0] + " " + key)
+
+
 def test_unpack_round_trip_all_depths():
     rng = np.random.default_rng(9)
     for nbits in (10, 12, 14, 16):
