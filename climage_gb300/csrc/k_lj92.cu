@@ -39,6 +39,7 @@ constexpr int kSegBits = 2048;    // bits per speculative segment
 constexpr int kChunk = 4096;      // source bytes per de-stuffing chunk
 constexpr int kSyncRounds = 2;    // parallel resynchronisation rounds before the walk
 constexpr int kPad = 16;          // zero bytes after each interval's de-stuffed data
+constexpr int kBnd = 8;           // MCU starts remembered per segment from the first pass
 
 struct LjTable {
     uint16_t look[256];  // (code length << 8) | value for codes of at most 8 bits; 0: longer
@@ -87,6 +88,9 @@ struct LjDev {
     int* chunk_stuff;
     long long* chunk_off;
     long long* start_used;  // per segment
+    long long* bnd;         // per segment: the first kBnd MCU starts of the pass-1 decode
+    int* p1cnt;             // per segment: MCUs of the pass-1 decode (from the segment's first bit)
+    int8_t* p1;             // per segment: the segment's values are still the pass-1 decode
     long long* end_a;
     long long* end_b;
     int* cnt;
@@ -317,7 +321,7 @@ __global__ void __launch_bounds__(256) lj_destuff_kernel(LjDev g) {
 // ---- speculative decoding ----
 
 __device__ __forceinline__ void seg_decode(const LjDev& g, int seg, long long start, long long* end_out,
-                                           int* cnt_out) {
+                                           int* cnt_out, long long* bnd = nullptr) {
     const int I = g.seg_interval[seg];
     const LjInterval iv = g.intervals[I];
     const LjStream st = g.streams[iv.stream];
@@ -333,13 +337,18 @@ __device__ __forceinline__ void seg_decode(const LjDev& g, int seg, long long st
         const long long want = (limit - pos + st.zero_mcu_bits - 1) / max(st.zero_mcu_bits, 1);
         const long long z = zero_mcus(st, base, pos, j > 0 ? want : min(want, total - n));
         if (z > 0) {
+            if (bnd)
+                for (long long m = 0; m < z && n + m < kBnd; m++) bnd[n + m] = pos + m * st.zero_mcu_bits;
             pos += z * st.zero_mcu_bits;
             n += (int)z;
             continue;
         }
+        if (bnd && n < kBnd) bnd[n] = pos;
         pos += mcu_bits(g, st, base, pos, d, &bad);
         n++;
     }
+    if (bnd)
+        for (int k = n; k < kBnd; k++) bnd[k] = -1;
     *end_out = pos;
     *cnt_out = n;
 }
@@ -355,13 +364,16 @@ __global__ void lj_phase1_kernel(LjDev g, int nseg) {
     if (j > 0 && start >= g.dlen[I] * 8) {
         g.end_a[seg] = start;
         g.cnt[seg] = 0;
+        g.p1[seg] = 0;
         return;
     }
     long long e;
     int n;
-    seg_decode(g, seg, start, &e, &n);
+    seg_decode(g, seg, start, &e, &n, g.bnd + (size_t)seg * kBnd);
     g.end_a[seg] = e;
     g.cnt[seg] = n;
+    g.p1cnt[seg] = n;
+    g.p1[seg] = 1;
 }
 
 // One resynchronisation round: a segment whose start differs from the end its predecessor
@@ -378,11 +390,21 @@ __global__ void lj_sync_kernel(LjDev g, int nseg, const long long* end_in, long 
     if (j == 0 || (long long)j * kSegBits >= g.dlen[I] * 8) return;
     const long long s = end_in[seg - 1];
     if (s == g.start_used[seg]) return;
+    if (g.p1[seg]) {  // the new start is an MCU start of the first pass: the rest of its path
+        const long long* b = g.bnd + (size_t)seg * kBnd;
+        for (int k = 0; k < kBnd; k++)
+            if (b[k] == s) {
+                g.start_used[seg] = s;
+                g.cnt[seg] = g.p1cnt[seg] - k;
+                return;
+            }
+    }
     long long e;
     int n;
     seg_decode(g, seg, s, &e, &n);
     g.start_used[seg] = s;
     g.cnt[seg] = n;
+    g.p1[seg] = 0;
     end_out[seg] = e;
 }
 
@@ -419,6 +441,7 @@ __global__ void lj_repair_kernel(LjDev g, int nseg, const long long* ends_in, lo
         seg_decode(g, sk, start, &e, &n);
         g.start_used[sk] = start;
         g.cnt[sk] = n;
+        g.p1[sk] = 0;
         ends_out[sk] = e;
         if (!next) break;
         k++;
@@ -440,11 +463,17 @@ __global__ void __launch_bounds__(256) lj_walk_kernel(LjDev g, long long* ends, 
     __shared__ int s_n;
     if (threadIdx.x == 0) s_n = 0;
     __syncthreads();
-    for (int b = 1; b < nact; b += 256) {
-        const int j = b + threadIdx.x;
-        const int f = (j < nact && g.start_used[iv.seg_base + j] != ends[iv.seg_base + j - 1]) ? 1 : 0;
-        const int off = block_exclusive<int>(f, &s_n);
-        if (f) list[iv.seg_base + off] = j;
+    for (int b = 1; b < nact; b += 256 * 16) {
+        const int j0 = b + threadIdx.x * 16;
+        unsigned f = 0;
+#pragma unroll
+        for (int k = 0; k < 16; k++) {
+            const int j = j0 + k;
+            if (j < nact && g.start_used[iv.seg_base + j] != ends[iv.seg_base + j - 1]) f |= 1u << k;
+        }
+        int off = block_exclusive<int>(__popc(f), &s_n);
+        for (int k = 0; k < 16; k++)
+            if (f & (1u << k)) list[iv.seg_base + off++] = j0 + k;
     }
     if (threadIdx.x != 0) return;
     int fixed = 0;
@@ -460,6 +489,7 @@ __global__ void __launch_bounds__(256) lj_walk_kernel(LjDev g, long long* ends, 
             const long long old = ends[seg];
             g.start_used[seg] = start;
             g.cnt[seg] = n;
+            g.p1[seg] = 0;
             ends[seg] = e;
             fixed = k;
             if (e == old || k + 1 >= nact) break;
@@ -469,17 +499,29 @@ __global__ void __launch_bounds__(256) lj_walk_kernel(LjDev g, long long* ends, 
     }
 }
 
-// per interval: exclusive scan of the segment counts (one block per interval)
+constexpr int kScanPer = 16;  // consecutive elements per thread in the per-interval scans
+
+// per interval: exclusive scan of the segment counts (one block per interval, kScanPer
+// consecutive segments per thread)
 __global__ void __launch_bounds__(256) lj_count_scan_kernel(LjDev g) {
     const LjInterval iv = g.intervals[blockIdx.x];
     __shared__ long long s_carry;
     if (threadIdx.x == 0) s_carry = 0;
     __syncthreads();
-    for (int b = 0; b < iv.nseg; b += 256) {
-        const int j = b + threadIdx.x;
-        const long long v = j < iv.nseg ? g.cnt[iv.seg_base + j] : 0;
-        const long long off = block_exclusive<long long>(v, &s_carry);
-        if (j < iv.nseg) g.seg_off[iv.seg_base + j] = off;
+    for (int b = 0; b < iv.nseg; b += 256 * kScanPer) {
+        const int j0 = b + threadIdx.x * kScanPer;
+        long long v[kScanPer], tot = 0;
+#pragma unroll
+        for (int k = 0; k < kScanPer; k++) {
+            v[k] = j0 + k < iv.nseg ? g.cnt[iv.seg_base + j0 + k] : 0;
+            tot += v[k];
+        }
+        long long off = block_exclusive<long long>(tot, &s_carry);
+#pragma unroll
+        for (int k = 0; k < kScanPer; k++) {
+            if (j0 + k < iv.nseg) g.seg_off[iv.seg_base + j0 + k] = off;
+            off += v[k];
+        }
     }
 }
 
@@ -941,6 +983,9 @@ extern "C" gls_status gls_dng_decode_lossless_jpeg(gls_ctx* ctx, const uint8_t* 
     const size_t o_cst = carve<int>(off, std::max(nchunk, 1));
     const size_t o_coff = carve<long long>(off, std::max(nchunk, 1));
     const size_t o_su = carve<long long>(off, nseg);
+    const size_t o_bnd = carve<long long>(off, (size_t)nseg * kBnd);
+    const size_t o_p1c = carve<int>(off, nseg);
+    const size_t o_p1 = carve<int8_t>(off, nseg);
     const size_t o_ea = carve<long long>(off, nseg);
     const size_t o_eb = carve<long long>(off, nseg);
     const size_t o_cnt = carve<int>(off, nseg);
@@ -982,6 +1027,9 @@ extern "C" gls_status gls_dng_decode_lossless_jpeg(gls_ctx* ctx, const uint8_t* 
     g.chunk_stuff = (int*)(S + o_cst);
     g.chunk_off = (long long*)(S + o_coff);
     g.start_used = (long long*)(S + o_su);
+    g.bnd = (long long*)(S + o_bnd);
+    g.p1cnt = (int*)(S + o_p1c);
+    g.p1 = (int8_t*)(S + o_p1);
     g.end_a = (long long*)(S + o_ea);
     g.end_b = (long long*)(S + o_eb);
     g.cnt = (int*)(S + o_cnt);
