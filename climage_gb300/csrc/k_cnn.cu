@@ -246,6 +246,8 @@ __global__ void __launch_bounds__(CT) conv3x3_kernel(ConvArgs a) {
 constexpr int TC5_R = 16, TC5_C = 8;  // output tile rows x columns
 constexpr int TC5_HR = TC5_R + 2, TC5_HC = TC5_C + 2;
 constexpr uint32_t kWaitLimit = 1u << 24;
+constexpr int kTc5Stack = 2;         // 16x8 tiles per persistent-block iteration
+constexpr int kTc5BlocksPerSm = 3;   // resident blocks per SM (shared memory: 62 KB each)
 
 __device__ __forceinline__ int cdiv_d(int a, int b) { return (a + b - 1) / b; }
 
@@ -264,44 +266,57 @@ __device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, bool v
 // Persistent: each block stages the weights once and walks tiles blockIdx.x, + gridDim.x,
 // ...; the halo of the next tile streams in (cp.async, zero-filled outside the image) into
 // the other of two buffers while the current tile's MMAs and epilogue run.
-__global__ void __launch_bounds__(CT) conv3x3_tc05_kernel(ConvArgs a, int nimg, int* err) {
-    constexpr int HALO_N = 4 * TC5_HR * TC5_HC, HALO_B = HALO_N * 16, W_B = 9 * 4 * 32 * 16;
-    __shared__ __align__(128) unsigned char s_a[2][HALO_B];
-    __shared__ __align__(128) unsigned char s_b[W_B];
+// MT stacked 16x8 tiles per iteration (MT * 128 threads, MT 32-column accumulators): more
+// work per barrier and per wait; dynamic shared memory (two halo buffers + the weights).
+template <int MT>
+struct Tc5 {
+    static constexpr int R = 16 * MT, HR = R + 2, HC = TC5_C + 2;
+    static constexpr int HALO_N = 4 * HR * HC, HALO_B = HALO_N * 16, W_B = 9 * 4 * 32 * 16;
+    static constexpr int THREADS = 128 * MT, COLS = 32 * MT;
+    static constexpr int SMEM = 2 * HALO_B + W_B;
+};
+
+template <int MT>
+__global__ void __launch_bounds__(Tc5<MT>::THREADS) conv3x3_tc05_kernel(ConvArgs a, int nimg, int* err) {
+    using K = Tc5<MT>;
+    extern __shared__ __align__(128) unsigned char tc5_smem[];
+    unsigned char* s_a0 = tc5_smem;
+    unsigned char* s_b = tc5_smem + 2 * K::HALO_B;
     __shared__ __align__(8) uint64_t s_bar;
     __shared__ uint32_t s_taddr;
     __shared__ float s_bias[32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t bar = smem_u32(&s_bar);
-    const int tiles_x = cdiv_d(a.w, TC5_C), tiles_y = cdiv_d(a.h, TC5_R);
+    const int tiles_x = cdiv_d(a.w, TC5_C), tiles_y = cdiv_d(a.h, K::R);
     if (threadIdx.x < 32) s_bias[threadIdx.x] = a.bias[threadIdx.x];
     const int tiles_img = tiles_x * tiles_y, ntiles = tiles_img * nimg;
 
     if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 32;\n" ::"r"(smem_u32(&s_taddr)));
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&s_taddr)),
+                     "n"(K::COLS));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
     }
     if (threadIdx.x == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar));
         asm volatile("fence.mbarrier_init.release.cluster;\n");
     }
-    for (int i = threadIdx.x; i < 9 * 4 * 32; i += CT) {
+    for (int i = threadIdx.x; i < 9 * 4 * 32; i += K::THREADS) {
         const int tap = i / 128, r = i - tap * 128, cb = r / 32, n = r - cb * 32;
         *reinterpret_cast<uint4*>(s_b + (size_t)i * 16) =
             *reinterpret_cast<const uint4*>(a.wt + (size_t)n * 288 + tap * 32 + cb * 8);
     }
     auto prefetch = [&](int t, int buf) {
         const int img = t / tiles_img, tt = t - img * tiles_img;
-        const int x0 = (tt % tiles_x) * TC5_C, y0 = (tt / tiles_x) * TC5_R;
+        const int x0 = (tt % tiles_x) * TC5_C, y0 = (tt / tiles_x) * K::R;
         const __nv_bfloat16* in = (const __nv_bfloat16*)a.in + img * a.in_stride;
-        const uint32_t base = smem_u32(s_a[buf]);
-        for (int i = threadIdx.x; i < HALO_N; i += CT) {
+        const uint32_t base = smem_u32(s_a0 + buf * K::HALO_B);
+        for (int i = threadIdx.x; i < K::HALO_N; i += K::THREADS) {
             // consecutive threads take consecutive 16-byte pieces of a pixel's 64 bytes
             const int p = i >> 2, cb = i & 3;
-            const int r = p / TC5_HC, c = p - r * TC5_HC;
+            const int r = p / K::HC, c = p - r * K::HC;
             const int x = x0 - 1 + c, y = y0 - 1 + r;
             const bool ok = x >= 0 && x < a.w && y >= 0 && y < a.h;
-            cp_async16(base + (uint32_t)(cb * TC5_HR * TC5_HC + p) * 16,
+            cp_async16(base + (uint32_t)(cb * K::HR * K::HC + p) * 16,
                        ok ? (const void*)(in + ((size_t)y * a.w + x) * 32 + cb * 8) : (const void*)in, ok);
         }
     };
@@ -322,20 +337,23 @@ __global__ void __launch_bounds__(CT) conv3x3_tc05_kernel(ConvArgs a, int nimg, 
         __syncthreads();
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
         if (threadIdx.x == 0) {
-            const uint32_t abase = smem_u32(s_a[buf]), bbase = smem_u32(s_b);
+            const uint32_t abase = smem_u32(s_a0 + buf * K::HALO_B), bbase = smem_u32(s_b);
+            const uint64_t a0 = tc5_desc(abase, K::HR * K::HC * 16, K::HC * 16);
+            const uint64_t b0 = tc5_desc(bbase, 32 * 16, 8 * 16);
 #pragma unroll 1
-            for (int tap = 0; tap < 9; tap++) {
-                const int dy = tap / 3, dx = tap % 3;
+            for (int mt = 0; mt < MT; mt++) {
 #pragma unroll
-                for (int kc = 0; kc < 2; kc++) {
-                    const uint64_t ad = tc5_desc(abase + (uint32_t)(((2 * kc * TC5_HR + dy) * TC5_HC + dx) * 16),
-                                                 TC5_HR * TC5_HC * 16, TC5_HC * 16);
-                    const uint64_t bd = tc5_desc(bbase + (uint32_t)((tap * 4 + 2 * kc) * 32 * 16), 32 * 16, 8 * 16);
-                    const uint32_t acc = (tap | kc) ? 1u : 0u;
-                    asm volatile(
-                        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-                        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(taddr),
-                        "l"(ad), "l"(bd), "r"(kIdescBf16M128N32), "r"(acc));
+                for (int tap = 0; tap < 9; tap++) {
+#pragma unroll
+                    for (int kc = 0; kc < 2; kc++) {
+                        const uint64_t ad =
+                            a0 + (uint64_t)((((2 * kc * K::HR + tap / 3 + 16 * mt) * K::HC + tap % 3) * 16) >> 4);
+                        const uint64_t bd = b0 + (uint64_t)(((tap * 4 + 2 * kc) * 32 * 16) >> 4);
+                        asm volatile(
+                            "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(taddr + 32u * mt),
+                            "l"(ad), "l"(bd), "r"(kIdescBf16M128N32), "r"((tap | kc) ? 1u : 0u));
+                    }
                 }
             }
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar)
@@ -356,6 +374,7 @@ __global__ void __launch_bounds__(CT) conv3x3_tc05_kernel(ConvArgs a, int nimg, 
         }
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
         {
+            const int mt = warp >> 2, q = warp & 3;  // warp -> (tile, TMEM lane quarter)
             uint32_t v[32];
             asm volatile(
                 "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
@@ -365,11 +384,11 @@ __global__ void __launch_bounds__(CT) conv3x3_tc05_kernel(ConvArgs a, int nimg, 
                   "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
                   "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]),
                   "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
-                : "r"(taddr + ((uint32_t)(warp * 32) << 16)));
+                : "r"(taddr + ((uint32_t)(q * 32) << 16) + 32u * mt));
             asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
             const int img = t / tiles_img, tt = t - img * tiles_img;
-            const int m = warp * 32 + lane;
-            const int x = (tt % tiles_x) * TC5_C + (m & 7), y = (tt / tiles_x) * TC5_R + (m >> 3);
+            const int m = q * 32 + lane;
+            const int x = (tt % tiles_x) * TC5_C + (m & 7), y = (tt / tiles_x) * K::R + 16 * mt + (m >> 3);
             if (x < a.w && y < a.h) {
                 __nv_bfloat16 o[32];
 #pragma unroll
@@ -378,7 +397,7 @@ __global__ void __launch_bounds__(CT) conv3x3_tc05_kernel(ConvArgs a, int nimg, 
                 uint4* dst =
                     reinterpret_cast<uint4*>((__nv_bfloat16*)a.out + img * a.out_stride + ((size_t)y * a.w + x) * 32);
 #pragma unroll
-                for (int q = 0; q < 4; q++) dst[q] = reinterpret_cast<const uint4*>(o)[q];
+                for (int qq = 0; qq < 4; qq++) dst[qq] = reinterpret_cast<const uint4*>(o)[qq];
             }
         }
         asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
@@ -387,7 +406,7 @@ __global__ void __launch_bounds__(CT) conv3x3_tc05_kernel(ConvArgs a, int nimg, 
     asm volatile("cp.async.wait_group 0;\n" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 32;\n" ::"r"(taddr));
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(taddr), "n"(K::COLS));
 }
 
 // ---------------------------------------------------------------------------------------
@@ -1047,9 +1066,19 @@ struct gls_cnn {
             if (backend == 1) {
                 ConvArgs a{act[l - 1], 32, wfwd[l], b + off[l] + 32 * 9 * 32, act[l], 32, nullptr, w, h,
                            px * 32, px * 32, 0};
-                const int tiles = cdiv(w, TC5_C) * cdiv(h, TC5_R) * n;
-                const int per = 4 * (ctx->num_sms > 0 ? ctx->num_sms : 148);
-                conv3x3_tc05_kernel<<<tiles < per ? tiles : per, CT, 0, ctx->stream>>>(a, n, err_dev);
+                using K = Tc5<kTc5Stack>;
+                static bool attr_set = false;
+                if (!attr_set) {
+                    GLS_CHECK(check_cuda(ctx, cudaFuncSetAttribute(conv3x3_tc05_kernel<kTc5Stack>,
+                                                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                                   K::SMEM),
+                                         "cudaFuncSetAttribute(tcgen05 convolution)"));
+                    attr_set = true;
+                }
+                const int tiles = cdiv(w, TC5_C) * cdiv(h, K::R) * n;
+                const int per = kTc5BlocksPerSm * (ctx->num_sms > 0 ? ctx->num_sms : 148);
+                conv3x3_tc05_kernel<kTc5Stack>
+                    <<<tiles < per ? tiles : per, K::THREADS, K::SMEM, ctx->stream>>>(a, n, err_dev);
                 ctx->launches++;
             } else {
                 conv<32, 32, 0, false>(act[l - 1], 32, px * 32, wfwd[l], b + off[l] + 32 * 9 * 32, act[l], 32,
