@@ -258,6 +258,7 @@ __device__ __forceinline__ uint64_t tc5_desc(uint32_t saddr, uint32_t lbo, uint3
 
 // kind::f16, BF16 A and B (K-major), FP32 D, M = 128, N = 32
 constexpr uint32_t kIdescBf16M128N32 = (1u << 4) | (1u << 7) | (1u << 10) | ((32u >> 3) << 17) | ((128u >> 4) << 24);
+constexpr uint32_t kIdescBf16M128N16 = (1u << 4) | (1u << 7) | (1u << 10) | ((16u >> 3) << 17) | ((128u >> 4) << 24);
 
 __device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, bool valid) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(valid ? 16 : 0) : "memory");
@@ -268,17 +269,26 @@ __device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, bool v
 // the other of two buffers while the current tile's MMAs and epilogue run.
 // MT stacked 16x8 tiles per iteration (MT * 128 threads, MT 32-column accumulators): more
 // work per barrier and per wait; dynamic shared memory (two halo buffers + the weights).
-template <int MT>
+// MODE 0: a hidden 32 -> 32 layer (bf16 in and out, bias + ReLU)
+// MODE 1: the first layer: fp32 input (R, G, B, sigma scaled), one 8-channel plane per pixel
+//         (4 channels + 4 zeros); its K = 16 reads the second core matrix 16 bytes on (the
+//         next pixel, finite) against zero weights
+// MODE 2: the head: 32 -> 4 channels (N = 16, weight rows 8..15 zero), fp32 out, bias only
+template <int MT, int MODE>
 struct Tc5 {
     static constexpr int R = 16 * MT, HR = R + 2, HC = TC5_C + 2;
-    static constexpr int HALO_N = 4 * HR * HC, HALO_B = HALO_N * 16, W_B = 9 * 4 * 32 * 16;
+    static constexpr int CB = MODE == 1 ? 1 : 4;    // 8-channel planes of the halo
+    static constexpr int WCB = MODE == 1 ? 2 : 4;   // 8-channel blocks of the weights
+    static constexpr int NB = MODE == 2 ? 16 : 32;  // MMA N
+    static constexpr int KCS = MODE == 1 ? 1 : 2;   // K steps of 16 per tap
+    static constexpr int HALO_N = CB * HR * HC, HALO_B = HALO_N * 16, W_B = 9 * WCB * NB * 16;
     static constexpr int THREADS = 128 * MT, COLS = 32 * MT;
     static constexpr int SMEM = 2 * HALO_B + W_B;
 };
 
-template <int MT>
-__global__ void __launch_bounds__(Tc5<MT>::THREADS) conv3x3_tc05_kernel(ConvArgs a, int nimg, int* err) {
-    using K = Tc5<MT>;
+template <int MT, int MODE>
+__global__ void __launch_bounds__(Tc5<MT, MODE>::THREADS) conv3x3_tc05_kernel(ConvArgs a, int nimg, int* err) {
+    using K = Tc5<MT, MODE>;
     extern __shared__ __align__(128) unsigned char tc5_smem[];
     unsigned char* s_a0 = tc5_smem;
     unsigned char* s_b = tc5_smem + 2 * K::HALO_B;
@@ -288,7 +298,12 @@ __global__ void __launch_bounds__(Tc5<MT>::THREADS) conv3x3_tc05_kernel(ConvArgs
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t bar = smem_u32(&s_bar);
     const int tiles_x = cdiv_d(a.w, TC5_C), tiles_y = cdiv_d(a.h, K::R);
-    if (threadIdx.x < 32) s_bias[threadIdx.x] = a.bias[threadIdx.x];
+    if (threadIdx.x < 32) s_bias[threadIdx.x] = threadIdx.x < (MODE == 2 ? 4 : 32) ? a.bias[threadIdx.x] : 0.0f;
+    if (MODE == 1) {  // everything the tensor cores may read stays finite
+        for (int i = threadIdx.x; i < 2 * K::HALO_B / 16; i += K::THREADS)
+            reinterpret_cast<uint4*>(tc5_smem)[i] = make_uint4(0, 0, 0, 0);
+        __syncthreads();  // before the first halo lands in the same bytes
+    }
     const int tiles_img = tiles_x * tiles_y, ntiles = tiles_img * nimg;
 
     if (warp == 0) {
@@ -300,14 +315,38 @@ __global__ void __launch_bounds__(Tc5<MT>::THREADS) conv3x3_tc05_kernel(ConvArgs
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar));
         asm volatile("fence.mbarrier_init.release.cluster;\n");
     }
-    for (int i = threadIdx.x; i < 9 * 4 * 32; i += K::THREADS) {
-        const int tap = i / 128, r = i - tap * 128, cb = r / 32, n = r - cb * 32;
-        *reinterpret_cast<uint4*>(s_b + (size_t)i * 16) =
-            *reinterpret_cast<const uint4*>(a.wt + (size_t)n * 288 + tap * 32 + cb * 8);
+    // weights [tap][8-channel block][n][8] from the packed [nout_p][9][cin_p]
+    for (int i = threadIdx.x; i < 9 * K::WCB * K::NB; i += K::THREADS) {
+        const int tap = i / (K::WCB * K::NB), r = i - tap * K::WCB * K::NB, cb = r / K::NB, n = r - cb * K::NB;
+        constexpr int CINP = MODE == 1 ? 16 : 32;
+        uint4 v = make_uint4(0, 0, 0, 0);
+        if (MODE != 2 || n < 8)
+            v = *reinterpret_cast<const uint4*>(a.wt + (size_t)n * 9 * CINP + tap * CINP + cb * 8);
+        *reinterpret_cast<uint4*>(s_b + (size_t)i * 16) = v;
     }
     auto prefetch = [&](int t, int buf) {
         const int img = t / tiles_img, tt = t - img * tiles_img;
         const int x0 = (tt % tiles_x) * TC5_C, y0 = (tt / tiles_x) * K::R;
+        if (MODE == 1) {  // fp32 network input: plain loads, converted to bf16
+            const float* in = (const float*)a.in + img * a.in_stride;
+            unsigned char* dst = s_a0 + buf * K::HALO_B;
+            for (int p = threadIdx.x; p < K::HR * K::HC; p += K::THREADS) {
+                const int r = p / K::HC, c = p - r * K::HC;
+                const int x = x0 - 1 + c, y = y0 - 1 + r;
+                __nv_bfloat16 v[8];
+#pragma unroll
+                for (int q = 0; q < 8; q++) v[q] = __float2bfloat16_rn(0.0f);
+                if (x >= 0 && x < a.w && y >= 0 && y < a.h) {
+                    const float4 f = __ldg(reinterpret_cast<const float4*>(in + ((size_t)y * a.w + x) * 4));
+                    v[0] = __float2bfloat16_rn(f.x);
+                    v[1] = __float2bfloat16_rn(f.y);
+                    v[2] = __float2bfloat16_rn(f.z);
+                    v[3] = __float2bfloat16_rn(f.w * kSigmaScale);
+                }
+                *reinterpret_cast<uint4*>(dst + (size_t)p * 16) = *reinterpret_cast<const uint4*>(v);
+            }
+            return;
+        }
         const __nv_bfloat16* in = (const __nv_bfloat16*)a.in + img * a.in_stride;
         const uint32_t base = smem_u32(s_a0 + buf * K::HALO_B);
         for (int i = threadIdx.x; i < K::HALO_N; i += K::THREADS) {
@@ -338,21 +377,22 @@ __global__ void __launch_bounds__(Tc5<MT>::THREADS) conv3x3_tc05_kernel(ConvArgs
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
         if (threadIdx.x == 0) {
             const uint32_t abase = smem_u32(s_a0 + buf * K::HALO_B), bbase = smem_u32(s_b);
-            const uint64_t a0 = tc5_desc(abase, K::HR * K::HC * 16, K::HC * 16);
-            const uint64_t b0 = tc5_desc(bbase, 32 * 16, 8 * 16);
+            const uint64_t a0 = tc5_desc(abase, MODE == 1 ? 16 : K::HR * K::HC * 16, K::HC * 16);
+            const uint64_t b0 = tc5_desc(bbase, K::NB * 16, 8 * 16);
+            constexpr uint32_t idesc = MODE == 2 ? kIdescBf16M128N16 : kIdescBf16M128N32;
 #pragma unroll 1
             for (int mt = 0; mt < MT; mt++) {
 #pragma unroll
                 for (int tap = 0; tap < 9; tap++) {
 #pragma unroll
-                    for (int kc = 0; kc < 2; kc++) {
+                    for (int kc = 0; kc < K::KCS; kc++) {
                         const uint64_t ad =
                             a0 + (uint64_t)((((2 * kc * K::HR + tap / 3 + 16 * mt) * K::HC + tap % 3) * 16) >> 4);
-                        const uint64_t bd = b0 + (uint64_t)(((tap * 4 + 2 * kc) * 32 * 16) >> 4);
+                        const uint64_t bd = b0 + (uint64_t)(((tap * K::WCB + 2 * kc) * K::NB * 16) >> 4);
                         asm volatile(
                             "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
                             "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(taddr + 32u * mt),
-                            "l"(ad), "l"(bd), "r"(kIdescBf16M128N32), "r"((tap | kc) ? 1u : 0u));
+                            "l"(ad), "l"(bd), "r"(idesc), "r"((tap | kc) ? 1u : 0u));
                     }
                 }
             }
@@ -389,7 +429,11 @@ __global__ void __launch_bounds__(Tc5<MT>::THREADS) conv3x3_tc05_kernel(ConvArgs
             const int img = t / tiles_img, tt = t - img * tiles_img;
             const int m = q * 32 + lane;
             const int x = (tt % tiles_x) * TC5_C + (m & 7), y = (tt / tiles_x) * K::R + 16 * mt + (m >> 3);
-            if (x < a.w && y < a.h) {
+            if (MODE == 2 && x < a.w && y < a.h) {
+                *reinterpret_cast<float4*>((float*)a.out + img * a.out_stride + ((size_t)y * a.w + x) * 4) =
+                    make_float4(__uint_as_float(v[0]) + s_bias[0], __uint_as_float(v[1]) + s_bias[1],
+                                __uint_as_float(v[2]) + s_bias[2], __uint_as_float(v[3]) + s_bias[3]);
+            } else if (MODE != 2 && x < a.w && y < a.h) {
                 __nv_bfloat16 o[32];
 #pragma unroll
                 for (int n = 0; n < 32; n++)
@@ -432,7 +476,6 @@ constexpr int FU_PLANE = FU_G * FU_G * 16;  // one 8-channel plane, bytes
 constexpr int FU_ACT = 4 * FU_PLANE;        // 32 channels
 constexpr int FU_W1 = 9 * 2 * 32 * 16, FU_WH = 9 * 4 * 32 * 16, FU_W5 = 9 * 4 * 16 * 16;
 constexpr int FU_SMEM = 2 * FU_ACT + FU_W1 + 3 * FU_WH + FU_W5 + 5 * 32 * 4 + 64;  // + 2 mbarriers, TMEM address
-constexpr uint32_t kIdescBf16M128N16 = (1u << 4) | (1u << 7) | (1u << 10) | ((16u >> 3) << 17) | ((128u >> 4) << 24);
 
 struct FusedArgs {
     const float* in;  // [n][h][w][4]
@@ -1032,6 +1075,25 @@ struct gls_cnn {
         ctx->launches++;
     }
 
+    // one layer on tcgen05 (MODE as conv3x3_tc05_kernel)
+    template <int MODE>
+    gls_status tc05(const ConvArgs& a, int w, int h, int n) {
+        using K = Tc5<kTc5Stack, MODE>;
+        static bool attr_set = false;
+        if (!attr_set) {
+            GLS_CHECK(check_cuda(ctx, cudaFuncSetAttribute(conv3x3_tc05_kernel<kTc5Stack, MODE>,
+                                                           cudaFuncAttributeMaxDynamicSharedMemorySize, K::SMEM),
+                                 "cudaFuncSetAttribute(tcgen05 convolution)"));
+            attr_set = true;
+        }
+        const int tiles = cdiv(w, TC5_C) * cdiv(h, K::R) * n;
+        const int per = kTc5BlocksPerSm * (ctx->num_sms > 0 ? ctx->num_sms : 148);
+        conv3x3_tc05_kernel<kTc5Stack, MODE><<<tiles < per ? tiles : per, K::THREADS, K::SMEM, ctx->stream>>>(
+            a, n, err_dev);
+        ctx->launches++;
+        return GLS_OK;
+    }
+
     // forward over n images [n][h][w][4] fp32 -> head [n][h][w][4] fp32 (out or this->head)
     gls_status forward(const float* in, int w, int h, int n, float* out) {
         const size_t px = (size_t)w * h;
@@ -1061,30 +1123,23 @@ struct gls_cnn {
         }
         GLS_CHECK(ensure_batch((int)(px * n)));
         const float* b = master;
-        conv<16, 32, 0, true>(in, 4, px * 4, wfwd[0], b + off[0] + 32 * 9 * 4, act[0], 32, px * 32, nullptr, 0, w, h, n);
-        for (int l = 1; l < kLayers - 1; l++) {
-            if (backend == 1) {
-                ConvArgs a{act[l - 1], 32, wfwd[l], b + off[l] + 32 * 9 * 32, act[l], 32, nullptr, w, h,
-                           px * 32, px * 32, 0};
-                using K = Tc5<kTc5Stack>;
-                static bool attr_set = false;
-                if (!attr_set) {
-                    GLS_CHECK(check_cuda(ctx, cudaFuncSetAttribute(conv3x3_tc05_kernel<kTc5Stack>,
-                                                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                                   K::SMEM),
-                                         "cudaFuncSetAttribute(tcgen05 convolution)"));
-                    attr_set = true;
-                }
-                const int tiles = cdiv(w, TC5_C) * cdiv(h, K::R) * n;
-                const int per = kTc5BlocksPerSm * (ctx->num_sms > 0 ? ctx->num_sms : 148);
-                conv3x3_tc05_kernel<kTc5Stack>
-                    <<<tiles < per ? tiles : per, K::THREADS, K::SMEM, ctx->stream>>>(a, n, err_dev);
-                ctx->launches++;
-            } else {
-                conv<32, 32, 0, false>(act[l - 1], 32, px * 32, wfwd[l], b + off[l] + 32 * 9 * 32, act[l], 32,
-                                       px * 32, nullptr, 0, w, h, n);
-            }
+        if (backend == 1) {  // every layer on tcgen05
+            GLS_CHECK(tc05<1>(ConvArgs{in, 4, wfwd[0], b + off[0] + 32 * 9 * 4, act[0], 32, nullptr, w, h, px * 4,
+                                       px * 32, 0},
+                              w, h, n));
+            for (int l = 1; l < kLayers - 1; l++)
+                GLS_CHECK(tc05<0>(ConvArgs{act[l - 1], 32, wfwd[l], b + off[l] + 32 * 9 * 32, act[l], 32, nullptr, w,
+                                           h, px * 32, px * 32, 0},
+                                  w, h, n));
+            GLS_CHECK(tc05<2>(ConvArgs{act[3], 32, wfwd[4], b + off[4] + 4 * 9 * 32, out ? out : head, 4, nullptr, w,
+                                       h, px * 32, px * 4, 0},
+                              w, h, n));
+            return check_launch(ctx, "CNN forward");
         }
+        conv<16, 32, 0, true>(in, 4, px * 4, wfwd[0], b + off[0] + 32 * 9 * 4, act[0], 32, px * 32, nullptr, 0, w, h, n);
+        for (int l = 1; l < kLayers - 1; l++)
+            conv<32, 32, 0, false>(act[l - 1], 32, px * 32, wfwd[l], b + off[l] + 32 * 9 * 32, act[l], 32, px * 32,
+                                   nullptr, 0, w, h, n);
         conv<32, 8, 1, false>(act[3], 32, px * 32, wfwd[4], b + off[4] + 4 * 9 * 32, out ? out : head, 4, px * 4,
                               nullptr, 0, w, h, n);
         return check_launch(ctx, "CNN forward");
