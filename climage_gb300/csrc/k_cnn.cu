@@ -292,11 +292,11 @@ __global__ void __launch_bounds__(Tc5<MT, MODE>::THREADS) conv3x3_tc05_kernel(Co
     extern __shared__ __align__(128) unsigned char tc5_smem[];
     unsigned char* s_a0 = tc5_smem;
     unsigned char* s_b = tc5_smem + 2 * K::HALO_B;
-    __shared__ __align__(8) uint64_t s_bar;
+    __shared__ __align__(8) uint64_t s_bar[2];
     __shared__ uint32_t s_taddr;
     __shared__ float s_bias[32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t bar = smem_u32(&s_bar);
+    const uint32_t bar0 = smem_u32(&s_bar[0]);
     const int tiles_x = cdiv_d(a.w, TC5_C), tiles_y = cdiv_d(a.h, K::R);
     if (threadIdx.x < 32) s_bias[threadIdx.x] = threadIdx.x < (MODE == 2 ? 4 : 32) ? a.bias[threadIdx.x] : 0.0f;
     if (MODE == 1) {  // everything the tensor cores may read stays finite
@@ -308,11 +308,12 @@ __global__ void __launch_bounds__(Tc5<MT, MODE>::THREADS) conv3x3_tc05_kernel(Co
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&s_taddr)),
-                     "n"(K::COLS));
+                     "n"(2 * K::COLS));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
     }
     if (threadIdx.x == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar0));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar0 + 8));
         asm volatile("fence.mbarrier_init.release.cluster;\n");
     }
     // weights [tap][8-channel block][n][8] from the packed [nout_p][9][cin_p]
@@ -366,11 +367,58 @@ __global__ void __launch_bounds__(Tc5<MT, MODE>::THREADS) conv3x3_tc05_kernel(Co
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     const uint32_t taddr = s_taddr;
-    for (int it = 0; t < ntiles; t += gridDim.x, it++) {
+    // bounded wait for MMA group `it` (barrier it & 1, its (it >> 1)-th completion)
+    auto wait_mma = [&](int it) -> bool {
+        uint32_t done = 0;
+        const uint32_t b = bar0 + 8u * (uint32_t)(it & 1), parity = (uint32_t)((it >> 1) & 1);
+        for (uint32_t k = 0; k < kWaitLimit && !done; k++) {
+            asm volatile(
+                "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+                : "=r"(done)
+                : "r"(b), "r"(parity)
+                : "memory");
+        }
+        return __syncthreads_and(done) != 0;
+    };
+    // the epilogue of tile tp, whose accumulators are TMEM set s
+    auto epilogue = [&](int tp, int s) {
+        const int mt = warp >> 2, q = warp & 3;  // warp -> (tile, TMEM lane quarter)
+        uint32_t v[32];
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+            "%14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];\n"
+            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+              "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+              "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
+              "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]),
+              "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+            : "r"(taddr + ((uint32_t)(q * 32) << 16) + (uint32_t)(s * K::COLS) + 32u * mt));
+        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+        const int img = tp / tiles_img, tt = tp - img * tiles_img;
+        const int m = q * 32 + lane;
+        const int x = (tt % tiles_x) * TC5_C + (m & 7), y = (tt / tiles_x) * K::R + 16 * mt + (m >> 3);
+        if (MODE == 2 && x < a.w && y < a.h) {
+            *reinterpret_cast<float4*>((float*)a.out + img * a.out_stride + ((size_t)y * a.w + x) * 4) =
+                make_float4(__uint_as_float(v[0]) + s_bias[0], __uint_as_float(v[1]) + s_bias[1],
+                            __uint_as_float(v[2]) + s_bias[2], __uint_as_float(v[3]) + s_bias[3]);
+        } else if (MODE != 2 && x < a.w && y < a.h) {
+            __nv_bfloat16 o[32];
+#pragma unroll
+            for (int n = 0; n < 32; n++) o[n] = __float2bfloat16_rn(fmaxf(__uint_as_float(v[n]) + s_bias[n], 0.0f));
+            uint4* dst =
+                reinterpret_cast<uint4*>((__nv_bfloat16*)a.out + img * a.out_stride + ((size_t)y * a.w + x) * 32);
+#pragma unroll
+            for (int qq = 0; qq < 4; qq++) dst[qq] = reinterpret_cast<const uint4*>(o)[qq];
+        }
+    };
+    // Tile t's MMAs (accumulator set it & 1) are issued; once tile t - 1's are done, tile
+    // t + 1's halo starts into the buffer t - 1 released and t - 1's accumulators are drained
+    // while tile t's MMAs run.
+    bool ok = true;
+    int it = 0, tprev = -1;
+    for (; t < ntiles; t += gridDim.x, it++) {
         const int buf = it & 1;
-        if (t + (int)gridDim.x < ntiles) prefetch(t + gridDim.x, buf ^ 1);
-        asm volatile("cp.async.commit_group;\n" ::: "memory");
-        asm volatile("cp.async.wait_group 1;\n" ::: "memory");  // this tile's halo has landed
+        asm volatile("cp.async.wait_group 0;\n" ::: "memory");  // this tile's halo has landed
         asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
         asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
         __syncthreads();
@@ -380,6 +428,7 @@ __global__ void __launch_bounds__(Tc5<MT, MODE>::THREADS) conv3x3_tc05_kernel(Co
             const uint64_t a0 = tc5_desc(abase, MODE == 1 ? 16 : K::HR * K::HC * 16, K::HC * 16);
             const uint64_t b0 = tc5_desc(bbase, K::NB * 16, 8 * 16);
             constexpr uint32_t idesc = MODE == 2 ? kIdescBf16M128N16 : kIdescBf16M128N32;
+            const uint32_t dcol = taddr + (uint32_t)(buf * K::COLS);
 #pragma unroll 1
             for (int mt = 0; mt < MT; mt++) {
 #pragma unroll
@@ -391,66 +440,38 @@ __global__ void __launch_bounds__(Tc5<MT, MODE>::THREADS) conv3x3_tc05_kernel(Co
                         const uint64_t bd = b0 + (uint64_t)(((tap * K::WCB + 2 * kc) * K::NB * 16) >> 4);
                         asm volatile(
                             "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-                            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(taddr + 32u * mt),
+                            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dcol + 32u * mt),
                             "l"(ad), "l"(bd), "r"(idesc), "r"((tap | kc) ? 1u : 0u));
                     }
                 }
             }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar)
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                             bar0 + 8u * (uint32_t)buf)
                          : "memory");
         }
-        // this tile's MMAs complete phase `it` of the barrier (bounded wait, block-uniform verdict)
-        uint32_t done = 0;
-        for (uint32_t k = 0; k < kWaitLimit && !done; k++) {
-            asm volatile(
-                "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
-                : "=r"(done)
-                : "r"(bar), "r"((uint32_t)(it & 1))
-                : "memory");
-        }
-        if (!__syncthreads_and(done)) {  // stop; drain the copies and free TMEM below
-            if (threadIdx.x == 0) atomicExch(err, 1);
-            break;
-        }
-        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-        {
-            const int mt = warp >> 2, q = warp & 3;  // warp -> (tile, TMEM lane quarter)
-            uint32_t v[32];
-            asm volatile(
-                "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
-                "%14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];\n"
-                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-                  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
-                  "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
-                  "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]),
-                  "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
-                : "r"(taddr + ((uint32_t)(q * 32) << 16) + 32u * mt));
-            asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-            const int img = t / tiles_img, tt = t - img * tiles_img;
-            const int m = q * 32 + lane;
-            const int x = (tt % tiles_x) * TC5_C + (m & 7), y = (tt / tiles_x) * K::R + 16 * mt + (m >> 3);
-            if (MODE == 2 && x < a.w && y < a.h) {
-                *reinterpret_cast<float4*>((float*)a.out + img * a.out_stride + ((size_t)y * a.w + x) * 4) =
-                    make_float4(__uint_as_float(v[0]) + s_bias[0], __uint_as_float(v[1]) + s_bias[1],
-                                __uint_as_float(v[2]) + s_bias[2], __uint_as_float(v[3]) + s_bias[3]);
-            } else if (MODE != 2 && x < a.w && y < a.h) {
-                __nv_bfloat16 o[32];
-#pragma unroll
-                for (int n = 0; n < 32; n++)
-                    o[n] = __float2bfloat16_rn(fmaxf(__uint_as_float(v[n]) + s_bias[n], 0.0f));
-                uint4* dst =
-                    reinterpret_cast<uint4*>((__nv_bfloat16*)a.out + img * a.out_stride + ((size_t)y * a.w + x) * 32);
-#pragma unroll
-                for (int qq = 0; qq < 4; qq++) dst[qq] = reinterpret_cast<const uint4*>(o)[qq];
-            }
+        if (it > 0 && !(ok = wait_mma(it - 1))) break;
+        // the other halo buffer is free once tile t - 1's MMAs are done: start tile t + 1's
+        // copy first, then drain tile t - 1's accumulators while tile t's MMAs run
+        if (t + (int)gridDim.x < ntiles) prefetch(t + gridDim.x, buf ^ 1);
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+        if (it > 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            epilogue(tprev, buf ^ 1);
         }
         asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-        __syncthreads();
+        tprev = t;
     }
+    if (ok && it > 0) {  // the last tile
+        if ((ok = wait_mma(it - 1))) {
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            epilogue(tprev, (it - 1) & 1);
+        }
+    }
+    if (!ok && threadIdx.x == 0) atomicExch(err, 1);
     asm volatile("cp.async.wait_group 0;\n" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(taddr), "n"(K::COLS));
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(taddr), "n"(2 * K::COLS));
 }
 
 // ---------------------------------------------------------------------------------------
