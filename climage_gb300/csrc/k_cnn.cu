@@ -246,8 +246,8 @@ __global__ void __launch_bounds__(CT) conv3x3_kernel(ConvArgs a) {
 constexpr int TC5_R = 16, TC5_C = 8;  // output tile rows x columns
 constexpr int TC5_HR = TC5_R + 2, TC5_HC = TC5_C + 2;
 constexpr uint32_t kWaitLimit = 1u << 24;
-constexpr int kTc5Stack = 2;         // 16x8 tiles per persistent-block iteration
-constexpr int kTc5BlocksPerSm = 3;   // resident blocks per SM (shared memory: 62 KB each)
+constexpr int kTc5Stack = 1;         // 16x8 tiles per persistent-block iteration
+constexpr int kTc5BlocksPerSm = 5;   // resident blocks per SM (shared memory: 41 KB each; TMEM 64 columns each)
 
 __device__ __forceinline__ int cdiv_d(int a, int b) { return (a + b - 1) / b; }
 
