@@ -54,6 +54,39 @@ def dist_env():
     return rank, world, local
 
 
+def init_replicas(backend):
+    """One process per GPU, each an independent replica of the whole step (the pipeline has
+    no exchange step, so frames are never split across ranks): the process group carries only
+    the barriers around the timed region and the max-over-ranks reduction of its duration."""
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group(backend, init_method="env://", rank=rank, world_size=world)
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(total_ms, world, dev):
+    """The slowest replica's timed-region duration (every rank returns the same number)."""
+    if world == 1:
+        return float(total_ms)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(total_ms)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(world, mpix_per_step, steps, total_ms):
+    """Whole-job throughput: every rank processed steps x mpix_per_step in at most total_ms."""
+    return world * mpix_per_step * steps / (total_ms / 1e3)
+
+
 def make_frames(cfg, rank):
     from climage_gb300 import configs, synthetic
     frames = []
@@ -264,9 +297,8 @@ def main():
     import torch
     rank, world, local = dist_env()
     if world > 1:
-        import torch.distributed as dist
         torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+    init_replicas("nccl")
     dev = torch.device("cuda", local if world > 1 else 0)
     torch.cuda.set_device(dev)
     from climage_gb300 import gls
@@ -292,8 +324,7 @@ def main():
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
+    barrier(world)
     launches0 = ctx.kernel_launches()
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
@@ -306,17 +337,12 @@ def main():
             step()
             ends[k].record(stream)
         torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
+    barrier(world)
     launches = ctx.kernel_launches() - launches0
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    total_ms = float(sum(step_ms))
-    if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(sum(step_ms), world, dev)
     mpix_per_step = len(frames) * w * h / 1e6
-    value = world * mpix_per_step * args.steps / (total_ms / 1e3)
+    value = replica_value(world, mpix_per_step, args.steps, total_ms)
 
     # ---- per-stage profile (separate pass) and roofline of the dominant kernel ----
     conv.profile(True)
@@ -349,11 +375,12 @@ def main():
         for _ in range(args.warmup):
             host_step()
         torch.cuda.synchronize()
+        barrier(world)
         t0 = time.perf_counter()
         for _ in range(args.steps):
             host_step()
-        e2e_s = time.perf_counter() - t0
-        e2e = {"value": round(world * mpix_per_step * args.steps / e2e_s, 3), "unit": "MPix/s",
+        e2e_s = max_over_ranks(time.perf_counter() - t0, world, dev)
+        e2e = {"value": round(replica_value(world, mpix_per_step, args.steps, 1e3 * e2e_s), 3), "unit": "MPix/s",
                "h2d_bytes_per_step": int(sum(f[0].nbytes for f in frames)),
                "d2h_bytes_per_step": int(len(frames) * w * h * 4)}
         # the same burst from packed 12-bit host frames (an uncompressed DNG strip's layout):
@@ -370,11 +397,12 @@ def main():
         for _ in range(args.warmup):
             packed_step()
         torch.cuda.synchronize()
+        barrier(world)
         t0 = time.perf_counter()
         for _ in range(args.steps):
             packed_step()
-        pk_s = time.perf_counter() - t0
-        e2e["packed_input"] = {"value": round(world * mpix_per_step * args.steps / pk_s, 3), "unit": "MPix/s",
+        pk_s = max_over_ranks(time.perf_counter() - t0, world, dev)
+        e2e["packed_input"] = {"value": round(replica_value(world, mpix_per_step, args.steps, 1e3 * pk_s), 3), "unit": "MPix/s",
                                "h2d_bytes_per_step": int(sum(t.numel() for t in packed)), "bits": cfg["bits"]}
 
     # ---- the learned form: the same burst with the learned stage (shipped parameters) ----
@@ -391,6 +419,7 @@ def main():
             for _ in range(args.warmup):
                 lb.demosaic(raws, params, outs)
             torch.cuda.synchronize()
+            barrier(world)
             ls = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
             le = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
             for k in range(args.steps):
@@ -399,9 +428,9 @@ def main():
                 lb.demosaic(raws, params, outs)
                 le[k].record(stream)
             torch.cuda.synchronize()
-            lms = float(sum(a.elapsed_time(b) for a, b in zip(ls, le)))
+            lms = max_over_ranks(sum(a.elapsed_time(b) for a, b in zip(ls, le)), world, dev)
             verdict = learned.judge(ctx, cnn, range(10**6, 10**6 + 2))
-            learned_line = {"value": round(world * mpix_per_step * args.steps / (lms / 1e3), 3), "unit": "MPix/s",
+            learned_line = {"value": round(replica_value(world, mpix_per_step, args.steps, lms), 3), "unit": "MPix/s",
                             "ms_per_step": round(lms / args.steps, 4),
                             "judge": {k: verdict[k] for k in ("plain", "learned", "linear_input", "linear_corrected")},
                             "judge_frames": "2 held-out 1024x768 scenes, read sigma 4-16 DN, gain 0.25-4"}
