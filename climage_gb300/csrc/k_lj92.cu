@@ -10,12 +10,15 @@
 //      first FF not followed by 00; the 00 after every data FF is dropped (chunked counts,
 //      per-interval offsets, compaction);
 //   3. speculative decoding: the de-stuffed bits of an interval are cut into segments of
-//      kSegBits; a thread decodes MCUs from the start of its segment to the first MCU
-//      boundary past its end.  Huffman codes resynchronise, so a thread started at a wrong
-//      bit soon falls onto the true MCU boundaries; kSyncRounds parallel rounds re-decode a
+//      kSegBits; a thread decodes units (single codewords when all the scan's tables split
+//      bits alike, else whole MCUs) from the start of its segment to the first unit
+//      boundary past its end.  A decode unit of one codeword has no component phase to
+//      lose: a decode started on the wrong component of a multi-component scan stays in
+//      step once its bits are.  Huffman codes resynchronise, so a thread started at a wrong
+//      bit soon falls onto the true unit boundaries; kSyncRounds parallel rounds re-decode a
 //      segment from the end its predecessor reached, then one thread per interval walks the
 //      segments still out of step (exact, serial only where the rounds left work).  A scan
-//      of the per-segment MCU counts gives every segment its first MCU index, and a last
+//      of the per-segment unit counts gives every segment its first unit index, and a last
 //      pass decodes again and writes the differences;
 //   4. reconstruction: column 0 runs down the rows (predictor: the row above, the
 //      interval's first row starting from 2^(P-Pt-1)); predictor 1 rows are prefix sums
@@ -39,7 +42,7 @@ constexpr int kSegBits = 2048;    // bits per speculative segment
 constexpr int kChunk = 4096;      // source bytes per de-stuffing chunk
 constexpr int kSyncRounds = 2;    // parallel resynchronisation rounds before the walk
 constexpr int kPad = 16;          // zero bytes after each interval's de-stuffed data
-constexpr int kBnd = 8;           // MCU starts remembered per segment from the first pass
+constexpr int kBnd = 8;           // unit starts remembered per segment from the first pass
 
 struct LjTable {
     uint16_t look[256];  // (code length << 8) | value for codes of at most 8 bits; 0: longer
@@ -51,7 +54,11 @@ struct LjTable {
 
 struct LjStream {
     int width, height, comps, precision, predictor, pt;
-    int zero_mcu_bits;  // bits of an MCU of all-zero codewords decoding to 0 differences (0: none)
+    // codewords per decode unit: comps (one MCU), or 1 when every table of the scan splits
+    // bits into codewords alike (then where a codeword starts does not depend on its
+    // component, which the codeword's index gives)
+    int upc;
+    int zero_unit_bits;  // bits of a unit of all-zero codewords decoding to 0 differences (0: none)
     int table[4];
     long long sample_off;  // first sample of the stream in the samples buffer
     int tile_x, tile_y, clip_w, clip_h;  // placement of the stream's samples in the image
@@ -89,7 +96,7 @@ struct LjDev {
     long long* chunk_off;
     long long* start_used;  // per segment
     long long* bnd;         // per segment: the first kBnd MCU starts of the pass-1 decode
-    int* p1cnt;             // per segment: MCUs of the pass-1 decode (from the segment's first bit)
+    int* p1cnt;             // per segment: units of the pass-1 decode (from the segment's first bit)
     int8_t* p1;             // per segment: the segment's values are still the pass-1 decode
     long long* end_a;
     long long* end_b;
@@ -169,10 +176,15 @@ __device__ __forceinline__ int decode_diff(const LjTable* __restrict__ t, const 
     return len;
 }
 
-__device__ __forceinline__ int mcu_bits(const LjDev& g, const LjStream& st, const BitSrc& base, long long pos,
-                                        int* d, bool* bad) {
+// One decode unit at bit pos whose first codeword belongs to component comp0 (always 0 for
+// a whole MCU; a single codeword may sit at any component).
+__device__ __forceinline__ int unit_bits(const LjDev& g, const LjStream& st, const BitSrc& base, long long pos,
+                                         int comp0, int* d, bool* bad) {
     int used = 0;
-    for (int k = 0; k < st.comps; k++) used += decode_diff(g.tables + st.table[k], base, pos + used, d + k, bad);
+    for (int k = 0; k < st.upc; k++) {
+        const int c = comp0 + k < st.comps ? comp0 + k : comp0 + k - st.comps;
+        used += decode_diff(g.tables + st.table[c], base, pos + used, d + k, bad);
+    }
     return used;
 }
 
@@ -192,13 +204,13 @@ __device__ __forceinline__ long long zero_run(const BitSrc& b, long long pos, lo
     return cap;
 }
 
-// MCUs of all-zero codewords that fit wholly in the zero run at pos (at most max_mcus): a
-// flat area of the image is such a run, and its MCUs all decode to zero differences.
-__device__ __forceinline__ long long zero_mcus(const LjStream& st, const BitSrc& b, long long pos,
-                                               long long max_mcus) {
-    if (st.zero_mcu_bits == 0 || max_mcus <= 0 || peek32(b, pos) != 0) return 0;
-    const long long P = st.zero_mcu_bits;
-    return min(max_mcus, zero_run(b, pos, max_mcus * P) / P);
+// Units of all-zero codewords that fit wholly in the zero run at pos (at most max_units): a
+// flat area of the image is such a run, and its units all decode to zero differences.
+__device__ __forceinline__ long long zero_units(const LjStream& st, const BitSrc& b, long long pos,
+                                                long long max_units) {
+    if (st.zero_unit_bits == 0 || max_units <= 0 || peek32(b, pos) != 0) return 0;
+    const long long P = st.zero_unit_bits;
+    return min(max_units, zero_run(b, pos, max_units * P) / P);
 }
 
 // ---- de-stuffing ----
@@ -328,23 +340,23 @@ __device__ __forceinline__ void seg_decode(const LjDev& g, int seg, long long st
     const BitSrc base = bits_of(g.dst, iv);
     const int j = seg - iv.seg_base;
     const long long limit = (long long)(j + 1) * kSegBits;
-    const long long total = (long long)iv.rows * st.width;
+    const long long total = (long long)iv.rows * st.width * st.comps / st.upc;
     long long pos = start;
     int n = 0;
     bool bad = false;
     int d[4];
     while (pos < limit && (j > 0 || n < total)) {
-        const long long want = (limit - pos + st.zero_mcu_bits - 1) / max(st.zero_mcu_bits, 1);
-        const long long z = zero_mcus(st, base, pos, j > 0 ? want : min(want, total - n));
+        const long long want = (limit - pos + st.zero_unit_bits - 1) / max(st.zero_unit_bits, 1);
+        const long long z = zero_units(st, base, pos, j > 0 ? want : min(want, total - n));
         if (z > 0) {
             if (bnd)
-                for (long long m = 0; m < z && n + m < kBnd; m++) bnd[n + m] = pos + m * st.zero_mcu_bits;
-            pos += z * st.zero_mcu_bits;
+                for (long long m = 0; m < z && n + m < kBnd; m++) bnd[n + m] = pos + m * st.zero_unit_bits;
+            pos += z * st.zero_unit_bits;
             n += (int)z;
             continue;
         }
         if (bnd && n < kBnd) bnd[n] = pos;
-        pos += mcu_bits(g, st, base, pos, d, &bad);
+        pos += unit_bits(g, st, base, pos, 0, d, &bad);  // positions only: any component parses alike
         n++;
     }
     if (bnd)
@@ -390,7 +402,7 @@ __global__ void lj_sync_kernel(LjDev g, int nseg, const long long* end_in, long 
     if (j == 0 || (long long)j * kSegBits >= g.dlen[I] * 8) return;
     const long long s = end_in[seg - 1];
     if (s == g.start_used[seg]) return;
-    if (g.p1[seg]) {  // the new start is an MCU start of the first pass: the rest of its path
+    if (g.p1[seg]) {  // the new start is a unit start of the first pass: the rest of its path
         const long long* b = g.bnd + (size_t)seg * kBnd;
         for (int k = 0; k < kBnd; k++)
             if (b[k] == s) {
@@ -537,7 +549,8 @@ __global__ void lj_write_kernel(LjDev g, int nseg) {
     // the segment holding the end of the data decodes on until the interval is complete
     const bool last = (long long)(j + 1) * kSegBits >= nbits;
     const long long limit = (long long)(j + 1) * kSegBits;
-    const long long total = (long long)iv.rows * st.width;
+    const int U = st.upc;
+    const long long total = (long long)iv.rows * st.width * st.comps / U;
     const BitSrc base = bits_of(g.dst, iv);
     long long pos = g.start_used[seg];
     long long m = g.seg_off[seg];
@@ -546,16 +559,17 @@ __global__ void lj_write_kernel(LjDev g, int nseg) {
     int d[4];
     while (m < total && (pos < limit || last)) {
         const long long want =
-            last ? total - m : min(total - m, (limit - pos + st.zero_mcu_bits - 1) / max(st.zero_mcu_bits, 1));
-        const long long z = zero_mcus(st, base, pos, want);
+            last ? total - m : min(total - m, (limit - pos + st.zero_unit_bits - 1) / max(st.zero_unit_bits, 1));
+        const long long z = zero_units(st, base, pos, want);
         if (z > 0) {
-            for (long long q = m * st.comps; q < (m + z) * st.comps; q++) out[q] = 0;
-            pos += z * st.zero_mcu_bits;
+            for (long long q = m * U; q < (m + z) * U; q++) out[q] = 0;
+            pos += z * st.zero_unit_bits;
             m += z;
             continue;
         }
-        pos += mcu_bits(g, st, base, pos, d, &bad);
-        for (int k = 0; k < st.comps; k++) out[m * st.comps + k] = (int16_t)d[k];
+        // the interval starts on an MCU, so codeword m * U belongs to component (m * U) % comps
+        pos += unit_bits(g, st, base, pos, (int)((m * U) % st.comps), d, &bad);
+        for (int k = 0; k < U; k++) out[m * U + k] = (int16_t)d[k];
         m++;
     }
     if (bad) atomicExch(g.error, 1);
@@ -834,6 +848,22 @@ void derive_table(const HostTable& h, LjTable& t) {
         }
 }
 
+// Whether two tables split every bit string into codewords of the same lengths: the same
+// number of codes of each length (so the same canonical codes) and, code by code, the same
+// number of extra bits (category s < 16 reads s bits, 16 none; a category above 16 is an
+// error and must match exactly).
+bool same_parse(const HostTable& a, const HostTable& b) {
+    int n = 0;
+    for (int l = 1; l <= 16; l++) {
+        if (a.bits[l] != b.bits[l]) return false;
+        n += a.bits[l];
+    }
+    auto extra = [](int s) { return s < 16 ? s : (s == 16 ? 0 : -s); };
+    for (int p = 0; p < n && p < 256; p++)
+        if (extra(a.val[p]) != extra(b.val[p])) return false;
+    return true;
+}
+
 template <class T>
 size_t carve(size_t& off, size_t count) {
     const size_t o = (off + 255) & ~(size_t)255;
@@ -896,15 +926,19 @@ extern "C" gls_status gls_dng_decode_lossless_jpeg(gls_ctx* ctx, const uint8_t* 
             derive_table(h.tab[h.scan_table[k]], t);
             tables.push_back(t);
         }
-        // an MCU whose codewords are all zero bits and all decode to category 0
-        st.zero_mcu_bits = 0;
+        // decode unit: a single codeword when the scan's tables all parse bits alike
+        bool alike = true;
+        for (int k = 1; k < h.ns; k++) alike = alike && same_parse(h.tab[h.scan_table[0]], h.tab[h.scan_table[k]]);
+        st.upc = alike ? 1 : h.ns;
+        // a unit whose codewords are all zero bits and all decode to category 0
+        st.zero_unit_bits = 0;
         for (int k = 0; k < h.ns; k++) {
             const uint16_t lk = tables[st.table[k]].look[0];
             if (lk == 0 || (lk & 0xFF) != 0) {
-                st.zero_mcu_bits = 0;
+                st.zero_unit_bits = 0;
                 break;
             }
-            st.zero_mcu_bits += lk >> 8;
+            if (k < st.upc) st.zero_unit_bits += lk >> 8;
         }
         // QuickPredict throws for a predictor above 7 once a row is predicted from the one
         // above (gls_dng_lossless_jpeg.cpp:1290); the first row's 2^(P-Pt-1) needs Pt < P
