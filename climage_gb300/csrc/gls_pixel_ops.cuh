@@ -439,7 +439,8 @@ template <class Acc4>
 __device__ __noinline__ float4 bilateral_literal(const Acc4& im, int px, int py, float sig0, float sig1, float sig2,
                                                  float e0, float e1) {
     const float4 c = im.at(px, py);
-    float f0 = 0.0f, f1 = 0.0f, f2 = 0.0f, n0 = 0.0f, n1 = 0.0f, n2 = 0.0f;
+    // the two chroma channels share their weights, so their normalisers are one sum
+    float f0 = 0.0f, f1 = 0.0f, f2 = 0.0f, n0 = 0.0f, n1 = 0.0f;
     for (int y = -2; y <= 2; y++) {
         for (int x = -2; x <= 2; x++) {
             const float4 s = im.at(px + x, py + y);
@@ -451,10 +452,9 @@ __device__ __noinline__ float4 bilateral_literal(const Acc4& im, int px, int py,
             f1 = f1 + w1 * s.y;
             n1 = n1 + w1;
             f2 = f2 + w1 * s.z;
-            n2 = n2 + w1;
         }
     }
-    return make_float4(div_(f0, n0), div_(f1, n1), div_(f2, n2), 0.0f);
+    return make_float4(div_(f0, n0), div_(f1, n1), div_(f2, n1), 0.0f);
 }
 
 template <class Acc4>
@@ -493,7 +493,7 @@ GLS_DI float4 bilateral_px(const Acc4& im, int px, int py, const Nlf6& n, float 
     const float r0 = dv0.y * dv0.y, r1 = dv1.y * dv1.y, r2 = dv2.y * dv2.y;
     const float lo0 = ge0.lo * (1.0f - kWiden), hi0 = ge0.hi * (1.0f + kWiden);
     const float lo1 = ge1.lo * (1.0f - kWiden), hi1 = ge1.hi * (1.0f + kWiden);
-    float f0 = 0.0f, f1 = 0.0f, f2 = 0.0f, n0 = 0.0f, n1 = 0.0f, n2 = 0.0f;
+    float f0 = 0.0f, f1 = 0.0f, f2 = 0.0f, n0 = 0.0f, n1 = 0.0f;  // one normaliser for both chroma channels
     bool redo = false;
 #pragma unroll 1
     for (int y = -2; y <= 2; y++) {
@@ -510,11 +510,10 @@ GLS_DI float4 bilateral_px(const Acc4& im, int px, int py, const Nlf6& n, float 
             f1 = glsm::fma_(w1, s.y, f1);
             n1 = n1 + w1;
             f2 = glsm::fma_(w1, s.z, f2);
-            n2 = n2 + w1;
         }
     }
     if (redo) return bilateral_literal(im, px, py, sig0, sig1, sig2, ge0.e, ge1.e);
-    return make_float4(div_(f0, n0), div_(f1, n1), div_(f2, n2), 0.0f);
+    return make_float4(div_(f0, n0), div_(f1, n1), div_(f2, n1), 0.0f);
 }
 
 // ---- a15: denoiseImageGuided / denoiseLumaChromaGuided (demosaic.cl:767-851) ----

@@ -404,8 +404,8 @@ __global__ void __launch_bounds__(kT) denoise_reasm_kernel(DenoiseArgs a) {
 // =========================================================================================
 // final: level-0 denoise + reassemble over the tile and a one-pixel ring (the local tone
 // mapping samples its input bilinearly), then the LTM mask, YCbCr -> camera and
-// convertTosRGB.  30x14 output tiles: with its ring the denoised tile is 32x16, two
-// positions per thread.
+// convertTosRGB.  30x22 output tiles: with its ring the denoised tile is 32x24, three
+// positions per thread (the ring is 16 % of the denoised positions).
 //
 // Every bilinear sample here splits into an x part that depends only on the column and a y
 // part that depends only on the row (tap1).  The block evaluates those parts once per
@@ -416,7 +416,7 @@ __global__ void __launch_bounds__(kT) denoise_reasm_kernel(DenoiseArgs a) {
 // texels a tile reaches: with the pyramid's sizes (w >> 1, w >> 3) that is at most
 // FW / 2 + 4 half-resolution and FW / 8 + 5 guide texels across.
 // =========================================================================================
-constexpr int FW = 30, FH = 14;
+constexpr int FW = 30, FH = 22;
 constexpr int EW = FW + 2, EH = FH + 2;        // denoised level 0 with its ring
 constexpr int HTW = EW / 2 + 6, HTH = EH / 2 + 6;  // half-resolution tile capacity
 constexpr int GTW = FW / 8 + 8, GTH = FH / 8 + 8;  // guide tile capacity
