@@ -444,13 +444,17 @@ GLS_DI float final_coord(int which, int k, int pos, float n) {
 
 template <class S, int ALGO, bool LTM, bool OUT_F32>
 __global__ void __launch_bounds__(kT) final_kernel(FinalArgs a) {
-    constexpr int PW = FW + 6, PH = FH + 6;  // level 0 (binary16), origin (x0 - 3, y0 - 3)
-    __shared__ half4 s_l0[PW * PH];
+    constexpr int PW = FW + 6, PH = FH + 6;  // level 0 (binary16 values, widened), origin (x0 - 3, y0 - 3)
+    constexpr int NRAW = 3 * EW + 3 * EH + FW + FH + 3 * FW + 3 * FH;
+    __shared__ float4 s_l0[PW * PH];
     __shared__ float4 s_den[EW * EH];            // origin (x0 - 1, y0 - 1)
     __shared__ float4 s_i1[HTW * HTH], s_d1[HTW * HTH];
     __shared__ float s_g[GTW * GTH];
-    __shared__ Tap1 s_raw[3 * EW + 3 * EH + FW + FH + 3 * FW + 3 * FH];
     __shared__ FinalTabs T;
+    // the raw table entries live only until the tables are built (phase 2); the denoised
+    // tile is first written in phase 3
+    static_assert(NRAW * sizeof(Tap1) <= sizeof(float4) * EW * EH, "raw table entries overflow the denoised tile");
+    Tap1* const s_raw = reinterpret_cast<Tap1*>(s_den);
     const int x0 = blockIdx.x * FW, y0 = blockIdx.y * FH;
     const int w = a.w, h = a.h;
     const float nx = div_(1.0f, (float)w), ny = div_(1.0f, (float)h);
@@ -459,8 +463,7 @@ __global__ void __launch_bounds__(kT) final_kernel(FinalArgs a) {
     for (int i = threadIdx.x; i < PW * PH; i += kT) {
         const int r = i / PW, c = i - r * PW;
         const int gx = clampi(x0 - 3 + c, 0, w - 1), gy = clampi(y0 - 3 + r, 0, h - 1);
-        const uint2 u = __ldg(reinterpret_cast<const uint2*>(a.level0 + (size_t)gy * a.l0_pitch + gx));
-        *reinterpret_cast<uint2*>(&s_l0[i]) = u;
+        s_l0[i] = Storage<__half>::cvt(a.level0[(size_t)gy * a.l0_pitch + gx]);
     }
     // entry layout: rx[3][EW], ry[3][EH], lx[FW], ly[FH], gx[3][FW], gy[3][FH]
     constexpr int NRX = 3 * EW, NRY = 3 * EH, NLX = FW, NLY = FH, NGX = 3 * FW, NGY = 3 * FH;
@@ -544,7 +547,7 @@ __global__ void __launch_bounds__(kT) final_kernel(FinalArgs a) {
     __syncthreads();
 
     // ---- phase 3: denoise + reassemble over the tile and its ring ----
-    const SAcc4h L0{s_l0, x0 - 3, y0 - 3, PW};
+    const SAcc4f L0{s_l0, x0 - 3, y0 - 3, PW};
     Nlf6 n;
 #pragma unroll
     for (int k = 0; k < 3; k++) {
