@@ -129,11 +129,84 @@ __device__ __forceinline__ BitSrc bits_of(const uint8_t* dst, const LjInterval& 
     return BitSrc{reinterpret_cast<const uint32_t*>(dst + iv.dst_off), iv.dst_words};
 }
 
-// One difference at bit pos: HuffDecode + HuffExtend (gls_dng_lossless_jpeg.cpp:1424-1500).
-// Returns the bits consumed; *bad is set for a category above 16 (the reference throws).
-__device__ __forceinline__ int decode_diff(const LjTable* __restrict__ t, const BitSrc& base, long long pos, int* d,
-                                           bool* bad) {
-    const uint32_t v = peek32(base, pos);
+// Length of the run of zero bits at pos, at most cap.
+__device__ __forceinline__ long long zero_run(const BitSrc& b, long long pos, long long cap) {
+    long long r = 0;
+    const uint32_t v = peek32(b, pos);
+    if (v) return min(cap, (long long)__clz(v));
+    r = 32 - (pos & 31);  // to the next word boundary
+    long long w = (pos >> 5) + 1;
+    while (r < cap) {
+        const uint32_t x = w < b.nwords ? bswap32(__ldg(b.w + w)) : 0u;
+        if (x) return min(cap, r + __clz(x));
+        r += 32;
+        w++;
+    }
+    return cap;
+}
+
+// Units of all-zero codewords that fit wholly in the zero run at pos (at most max_units): a
+// flat area of the image is such a run, and its units all decode to zero differences.
+__device__ __forceinline__ long long zero_units(const LjStream& st, const BitSrc& b, long long pos,
+                                                long long max_units) {
+    if (st.zero_unit_bits == 0 || max_units <= 0 || peek32(b, pos) != 0) return 0;
+    const long long P = st.zero_unit_bits;
+    return min(max_units, zero_run(b, pos, max_units * P) / P);
+}
+
+// Sequential reader over an interval's de-stuffed bits: a 64-bit buffer of the next bits
+// (most significant first, at least 33 valid after every step) and the word after them
+// loaded ahead, so a serial decode waits on a memory load only once per 32 bits consumed.
+struct BitReader {
+    const uint32_t* w;
+    long long nwords;
+    long long widx;  // index of the word held in nw
+    long long pos;   // bit position of the buffer's first bit
+    uint64_t acc;
+    int avail;
+    uint32_t nw;
+    __device__ __forceinline__ uint32_t word(long long i) const { return i < nwords ? bswap32(__ldg(w + i)) : 0u; }
+    __device__ __forceinline__ void refill() {
+        if (avail <= 32) {
+            acc |= (uint64_t)nw << (32 - avail);
+            avail += 32;
+            widx++;
+            nw = word(widx);
+        }
+    }
+    __device__ __forceinline__ void seek(long long p) {
+        pos = p;
+        const long long i = p >> 5;
+        const int o = (int)(p & 31);
+        acc = (uint64_t)word(i) << (32 + o);
+        avail = 32 - o;
+        widx = i + 1;
+        nw = word(widx);
+        refill();
+    }
+    __device__ __forceinline__ uint32_t peek() const { return (uint32_t)(acc >> 32); }
+    __device__ __forceinline__ void skip(int n) {  // n <= 32
+        acc <<= n;
+        avail -= n;
+        pos += n;
+        refill();
+    }
+};
+
+__device__ __forceinline__ BitReader reader_at(const BitSrc& b, long long pos) {
+    BitReader r;
+    r.w = b.w;
+    r.nwords = b.nwords;
+    r.seek(pos);
+    return r;
+}
+
+// One difference: HuffDecode + HuffExtend (gls_dng_lossless_jpeg.cpp:1424-1500), on the
+// reader (a code of at most 16 bits and at most 15 extra bits, or an invalid code of 17
+// bits: never more than 32 bits at a time).  Returns the bits consumed; *bad is set for a
+// category above 16 (the reference throws).
+__device__ __forceinline__ int decode_diff_r(const LjTable* __restrict__ t, BitReader& br, int* d, bool* bad) {
+    const uint32_t v = br.peek();
     const uint32_t c8 = v >> 24;
     const uint32_t lk = t->look[c8];
     int len, s;
@@ -163,54 +236,25 @@ __device__ __forceinline__ int decode_diff(const LjTable* __restrict__ t, const 
         *bad = true;
         *d = 0;
     } else {
-        int x;
-        if (len + s <= 32) {
-            x = (int)((v << len) >> (32 - s));
-        } else {
-            x = (int)(peek32(base, pos + len) >> (32 - s));
-        }
+        int x = (int)((v << len) >> (32 - s));
         if (x < (0x8000 >> (16 - s))) x += (-1 << s) + 1;
         *d = x;
         len += s;
     }
+    br.skip(len);
     return len;
 }
 
-// One decode unit at bit pos whose first codeword belongs to component comp0 (always 0 for
-// a whole MCU; a single codeword may sit at any component).
-__device__ __forceinline__ int unit_bits(const LjDev& g, const LjStream& st, const BitSrc& base, long long pos,
-                                         int comp0, int* d, bool* bad) {
+// One decode unit whose first codeword belongs to component comp0 (always 0 for a whole
+// MCU; a single codeword may sit at any component).
+__device__ __forceinline__ int unit_bits_r(const LjDev& g, const LjStream& st, BitReader& br, int comp0, int* d,
+                                           bool* bad) {
     int used = 0;
     for (int k = 0; k < st.upc; k++) {
         const int c = comp0 + k < st.comps ? comp0 + k : comp0 + k - st.comps;
-        used += decode_diff(g.tables + st.table[c], base, pos + used, d + k, bad);
+        used += decode_diff_r(g.tables + st.table[c], br, d + k, bad);
     }
     return used;
-}
-
-// Length of the run of zero bits at pos, at most cap.
-__device__ __forceinline__ long long zero_run(const BitSrc& b, long long pos, long long cap) {
-    long long r = 0;
-    const uint32_t v = peek32(b, pos);
-    if (v) return min(cap, (long long)__clz(v));
-    r = 32 - (pos & 31);  // to the next word boundary
-    long long w = (pos >> 5) + 1;
-    while (r < cap) {
-        const uint32_t x = w < b.nwords ? bswap32(__ldg(b.w + w)) : 0u;
-        if (x) return min(cap, r + __clz(x));
-        r += 32;
-        w++;
-    }
-    return cap;
-}
-
-// Units of all-zero codewords that fit wholly in the zero run at pos (at most max_units): a
-// flat area of the image is such a run, and its units all decode to zero differences.
-__device__ __forceinline__ long long zero_units(const LjStream& st, const BitSrc& b, long long pos,
-                                                long long max_units) {
-    if (st.zero_unit_bits == 0 || max_units <= 0 || peek32(b, pos) != 0) return 0;
-    const long long P = st.zero_unit_bits;
-    return min(max_units, zero_run(b, pos, max_units * P) / P);
 }
 
 // ---- de-stuffing ----
@@ -341,27 +385,30 @@ __device__ __forceinline__ void seg_decode(const LjDev& g, int seg, long long st
     const int j = seg - iv.seg_base;
     const long long limit = (long long)(j + 1) * kSegBits;
     const long long total = (long long)iv.rows * st.width * st.comps / st.upc;
-    long long pos = start;
+    BitReader br = reader_at(base, start);
     int n = 0;
     bool bad = false;
     int d[4];
-    while (pos < limit && (j > 0 || n < total)) {
-        const long long want = (limit - pos + st.zero_unit_bits - 1) / max(st.zero_unit_bits, 1);
-        const long long z = zero_units(st, base, pos, j > 0 ? want : min(want, total - n));
-        if (z > 0) {
-            if (bnd)
-                for (long long m = 0; m < z && n + m < kBnd; m++) bnd[n + m] = pos + m * st.zero_unit_bits;
-            pos += z * st.zero_unit_bits;
-            n += (int)z;
-            continue;
+    while (br.pos < limit && (j > 0 || n < total)) {
+        if (st.zero_unit_bits && br.peek() == 0) {
+            const long long pos = br.pos;
+            const long long want = (limit - pos + st.zero_unit_bits - 1) / st.zero_unit_bits;
+            const long long z = zero_units(st, base, pos, j > 0 ? want : min(want, total - n));
+            if (z > 0) {
+                if (bnd)
+                    for (long long m = 0; m < z && n + m < kBnd; m++) bnd[n + m] = pos + m * st.zero_unit_bits;
+                br.seek(pos + z * st.zero_unit_bits);
+                n += (int)z;
+                continue;
+            }
         }
-        if (bnd && n < kBnd) bnd[n] = pos;
-        pos += unit_bits(g, st, base, pos, 0, d, &bad);  // positions only: any component parses alike
+        if (bnd && n < kBnd) bnd[n] = br.pos;
+        unit_bits_r(g, st, br, 0, d, &bad);  // positions only: any component parses alike
         n++;
     }
     if (bnd)
         for (int k = n; k < kBnd; k++) bnd[k] = -1;
-    *end_out = pos;
+    *end_out = br.pos;
     *cnt_out = n;
 }
 
@@ -552,23 +599,26 @@ __global__ void lj_write_kernel(LjDev g, int nseg) {
     const int U = st.upc;
     const long long total = (long long)iv.rows * st.width * st.comps / U;
     const BitSrc base = bits_of(g.dst, iv);
-    long long pos = g.start_used[seg];
+    BitReader br = reader_at(base, g.start_used[seg]);
     long long m = g.seg_off[seg];
     int16_t* out = g.diff + st.sample_off + iv.mcu_off * st.comps;
     bool bad = false;
     int d[4];
-    while (m < total && (pos < limit || last)) {
-        const long long want =
-            last ? total - m : min(total - m, (limit - pos + st.zero_unit_bits - 1) / max(st.zero_unit_bits, 1));
-        const long long z = zero_units(st, base, pos, want);
-        if (z > 0) {
-            for (long long q = m * U; q < (m + z) * U; q++) out[q] = 0;
-            pos += z * st.zero_unit_bits;
-            m += z;
-            continue;
+    while (m < total && (br.pos < limit || last)) {
+        if (st.zero_unit_bits && br.peek() == 0) {
+            const long long pos = br.pos;
+            const long long want =
+                last ? total - m : min(total - m, (limit - pos + st.zero_unit_bits - 1) / st.zero_unit_bits);
+            const long long z = zero_units(st, base, pos, want);
+            if (z > 0) {
+                for (long long q = m * U; q < (m + z) * U; q++) out[q] = 0;
+                br.seek(pos + z * st.zero_unit_bits);
+                m += z;
+                continue;
+            }
         }
         // the interval starts on an MCU, so codeword m * U belongs to component (m * U) % comps
-        pos += unit_bits(g, st, base, pos, (int)((m * U) % st.comps), d, &bad);
+        unit_bits_r(g, st, br, (int)((m * U) % st.comps), d, &bad);
         for (int k = 0; k < U; k++) out[m * U + k] = (int16_t)d[k];
         m++;
     }
