@@ -84,7 +84,7 @@ constexpr int RQ = 32;               // quads per tile side
 constexpr int RP = 2 * RQ + 8;       // staged pixels per side (halo of 2 quads)
 
 template <class S>
-__global__ void __launch_bounds__(kT) raw_pass1_kernel(RawPass1Args a) {
+__global__ void __launch_bounds__(kT, 3) raw_pass1_kernel(RawPass1Args a) {  // 3 resident blocks per SM
     __shared__ float s_raw[RP * RP];
     Pass1Acc<4, 4> acc;
     acc.init();
