@@ -624,12 +624,19 @@ int persistent_grid(gls_ctx* ctx, long tiles, int per_sm) {
 
 // A persistent grid of as many blocks as are resident at once: every block walks an equal
 // share of the tiles, so blocks beyond the resident ones would run as a second, sparse wave.
-template <class K>
-int resident_grid(gls_ctx* ctx, K kernel, long tiles) {
-    int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kT, 0) != cudaSuccess || per_sm < 1) {
-        cudaGetLastError();
-        per_sm = 1;
+// The count depends only on the kernel's resources, so the first query is kept (one static
+// per kernel instantiation; concurrent first calls store the same value).
+template <auto Kernel>
+int resident_grid(gls_ctx* ctx, long tiles) {
+    static int s_per_sm = 0;
+    int per_sm = s_per_sm;
+    if (per_sm < 1) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, Kernel, kT, 0) != cudaSuccess || per_sm < 1) {
+            cudaGetLastError();
+            per_sm = 1;
+        } else {
+            s_per_sm = per_sm;
+        }
     }
     return persistent_grid(ctx, tiles, per_sm);
 }
@@ -663,13 +670,13 @@ gls_status fused_raw_fit(gls_ctx* ctx, const RawPass1Args& args, bool half, NlfS
     const int qw = a.w / 2, qh = a.h / 2;
     const long tiles = (long)((qw + RQ - 1) / RQ) * ((qh + RQ - 1) / RQ);
     if (half) {
-        const int grid = resident_grid(ctx, raw_pass1_kernel<__half>, tiles);
+        const int grid = resident_grid<raw_pass1_kernel<__half>>(ctx, tiles);
         raw_pass1_kernel<__half><<<grid, kT, 0, ctx->stream>>>(a);
         RawU16SrcS<__half> src{{a.raw, a.w, a.h, a.pitch}, {a.sm[0], a.sm[1], a.sm[2], a.sm[3]}, a.black, a.bayer};
         ctx->launches++;
         nlf_finish<4, 4>(ctx, src, qw, qh, s, out_dev);
     } else {
-        const int grid = resident_grid(ctx, raw_pass1_kernel<float>, tiles);
+        const int grid = resident_grid<raw_pass1_kernel<float>>(ctx, tiles);
         raw_pass1_kernel<float><<<grid, kT, 0, ctx->stream>>>(a);
         RawU16SrcS<float> src{{a.raw, a.w, a.h, a.pitch}, {a.sm[0], a.sm[1], a.sm[2], a.sm[3]}, a.black, a.bayer};
         ctx->launches++;
@@ -711,13 +718,13 @@ gls_status fused_level_fit(gls_ctx* ctx, const LevelPass1Args& args, bool in_hal
     a.nlf_out = out_dev;
     const long tiles = (long)((a.w + LT - 1) / LT) * ((a.h + LT - 1) / LT);
     if (in_half) {
-        if (half) level_pass1_kernel<__half, __half><<<resident_grid(ctx, level_pass1_kernel<__half, __half>, tiles), kT, 0, ctx->stream>>>(a);
-        else level_pass1_kernel<__half, float><<<resident_grid(ctx, level_pass1_kernel<__half, float>, tiles), kT, 0, ctx->stream>>>(a);
+        if (half) level_pass1_kernel<__half, __half><<<resident_grid<level_pass1_kernel<__half, __half>>(ctx, tiles), kT, 0, ctx->stream>>>(a);
+        else level_pass1_kernel<__half, float><<<resident_grid<level_pass1_kernel<__half, float>>(ctx, tiles), kT, 0, ctx->stream>>>(a);
         LevelSrc<__half> src{{(const half4*)a.in, a.w, a.h, a.pitch}};
         ctx->launches++;
         nlf_finish<1, 3>(ctx, src, a.w, a.h, s, out_dev);
     } else {
-        level_pass1_kernel<float, float><<<resident_grid(ctx, level_pass1_kernel<float, float>, tiles), kT, 0, ctx->stream>>>(a);
+        level_pass1_kernel<float, float><<<resident_grid<level_pass1_kernel<float, float>>(ctx, tiles), kT, 0, ctx->stream>>>(a);
         LevelSrc<float> src{{(const float4*)a.in, a.w, a.h, a.pitch}};
         ctx->launches++;
         nlf_finish<1, 3>(ctx, src, a.w, a.h, s, out_dev);
