@@ -8,6 +8,10 @@
 //                                 unmapImage through pinned staging, toImage)
 //   free functions                demosaic_cl.hpp:23-129 (same names and arguments)
 //   gls::RawConverter             raw_converter.hpp:22-62
+//   autoWhiteBalance, colorCheckerRawStats, estimateRawParameters
+//                                 demosaic.hpp:207-222 (raw frame on the host)
+//   decodeLosslessJPEGTiles       the DNG reader's DecodeLosslessJPEG loop,
+//                                 src/gls_image_tiff.cpp:369-440
 //
 // Errors: every failing status throws gls::cuda_error (the reference throws cl::Error).
 #ifndef GLS_CUDA_HPP
@@ -346,6 +350,77 @@ std::array<float, 8> computeRawNoiseStatistics(CudaContext* c, const cuda_image_
     std::array<float, 8> r{};
     check(gls_compute_raw_noise_statistics(c->ctx(), &a, bayer, r.data()), "computeRawNoiseStatistics", c->ctx());
     return r;
+}
+
+// ---- raw-frame utilities (demosaic.hpp:207-222): the reference's arguments, the frame
+// copied to the device; each call synchronises the context's stream ----
+struct RawPatchStats {
+    std::array<float, 4> mean;
+    std::array<float, 4> variance;
+};
+
+inline std::array<float, 3> autoWhiteBalance(CudaContext* c, const image<luma_pixel_16>& rawImage,
+                                             const std::array<std::array<float, 3>, 3>& rgb_ycbcr,
+                                             const std::array<float, 4>& scale_mul, float white, float black,
+                                             BayerPattern bayerPattern, float* highlights = nullptr) {
+    cuda_image_2d<luma_pixel_16> raw(c, rawImage);
+    const gls_image_desc r = raw.desc();
+    float m[9];
+    for (int i = 0; i < 9; i++) m[i] = rgb_ycbcr[i / 3][i % 3];
+    std::array<float, 3> wb{};
+    float hl = 0;
+    check(gls_auto_white_balance(c->ctx(), &r, m, scale_mul.data(), white, black, bayerPattern, wb.data(), &hl),
+          "autoWhiteBalance", c->ctx());
+    if (highlights) *highlights = hl;
+    return wb;
+}
+
+inline void colorCheckerRawStats(CudaContext* c, const image<luma_pixel_16>& rawImage, float black_level,
+                                 float white_level, BayerPattern bayerPattern, const rectangle& gmb_position,
+                                 bool rotate_180, std::array<RawPatchStats, 24>* stats) {
+    cuda_image_2d<luma_pixel_16> raw(c, rawImage);
+    const gls_image_desc r = raw.desc();
+    const int g[4] = {gmb_position.x, gmb_position.y, gmb_position.width, gmb_position.height};
+    float mean[96], var[96];
+    check(gls_color_checker_raw_stats(c->ctx(), &r, black_level, white_level, bayerPattern, g, rotate_180, mean, var),
+          "colorCheckerRawStats", c->ctx());
+    for (int p = 0; p < 24; p++)
+        for (int k = 0; k < 4; k++) {
+            (*stats)[p].mean[k] = mean[4 * p + k];
+            (*stats)[p].variance[k] = var[4 * p + k];
+        }
+}
+
+// returns the raw noise slopes; cam_xyz and pre_mul as the reference fills them
+inline std::array<float, 4> estimateRawParameters(CudaContext* c, const image<luma_pixel_16>& rawImage,
+                                                  std::array<std::array<float, 3>, 3>* cam_xyz,
+                                                  std::array<float, 3>* pre_mul, float black_level, float white_level,
+                                                  BayerPattern bayerPattern, const rectangle& gmb_position,
+                                                  bool rotate_180) {
+    cuda_image_2d<luma_pixel_16> raw(c, rawImage);
+    const gls_image_desc r = raw.desc();
+    const int g[4] = {gmb_position.x, gmb_position.y, gmb_position.width, gmb_position.height};
+    float m[9];
+    std::array<float, 4> nlf{};
+    check(gls_estimate_raw_parameters(c->ctx(), &r, black_level, white_level, bayerPattern, g, rotate_180, m,
+                                      pre_mul->data(), nlf.data()),
+          "estimateRawParameters", c->ctx());
+    for (int i = 0; i < 9; i++) (*cam_xyz)[i / 3][i % 3] = m[i];
+    return nlf;
+}
+
+// The DNG reader's lossless-JPEG loop (src/gls_image_tiff.cpp:369-440, DecodeLosslessJPEG per
+// tile): the file's bytes, the tiles' (or the strip's) offsets and byte counts, into a device
+// raw frame of the image's size.
+inline void decodeLosslessJPEGTiles(CudaContext* c, const uint8_t* file, size_t file_size,
+                                    const std::vector<uint64_t>& offsets, const std::vector<uint64_t>& byte_counts,
+                                    int tile_width, int tile_height, cuda_image_2d<luma_pixel_16>* raw) {
+    if (offsets.size() != byte_counts.size())
+        throw cuda_error(GLS_ERR_INVALID_ARGUMENT, "decodeLosslessJPEGTiles: offsets and byte counts differ in number");
+    const gls_image_desc r = raw->desc();
+    check(gls_dng_decode_lossless_jpeg(c->ctx(), file, file_size, (int)offsets.size(), offsets.data(),
+                                       byte_counts.data(), tile_width, tile_height, &r),
+          "decodeLosslessJPEGTiles", c->ctx());
 }
 
 // ---- RawConverter (raw_converter.hpp:22-62) ----

@@ -1,9 +1,11 @@
 // Drives the header-only C++ layer (include/gls_cuda.hpp) the way a port of CLImage's
 // RawPipeline driver would: host gls::image<luma_pixel_16> in, RawConverter::demosaicImage,
-// RawConverter::convertToRGBImage out.  Reads a raw frame and its parameters from files
-// written by tests/test_gpu_cpp_layer.py and writes the RGB result next to them.
+// RawConverter::convertToRGBImage out, then autoWhiteBalance and colorCheckerRawStats on the
+// same frame.  Reads a raw frame and its parameters from files written by
+// tests/test_gpu_cpp_layer.py and writes the results next to them.
 //
-//   test_cpp_layer <dir>     reads <dir>/raw.u16 <dir>/params.txt, writes <dir>/rgb.u8
+//   test_cpp_layer <dir>     reads <dir>/raw.u16 <dir>/params.txt, writes <dir>/rgb.u8,
+//                            <dir>/nlf.txt, <dir>/awb.txt, <dir>/patches.f32
 #include <cstdio>
 #include <fstream>
 #include <iostream>
@@ -70,6 +72,27 @@ int main(int argc, char** argv) {
         if (!threw) {
             std::cerr << "rotate_180 did not throw\n";
             return 1;
+        }
+        // autoWhiteBalance with the camera -> YCbCr matrix of the frame's rgb_cam
+        float rgb_cam[9], cy[9];
+        for (int i = 0; i < 9; i++) rgb_cam[i] = p.rgb_cam[i / 3][i % 3];
+        gls::check(gls_cam_ycbcr(rgb_cam, cy), "cam_ycbcr");
+        std::array<std::array<float, 3>, 3> rgb_ycbcr;
+        for (int i = 0; i < 9; i++) rgb_ycbcr[i / 3][i % 3] = cy[i];
+        float highlights = -1;
+        const auto wb = gls::autoWhiteBalance(&ctx, raw, rgb_ycbcr, p.scale_mul, p.white_level, p.black_level,
+                                              p.bayerPattern, &highlights);
+        std::ofstream af(dir + "/awb.txt");
+        af.precision(9);
+        af << wb[0] << " " << wb[1] << " " << wb[2] << " " << highlights << "\n";
+        // colorCheckerRawStats over a chart placed inside the frame
+        std::array<gls::RawPatchStats, 24> stats;
+        gls::colorCheckerRawStats(&ctx, raw, p.black_level, p.white_level, p.bayerPattern,
+                                  gls::rectangle{12, 10, w - 30, h - 24}, false, &stats);
+        std::ofstream sf(dir + "/patches.f32", std::ios::binary);
+        for (const auto& s : stats) {
+            sf.write(reinterpret_cast<const char*>(s.mean.data()), 16);
+            sf.write(reinterpret_cast<const char*>(s.variance.data()), 16);
         }
     } catch (const std::exception& e) {
         std::cerr << "error: " << e.what() << "\n";

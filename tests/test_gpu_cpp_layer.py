@@ -1,6 +1,6 @@
 """The header-only C++ layer (include/gls_cuda.hpp): a C++ program written against the
-reference's API (gls::image, RawConverter::demosaicImage, convertToRGBImage) produces the
-oracle's RGB output."""
+reference's API (gls::image, RawConverter::demosaicImage, convertToRGBImage,
+autoWhiteBalance, colorCheckerRawStats) produces the oracle's results."""
 import os
 import subprocess
 import tempfile
@@ -8,7 +8,7 @@ import tempfile
 import numpy as np
 import pytest
 
-from climage_gb300 import build, configs, synthetic
+from climage_gb300 import build, configs, gls, synthetic
 from oracle import oracle as orc
 from tests.helpers import oracle_params
 
@@ -38,6 +38,19 @@ def test_cpp_layer_raw_converter(cuda):
         assert res.returncode == 0, res.stderr
         got = np.fromfile(os.path.join(d, "rgb.u8"), np.uint8).reshape(128, 192, 3)
         nlf = np.array(open(os.path.join(d, "nlf.txt")).read().split(), np.float32)
+        awb = np.array(open(os.path.join(d, "awb.txt")).read().split(), np.float32)
+        patches = np.fromfile(os.path.join(d, "patches.f32"), np.float32).reshape(24, 2, 4)
     ref = orc.demosaic(raw, oracle_params(spec), orc.F32, want=("rgba8",))
     np.testing.assert_array_equal(got, ref["rgba8"][..., :3])
     np.testing.assert_allclose(nlf, ref["raw_nlf"], rtol=1e-6)
+    # autoWhiteBalance: the gains and the highlight fraction (printed with 9 digits: exact floats)
+    cy = gls.cam_ycbcr(np.array(spec["rgb_cam"], np.float32).reshape(3, 3))
+    owb, ohl = orc.auto_white_balance(raw, cy, spec["scale_mul"], spec["white_level"], spec["black_level"],
+                                      spec["bayer_pattern"])
+    np.testing.assert_array_equal(awb[:3], owb)
+    assert awb[3] == np.float32(ohl)
+    # colorCheckerRawStats over the chart rectangle the program used
+    om, ov = orc.color_checker_raw_stats(raw, spec["black_level"], spec["white_level"], spec["bayer_pattern"],
+                                         (12, 10, 192 - 30, 128 - 24))
+    np.testing.assert_array_equal(patches[:, 0], om)
+    np.testing.assert_array_equal(patches[:, 1], ov)
