@@ -926,6 +926,25 @@ size_t carve(size_t& off, size_t count) {
 
 using namespace gls;
 
+extern "C" gls_status gls_lossless_jpeg_info(const uint8_t* data, size_t size, gls_ljpeg_info* info) {
+    if (!data || !info) return GLS_ERR_INVALID_ARGUMENT;
+    HostHeader h;
+    if (size < 4 || !parse_header(data, size, h)) return GLS_ERR_BAD_STREAM;
+    // the decoder's predictor rule (QuickPredict, gls_dng_lossless_jpeg.cpp:1290)
+    if (h.ss > 7 && h.width > 1 && h.height > 1 && h.restart / h.width != 1) return GLS_ERR_BAD_STREAM;
+    bool alike = true;
+    for (int k = 1; k < h.ns; k++) alike = alike && same_parse(h.tab[h.scan_table[0]], h.tab[h.scan_table[k]]);
+    info->width = h.width;
+    info->height = h.height;
+    info->components = h.ns;
+    info->precision = h.precision;
+    info->predictor = h.ss;
+    info->point_transform = h.pt;
+    info->restart_interval = h.restart;
+    info->tables_alike = alike ? 1 : 0;
+    return GLS_OK;
+}
+
 extern "C" gls_status gls_dng_decode_lossless_jpeg(gls_ctx* ctx, const uint8_t* data, size_t data_size, int n_streams,
                                                    const uint64_t* offsets, const uint64_t* sizes, int tile_width,
                                                    int tile_height, const gls_image_desc* out) {

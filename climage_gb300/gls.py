@@ -37,6 +37,11 @@ class GlsError(RuntimeError):
         self.status = status
 
 
+class LjpegInfo(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int) for n in ("width", "height", "components", "precision", "predictor",
+                                            "point_transform", "restart_interval", "tables_alike")]
+
+
 class ImageDesc(ctypes.Structure):
     _fields_ = [("ptr", ctypes.c_void_p), ("width", ctypes.c_int), ("height", ctypes.c_int),
                 ("stride_bytes", ctypes.c_int), ("format", ctypes.c_int)]
@@ -120,6 +125,7 @@ SIGNATURES = [
     ("gls_auto_white_balance", _I, [_P, _D, _FP, _FP, _F, _F, _I, _FP, _FP]),
     ("gls_dng_decode_lossless_jpeg", _I, [_P, _P, ctypes.c_size_t, _I, ctypes.POINTER(ctypes.c_uint64),
                                           ctypes.POINTER(ctypes.c_uint64), _I, _I, _D]),
+    ("gls_lossless_jpeg_info", _I, [_P, ctypes.c_size_t, ctypes.POINTER(LjpegInfo)]),
     ("gls_color_checker_raw_stats", _I, [_P, _D, _F, _F, _I, ctypes.POINTER(ctypes.c_int), _I, _FP, _FP]),
     ("gls_estimate_raw_parameters", _I, [_P, _D, _F, _F, _I, ctypes.POINTER(ctypes.c_int), _I, _FP, _FP, _FP]),
     ("gls_selftest", _I, [_P, ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)]),
@@ -211,6 +217,19 @@ def inverse3x3(m):
     if s != GLS_OK:
         raise GlsError(s, "inverse3x3")
     return np.array(out[:], np.float32).reshape(3, 3)
+
+
+def lossless_jpeg_info(data):
+    """The header of one lossless-JPEG stream (bytes or a uint8 array), as the DNG decoder reads
+    it: a dict of width, height, components, precision, predictor, point_transform,
+    restart_interval and tables_alike.  Host only; raises GlsError for a header the decoder
+    rejects."""
+    buf = np.frombuffer(bytes(data), np.uint8) if isinstance(data, (bytes, bytearray)) else np.ascontiguousarray(data, np.uint8)
+    info = LjpegInfo()
+    s = lib().gls_lossless_jpeg_info(ctypes.c_void_p(buf.ctypes.data), buf.size, ctypes.byref(info))
+    if s != GLS_OK:
+        raise GlsError(s, "lossless_jpeg_info")
+    return {n: getattr(info, n) for n, _ in LjpegInfo._fields_}
 
 
 # ---- device images ----

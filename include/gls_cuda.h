@@ -255,6 +255,21 @@ GLS_API gls_status gls_dng_decode_lossless_jpeg(gls_ctx* ctx, const uint8_t* dat
                                                 const uint64_t* offsets, const uint64_t* sizes, int tile_width,
                                                 int tile_height, const gls_image_desc* out);
 
+/* The header of one lossless-JPEG stream as the decoder reads it (ReadFileHeader, GetDht,
+ * GetDri, GetSof, GetSos: src/gls_dng_lossless_jpeg.cpp:590-1000).  Host only, no context or
+ * device needed.  GLS_ERR_BAD_STREAM where gls_dng_decode_lossless_jpeg rejects the header. */
+typedef struct {
+    int width;            /* samples per component per row (the frame's X) */
+    int height;           /* rows (the frame's Y) */
+    int components;       /* components of the scan (interleaved per MCU) */
+    int precision;        /* bits per sample */
+    int predictor;        /* 1-7 (0: none) */
+    int point_transform;  /* Pt */
+    int restart_interval; /* MCUs per restart interval, 0: none */
+    int tables_alike;     /* 1 when every table of the scan splits bits into codewords alike */
+} gls_ljpeg_info;
+GLS_API gls_status gls_lossless_jpeg_info(const uint8_t* data, size_t size, gls_ljpeg_info* info);
+
 /* ---- host colour math (demosaic_utils.cpp:25-52, 809-822; gls_linalg.hpp:545-556) ---- */
 GLS_API gls_status gls_cam_xyz_coeff(const float cam_xyz[9], float pre_mul[3], float rgb_cam[9]);
 GLS_API gls_status gls_cam_ycbcr(const float rgb_cam[9], float out[9]);
