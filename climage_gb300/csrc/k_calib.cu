@@ -265,3 +265,15 @@ extern "C" gls_status gls_estimate_raw_parameters(gls_ctx* ctx, const gls_image_
                          "estimateRawParameters: the fitted camera matrix has a white at or below 1e-5");
     return GLS_OK;
 }
+
+extern "C" gls_status gls_fit_color_checker(const float mean[96], const float var[96], float cam_xyz[9],
+                                            float pre_mul[3], float raw_nlf[4]) {
+    if (!mean || !var || !cam_xyz || !pre_mul || !raw_nlf) return GLS_ERR_INVALID_ARGUMENT;
+    float st[24 * 8];
+    for (int q = 0; q < 24; q++)
+        for (int c = 0; c < 4; c++) {
+            st[q * 8 + c] = mean[q * 4 + c];
+            st[q * 8 + 4 + c] = var[q * 4 + c];
+        }
+    return chart_fit(st, cam_xyz, pre_mul, raw_nlf) ? GLS_OK : GLS_ERR_INVALID_ARGUMENT;
+}

@@ -126,6 +126,7 @@ SIGNATURES = [
     ("gls_dng_decode_lossless_jpeg", _I, [_P, _P, ctypes.c_size_t, _I, ctypes.POINTER(ctypes.c_uint64),
                                           ctypes.POINTER(ctypes.c_uint64), _I, _I, _D]),
     ("gls_lossless_jpeg_info", _I, [_P, ctypes.c_size_t, ctypes.POINTER(LjpegInfo)]),
+    ("gls_fit_color_checker", _I, [_FP, _FP, _FP, _FP, _FP]),
     ("gls_color_checker_raw_stats", _I, [_P, _D, _F, _F, _I, ctypes.POINTER(ctypes.c_int), _I, _FP, _FP]),
     ("gls_estimate_raw_parameters", _I, [_P, _D, _F, _F, _I, ctypes.POINTER(ctypes.c_int), _I, _FP, _FP, _FP]),
     ("gls_selftest", _I, [_P, ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)]),
@@ -230,6 +231,16 @@ def lossless_jpeg_info(data):
     if s != GLS_OK:
         raise GlsError(s, "lossless_jpeg_info")
     return {n: getattr(info, n) for n, _ in LjpegInfo._fields_}
+
+
+def fit_color_checker(mean, var):
+    """The fit half of estimateRawParameters from colorCheckerRawStats' (mean, var), each (24, 4):
+    (cam_xyz (3, 3), pre_mul (3,), raw NLF slopes (4,)).  Host only."""
+    cx, pm, nlf = (ctypes.c_float * 9)(), (ctypes.c_float * 3)(), (ctypes.c_float * 4)()
+    s = lib().gls_fit_color_checker(farr(np.ravel(mean), 96), farr(np.ravel(var), 96), cx, pm, nlf)
+    if s != GLS_OK:
+        raise GlsError(s, "fit_color_checker")
+    return (np.array(cx[:], np.float32).reshape(3, 3), np.array(pm[:], np.float32), np.array(nlf[:], np.float32))
 
 
 # ---- device images ----

@@ -242,6 +242,14 @@ GLS_API gls_status gls_estimate_raw_parameters(gls_ctx* ctx, const gls_image_des
                                                float white_level, int bayer_pattern, const int gmb_rect[4],
                                                int rotate_180, float cam_xyz[9], float pre_mul[3], float raw_nlf[4]);
 
+/* The fit half of estimateRawParameters from colorCheckerRawStats' output (mean and var as
+ * that call returns them, patch-major, 4 CFA channels each): matrixFromColorChecker
+ * (demosaic_utils.cpp:83-129) and the raw noise regression over the six neutral patches
+ * (linear_regression, 604-621, as estimateRawParameters applies them at 764-784).  Host only.  GLS_ERR_INVALID_ARGUMENT when the fitted matrix has a
+ * white at or below 1e-5, as gls_estimate_raw_parameters. */
+GLS_API gls_status gls_fit_color_checker(const float mean[96], const float var[96], float cam_xyz[9],
+                                         float pre_mul[3], float raw_nlf[4]);
+
 /* DecodeLosslessJPEG (src/gls_dng_lossless_jpeg.cpp:3253-3275) over the tiles or the strip of
  * a DNG image, as the DNG reader calls it (src/gls_image_tiff.cpp:369-440): data is host
  * memory holding the n_streams lossless-JPEG streams (stream i at offsets[i], sizes[i] bytes:

@@ -207,3 +207,21 @@ def test_fp64_error_oracle_close_to_fp32():
     assert np.percentile(d, 99) < 5e-3
     mse = np.mean(np.clip(d, 0, 1) ** 2)
     assert 10 * np.log10(1.0 / max(mse, 1e-20)) > 50.0
+
+
+def test_product_chart_fit_equals_reference():
+    """The product's host-side fit (gls_fit_color_checker, no GPU needed), fed the oracle's
+    patch statistics, gives the reference's matrix, white point and noise slopes bit for bit."""
+    from tests import calib_frames
+    with open(os.path.join(GOLDEN, "ref_calib.json")) as f:
+        golden = json.load(f)
+    for case in calib_frames.CASES:
+        fx = golden[case[0]]
+        raw, black, white, bayer, gmb, rot = calib_frames.make(case)
+        mean, var = orc.color_checker_raw_stats(raw, black, white, bayer, gmb, rot)
+        cx, pm, nlf = gls.fit_color_checker(mean, var)
+        for got, key in ((cx, "cam_xyz"), (pm, "pre_mul"), (nlf, "raw_nlf")):
+            np.testing.assert_array_equal(np.ravel(got).view(np.uint32), np.array(fx[key], np.uint32),
+                                          err_msg=case[0] + " " + key)
+    with pytest.raises(gls.GlsError):  # a chart with no signal has no white point
+        gls.fit_color_checker(np.zeros((24, 4), np.float32), np.zeros((24, 4), np.float32))
