@@ -492,3 +492,175 @@ def matmul3x3(a, b):
 
 def atan2pi(y, x):
     return lib().oracle_atan2pi(y, x)
+
+
+# ---- the reference's own kernel file (demosaic.cl) run on the CPU through oracle/clref ----
+# (built by `make -C oracle clref` where the reference sources are; a checker of this
+# oracle's restatement, never of the product directly)
+CLREF_PATH = os.path.join(HERE, "_ref", "libclref.so")
+_clref = None
+
+
+def clref_lib():
+    """The reference's demosaic.cl compiled as C++ against oracle/clref/cl_shim.h, or None."""
+    global _clref
+    if _clref is None and os.path.exists(CLREF_PATH):
+        _clref = ctypes.CDLL(CLREF_PATH)
+    return _clref
+
+
+def _clref_call(name, *args):
+    if clref_lib() is None:
+        raise FileNotFoundError(CLREF_PATH)
+    rc = getattr(clref_lib(), name)(*args)
+    if rc != 0:
+        raise ValueError("%s: a vector condition had components that disagree" % name)
+
+
+def clref_scale_raw(raw, bayer, scale_mul, black_norm):
+    raw = np.ascontiguousarray(raw, dtype=np.uint16)
+    h, w = raw.shape
+    out = np.zeros((h, w), np.float32)
+    _clref_call("clref_scale_raw", _p(raw), w, h, bayer, _arr(scale_mul, 4), ctypes.c_float(black_norm), _p(out))
+    return out
+
+
+def clref_interpolate_green(scaled, bayer, luma_variance):
+    s = _f32(scaled)
+    h, w = s.shape
+    out = np.zeros((h, w), np.float32)
+    _clref_call("clref_interpolate_green", _p(s), w, h, bayer, ctypes.c_float(luma_variance), _p(out))
+    return out
+
+
+def clref_interpolate_red_blue(scaled, green, bayer, chroma_variance):
+    s, g = _f32(scaled), _f32(green)
+    h, w = s.shape
+    out = np.zeros((h, w, 4), np.float32)
+    _clref_call("clref_interpolate_red_blue", _p(s), _p(g), w, h, bayer, ctypes.c_float(chroma_variance), _p(out))
+    return out
+
+
+def clref_blend_highlights(img, clip=1.0):
+    a = _f32(img)
+    h, w, _ = a.shape
+    out = np.zeros_like(a)
+    _clref_call("clref_blend_highlights", _p(a), w, h, ctypes.c_float(clip), _p(out))
+    return out
+
+
+def clref_transform(img, m):
+    a = _f32(img)
+    h, w, _ = a.shape
+    out = np.zeros_like(a)
+    _clref_call("clref_transform", _p(a), w, h, _arr(np.ravel(m), 9), _p(out))
+    return out
+
+
+def clref_noise_statistics(img):
+    a = _f32(img)
+    h, w, _ = a.shape
+    out = np.zeros_like(a)
+    _clref_call("clref_noise_statistics", _p(a), w, h, _p(out))
+    return out
+
+
+def clref_raw_noise_statistics(scaled, bayer):
+    s = _f32(scaled)
+    h, w = s.shape
+    mean = np.zeros((h // 2, w // 2, 4), np.float32)
+    var = np.zeros((h // 2, w // 2, 4), np.float32)
+    _clref_call("clref_raw_noise_statistics", _p(s), w, h, bayer, _p(mean), _p(var))
+    return mean, var
+
+
+def clref_denoise_bilateral(img, var_a, var_b, chroma_boost, gradient_boost):
+    a = _f32(img)
+    h, w, _ = a.shape
+    out = np.zeros_like(a)
+    _clref_call("clref_denoise_bilateral", _p(a), w, h, _arr(var_a, 3), _arr(var_b, 3), ctypes.c_float(chroma_boost),
+                ctypes.c_float(gradient_boost), _p(out))
+    return out
+
+
+def clref_downsample(img, ow, oh):
+    a = _f32(img)
+    h, w, _ = a.shape
+    out = np.zeros((oh, ow, 4), np.float32)
+    _clref_call("clref_downsample", _p(a), w, h, ow, oh, _p(out))
+    return out
+
+
+def clref_reassemble(den0, img1, den1, sharpening, nlf):
+    d0, i1, d1 = _f32(den0), _f32(img1), _f32(den1)
+    h, w, _ = d0.shape
+    h1, w1, _ = i1.shape
+    out = np.zeros_like(d0)
+    _clref_call("clref_reassemble", _p(d0), w, h, _p(i1), _p(d1), w1, h1, ctypes.c_float(sharpening), _arr(nlf, 2),
+                _p(out))
+    return out
+
+
+def clref_ltm_mask(img, guide, ltm, m):
+    """ltm: (guidedFilterEps, shadows, highlights, detail)."""
+    a, g = _f32(img), _f32(guide)
+    h, w, _ = a.shape
+    gh, gw, _ = g.shape
+    out = np.zeros((h, w), np.float32)
+    _clref_call("clref_ltm_mask", _p(a), w, h, _p(g), gw, gh, _arr(ltm, 4), _arr(np.ravel(m), 9), _p(out))
+    return out
+
+
+def clref_convert_to_srgb(img, mask, m, rgb, local_tone_mapping, out_u8=True):
+    """rgb: (contrast, saturation, toneCurveSlope, exposureBias, blacks)."""
+    a, mk = _f32(img), _f32(mask)
+    h, w, _ = a.shape
+    if out_u8:
+        out = np.zeros((h, w, 4), np.uint8)
+        _clref_call("clref_convert_to_srgb", _p(a), _p(mk), w, h, _arr(np.ravel(m), 9), _arr(rgb, 5),
+                    int(local_tone_mapping), _p(out), None)
+    else:
+        out = np.zeros((h, w, 4), np.float32)
+        _clref_call("clref_convert_to_srgb", _p(a), _p(mk), w, h, _arr(np.ravel(m), 9), _arr(rgb, 5),
+                    int(local_tone_mapping), None, _p(out))
+    return out
+
+
+def clref_fast_debayer(scaled, bayer):
+    s = _f32(scaled)
+    h, w = s.shape
+    out = np.zeros((h // 2, w // 2, 4), np.float32)
+    _clref_call("clref_fast_debayer", _p(s), w, h, bayer, _p(out))
+    return out
+
+
+def clref_bayer_to_rgba(scaled, bayer):
+    s = _f32(scaled)
+    h, w = s.shape
+    out = np.zeros((h // 2, w // 2, 4), np.float32)
+    _clref_call("clref_bayer_to_rgba", _p(s), w, h, bayer, _p(out))
+    return out
+
+
+def clref_rgba_to_bayer(rgba, bayer):
+    a = _f32(rgba)
+    qh, qw, _ = a.shape
+    out = np.zeros((2 * qh, 2 * qw), np.float32)
+    _clref_call("clref_rgba_to_bayer", _p(a), qw, qh, bayer, _p(out))
+    return out
+
+
+def clref_denoise_rgba(img, raw_variance):
+    a = _f32(img)
+    h, w, _ = a.shape
+    out = np.zeros_like(a)
+    _clref_call("clref_denoise_rgba", _p(a), w, h, _arr(raw_variance, 4), _p(out))
+    return out
+
+
+def clref_denoise_guided(img, var_a, var_b):
+    a = _f32(img)
+    h, w, _ = a.shape
+    out = np.zeros_like(a)
+    _clref_call("clref_denoise_guided", _p(a), w, h, _arr(var_a, 3), _arr(var_b, 3), _p(out))
+    return out
