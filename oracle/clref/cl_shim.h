@@ -9,7 +9,8 @@
 //     from scalars and vectors, component-wise arithmetic, comparisons (true = -1) and
 //     && / ||, any / all; a vector used as a condition must agree in every component
 //     (C++ cannot select per component there): otherwise the run is reported as failed;
-//   * built-ins: sqrt, fabs, fmin/fmax, mix, clamp, smoothstep, step, length, dot, atan2pi,
+//   * built-ins (half-precision mix and smoothstep round every operation to binary16, as an
+//     fp16 ALU does): sqrt, fabs, fmin/fmax, mix, clamp, smoothstep, step, length, dot, atan2pi,
 //     tanh, pow/powr, native_powr(x, 0.5) = sqrt(x), copysign, convert_float2..4, and
 //     min / max / abs with the selects of the kernel file's own macros, applied per
 //     component to vectors;
@@ -294,6 +295,15 @@ inline float powr(float x, float y) { return glsm::powr_(x, y); }
 inline float native_powr(float x, float y) { return y == 0.5f ? glsm::sqrt_(x) : glsm::powr_(x, y); }
 inline float copysign(float x, float s) { return glsm::copysign_(x, s); }
 inline float mix(float a, float b, float t) { return glsm::mix_(a, b, t); }
+// half arithmetic: every operation rounded to binary16, as an fp16 ALU computes it
+inline float hr(float v) { return glsm::round_half(v); }
+inline half mix(half x, half y, half t) {
+    return (half)hr((float)x + hr(hr((float)y - (float)x) * (float)t));
+}
+inline half smoothstep(half e0, half e1, half x) {
+    const float u = glsm::clamp_(hr(glsm::div_(hr((float)x - (float)e0), hr((float)e1 - (float)e0))), 0.0f, 1.0f);
+    return (half)hr(hr(u * u) * hr(3.0f - hr(2.0f * u)));
+}
 inline float clamp(float x, float lo, float hi) { return glsm::clamp_(x, lo, hi); }
 inline float smoothstep(float e0, float e1, float x) { return glsm::smoothstep_ref(e0, e1, x); }
 
@@ -338,6 +348,24 @@ inline float length(const float4& a) { return glsm::length4_(a.x, a.y, a.z, a.w)
 inline float2 convert_float2(const int2& a) { return float2((float)a.x, (float)a.y); }
 inline float3 convert_float3(const int3& a) { return float3((float)a.x, (float)a.y, (float)a.z); }
 inline float4 convert_float4(const int4& a) { return float4((float)a.x, (float)a.y, (float)a.z, (float)a.w); }
+
+// cond ? a : b with OpenCL's semantics: a vector condition selects per component (true = the
+// sign bit set), a scalar one picks a side
+template <class A, class B, class Cd>
+inline A clref_select(const A& a, const B& b, const Cd& cond) {
+    if constexpr (clshim::scalar_v<Cd> || std::is_same_v<Cd, bool>) {
+        return cond ? a : (A)b;
+    } else {
+        A r;
+        for (int k = 0; k < ncomp<Cd>::value; k++) {
+            decltype(r.c[0] + 0) ak, bk;
+            if constexpr (clshim::scalar_v<A>) ak = a; else ak = a.c[k];
+            if constexpr (clshim::scalar_v<B>) bk = b; else bk = b.c[k];
+            r.c[k] = cond.c[k] < 0 ? ak : bk;
+        }
+        return r;
+    }
+}
 
 // min / max / abs: the kernel file's own macros (plain selects), per component on vectors;
 // the macros are redirected here so that they still expand before name lookup.

@@ -154,4 +154,15 @@ int clref_denoise_guided(const float* in_p, int w, int h, const float var_a[3], 
     return run2d(w, h, [&] { denoiseImageGuided(&in, a, b, &o); });
 }
 
+int clref_despeckle(const float* in_p, int w, int h, const float var_a[3], const float var_b[3], float* out) {
+    cl_image in = img(in_p, w, h, 4, CLSHIM_F32), o = img(out, w, h, 4, CLSHIM_F32);
+    const float3 a(var_a[0], var_a[1], var_a[2]), b(var_b[0], var_b[1], var_b[2]);
+    return run2d(w, h, [&] { despeckleLumaMedianChromaImage(&in, a, b, &o); });
+}
+
+int clref_despeckle_rgba(const float* in_p, int w, int h, float* out) {
+    cl_image in = img(in_p, w, h, 4, CLSHIM_F32), o = img(out, w, h, 4, CLSHIM_F32);
+    return run2d(w, h, [&] { despeckleRawRGBAImage(&in, &o); });
+}
+
 }  // extern "C"

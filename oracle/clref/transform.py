@@ -6,7 +6,9 @@ syntax C++ lacks is rewritten; no statement of a kernel changes:
   * half literals such as 1.0h become float literals (converted where they are used);
   * the file's min / max / abs macros (GNU statement expressions that C++ cannot apply to
     vectors) expand to cl_shim.h's functions instead, the same selects per component;
-  * a swizzle that is assigned to (.yz *= s) becomes a write proxy, .yz_ref().
+  * a swizzle that is assigned to (.yz *= s) becomes a write proxy, .yz_ref();
+  * x = cond ? a : b; (plain identifiers) becomes clref_select(a, b, cond), which selects
+    per component when cond is a vector, as OpenCL does.
 
     python transform.py <demosaic.cl> <out.cpp>
 """
@@ -21,6 +23,9 @@ def transform(src):
     src = re.sub(r"\.xyz\b(?!\s*\(|_ref)", ".xyz()", src)
     src = re.sub(r"\.yz\b(?!\s*\(|_ref)", ".yz()", src)
     src = re.sub(r"\b(\d+\.\d*)h\b", r"\1f", src)
+    # x = cond ? a : b; with plain identifiers: OpenCL selects per component when cond is a
+    # vector, which C++'s ?: cannot do; clref_select does both (a scalar cond picks one side)
+    src = re.sub(r"(\b\w+) = ([^;?]+?) \? (\w+) : (\w+);", r"\1 = clref_select(\3, \4, \2);", src)
     # the min / max / abs macros: same names, expanded to the shim's per-component selects
     for name, args in (("min", "a, b"), ("max", "a, b"), ("abs", "a")):
         src = re.sub(r"#define %s\(%s\)(?:[^\n]*\\\n)*[^\n]*\n" % (name, re.escape(args)),

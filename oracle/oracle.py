@@ -664,3 +664,19 @@ def clref_denoise_guided(img, var_a, var_b):
     out = np.zeros_like(a)
     _clref_call("clref_denoise_guided", _p(a), w, h, _arr(var_a, 3), _arr(var_b, 3), _p(out))
     return out
+
+
+def clref_despeckle(img, var_a, var_b):
+    a = _f32(img)
+    h, w, _ = a.shape
+    out = np.zeros_like(a)
+    _clref_call("clref_despeckle", _p(a), w, h, _arr(var_a, 3), _arr(var_b, 3), _p(out))
+    return out
+
+
+def clref_despeckle_rgba(img):
+    a = _f32(img)
+    h, w, _ = a.shape
+    out = np.zeros_like(a)
+    _clref_call("clref_despeckle_rgba", _p(a), w, h, _p(out))
+    return out

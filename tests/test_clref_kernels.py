@@ -4,10 +4,10 @@ source: CLImage's demosaic.cl, rewritten only where C++ syntax differs
 and run on the CPU (oracle/_ref/libclref.so, `make -C oracle clref`).  Both sides use the same
 conventions for what OpenCL leaves open (gls_clmath.h: edge clamping, the linear sampler's
 8-bit fractions, IEEE fp32 without contraction, the transcendental fits), so every kernel
-below must give the oracle's bits exactly, on every CFA phase and at two noise levels.  Runs
-where the reference sources are (skipped elsewhere).  Not covered here: the kernels whose
-arithmetic is in half precision (despeckleLumaMedianChromaImage, the median filters,
-despeckleRawRGBAImage) and guided_filter.cl."""
+below must give the oracle's bits exactly, on every CFA phase and at two noise levels
+(half-precision arithmetic rounds every operation to binary16, as an fp16 ALU does).  Runs
+where the reference sources are (skipped elsewhere).  Not covered here: guided_filter.cl and
+the kernels the pipeline never binds (median filters, false-colour removal, sharpening)."""
 import numpy as np
 import pytest
 
@@ -60,6 +60,7 @@ def test_raw_domain_kernels(frame):
     same(orc.clref_rgba_to_bayer(q, bayer), orc.rgba_to_bayer(q, bayer))
     rv = [2e-4, 1e-4, 2.5e-4, 1e-4]
     same(orc.clref_denoise_rgba(q, rv), orc.denoise_rgba(q, rv))
+    same(orc.clref_despeckle_rgba(q), orc.despeckle_rgba(q))  # float4 selects per component
 
 
 def test_colour_and_denoise_kernels(frame):
@@ -76,6 +77,9 @@ def test_colour_and_denoise_kernels(frame):
     for cb, gb in ((1.0, 1.0), (2.0, 4.0)):
         same(orc.clref_denoise_bilateral(y, va, vb, cb, gb), orc.denoise_bilateral(y, va, vb, cb, gb))
     same(orc.clref_denoise_guided(y, va, vb), orc.denoise_guided(y, va, vb))
+    # despeckleImage binds despeckleLumaMedianChromaImage: fp16 reads and fp16 arithmetic
+    dsa, dsb = [2e-5, 1e-5, 1e-5], [4e-4, 2e-4, 2e-4]
+    same(orc.clref_despeckle(y, dsa, dsb), orc.despeckle(y, dsa, dsb))
 
 
 def test_pyramid_ltm_and_srgb_kernels(frame):
