@@ -5,7 +5,7 @@
 // What it provides, under the conventions the oracle and the CUDA kernels share
 // (climage_gb300/csrc/gls_clmath.h):
 //   * vector types int2..int4, float2..float4, half2..half4 with component access, the
-//     .xyz / .yz swizzles (read as values, written through a proxy), literals flattened
+//     .xyz / .yz / .xy swizzles (read as values; .xyz / .yz written through a proxy), literals flattened
 //     from scalars and vectors, component-wise arithmetic, comparisons (true = -1) and
 //     && / ||, any / all; a vector used as a condition must agree in every component
 //     (C++ cannot select per component there): otherwise the run is reported as failed;
@@ -17,7 +17,7 @@
 //   * images: read_imagef / read_imageh without a sampler (clamp to the edge), with the
 //     linear sampler (normalised coordinates, clamp to the edge, fractions quantised to 8
 //     bits, the four texels blended in the order w00, w10, w01, w11), write_imagef /
-//     write_imageh, get_image_dim; UNORM16 reads divide by 65535;
+//     write_imageh, get_image_dim; 1-, 2- and 4-channel images; UNORM16 reads divide by 65535;
 //   * get_global_id, set per work item by the driver.
 // The kernel file is compiled with -fsingle-precision-constant (the reference builds it with
 // -cl-single-precision-constant) and -ffp-contract=off.
@@ -108,6 +108,7 @@ struct V<T, 3> {
     CLSHIM_VEC_BODY(3)
     V<T, 3> xyz() const { return V<T, 3>(x, y, z); }
     V<T, 2> yz() const { return V<T, 2>(y, z); }
+    V<T, 2> xy() const { return V<T, 2>(x, y); }
     Swz<T, 3, 3> xyz_ref() { return Swz<T, 3, 3>{*this, 0}; }
     Swz<T, 3, 2> yz_ref() { return Swz<T, 3, 2>{*this, 1}; }
 };
@@ -122,6 +123,7 @@ struct V<T, 4> {
     CLSHIM_VEC_BODY(4)
     V<T, 3> xyz() const { return V<T, 3>(x, y, z); }
     V<T, 2> yz() const { return V<T, 2>(y, z); }
+    V<T, 2> xy() const { return V<T, 2>(x, y); }
     Swz<T, 4, 3> xyz_ref() { return Swz<T, 4, 3>{*this, 0}; }
     Swz<T, 4, 2> yz_ref() { return Swz<T, 4, 2>{*this, 1}; }
 };
@@ -433,6 +435,7 @@ inline float clshim_get(const cl_image* im, int x, int y, int k) {
 
 inline float4 read_imagef(image2d_t im, int2 pos) {
     if (im->ch == 1) return float4(clshim_get(im, pos.x, pos.y, 0), 0.0f, 0.0f, 1.0f);
+    if (im->ch == 2) return float4(clshim_get(im, pos.x, pos.y, 0), clshim_get(im, pos.x, pos.y, 1), 0.0f, 1.0f);
     return float4(clshim_get(im, pos.x, pos.y, 0), clshim_get(im, pos.x, pos.y, 1), clshim_get(im, pos.x, pos.y, 2),
                   clshim_get(im, pos.x, pos.y, 3));
 }

@@ -8,8 +8,11 @@
 #include <cstdint>
 #include <cstring>
 
+#include <vector>
+
 #include "cl_shim.h"
 #include CLREF_SOURCE
+#include CLREF_GF_SOURCE
 
 namespace {
 
@@ -163,6 +166,40 @@ int clref_despeckle(const float* in_p, int w, int h, const float var_a[3], const
 int clref_despeckle_rgba(const float* in_p, int w, int h, float* out) {
     cl_image in = img(in_p, w, h, 4, CLSHIM_F32), o = img(out, w, h, 4, CLSHIM_F32);
     return run2d(w, h, [&] { despeckleRawRGBAImage(&in, &o); });
+}
+
+// GuidedFilter::filter (guided_filter.cpp:195-225): the reference's host sequence of
+// guided_filter.cl kernels, every BoxBlur::blur (guided_filter.cpp:25-48) two boxBlurX passes
+// through a transposed temporary; fp32 intermediates, mean_I in the input's storage (fp32).
+int clref_guided_filter(const float* in_p, int w, int h, int filter_size, const float eps_p[3], float* out) {
+    const size_t n = (size_t)w * h;
+    std::vector<float> mean_I(4 * n), inv1(4 * n), inv2(2 * n), cr(4 * n), cg(4 * n), cb(4 * n), tmp(4 * n);
+    cl_image in = img(in_p, w, h, 4, CLSHIM_F32), o = img(out, w, h, 4, CLSHIM_F32);
+    cl_image mI = img(mean_I.data(), w, h, 4, CLSHIM_F32), s1 = img(inv1.data(), w, h, 4, CLSHIM_F32),
+             s2 = img(inv2.data(), w, h, 2, CLSHIM_F32), r = img(cr.data(), w, h, 4, CLSHIM_F32),
+             g = img(cg.data(), w, h, 4, CLSHIM_F32), b = img(cb.data(), w, h, 4, CLSHIM_F32);
+    int rc = 0;
+    auto blur = [&](cl_image* src, cl_image* dst) {
+        cl_image t = img(tmp.data(), src->h, src->w, src->ch, CLSHIM_F32);
+        rc |= run2d(src->w, src->h, [&] { boxBlurX(src, filter_size, &t); });
+        rc |= run2d(t.w, t.h, [&] { boxBlurX(&t, filter_size, dst); });
+    };
+    const float3 eps(eps_p[0], eps_p[1], eps_p[2]);
+    blur(&in, &mI);
+    rc |= run2d(w, h, [&] { covMatrixProducts(&in, &s1, &s2); });
+    blur(&s1, &s1);
+    blur(&s2, &s2);
+    rc |= run2d(w, h, [&] { invSigma(&mI, &s1, &s2, eps, &s1, &s2); });
+    rc |= run2d(w, h, [&] { meanIpProducts(&in, &r, &g, &b); });
+    blur(&r, &r);
+    blur(&g, &g);
+    blur(&b, &b);
+    rc |= run2d(w, h, [&] { computeAb(&mI, &r, &g, &b, &s1, &s2, &r, &g, &b); });
+    blur(&r, &r);
+    blur(&g, &g);
+    blur(&b, &b);
+    rc |= run2d(w, h, [&] { computeResult(&in, &r, &g, &b, &o); });
+    return rc;
 }
 
 }  // extern "C"

@@ -1,8 +1,8 @@
-"""Rewrites CLImage's demosaic.cl so that it compiles as C++ against cl_shim.h (TEST
+"""Rewrites CLImage's OpenCL kernel files (demosaic.cl, guided_filter.cl) so that they compile as C++ against cl_shim.h (TEST
 INFRASTRUCTURE ONLY).  The output goes to oracle/_ref/ and is never committed.  Only the
 syntax C++ lacks is rewritten; no statement of a kernel changes:
   * vector literals (int2)(a, b) / (float4) (v, 0) become constructor calls int2(a, b);
-  * the .xyz and .yz swizzles (only ever read) become calls .xyz() / .yz();
+  * the .xyz, .yz and .xy swizzles that are read become calls .xyz() / .yz() / .xy();
   * half literals such as 1.0h become float literals (converted where they are used);
   * the file's min / max / abs macros (GNU statement expressions that C++ cannot apply to
     vectors) expand to cl_shim.h's functions instead, the same selects per component;
@@ -10,7 +10,7 @@ syntax C++ lacks is rewritten; no statement of a kernel changes:
   * x = cond ? a : b; (plain identifiers) becomes clref_select(a, b, cond), which selects
     per component when cond is a vector, as OpenCL does.
 
-    python transform.py <demosaic.cl> <out.cpp>
+    python transform.py <kernels.cl> <out.cpp>
 """
 import re
 import sys
@@ -22,6 +22,7 @@ def transform(src):
     src = re.sub(r"\.(xyz|yz)\b(?=\s*[-+*/]?=(?!=))", r".\1_ref()", src)
     src = re.sub(r"\.xyz\b(?!\s*\(|_ref)", ".xyz()", src)
     src = re.sub(r"\.yz\b(?!\s*\(|_ref)", ".yz()", src)
+    src = re.sub(r"\.xy\b(?!\s*\(|_ref|z)", ".xy()", src)
     src = re.sub(r"\b(\d+\.\d*)h\b", r"\1f", src)
     # x = cond ? a : b; with plain identifiers: OpenCL selects per component when cond is a
     # vector, which C++'s ?: cannot do; clref_select does both (a scalar cond picks one side)

@@ -680,3 +680,11 @@ def clref_despeckle_rgba(img):
     out = np.zeros_like(a)
     _clref_call("clref_despeckle_rgba", _p(a), w, h, _p(out))
     return out
+
+
+def clref_guided_filter(img, filter_size, eps):
+    a = _f32(img)
+    h, w, _ = a.shape
+    out = np.zeros_like(a)
+    _clref_call("clref_guided_filter", _p(a), w, h, int(filter_size), _arr(eps, 3), _p(out))
+    return out

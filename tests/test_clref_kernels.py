@@ -1,13 +1,13 @@
 """The oracle's restatement of the reference's kernels against the reference's own kernel
-source: CLImage's demosaic.cl, rewritten only where C++ syntax differs
+source: CLImage's demosaic.cl and guided_filter.cl, rewritten only where C++ syntax differs
 (oracle/clref/transform.py), compiled as C++ against the OpenCL-C shim oracle/clref/cl_shim.h
 and run on the CPU (oracle/_ref/libclref.so, `make -C oracle clref`).  Both sides use the same
 conventions for what OpenCL leaves open (gls_clmath.h: edge clamping, the linear sampler's
 8-bit fractions, IEEE fp32 without contraction, the transcendental fits), so every kernel
 below must give the oracle's bits exactly, on every CFA phase and at two noise levels
 (half-precision arithmetic rounds every operation to binary16, as an fp16 ALU does).  Runs
-where the reference sources are (skipped elsewhere).  Not covered here: guided_filter.cl and
-the kernels the pipeline never binds (median filters, false-colour removal, sharpening)."""
+where the reference sources are (skipped elsewhere).  Not covered here: the kernels the
+pipeline never binds (median filters, false-colour removal, sharpening)."""
 import numpy as np
 import pytest
 
@@ -80,6 +80,9 @@ def test_colour_and_denoise_kernels(frame):
     # despeckleImage binds despeckleLumaMedianChromaImage: fp16 reads and fp16 arithmetic
     dsa, dsb = [2e-5, 1e-5, 1e-5], [4e-4, 2e-4, 2e-4]
     same(orc.clref_despeckle(y, dsa, dsb), orc.despeckle(y, dsa, dsb))
+    # GuidedFilter::filter: guided_filter.cl's six kernels in the reference's host sequence
+    for fs in (3, 5):
+        same(orc.clref_guided_filter(y, fs, [1e-4, 1e-5, 1e-5]), orc.guided_filter(y, fs, [1e-4, 1e-5, 1e-5]))
 
 
 def test_pyramid_ltm_and_srgb_kernels(frame):
