@@ -1,0 +1,39 @@
+// gls_cl_image.hpp (stand-in) -- the few members of gls::cl_image_2d and gls::OpenCLContext
+// that the reference's pipeline host code (pyramidal_denoise.cpp and its headers) uses,
+// backed by host memory, so that its noise-model regressions compile and run on the CPU
+// without an OpenCL runtime.  TEST INFRASTRUCTURE ONLY (oracle/clref/ref_regress.cpp).
+#ifndef GLS_CL_IMAGE_STUB_HPP
+#define GLS_CL_IMAGE_STUB_HPP
+
+#include <memory>
+#include <span>
+#include <vector>
+
+#include "gls_image.hpp"
+
+namespace cl {
+struct Context {};
+}  // namespace cl
+
+namespace gls {
+
+class OpenCLContext {
+   public:
+    cl::Context clContext() { return {}; }
+};
+
+template <typename T>
+class cl_image_2d {
+   public:
+    typedef std::unique_ptr<cl_image_2d<T>> unique_ptr;
+    const int width, height;
+    mutable std::vector<T> pixels;
+
+    cl_image_2d(cl::Context, int w, int h) : width(w), height(h), pixels((size_t)w * h) {}
+    image<T> mapImage() const { return image<T>(width, height, std::span<T>(pixels.data(), pixels.size())); }
+    void unmapImage(const image<T>&) const {}
+};
+
+}  // namespace gls
+
+#endif

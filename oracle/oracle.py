@@ -688,3 +688,34 @@ def clref_guided_filter(img, filter_size, eps):
     out = np.zeros_like(a)
     _clref_call("clref_guided_filter", _p(a), w, h, int(filter_size), _arr(eps, 3), _p(out))
     return out
+
+
+# ---- the reference's own noise-model regressions (pyramidal_denoise.cpp) on given statistics ----
+REGRESS_PATH = os.path.join(HERE, "_ref", "libref_regress.so")
+_regress = None
+
+
+def ref_regress_lib():
+    """computeRawNoiseStatistics / computeNoiseStatistics compiled from the reference's source, or None."""
+    global _regress
+    if _regress is None and os.path.exists(REGRESS_PATH):
+        _regress = ctypes.CDLL(REGRESS_PATH, mode=os.RTLD_LAZY)
+    return _regress
+
+
+def ref_regress_raw(mean, var):
+    """computeRawNoiseStatistics' fit on quad statistics (h/2, w/2, 4): A0..A3, B0..B3."""
+    m, v = _f32(mean), _f32(var)
+    qh, qw, _ = m.shape
+    out = np.zeros(8, np.float32)
+    ref_regress_lib().ref_regress_raw(_p(m), _p(v), 2 * qw, 2 * qh, _p(out))
+    return out
+
+
+def ref_regress_level(stats):
+    """computeNoiseStatistics' fit on a noiseStatistics image (h, w, 4): A0..A2, B0..B2."""
+    s = _f32(stats)
+    h, w, _ = s.shape
+    out = np.zeros(6, np.float32)
+    ref_regress_lib().ref_regress_level(_p(s), w, h, _p(out))
+    return out

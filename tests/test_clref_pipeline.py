@@ -2,11 +2,13 @@
 kernels of demosaic.cl and guided_filter.cl run on the CPU (oracle/_ref/libclref.so), called
 in the order and with the parameters of RawConverter::demosaicImage
 (raw_converter.cpp:73-186) and PyramidalDenoise::denoise (pyramidal_denoise.cpp:104-149),
-the noise models fitted by the oracle's regression on the statistics those kernels produce
-(computeRawNoiseStatistics / computeNoiseStatistics feed every pixel of the statistics
-image to the fit).  The fitted noise models and every RGBA8 code must equal the oracle's
-demosaic: this pins the oracle's sequencing and parameter plumbing, the part of the path the
-kernel-by-kernel check leaves out.  Runs where the reference sources are (skipped elsewhere)."""
+the noise models fitted by the reference's own computeRawNoiseStatistics /
+computeNoiseStatistics (pyramidal_denoise.cpp, oracle/_ref/libref_regress.so) on the
+statistics those kernels produce.  Only the order of the calls is written here; every value
+comes from the reference's code.  The fitted noise models and every RGBA8 code must equal
+the oracle's demosaic: this pins the oracle's sequencing, parameter plumbing and regressions,
+the parts the kernel-by-kernel check leaves out.  Runs where the reference sources are
+(skipped elsewhere)."""
 import numpy as np
 import pytest
 
@@ -14,7 +16,8 @@ from climage_gb300 import configs, gls, synthetic
 from oracle import oracle as orc
 from tests.helpers import oracle_params
 
-pytestmark = pytest.mark.skipif(orc.clref_lib() is None, reason="the reference's kernel files are not built here")
+pytestmark = pytest.mark.skipif(orc.clref_lib() is None or orc.ref_regress_lib() is None,
+                                reason="the reference's kernel files and host code are not built here")
 
 F = np.float32
 
@@ -30,7 +33,7 @@ def reference_pipeline(raw, spec):
     h, w = raw.shape
     s = orc.clref_scale_raw(raw, bayer, spec["scale_mul"], F(spec["black_level"]) / F(65535))
     mean, var = orc.clref_raw_noise_statistics(s, bayer)
-    raw_nlf = orc.regress(mean.reshape(-1, 4), var.reshape(-1, 4))[4:8]
+    raw_nlf = orc.ref_regress_raw(mean, var)[4:8]  # noiseModel.rawNlf = B (raw_converter.cpp:108-109)
     if spec["noise_level"] > 0.6:  # high_noise_image
         q = orc.clref_bayer_to_rgba(s, bayer)
         q = orc.clref_despeckle_rgba(q)
@@ -49,8 +52,7 @@ def reference_pipeline(raw, spec):
         src = image if i == 0 else pyr[i - 1]
         if i < levels - 1:
             pyr.append(orc.clref_downsample(src, w >> (i + 1), h >> (i + 1)))
-        stats = orc.clref_noise_statistics(src).reshape(-1, 4)
-        nlf.append(orc.regress(stats[:, 0], stats[:, 1:]))
+        nlf.append(orc.ref_regress_level(orc.clref_noise_statistics(src)))
         cal.append(nlf[i] * nfl_multiplier(spec["denoise"][i]))
     den = [None] * levels
     d = spec["denoise"][levels - 1]
@@ -85,3 +87,20 @@ def test_pipeline_equals_one_built_from_the_reference_kernels(bayer, noise_level
     np.testing.assert_array_equal(raw_nlf, ref["raw_nlf"])
     np.testing.assert_array_equal(pyr_nlf, ref["pyramid_nlf"])
     np.testing.assert_array_equal(out[..., :3], ref["rgba8"][..., :3])
+
+
+@pytest.mark.parametrize("seed,gain,sigma,bayer", [(3, 4.0, 3.0, 2), (5, 16.0, 12.0, 0), (7, 1.0, 2.0, 1)])
+def test_oracle_regressions_equal_the_reference(seed, gain, sigma, bayer):
+    """The oracle's noise-model fits (raw and per level) against the reference's own
+    computeRawNoiseStatistics / computeNoiseStatistics on the same statistics images."""
+    raw, _, meta = synthetic.make_frame(256, 192, bayer=bayer, gain=gain, read_sigma=sigma, seed=seed)
+    spec = configs.make_spec(meta, levels=4)
+    s = orc.scale_raw(raw, bayer, spec["scale_mul"], spec["black_level"] / 65535.0)
+    m, v = orc.raw_noise_statistics(s, bayer)
+    np.testing.assert_array_equal(orc.regress(m.reshape(-1, 4), v.reshape(-1, 4)).view(np.uint32),
+                                  orc.ref_regress_raw(m, v).view(np.uint32))
+    g = orc.interpolate_green(s, bayer, 1e-3)
+    cy = gls.cam_ycbcr(np.array(spec["rgb_cam"], F).reshape(3, 3))
+    st = orc.noise_statistics(orc.transform(orc.interpolate_red_blue(s, g, bayer, 5e-4), cy))
+    np.testing.assert_array_equal(orc.regress(st.reshape(-1, 4)[:, 0], st.reshape(-1, 4)[:, 1:]).view(np.uint32),
+                                  orc.ref_regress_level(st).view(np.uint32))
