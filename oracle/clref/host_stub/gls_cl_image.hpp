@@ -31,6 +31,10 @@ class cl_image_2d {
 
     cl_image_2d(cl::Context, int w, int h) : width(w), height(h), pixels((size_t)w * h) {}
     image<T> mapImage() const { return image<T>(width, height, std::span<T>(pixels.data(), pixels.size())); }
+    void copyPixelsFrom(const image<T>& other) const {
+        for (int y = 0; y < height; y++)
+            for (int x = 0; x < width; x++) pixels[(size_t)y * width + x] = other[y][x];
+    }
     void unmapImage(const image<T>&) const {}
 };
 

@@ -3,7 +3,9 @@ INFRASTRUCTURE ONLY).  The output goes to oracle/_ref/ and is never committed.  
 syntax C++ lacks is rewritten; no statement of a kernel changes:
   * vector literals (int2)(a, b) / (float4) (v, 0) become constructor calls int2(a, b);
   * the .xyz, .yz and .xy swizzles that are read become calls .xyz() / .yz() / .xy();
-  * half literals such as 1.0h become float literals (converted where they are used);
+  * half literals such as 1.0h become float literals (converted where they are used), and
+    every floating constant gets an f suffix (the reference compiles the kernels with
+    -cl-single-precision-constant);
   * the file's min / max / abs macros (GNU statement expressions that C++ cannot apply to
     vectors) expand to cl_shim.h's functions instead, the same selects per component;
   * a swizzle that is assigned to (.yz *= s) becomes a write proxy, .yz_ref();
@@ -24,6 +26,8 @@ def transform(src):
     src = re.sub(r"\.yz\b(?!\s*\(|_ref)", ".yz()", src)
     src = re.sub(r"\.xy\b(?!\s*\(|_ref|z)", ".xy()", src)
     src = re.sub(r"\b(\d+\.\d*)h\b", r"\1f", src)
+    # floating constants are single precision (-cl-single-precision-constant): suffix them
+    src = re.sub(r"(?<![\w.])((?:\d+\.\d*|\.\d+)(?:[eE][-+]?\d+)?|\d+[eE][-+]?\d+)(?![\w.])", r"\1f", src)
     # x = cond ? a : b; with plain identifiers: OpenCL selects per component when cond is a
     # vector, which C++'s ?: cannot do; clref_select does both (a scalar cond picks one side)
     src = re.sub(r"(\b\w+) = ([^;?]+?) \? (\w+) : (\w+);", r"\1 = clref_select(\3, \4, \2);", src)

@@ -719,3 +719,40 @@ def ref_regress_level(stats):
     out = np.zeros(6, np.float32)
     ref_regress_lib().ref_regress_level(_p(s), w, h, _p(out))
     return out
+
+
+# ---- the reference's own RawConverter::demosaicImage, run on the CPU (oracle/clref/ref_pipeline.cpp) ----
+PIPELINE_PATH = os.path.join(HERE, "_ref", "libref_pipeline.so")
+_pipeline = None
+
+
+def ref_pipeline_lib():
+    global _pipeline
+    if _pipeline is None and os.path.exists(PIPELINE_PATH):
+        _pipeline = ctypes.CDLL(PIPELINE_PATH, mode=os.RTLD_LAZY)
+    return _pipeline
+
+
+def ref_raw_converter(raw, spec):
+    """The reference's RawConverter::demosaicImage (5 pyramid levels, bilateral denoiser) on a
+    uint16 frame with a spec dict (climage_gb300.configs.make_spec): (RGBA8, raw NLF (4,),
+    pyramid NLF (5, 6))."""
+    raw = np.ascontiguousarray(raw, np.uint16)
+    h, w = raw.shape
+    p = [spec["black_level"], spec["white_level"], spec["exposure_multiplier"], spec["noise_level"]]
+    p += list(spec["scale_mul"]) + list(spec["rgb_cam"]) + list(spec["raw_nlf"])
+    for row in spec["pyramid_nlf"]:
+        p += list(row)
+    for d in spec["denoise"]:
+        p += [d["luma"], d["chroma"], d["chromaBoost"], d["gradientBoost"], d["sharpening"]]
+    r, l = spec["rgb"], spec["ltm"]
+    p += [r["contrast"], r["saturation"], r["toneCurveSlope"], r["exposureBias"], r["blacks"]]
+    p += [l["guidedFilterEps"], l["shadows"], l["highlights"], l["detail"]]
+    params = np.array(p, np.float32)
+    out = np.zeros((h, w, 4), np.uint8)
+    rn, pn = np.zeros(4, np.float32), np.zeros(30, np.float32)
+    rc = ref_pipeline_lib().ref_raw_converter(_p(raw), w, h, int(spec["bayer_pattern"]), _p(params),
+                                              int(r["localToneMapping"]), _p(out), _p(rn), _p(pn))
+    if rc != 0:
+        raise ValueError("ref_raw_converter: a vector condition had components that disagree")
+    return out, rn, pn.reshape(5, 6)

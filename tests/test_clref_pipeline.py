@@ -104,3 +104,20 @@ def test_oracle_regressions_equal_the_reference(seed, gain, sigma, bayer):
     st = orc.noise_statistics(orc.transform(orc.interpolate_red_blue(s, g, bayer, 5e-4), cy))
     np.testing.assert_array_equal(orc.regress(st.reshape(-1, 4)[:, 0], st.reshape(-1, 4)[:, 1:]).view(np.uint32),
                                   orc.ref_regress_level(st).view(np.uint32))
+
+
+@pytest.mark.skipif(orc.ref_pipeline_lib() is None, reason="the reference's RawConverter is not built here")
+@pytest.mark.parametrize("bayer,noise_level,gain", [(2, 0.2, 2.0), (0, 0.45, 4.0), (3, 0.7, 16.0), (1, 0.2, 1.0)],
+                         ids=["rggb", "grbg", "bggr_high_noise", "gbrg"])
+def test_oracle_equals_the_reference_raw_converter(bayer, noise_level, gain):
+    """The reference's own RawConverter::demosaicImage (raw_converter.cpp, pyramidal_denoise.cpp,
+    demosaic_utils.cpp compiled unmodified; its OpenCL bindings supplied by
+    oracle/clref/ref_pipeline.cpp, each running its own demosaic.cl kernel on the CPU) against
+    the oracle on the same frame: the fitted noise models and every RGBA8 code equal."""
+    raw, _, meta = synthetic.make_frame(256, 192, bayer=bayer, gain=gain, read_sigma=6.0, seed=90 + bayer)
+    spec = configs.make_spec(meta, levels=5, noise_level=noise_level)
+    out, raw_nlf, pyr_nlf = orc.ref_raw_converter(raw, spec)
+    ref = orc.demosaic(raw, oracle_params(spec), orc.F32, want=("rgba8",))
+    np.testing.assert_array_equal(raw_nlf, ref["raw_nlf"])
+    np.testing.assert_array_equal(pyr_nlf, ref["pyramid_nlf"])
+    np.testing.assert_array_equal(out[..., :3], ref["rgba8"][..., :3])
