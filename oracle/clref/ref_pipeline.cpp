@@ -23,6 +23,7 @@ using clk::sampler_t;
 using clk::CLSHIM_U16;
 using clk::CLSHIM_U8;
 using clk::CLSHIM_F32;
+using clk::CLSHIM_F16;
 namespace clshim = clk::clshim;
 
 namespace {
@@ -30,7 +31,10 @@ namespace {
 template <class T>
 cl_image view(const gls::cl_image_2d<T>& im) {
     typedef typename T::dataType D;
-    const int kind = std::is_same_v<D, uint16_t> ? CLSHIM_U16 : (std::is_same_v<D, uint8_t> ? CLSHIM_U8 : CLSHIM_F32);
+    const int kind = std::is_same_v<D, uint16_t> ? CLSHIM_U16
+                     : std::is_same_v<D, uint8_t>  ? CLSHIM_U8
+                     : std::is_same_v<D, float>    ? CLSHIM_F32
+                                                   : CLSHIM_F16;  // the shipped build's __fp16 storage
     return cl_image{im.width, im.height, T::channels, kind, (void*)im.pixels.data()};
 }
 

@@ -122,7 +122,7 @@ C len4(C x, C y, C z, C w) { return M<C>::sqrt(x * x + y * y + z * z + w * w); }
 // how read_imageh converts a value to half.
 struct Pol {
     int prec;
-    bool half_storage() const { return prec == ORACLE_F16; }
+    bool half_storage() const { return prec == ORACLE_F16 || prec == ORACLE_F16_STATS; }
     bool half_reads() const { return prec != ORACLE_F64; }
 };
 
@@ -345,8 +345,15 @@ void regress(long n, int mc, int nc, GetMV get, double* outA, double* outB) {
     }
 }
 
+// One statistic as the regression reads it: an fp32 value, or the fp16 one an rgba_pixel_float
+// image of the shipped build holds (the host converts it to double exactly).
 template <class C>
-void compute_raw_nlf(const Img<C>& scaled, int bayer, float out[8]) {
+double stat_value(C v, bool half_stats) {
+    return half_stats ? (double)glsm::round_half((float)v) : (double)(float)v;
+}
+
+template <class C>
+void compute_raw_nlf(const Img<C>& scaled, int bayer, float out[8], bool half_stats = false) {
     Img<C> mean, var;
     raw_noise_statistics(scaled, bayer, mean, var);
     const long n = (long)mean.w * mean.h;
@@ -354,9 +361,10 @@ void compute_raw_nlf(const Img<C>& scaled, int bayer, float out[8]) {
     regress(n, 4, 4,
             [&](long i, double* m, double* v) {
                 for (int c = 0; c < 4; c++) {
-                    // statistics are kept in fp32 (the noise-model fit is an fp32 stage)
-                    m[c] = (double)(float)mean.d[(size_t)i * 4 + c];
-                    v[c] = (double)(float)var.d[(size_t)i * 4 + c];
+                    // statistics are kept in fp32 (the noise-model fit is an fp32 stage), or
+                    // in fp16 as the shipped build's meanImage/varImage hold them
+                    m[c] = stat_value(mean.d[(size_t)i * 4 + c], half_stats);
+                    v[c] = stat_value(var.d[(size_t)i * 4 + c], half_stats);
                 }
             },
             A, B);
@@ -397,15 +405,15 @@ void noise_statistics(const Img<C>& in, Img<C>& out) {
 }
 
 template <class C>
-void compute_nlf(const Img<C>& in, float out[6]) {
+void compute_nlf(const Img<C>& in, float out[6], bool half_stats = false) {
     Img<C> st;
     noise_statistics(in, st);
     const long n = (long)st.w * st.h;
     double A[4], B[4];
     regress(n, 1, 3,
             [&](long i, double* m, double* v) {
-                m[0] = (double)(float)st.d[(size_t)i * 4 + 0];
-                for (int c = 0; c < 3; c++) v[c] = (double)(float)st.d[(size_t)i * 4 + 1 + c];
+                m[0] = stat_value(st.d[(size_t)i * 4 + 0], half_stats);
+                for (int c = 0; c < 3; c++) v[c] = stat_value(st.d[(size_t)i * 4 + 1 + c], half_stats);
             },
             A, B);
     for (int c = 0; c < 3; c++) {
@@ -1312,7 +1320,7 @@ int demosaic(const uint16_t* raw, int w, int h, int stride, oracle_params* p, in
     Img<C> scaled;
     scale_raw(pol, raw, w, h, stride, p->bayer_pattern, p->scale_mul, p->black_level / 0xffff, scaled);
     float raw_nlf[8];
-    compute_raw_nlf(scaled, p->bayer_pattern, raw_nlf);
+    compute_raw_nlf(scaled, p->bayer_pattern, raw_nlf, prec == ORACLE_F16_STATS);
     for (int c = 0; c < 4; c++) p->raw_nlf[c] = raw_nlf[4 + c];
 
     if (high_noise) {
@@ -1351,7 +1359,7 @@ int demosaic(const uint16_t* raw, int w, int h, int stride, oracle_params* p, in
     for (int i = 0; i < L; i++) {
         const Img<C>& src = i == 0 ? image : pyr[i - 1];
         if (i < L - 1) downsample(pol, src, w >> (i + 1), h >> (i + 1), pyr[i]);
-        compute_nlf(src, p->pyramid_nlf[i]);
+        compute_nlf(src, p->pyramid_nlf[i], prec == ORACLE_F16_STATS);
         const float lm = p->denoise[i].luma * p->denoise[i].luma;
         const float cm = p->denoise[i].chroma * p->denoise[i].chroma;
         const float mul[6] = {lm, cm, cm, lm, cm, cm};

@@ -26,6 +26,8 @@ enum {
     ORACLE_F32 = 0,  // fp32 image storage, fp32 arithmetic (x86 macOS build of the reference)
     ORACLE_F16 = 1,  // fp16 image storage, fp32 arithmetic (the reference as shipped on ARM)
     ORACLE_F64 = 2,  // fp64 everywhere, no fp16 rounding: the error oracle
+    ORACLE_F16_STATS = 3,  // ORACLE_F16 with the noise-statistics images in fp16 too, as the
+                           // shipped build stores them (rgba_pixel_float, pyramidal_denoise.cpp:162,260-261)
 };
 
 typedef struct {

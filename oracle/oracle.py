@@ -13,6 +13,7 @@ LIB_PATH = os.path.join(HERE, "liboracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "libref_host.so")
 
 F32, F16, F64 = 0, 1, 2
+F16_STATS = 3  # F16 storage with the noise-statistics images in fp16 too (the shipped build)
 MAX_LEVELS = 8
 
 
@@ -722,21 +723,23 @@ def ref_regress_level(stats):
 
 
 # ---- the reference's own RawConverter::demosaicImage, run on the CPU (oracle/clref/ref_pipeline.cpp) ----
-PIPELINE_PATH = os.path.join(HERE, "_ref", "libref_pipeline.so")
-_pipeline = None
+PIPELINE_PATHS = {F32: os.path.join(HERE, "_ref", "libref_pipeline.so"),
+                  F16: os.path.join(HERE, "_ref", "libref_pipeline16.so")}
+_pipelines = {}
 
 
-def ref_pipeline_lib():
-    global _pipeline
-    if _pipeline is None and os.path.exists(PIPELINE_PATH):
-        _pipeline = ctypes.CDLL(PIPELINE_PATH, mode=os.RTLD_LAZY)
-    return _pipeline
+def ref_pipeline_lib(prec=F32):
+    """The reference's RawConverter built with fp32 image storage (prec F32) or with the fp16
+    storage it ships with (F16), or None."""
+    if prec not in _pipelines and os.path.exists(PIPELINE_PATHS[prec]):
+        _pipelines[prec] = ctypes.CDLL(PIPELINE_PATHS[prec], mode=os.RTLD_LAZY)
+    return _pipelines.get(prec)
 
 
-def ref_raw_converter(raw, spec):
+def ref_raw_converter(raw, spec, prec=F32):
     """The reference's RawConverter::demosaicImage (5 pyramid levels, bilateral denoiser) on a
     uint16 frame with a spec dict (climage_gb300.configs.make_spec): (RGBA8, raw NLF (4,),
-    pyramid NLF (5, 6))."""
+    pyramid NLF (5, 6)); prec selects the image storage it was built with."""
     raw = np.ascontiguousarray(raw, np.uint16)
     h, w = raw.shape
     p = [spec["black_level"], spec["white_level"], spec["exposure_multiplier"], spec["noise_level"]]
@@ -751,7 +754,7 @@ def ref_raw_converter(raw, spec):
     params = np.array(p, np.float32)
     out = np.zeros((h, w, 4), np.uint8)
     rn, pn = np.zeros(4, np.float32), np.zeros(30, np.float32)
-    rc = ref_pipeline_lib().ref_raw_converter(_p(raw), w, h, int(spec["bayer_pattern"]), _p(params),
+    rc = ref_pipeline_lib(prec).ref_raw_converter(_p(raw), w, h, int(spec["bayer_pattern"]), _p(params),
                                               int(r["localToneMapping"]), _p(out), _p(rn), _p(pn))
     if rc != 0:
         raise ValueError("ref_raw_converter: a vector condition had components that disagree")

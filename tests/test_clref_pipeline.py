@@ -121,3 +121,25 @@ def test_oracle_equals_the_reference_raw_converter(bayer, noise_level, gain):
     np.testing.assert_array_equal(raw_nlf, ref["raw_nlf"])
     np.testing.assert_array_equal(pyr_nlf, ref["pyramid_nlf"])
     np.testing.assert_array_equal(out[..., :3], ref["rgba8"][..., :3])
+
+
+@pytest.mark.skipif(orc.ref_pipeline_lib(orc.F16) is None,
+                    reason="the reference's RawConverter with fp16 storage is not built here")
+@pytest.mark.parametrize("bayer,noise_level,gain", [(2, 0.2, 2.0), (0, 0.45, 4.0), (3, 0.7, 16.0), (1, 0.2, 1.0)],
+                         ids=["rggb", "grbg", "bggr_high_noise", "gbrg"])
+def test_oracle_equals_the_reference_raw_converter_with_fp16_storage(bayer, noise_level, gain):
+    """The same RawConverter built with the image storage it ships with (USE_FP16_FLOATS,
+    gls_image.hpp:32,189-200: every rgba_pixel_float / luma_pixel_float image in binary16).
+    That build also keeps the noise-statistics images in fp16 (pyramidal_denoise.cpp:162,
+    260-261), so the oracle's F16_STATS mode equals it bit for bit: noise models (NaN where a
+    level has no pixel in the fit's range, on both sides) and every RGBA8 code.  The F16 mode,
+    which fits on fp32 statistics as the CUDA pipeline does, stays within 2 codes of it."""
+    raw, _, meta = synthetic.make_frame(256, 192, bayer=bayer, gain=gain, read_sigma=6.0, seed=90 + bayer)
+    spec = configs.make_spec(meta, levels=5, noise_level=noise_level, storage=gls.STORAGE_F16)
+    out, raw_nlf, pyr_nlf = orc.ref_raw_converter(raw, spec, orc.F16)
+    ref = orc.demosaic(raw, oracle_params(spec), orc.F16_STATS, want=("rgba8",))
+    np.testing.assert_array_equal(raw_nlf, ref["raw_nlf"])
+    np.testing.assert_array_equal(pyr_nlf, ref["pyramid_nlf"])
+    np.testing.assert_array_equal(out[..., :3], ref["rgba8"][..., :3])
+    f16 = orc.demosaic(raw, oracle_params(spec), orc.F16, want=("rgba8",))["rgba8"]
+    assert int(np.abs(out[..., :3].astype(int) - f16[..., :3].astype(int)).max()) <= 2
