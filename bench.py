@@ -12,11 +12,18 @@ value: MPix/s with the raw frames already in HBM, CUDA-event timed per step with
 flush (a 256 MB write) between steps, max over ranks.  e2e: the same frames through the
 host-buffer burst entry point (pinned uint16 in, RGBA8 out, copies inside the timed region).
 --impl reference times the CPU restatement of the reference pipeline (the oracle; the
-reference's OpenCL kernels cannot run on this machine) with every host thread.
+reference's OpenCL kernels cannot run on this machine) with every host thread, three frames
+per step as above; that arm imports no module of the product package and maps none of its
+libraries (the workload tables and the scene generator, plain numpy, are loaded from their
+files; the camera matrices come from the oracle's host math).
+--gpus N without a launcher's environment (WORLD_SIZE unset) starts N replicas itself under
+torch.distributed.run on 127.0.0.1.
 """
 import argparse
+import importlib.util
 import json
 import os
+import socket
 import subprocess
 import sys
 import threading
@@ -30,7 +37,7 @@ sys.path.insert(0, ROOT)
 METRIC = "RAW→RGB MPix/s on 1 GB300 (plain vs batched/learned) at PSNR vs FP64 oracle"
 
 
-def parse():
+def parse(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
@@ -44,7 +51,48 @@ def parse():
     ap.add_argument("--no-dng", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--profile-only", action="store_true", help="a short run for ncu: no clocks, no cpu leg")
-    return ap.parse_args()
+    ap.add_argument("--cpu-replicas", action="store_true",
+                    help="check the replica plumbing on the CPU (gloo): each rank runs the oracle on a tiny "
+                         "workload of its own frames; prints one check line, not a bench line")
+    return ap.parse_args(argv)
+
+
+def free_port():
+    with socket.socket(socket.AF_INET, socket.SOCK_STREAM) as sk:
+        sk.bind(("127.0.0.1", 0))
+        return sk.getsockname()[1]
+
+
+def launch_replicas(args, argv):
+    """--gpus N > 1 outside a launcher: start N processes of this script under
+    torch.distributed.run (one per GPU, rendezvous on 127.0.0.1) and return their exit code;
+    None when this process is already a rank (WORLD_SIZE set) or N == 1."""
+    if args.gpus <= 1 or "WORLD_SIZE" in os.environ:
+        return None
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node=%d" % args.gpus,
+           "--master-addr=127.0.0.1", "--master-port=%d" % free_port(), os.path.abspath(__file__)] + list(argv)
+    return subprocess.call(cmd, cwd=ROOT)
+
+
+def load_file(name, rel):
+    """A module loaded from its file alone (no package import, so nothing else of the package
+    and none of its native libraries comes with it)."""
+    spec = importlib.util.spec_from_file_location(name, os.path.join(ROOT, rel))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def workload_modules(reference=False):
+    """(configs, synthetic, cam_xyz_coeff): the workload tables, the scene generator and the
+    camera-matrix conversion.  The reference arm takes the tables and the generator from their
+    files and the conversion from the oracle; the GPU arm from the product package."""
+    if reference:
+        from oracle import oracle as orc
+        return (load_file("gls_workload_configs", "climage_gb300/configs.py"),
+                load_file("gls_workload_synthetic", "climage_gb300/synthetic.py"), orc.cam_xyz_coeff)
+    from climage_gb300 import configs, synthetic
+    return configs, synthetic, None
 
 
 def dist_env():
@@ -87,16 +135,26 @@ def replica_value(world, mpix_per_step, steps, total_ms):
     return world * mpix_per_step * steps / (total_ms / 1e3)
 
 
-def make_frames(cfg, rank):
-    from climage_gb300 import configs, synthetic
+def make_frames(cfg, rank, reference=False):
+    configs, synthetic, cam_xyz_coeff = workload_modules(reference)
     frames = []
     for i, (sigma, gain, nl) in enumerate(cfg["noise"]):
         raw, scene, meta = synthetic.make_frame(cfg["width"], cfg["height"], bayer=cfg["bayer"], bits=cfg["bits"],
                                                 black=cfg["black"], white=cfg["white"], wb=cfg["wb"], gain=gain,
                                                 read_sigma=sigma, seed=1000 * rank + i)
-        spec = configs.make_spec(meta, levels=cfg["levels"], storage=cfg["storage"], noise_level=nl)
+        spec = configs.make_spec(meta, levels=cfg["levels"], storage=cfg["storage"], noise_level=nl,
+                                 cam_xyz_coeff=cam_xyz_coeff)
         frames.append((raw, scene, spec))
     return frames
+
+
+def workload_config(cfg, world):
+    """The line's config: the same dict on both arms (GPU and reference)."""
+    return {"workload": cfg["name"], "frames_per_step": len(cfg["noise"]), "width": cfg["width"],
+            "height": cfg["height"], "levels": cfg["levels"], "storage": "fp16" if cfg["storage"] else "fp32",
+            "output": "rgba8", "local_tone_mapping": True, "noise": [list(n) for n in cfg["noise"]],
+            "l2": "GPU arm: flushed between steps (256 MB write); CPU arm: 3 x 24 MB raw in, well above its caches",
+            "parallelism": "replicas" if world > 1 else "single"}
 
 
 def make_burst(bases, dev, n=64, seed=4):
@@ -258,42 +316,90 @@ def cpu_leg(frames, max_seconds=30.0, gpu_rgb=None):
                       % (n, raw.shape[1], raw.shape[0], 2.0, 1.0, threads, dt)}, psnr
 
 
-def run_reference(args, cfg):
+def run_reference(args, cfg=None):
+    """The reference arm: the oracle (the CPU restatement of the reference's pipeline) on the
+    host cores, every thread, on the GPU arm's workload -- each step converts the same three
+    frames (RGBA8 out).  Rank 0 alone runs and prints; other ranks return at once."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
     from oracle import oracle as orc
     from tests.helpers import oracle_params
-    frames = make_frames(cfg, 0)
+    if cfg is None:
+        cfg = load_file("gls_workload_configs", "climage_gb300/configs.py").CONFIG2
+    frames = make_frames(cfg, 0, reference=True)
+    params = [oracle_params(f[2]) for f in frames]
     threads = orc.threads()
     times = []
     for i in range(args.warmup + args.steps):
-        raw, _, spec = frames[i % len(frames)]
         t0 = time.perf_counter()
-        orc.demosaic(raw, oracle_params(spec), orc.F32, want=("rgba8",))
+        for (raw, _, _), p in zip(frames, params):
+            orc.demosaic(raw, p, orc.F32, want=("rgba8",))
         dt = time.perf_counter() - t0
         if i >= args.warmup:
             times.append(dt)
-    mpix = cfg["width"] * cfg["height"] / 1e6
-    value = mpix * len(times) / sum(times)
+    mpix_per_step = len(frames) * cfg["width"] * cfg["height"] / 1e6
+    value = mpix_per_step * len(times) / sum(times)
     line = {"metric": METRIC, "value": round(value, 3), "unit": "MPix/s", "impl": "reference", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1000 * sum(times) / len(times), 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": cfg["name"] + " (one frame per step)", "frames_per_step": 1,
-                       "width": cfg["width"], "height": cfg["height"], "levels": cfg["levels"]},
+            "config": workload_config(cfg, world),
             "cpu_baseline": {"value": round(value, 3), "unit": "MPix/s", "cores": threads, "kind": "port",
-                             "sample": "one full frame per step, cycling the three noise levels"},
+                             "sample": "each step the workload's %d full frames (one per noise level), oracle fp32, "
+                                       "%d threads" % (len(frames), threads)},
             "e2e": {"value": round(value, 3), "unit": "MPix/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
-def main():
-    args = parse()
+def run_cpu_replicas(args, cfg):
+    """--cpu-replicas: the replica plumbing of the GPU arm on the CPU (gloo) -- process group,
+    barriers, each rank converting frames of its own (the oracle stands in for the GPU),
+    max-over-ranks timing -- and one check line from rank 0."""
+    import hashlib
+
+    import torch
+    import torch.distributed as dist
+    from oracle import oracle as orc
+    from tests.helpers import oracle_params
+
+    rank, world, _ = init_replicas("gloo")
+    frames = make_frames(cfg, rank, reference=True)
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        outs = [orc.demosaic(f[0], oracle_params(f[2]), orc.F32, want=("rgba8",))["rgba8"] for f in frames]
+    total_ms = max_over_ranks(1e3 * (time.perf_counter() - t0), world, torch.device("cpu"))
+    barrier(world)
+    digest = hashlib.sha256(b"".join(o.tobytes() for o in outs)).hexdigest()
+    digests = [None] * world
+    if world > 1:
+        dist.all_gather_object(digests, digest)
+    else:
+        digests = [digest]
+    if rank == 0:
+        mpix = len(frames) * cfg["width"] * cfg["height"] / 1e6
+        print(json.dumps({"check": "cpu-replicas", "n_ranks": world, "steps": args.steps,
+                          "value": round(replica_value(world, mpix, args.steps, total_ms), 3), "unit": "MPix/s",
+                          "slowest_ms": round(total_ms, 3), "digests": digests,
+                          "config": workload_config(cfg, world)}), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main(argv=None):
+    argv = sys.argv[1:] if argv is None else argv
+    args = parse(argv)
+    rc = launch_replicas(args, argv)
+    if rc is not None:
+        sys.exit(rc)
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    if args.cpu_replicas:
+        run_cpu_replicas(args, load_file("gls_workload_configs", "climage_gb300/configs.py").CPU_REPLICA_CHECK)
+        return
     from climage_gb300 import configs
     cfg = configs.CONFIG2
-    if args.impl == "reference":
-        run_reference(args, cfg)
-        return
     import torch
     rank, world, local = dist_env()
     if world > 1:
@@ -554,11 +660,8 @@ def main():
             "metric": METRIC, "value": round(value, 3), "unit": "MPix/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": cfg["name"], "frames_per_step": len(frames), "width": w, "height": h,
-                       "levels": cfg["levels"], "storage": "fp32", "output": "rgba8", "local_tone_mapping": True,
-                       "noise": cfg["noise"], "l2": "flushed between steps (256 MB write)",
-                       "parallelism": "replicas" if world > 1 else "single",
-                       "schedule": "the step's frames as one burst over %d streams (gls_raw_batch)" % lanes},
+            "config": workload_config(cfg, world),
+            "schedule": "the step's frames as one burst over %d streams (gls_raw_batch)" % lanes,
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
                          "traffic": NCU_TRAFFIC[dom][0] if dom in NCU_TRAFFIC else None, "traffic_unit": "B/launch",

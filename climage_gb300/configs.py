@@ -12,12 +12,19 @@ Parameter sources in the reference:
     (raw_pipeline.cpp:89-146);
   * the "strong" denoise parameters: Sonya6400DenoiseParameters (Sonya6400Calibration.cpp:182-233);
   * tone mapping with LTM: demosaicIMX571DNG (IMX571Calibration.cpp:287-304).
+
+This module loads no native library by itself: the camera-matrix conversion is the
+product's (gls.cam_xyz_coeff) unless the caller passes another implementation of it, and
+only to_gls_params needs the product's parameter block.  bench.py's reference arm loads
+this file on its own and passes the oracle's cam_xyz_coeff, so that arm never maps the
+product's library.
 """
 import math
 
 import numpy as np
 
-from . import gls
+# image storage precision (gls_cuda.h GLS_STORAGE_F32 / GLS_STORAGE_F16)
+STORAGE_F32, STORAGE_F16 = 0, 1
 
 CAM_XYZ = [1.4955, -0.6760, -0.1453, -0.1341, 1.0072, 0.1269, -0.0647, 0.1987, 0.4304]
 
@@ -67,9 +74,12 @@ def denoise_strong(levels, iso=1600):
     return out
 
 
-def make_spec(meta, levels=5, storage=gls.STORAGE_F32, ltm=True, noise_level=0.2, denoise="plain", algorithm=0,
-              exposure_multiplier=1.0):
-    pre_mul, rgb_cam = gls.cam_xyz_coeff(CAM_XYZ)
+def make_spec(meta, levels=5, storage=STORAGE_F32, ltm=True, noise_level=0.2, denoise="plain", algorithm=0,
+              exposure_multiplier=1.0, cam_xyz_coeff=None):
+    if cam_xyz_coeff is None:
+        from . import gls
+        cam_xyz_coeff = gls.cam_xyz_coeff
+    pre_mul, rgb_cam = cam_xyz_coeff(CAM_XYZ)
     wb = meta["wb"]
     pyr = [PYRAMID_NLF0[min(i, 4)] for i in range(levels)]
     return dict(
@@ -92,6 +102,7 @@ def make_spec(meta, levels=5, storage=gls.STORAGE_F32, ltm=True, noise_level=0.2
 
 
 def to_gls_params(spec):
+    from . import gls
     p = gls.DemosaicParams()
     p.bayer_pattern = spec["bayer_pattern"]
     p.black_level = spec["black_level"]
@@ -123,9 +134,14 @@ def to_gls_params(spec):
 # ---- benchmark workloads (synthetic frames stand in for DNG captures) ----
 
 CONFIG1 = dict(name="plain-1024x768-rggb12-4lvl", width=1024, height=768, bayer=2, bits=12, black=64, white=4095,
-               wb=(2.0, 1.0, 1.6), noise=[(3.0, 2.0, 0.2)], levels=4, storage=gls.STORAGE_F32, out="rgba_f32")
+               wb=(2.0, 1.0, 1.6), noise=[(3.0, 2.0, 0.2)], levels=4, storage=STORAGE_F32, out="rgba_f32")
 CONFIG2 = dict(name="plain-4032x3024-rggb12-5lvl", width=4032, height=3024, bayer=2, bits=12, black=64, white=4095,
                wb=(2.0, 1.0, 1.6), noise=[(2.0, 1.0, 0.2), (6.0, 4.0, 0.45), (12.0, 16.0, 0.7)], levels=5,
-               storage=gls.STORAGE_F32, out="rgba8")
+               storage=STORAGE_F32, out="rgba8")
 CONFIG3 = dict(name="fp16-8064x6048-grbg14-6lvl", width=8064, height=6048, bayer=0, bits=14, black=256, white=16383,
-               wb=(2.0, 1.0, 1.6), noise=[(3.0, 2.0, 0.2)], levels=6, storage=gls.STORAGE_F16, out="rgba8")
+               wb=(2.0, 1.0, 1.6), noise=[(3.0, 2.0, 0.2)], levels=6, storage=STORAGE_F16, out="rgba8")
+# the replica plumbing check on the CPU (bench.py --cpu-replicas): frames small enough for
+# the oracle to convert in well under a second
+CPU_REPLICA_CHECK = dict(name="plain-64x48-rggb12-5lvl", width=64, height=48, bayer=2, bits=12, black=64, white=4095,
+                         wb=(2.0, 1.0, 1.6), noise=[(2.0, 1.0, 0.2), (6.0, 4.0, 0.45), (12.0, 16.0, 0.7)], levels=5,
+                         storage=STORAGE_F32, out="rgba8")

@@ -175,7 +175,11 @@ GLS_API gls_status gls_guided_filter(gls_ctx* ctx, const gls_image_desc* in, int
  * Set-up: the first call on a device, with the context's device current (required on every
  * call), looks up the array's address there with cudaGetSymbolAddress, which loads the array
  * onto that device; make that first call before any stream capture.  Later calls only launch
- * kernels on the context's stream.  All calls on a device share the one array: calls whose
+ * kernels on the context's stream.  The address is remembered together with the CUDA
+ * context it belongs to: after a device reset (cudaDeviceReset) the next call, again before
+ * any capture, repeats the set-up in the new context.  Under lazy module loading (CUDA's
+ * default) a device holds the 16 MiB from that first call on; with
+ * CUDA_MODULE_LOADING=EAGER every context reserves it when it is created.  All calls on a device share the one array: calls whose
  * work overlaps on the GPU (other streams, other contexts or threads) race on it and corrupt
  * each other's results, so serialise them.  Nothing in the array has to start at zero (each
  * call writes every buffer in full before reading it), so no call clears it. */

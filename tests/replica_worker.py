@@ -35,7 +35,7 @@ def main(out_dir):
     # each rank "timed" a different duration: the job is as slow as its slowest replica
     slowest = bench.max_over_ranks(10.0 + 5.0 * rank, world, cpu)
     value = bench.replica_value(world, 12.0, 4, slowest)
-    frames = bench.make_frames(TINY, rank)
+    frames = bench.make_frames(TINY, rank, reference=True)
     digest = hashlib.sha256(b"".join(f[0].tobytes() for f in frames)).hexdigest()
     digests = [None] * world
     dist.all_gather_object(digests, digest)
@@ -43,9 +43,15 @@ def main(out_dir):
     with contextlib.redirect_stdout(printed):
         bench.run_reference(types.SimpleNamespace(steps=1, warmup=0, gpus=world), TINY)
     bench.barrier(world)
+    # what the reference arm brought into the process: no module of the product package and
+    # none of its native libraries
+    with open("/proc/self/maps") as f:
+        maps = f.read()
+    product = sorted(m for m in sys.modules if m == "climage_gb300" or m.startswith("climage_gb300."))
     with open(os.path.join(out_dir, "rank%d.json" % rank), "w") as f:
         json.dump({"rank": rank, "world": world, "local": local, "slowest_ms": slowest, "value": value,
-                   "digests": digests, "printed": printed.getvalue()}, f)
+                   "digests": digests, "printed": printed.getvalue(), "product_modules": product,
+                   "product_library_mapped": "libgls_cuda" in maps}, f)
     dist.destroy_process_group()
 
 

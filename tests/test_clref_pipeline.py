@@ -123,6 +123,24 @@ def test_oracle_equals_the_reference_raw_converter(bayer, noise_level, gain):
     np.testing.assert_array_equal(out[..., :3], ref["rgba8"][..., :3])
 
 
+@pytest.mark.skipif(orc.ref_pipeline_lib() is None, reason="the reference's RawConverter is not built here")
+@pytest.mark.parametrize("width,height,bayer,noise_level,gain,sigma",
+                         [(1024, 768, 2, 0.2, 2.0, 3.0), (4032, 3024, 2, 0.7, 16.0, 12.0)],
+                         ids=["config1_1024x768", "bench_4032x3024_high_noise"])
+def test_oracle_equals_the_reference_raw_converter_at_timed_sizes(width, height, bayer, noise_level, gain, sigma):
+    """The same pin at the sizes the product is timed on: the small plain frame (1024x768
+    RGGB 12-bit, read noise 3 DN, gain 2) and the bench's 4032x3024 frame at gain 16, which
+    takes the high-noise raw branch.  The reference's RawConverter runs its fixed 5-level
+    pyramid; about 5 s and 70 s of one CPU core."""
+    raw, _, meta = synthetic.make_frame(width, height, bayer=bayer, gain=gain, read_sigma=sigma, seed=1000 + width)
+    spec = configs.make_spec(meta, levels=5, noise_level=noise_level)
+    out, raw_nlf, pyr_nlf = orc.ref_raw_converter(raw, spec)
+    ref = orc.demosaic(raw, oracle_params(spec), orc.F32, want=("rgba8",))
+    np.testing.assert_array_equal(raw_nlf, ref["raw_nlf"])
+    np.testing.assert_array_equal(pyr_nlf, ref["pyramid_nlf"])
+    np.testing.assert_array_equal(out[..., :3], ref["rgba8"][..., :3])
+
+
 @pytest.mark.skipif(orc.ref_pipeline_lib(orc.F16) is None,
                     reason="the reference's RawConverter with fp16 storage is not built here")
 @pytest.mark.parametrize("bayer,noise_level,gain", [(2, 0.2, 2.0), (0, 0.45, 4.0), (3, 0.7, 16.0), (1, 0.2, 1.0)],

@@ -77,6 +77,46 @@ def test_reference_arm_runs_on_rank_zero_only(ranks):
     assert line["e2e"]["h2d_bytes_per_step"] == 0
 
 
+def test_reference_arm_loads_nothing_of_the_product(ranks):
+    """The reference arm (and the frames it converts) must not run or even map the product: no
+    module of climage_gb300 imported, libgls_cuda.so not mapped."""
+    for x in ranks:
+        assert x["product_modules"] == []
+        assert not x["product_library_mapped"]
+
+
+def test_reference_arm_times_the_gpu_arms_workload(ranks):
+    """Both arms describe the workload with the same config dict; each reference step
+    converts every frame of the workload (three here, one per noise level)."""
+    line = json.loads(ranks[0]["printed"].strip().splitlines()[-1])
+    sys.path.insert(0, ROOT)
+    sys.path.insert(0, HERE)
+    import bench
+    import replica_worker
+
+    assert line["config"] == bench.workload_config(replica_worker.TINY, 2)
+    assert line["config"]["frames_per_step"] == 3
+
+
+def test_bench_starts_its_own_replicas(tmp_path):
+    """bench.py --gpus 2 outside a launcher starts two ranks itself (torch.distributed.run on
+    127.0.0.1); with --cpu-replicas each rank converts its own frames with the oracle over
+    gloo and rank 0 prints the one check line."""
+    env = {k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK", "MASTER_ADDR",
+                                                             "MASTER_PORT")}
+    env["CUDA_VISIBLE_DEVICES"] = ""
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--gpus", "2", "--cpu-replicas", "--steps",
+                        "1", "--warmup", "0"], cwd=str(tmp_path), env=env, capture_output=True, text=True,
+                       timeout=240)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-3000:]
+    lines = [json.loads(l) for l in r.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    line = lines[0]
+    assert line["check"] == "cpu-replicas" and line["n_ranks"] == 2
+    assert len(set(line["digests"])) == 2  # each rank converted frames of its own
+    assert line["config"]["parallelism"] == "replicas"
+
+
 def test_single_process_needs_no_group():
     sys.path.insert(0, ROOT)
     import bench

@@ -8,6 +8,7 @@ must pass.
 """
 import os
 import re
+import subprocess
 
 import numpy as np
 import pytest
@@ -91,21 +92,55 @@ def test_two_calls_in_a_row_match_existing_entry_point(nctx, half):
 
 
 @pytest.mark.gpu
-def test_matches_oracle():
+def test_matches_oracle(nctx):
     import torch
 
     from oracle import oracle as orc
-    c = gls.Context(0)
-    try:
-        rng = np.random.default_rng(7)
-        img = _image(rng, 67, 45, False)
-        out = _like(img, float("nan"))
-        c.guidedFilterNoAlloc(img, 5, EPS_A, out)
-        torch.cuda.synchronize()
-        want = orc.guided_filter(img.cpu().numpy(), 5, EPS_A)
-        assert np.array_equal(out.cpu().numpy().view(np.int32), want.view(np.int32))
-    finally:
-        c.close()
+    rng = np.random.default_rng(7)
+    img = _image(rng, 67, 45, False)
+    out = _like(img, float("nan"))
+    nctx.guidedFilterNoAlloc(img, 5, EPS_A, out)
+    torch.cuda.synchronize()
+    want = orc.guided_filter(img.cpu().numpy(), 5, EPS_A)
+    assert np.array_equal(out.cpu().numpy().view(np.int32), want.view(np.int32))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("half", [False, True], ids=["f32", "f16"])
+def test_pitched_images_match_existing_entry_point(nctx, half):
+    """Input and output rows padded (column slices of wider images: the row pitch is larger
+    than the width), which the first box-blur pass and the final write must honour."""
+    import torch
+    rng = np.random.default_rng(41 + half)
+    wide = _image(rng, 160, 90, half)
+    img = wide[:, 7:7 + 121]  # pitch 160 pixels, width 121
+    assert img.stride(0) == 160 * 4
+    ref_wide, out_wide = _like(wide, 0.5), _like(wide, float("nan"))
+    ref, out = ref_wide[:, 13:13 + 121], out_wide[:, 13:13 + 121]
+    nctx.guidedFilter(img, 5, EPS_A, ref)
+    nctx.guidedFilterNoAlloc(img, 5, EPS_A, out)
+    nctx.guidedFilterNoAlloc(img, 5, EPS_A, out)
+    torch.cuda.synchronize()
+    assert _same(out, ref)
+    # the padding columns of the output stay as they were
+    assert bool(torch.isnan(out_wide[:, :13]).all()) and bool(torch.isnan(out_wide[:, 13 + 121:]).all())
+
+
+@pytest.mark.gpu
+def test_other_current_device_is_rejected(nctx):
+    """Every call needs the context's device current; with another device current the call is
+    rejected before it launches anything (needs two GPUs)."""
+    import torch
+    if torch.cuda.device_count() < 2:
+        pytest.skip("needs two GPUs")
+    img = _image(np.random.default_rng(8), 40, 30, False)
+    out = _like(img, 0.25)
+    launches = nctx.kernel_launches()
+    with torch.cuda.device(1):
+        with pytest.raises(gls.GlsError) as err:
+            nctx.guidedFilterNoAlloc(img, 3, EPS_A, out)
+    assert err.value.status == gls.GLS_ERR_INVALID_ARGUMENT
+    assert nctx.kernel_launches() == launches
 
 
 @pytest.mark.gpu
@@ -142,3 +177,46 @@ def test_larger_image_is_rejected(nctx, w, h):
     nctx.guidedFilterNoAlloc(small, 3, EPS_B, res)
     torch.cuda.synchronize()
     assert _same(res, ref)
+
+
+
+SLOT_TEST = r"""
+#include <cstdio>
+#include "gls_scratch_slot.h"
+static int lookups = 0;
+static unsigned long long live = 0;  // the context a lookup finds current
+static char mem[3];
+int main() {
+    gls::ScratchSlot s;
+    auto lookup = [](unsigned long long* id) -> void* { ++lookups; *id = live; return live ? &mem[live - 1] : nullptr; };
+    int bad = 0;
+    live = 1;
+    bad += gls::scratch_slot_get(s, 0, lookup) != &mem[0] || lookups != 1;   // nothing current yet: set-up
+    bad += gls::scratch_slot_get(s, 1, lookup) != &mem[0] || lookups != 1;   // same context: cached
+    bad += gls::scratch_slot_get(s, 1, lookup) != &mem[0] || lookups != 1;
+    live = 2;                                                                // a device reset: new context id
+    bad += gls::scratch_slot_get(s, 2, lookup) != &mem[1] || lookups != 2;   // looked up again
+    bad += gls::scratch_slot_get(s, 2, lookup) != &mem[1] || lookups != 2;
+    live = 0;                                                                // a failed lookup
+    bad += gls::scratch_slot_get(s, 3, lookup) != nullptr || lookups != 3;
+    bad += s.ctx_id != 2 || s.ptr != &mem[1];                                // cache unchanged
+    live = 3;
+    bad += gls::scratch_slot_get(s, 3, lookup) != &mem[2] || lookups != 4;
+    std::printf("%d\n", bad);
+    return bad;
+}
+"""
+
+
+def test_address_is_looked_up_again_in_a_new_context(tmp_path):
+    """The cache of the array's address is keyed on the CUDA context: the same context reuses
+    it, a new one (after a device reset) repeats the lookup, a failed lookup caches nothing.
+    Host logic, compiled with the host compiler against the header the library uses."""
+    src = tmp_path / "slot.cpp"
+    src.write_text(SLOT_TEST)
+    exe = tmp_path / "slot"
+    cc = subprocess.run(["g++", "-std=c++17", "-O1", "-I", os.path.join(ROOT, "climage_gb300", "csrc"), str(src), "-o",
+                         str(exe)], capture_output=True, text=True)
+    assert cc.returncode == 0, cc.stderr
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0 and r.stdout.strip() == "0", r.stdout + r.stderr
