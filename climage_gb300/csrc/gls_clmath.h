@@ -322,8 +322,24 @@ GLS_HD float atan2pi_(float y, float x) {
     return copysign_(r, y);
 }
 
+// 2^x on (-126, 126), where no special case applies: n = x rounded to an integer, the
+// polynomial on the fraction, and an exact scaling by 2^n (the general form below, bit for bit)
+GLS_HD float exp2_core(float x) {
+    const float n = floor_(x + 0.5f);
+    const float f = x - n;  // [-0.5, 0.5], exact
+    float p = 1.534580750e-04f;
+    p = p * f + 1.339993118e-03f;
+    p = p * f + 9.618488974e-03f;
+    p = p * f + 5.550328777e-02f;
+    p = p * f + 2.402264689e-01f;
+    p = p * f + 6.931472057e-01f;
+    p = p * f + 1.000000001e+00f;
+    return p * u2f((uint32_t)((int)n + 127) << 23);
+}
+
 // 2^x
 GLS_HD float exp2_(float x) {
+    if (fabs_(x) < 126.0f) return exp2_core(x);  // NaN goes on
     if (isnan_(x)) return x;
     if (x >= 128.0f) return inf_();
     if (x < -150.0f) return 0.0f;
@@ -349,8 +365,32 @@ GLS_HD float exp2_(float x) {
     return p * u2f((uint32_t)(e + 127) << 23);
 }
 
+// true for a positive, normal, finite x (one unsigned compare on the bits)
+GLS_HD bool is_pos_normal_(float x) { return f2u(x) - 0x00800000u < 0x7f000000u; }
+
+// log2 of a positive normal finite x: the general form below with k = 0 (e + 0.0f == e)
+GLS_HD float log2_core(float x) {
+    uint32_t b = f2u(x);
+    int e = (int)((b >> 23) & 0xffu) - 127;
+    float m = u2f((b & 0x007fffffu) | 0x3f800000u);  // [1, 2)
+    if (m > 1.41421356f) {
+        m = m * 0.5f;
+        e += 1;
+    }
+    const float z = div_(m - 1.0f, m + 1.0f);
+    const float s = z * z;
+    float p = 2.381667258e-02f;
+    p = p * s + 3.386064467e-01f;
+    p = p * s + 4.117443166e-01f;
+    p = p * s + 5.770824732e-01f;
+    p = p * s + 9.617966808e-01f;
+    p = p * s + 2.885390082e+00f;
+    return (float)e + z * p;
+}
+
 // log2(x)
 GLS_HD float log2_(float x) {
+    if (is_pos_normal_(x)) return log2_core(x);
     if (isnan_(x)) return x;
     if (x < 0.0f) return nan_();
     if (x == 0.0f) return -inf_();
@@ -383,6 +423,8 @@ GLS_HD bool is_integer_(float y) { return floor_(y) == y; }
 // OpenCL pow(x, y) for the cases the pipeline meets: finite or infinite x, finite y.
 GLS_HD float pow_(float x, float y) {
     if (y == 0.0f || x == 1.0f) return 1.0f;
+    // positive normal x and finite y: the general case, without its special-case tests
+    if (is_pos_normal_(x) && fabs_(y) < inf_()) return exp2_(y * log2_core(x));
     if (isnan_(x) || isnan_(y)) return x + y;
     if (x == 0.0f) return y < 0.0f ? inf_() : 0.0f;
     if (x < 0.0f) {

@@ -16,6 +16,7 @@ struct RawPass1Args {
     NlfThresholds th;
     NlfScratch nlf;  // regression scratch (set by the launcher)
     float* nlf_out;  // fitted {A0..3, B0..3}
+    int sums_exact;  // set by the launcher: every 5x5 sum and its square lie where x / 25 has its exact shortcut
 };
 
 struct DemosaicArgs {

@@ -7,6 +7,7 @@
 #ifndef GLS_NLF_CUH
 #define GLS_NLF_CUH
 
+#include "gls_f32x2.cuh"
 #include "gls_internal.h"
 #include "gls_pixel_ops.cuh"
 
@@ -324,6 +325,145 @@ struct Pass1Acc {
     }
 
     GLS_DI void write_minmax(float* part_f) { block_minmax_write<2 * NC>(mn, mx, part_f + (size_t)blockIdx.x * kNlfKF); }
+};
+
+// The raw fit's pass-1 accumulator with the four channels as two packed pairs (0, 1) and
+// (2, 3): the same float-float sums as Pass1Acc<4, 4>, pixel by pixel in the same order, at
+// half the instructions; unpack() hands them to Pass1Acc's writers.
+struct RawPass1Acc2 {
+    FF2 sx[2], sxx[2], sy[2], sxy[2], syy[2];
+    float mn[8], mx[8];
+    int n;
+
+    GLS_DI void init() {
+#pragma unroll
+        for (int p = 0; p < 2; p++) {
+            ff2_zero(sx[p]);
+            ff2_zero(sxx[p]);
+            ff2_zero(sy[p]);
+            ff2_zero(sxy[p]);
+            ff2_zero(syy[p]);
+        }
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            mn[k] = glsm::inf_();
+            mx[k] = -glsm::inf_();
+        }
+        n = 0;
+    }
+
+    // m[p], v[p]: the statistics of channels 2p, 2p + 1 of a selected quad
+    GLS_DI void add_selected(const float2 (&m)[2], const float2 (&v)[2]) {
+        n++;
+#pragma unroll
+        for (int p = 0; p < 2; p++) {
+            ff2_add(sx[p], m[p]);
+            ff2_add_prod(sxx[p], m[p], m[p]);
+            ff2_add(sy[p], v[p]);
+            ff2_add_prod(sxy[p], m[p], v[p]);
+            ff2_add_prod(syy[p], v[p], v[p]);
+            mn[2 * p] = fminf(mn[2 * p], m[p].x);
+            mx[2 * p] = fmaxf(mx[2 * p], m[p].x);
+            mn[2 * p + 1] = fminf(mn[2 * p + 1], m[p].y);
+            mx[2 * p + 1] = fmaxf(mx[2 * p + 1], m[p].y);
+            mn[4 + 2 * p] = fminf(mn[4 + 2 * p], v[p].x);
+            mx[4 + 2 * p] = fmaxf(mx[4 + 2 * p], v[p].x);
+            mn[5 + 2 * p] = fminf(mn[5 + 2 * p], v[p].y);
+            mx[5 + 2 * p] = fmaxf(mx[5 + 2 * p], v[p].y);
+        }
+    }
+
+    GLS_DI void unpack(Pass1Acc<4, 4>& a) const {
+        auto put = [](FF& lo_ch, FF& hi_ch, const FF2& f) {
+            lo_ch.hi = f.hi.x;
+            lo_ch.lo = f.lo.x;
+            hi_ch.hi = f.hi.y;
+            hi_ch.lo = f.lo.y;
+        };
+#pragma unroll
+        for (int p = 0; p < 2; p++) {
+            put(a.sx[2 * p], a.sx[2 * p + 1], sx[p]);
+            put(a.sxx[2 * p], a.sxx[2 * p + 1], sxx[p]);
+            put(a.sy[2 * p], a.sy[2 * p + 1], sy[p]);
+            put(a.sxy[2 * p], a.sxy[2 * p + 1], sxy[p]);
+            put(a.syy[2 * p], a.syy[2 * p + 1], syy[p]);
+        }
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            a.mn[k] = mn[k];
+            a.mx[k] = mx[k];
+        }
+        a.n = n;
+    }
+};
+
+// The level fits' pass-1 accumulator (one mean, three variances) with the sums packed in
+// pairs of independent accumulators: (sx, sy2), (sxx, syy2), (sy0, sy1), (sxy0, sxy1),
+// (syy0, syy1), and sxy2 alone -- the same float-float sums as Pass1Acc<1, 3>, pixel by
+// pixel in the same order; unpack() hands them to Pass1Acc's writers.
+struct LevelPass1Acc2 {
+    FF2 a_sx_sy2, a_sxx_syy2, a_sy01, a_sxy01, a_syy01;
+    FF sxy2;
+    float mn[6], mx[6];
+    int n;
+
+    GLS_DI void init() {
+        ff2_zero(a_sx_sy2);
+        ff2_zero(a_sxx_syy2);
+        ff2_zero(a_sy01);
+        ff2_zero(a_sxy01);
+        ff2_zero(a_syy01);
+        ff_zero(sxy2);
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+            mn[k] = glsm::inf_();
+            mx[k] = -glsm::inf_();
+        }
+        n = 0;
+    }
+
+    GLS_DI void add_selected(float m, float2 v01, float v2) {
+        n++;
+        const float2 mv2 = make_float2(m, v2);
+        ff2_add(a_sx_sy2, mv2);
+        ff2_add_prod(a_sxx_syy2, mv2, mv2);
+        ff2_add(a_sy01, v01);
+        ff2_add_prod(a_sxy01, make_float2(m, m), v01);
+        ff2_add_prod(a_syy01, v01, v01);
+        ff_add_prod(sxy2, m, v2);
+        const float vv[3] = {v01.x, v01.y, v2};
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            mn[c] = fminf(mn[c], m);
+            mx[c] = fmaxf(mx[c], m);
+            mn[3 + c] = fminf(mn[3 + c], vv[c]);
+            mx[3 + c] = fmaxf(mx[3 + c], vv[c]);
+        }
+    }
+
+    GLS_DI void unpack(Pass1Acc<1, 3>& a) const {
+        auto lane = [](FF& d, const FF2& f, int k) {
+            d.hi = k ? f.hi.y : f.hi.x;
+            d.lo = k ? f.lo.y : f.lo.x;
+        };
+        lane(a.sx[0], a_sx_sy2, 0);
+        lane(a.sy[2], a_sx_sy2, 1);
+        lane(a.sxx[0], a_sxx_syy2, 0);
+        lane(a.syy[2], a_sxx_syy2, 1);
+        lane(a.sy[0], a_sy01, 0);
+        lane(a.sy[1], a_sy01, 1);
+        lane(a.sxy[0], a_sxy01, 0);
+        lane(a.sxy[1], a_sxy01, 1);
+        lane(a.syy[0], a_syy01, 0);
+        lane(a.syy[1], a_syy01, 1);
+        a.sxy[2] = sxy2;
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+            a.mn[k] = mn[k];
+            a.mx[k] = mx[k];
+        }
+        a.n = n;
+    }
 };
 
 // Ticket of a pass: true in the one block that finishes last, once every block's row is

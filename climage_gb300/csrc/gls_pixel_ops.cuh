@@ -11,6 +11,7 @@
 #define GLS_PIXEL_OPS_CUH
 
 #include "gls_device.cuh"
+#include "gls_f32x2.cuh"
 
 namespace gls {
 
@@ -42,9 +43,20 @@ GLS_DI FastDiv div25() {
     return f;
 }
 
+// UNORM16 read, (float)raw / 65535 correctly rounded: with y = RN(1/65535) (0x37800080) and
+// q0 = RN(x * y), one Markstein correction RN(q0 + RN(x - q0 * 65535) * y) is the quotient of
+// the division for every one of the 65536 inputs (checked exhaustively, on the GPU by
+// test_unorm16_read_is_the_division), at three instructions instead of a division.
+GLS_DI float unorm16(uint16_t raw) {
+    const float x = (float)raw;
+    const float y = __uint_as_float(0x37800080u);
+    const float q0 = x * y;
+    return glsm::fma_(glsm::fma_(-q0, 65535.0f, x), y, q0);
+}
+
 // ---- a4: scaleRawData (demosaic.cl:69-78) ----
 GLS_DI float scale_value(uint16_t raw, float scale_mul, float black) {
-    const float v = div_((float)raw, 65535.0f);
+    const float v = unorm16(raw);
     const float r = scale_mul * (v - black);
     return r > 0.0f ? r : 0.0f;
 }
@@ -457,8 +469,21 @@ __device__ __noinline__ float4 bilateral_literal(const Acc4& im, int px, int py,
     return make_float4(div_(f0, n0), div_(f1, n1), div_(f2, n1), 0.0f);
 }
 
+// Accessors whose samples all have .w == 1 (a staged tile whose alpha the kernel set) declare
+// `static constexpr bool kUnitW = true`; the bilateral then counts its normaliser in the
+// packed (z, w) accumulation instead of a separate add.
+template <class A, class = void>
+struct unit_w {
+    static constexpr bool value = false;
+};
+template <class A>
+struct unit_w<A, decltype((void)A::kUnitW)> {
+    static constexpr bool value = A::kUnitW;
+};
+
 template <class Acc4>
 GLS_DI float4 bilateral_px(const Acc4& im, int px, int py, const Nlf6& n, float chromaBoost, float gradientBoost) {
+    constexpr bool UW = unit_w<Acc4>::value;
     const float4 c = im.at(px, py);
     const float sig0 = sqrt_(n.a[0] + n.b[0] * c.x);
     const float sig1 = sqrt_(n.a[1] + n.b[1] * c.x);
@@ -477,9 +502,11 @@ GLS_DI float4 bilateral_px(const Acc4& im, int px, int py, const Nlf6& n, float 
     // a tap whose qa clears the square-root band of the edge (2^-20) widened by 2^-18 has the
     // same weight either way.  The fast path keeps edges below 2^20 and 2^-60 <= sigma <= 2^30,
     // so an overflowing diff^2 (or product) means d^2 > 2^68 and weight 0 on both sides, and
-    // qa is never NaN for finite samples; a tap that stays undecided, or a sample that is not
-    // finite, sends the pixel to the literal evaluation.  The weights are 0 or 1, so w * s is exact and the multiply-add can
-    // be fused without changing a bit.
+    // qa is never NaN for finite samples.  A tap inside the band, or a NaN qa (the literal
+    // weight of a NaN sample is 1), is counted by !(qa > hi) but not by qa < lo: when the two
+    // counts differ the pixel takes the literal evaluation.  The weights are 0 or 1, so w * s
+    // is exact and the multiply-adds can be fused without changing a bit; channel pairs go
+    // through the packed fp32x2 operations, each lane rounded exactly as the scalar one.
     SqrtGe ge0, ge1;
     ge0.init(lumaBoost * GLS_SQRT2_F);
     ge1.init(chromaBoost * GLS_SQRT2_F);
@@ -493,27 +520,51 @@ GLS_DI float4 bilateral_px(const Acc4& im, int px, int py, const Nlf6& n, float 
     const float r0 = dv0.y * dv0.y, r1 = dv1.y * dv1.y, r2 = dv2.y * dv2.y;
     const float lo0 = ge0.lo * (1.0f - kWiden), hi0 = ge0.hi * (1.0f + kWiden);
     const float lo1 = ge1.lo * (1.0f - kWiden), hi1 = ge1.hi * (1.0f + kWiden);
-    float f0 = 0.0f, f1 = 0.0f, f2 = 0.0f, n0 = 0.0f, n1 = 0.0f;  // one normaliser for both chroma channels
-    bool redo = false;
+    const float2 nc = make_float2(-c.x, -c.y);  // s - c == s + (-c), bit for bit
+    float2 fxy = make_float2(0.0f, 0.0f);       // (f0, f1)
+    float2 fzn = make_float2(0.0f, 0.0f);       // (f2, n1): the two chroma channels share their normaliser
+    if (ge0.e == ge1.e) {
+        // one edge for luma and chroma: one weight per tap, n0 == n1
+        float nhi = 0.0f;
+#pragma unroll 1
+        for (int y = -2; y <= 2; y++) {
+#pragma unroll
+            for (int x = -2; x <= 2; x++) {
+                const float4 s = im.at(px + x, py + y);
+                const float2 dxy = add2(make_float2(s.x, s.y), nc);
+                const float2 qxy = mul2(dxy, dxy);  // feeds multiplicands only
+                const float d2 = s.z - c.z;
+                const float qa = glsm::fma_(qxy.x, r0, glsm::fma_(qxy.y, r1, (d2 * d2) * r2));
+                const float w = qa < lo0 ? 1.0f : 0.0f;
+                nhi = nhi + (qa > hi0 ? 0.0f : 1.0f);
+                const float2 ww = make_float2(w, w);
+                fxy = fma2(ww, make_float2(s.x, s.y), fxy);
+                fzn = fma2(ww, make_float2(s.z, UW ? s.w : 1.0f), fzn);
+            }
+        }
+        if (nhi != fzn.y) return bilateral_literal(im, px, py, sig0, sig1, sig2, ge0.e, ge1.e);
+        return make_float4(div_(fxy.x, fzn.y), div_(fxy.y, fzn.y), div_(fzn.x, fzn.y), 0.0f);
+    }
+    float n0 = 0.0f, nhi0 = 0.0f, nhi1 = 0.0f;
 #pragma unroll 1
     for (int y = -2; y <= 2; y++) {
 #pragma unroll
         for (int x = -2; x <= 2; x++) {
             const float4 s = im.at(px + x, py + y);
-            const float x0 = s.x - c.x, x1 = s.y - c.y, x2 = s.z - c.z;
-            const float qa = glsm::fma_(x0 * x0, r0, glsm::fma_(x1 * x1, r1, (x2 * x2) * r2));
-            const bool in0 = qa < lo0, in1 = qa < lo1;
-            redo |= !(in0 || qa > hi0) || !(in1 || qa > hi1);
-            const float w0 = in0 ? 1.0f : 0.0f, w1 = in1 ? 1.0f : 0.0f;
-            f0 = glsm::fma_(w0, s.x, f0);
+            const float2 dxy = add2(make_float2(s.x, s.y), nc);
+            const float2 qxy = mul2(dxy, dxy);
+            const float d2 = s.z - c.z;
+            const float qa = glsm::fma_(qxy.x, r0, glsm::fma_(qxy.y, r1, (d2 * d2) * r2));
+            const float w0 = qa < lo0 ? 1.0f : 0.0f, w1 = qa < lo1 ? 1.0f : 0.0f;
+            nhi0 = nhi0 + (qa > hi0 ? 0.0f : 1.0f);
+            nhi1 = nhi1 + (qa > hi1 ? 0.0f : 1.0f);
             n0 = n0 + w0;
-            f1 = glsm::fma_(w1, s.y, f1);
-            n1 = n1 + w1;
-            f2 = glsm::fma_(w1, s.z, f2);
+            fxy = fma2(make_float2(w0, w1), make_float2(s.x, s.y), fxy);
+            fzn = fma2(make_float2(w1, w1), make_float2(s.z, UW ? s.w : 1.0f), fzn);
         }
     }
-    if (redo) return bilateral_literal(im, px, py, sig0, sig1, sig2, ge0.e, ge1.e);
-    return make_float4(div_(f0, n0), div_(f1, n1), div_(f2, n1), 0.0f);
+    if (nhi0 != n0 || nhi1 != fzn.y) return bilateral_literal(im, px, py, sig0, sig1, sig2, ge0.e, ge1.e);
+    return make_float4(div_(fxy.x, n0), div_(fxy.y, fzn.y), div_(fzn.x, fzn.y), 0.0f);
 }
 
 // ---- a15: denoiseImageGuided / denoiseLumaChromaGuided (demosaic.cl:767-851) ----
@@ -634,11 +685,22 @@ GLS_DI float ltm_mask_from(const float (&gs)[9], float4 inp, const LtmParams& lp
     const float mean = sum, var = sumSq - sum * sum;
     const float luma = inp.x;
     float filtered = 0.0f, knorm = 0.0f;
+    const float den = var + lp.eps;
     FastDiv dv;
-    dv.init(var + lp.eps);
+    dv.init(den);
+    // The numerators (gs_i - mean) * (luma - mean): when the samples and the luma are finite
+    // with magnitudes summing to at most 2^20, every numerator is below 2^42, inside the
+    // shortcut's range; a numerator under its lower bound (2^-83) gives, with den >= 2^-20, a
+    // quotient below 2^-62 either way, and 1 + q rounds to 1 for both.  So the shortcut gives
+    // every tap its literal weight and the per-tap range test is dropped.
+    float mag = glsm::fabs_(luma);
+#pragma unroll
+    for (int i = 0; i < 9; i++) mag = mag + glsm::fabs_(gs[i]);
+    const bool fast = dv.ok && den >= 9.5367431640625e-07f && mag <= 1048576.0f;  // 2^-20, 2^20; NaN fails
 #pragma unroll
     for (int i = 0; i < 9; i++) {
-        const float wgt = bw[i] * (1.0f + dv((gs[i] - mean) * (luma - mean)));
+        const float num = (gs[i] - mean) * (luma - mean);
+        const float wgt = bw[i] * (1.0f + (fast ? dv.fast(num) : dv(num)));
         filtered = filtered + wgt * gs[i];
         knorm = knorm + wgt;
     }

@@ -45,6 +45,11 @@ struct SAcc4f {
     GLS_DI float4 at(int x, int y) const { return s[(y - y0) * ld + (x - x0)]; }
 };
 
+// a staged RGBA tile whose .w the kernel set to 1 (see unit_w in gls_pixel_ops.cuh)
+struct SAcc4f1 : SAcc4f {
+    static constexpr bool kUnitW = true;
+};
+
 struct SobelMap {
     const float4* base;  // {|gx|, |gy|, length, -}
     int x0, y0, ld, x, y;
@@ -77,44 +82,101 @@ GLS_DI float4 round4(float4 v) {
 
 // =========================================================================================
 // raw_pass1: per 2x2 quad, the 5x5-quad statistics of the scaled raw planes and the
-// pass-1 sums of computeRawNoiseStatistics.  Tiles of 32x32 quads, scaled values staged
-// in shared memory (one division per pixel instead of one per tap).
+// pass-1 sums of computeRawNoiseStatistics.  Tiles of 32x32 quads: the scaled values are
+// staged once per quad as a float4 of its four CFA channels (kernel order), each thread
+// sums the windows of 4 quads of a column from one pass over 8 staged rows (every window
+// still sums its taps in the reference's row-major order), the channel pairs (0, 1) and
+// (2, 3) run as packed fp32x2 chains, and the regression sums are packed likewise.
 // =========================================================================================
-constexpr int RQ = 32;               // quads per tile side
-constexpr int RP = 2 * RQ + 8;       // staged pixels per side (halo of 2 quads)
+constexpr int RQ = 32;        // quads per tile side
+constexpr int RQS = RQ + 4;   // staged quads per side (halo of 2 quads)
 
-template <class S>
-__global__ void __launch_bounds__(kT, 3) raw_pass1_kernel(RawPass1Args a) {  // 3 resident blocks per SM
-    __shared__ float s_raw[RP * RP];
-    Pass1Acc<4, 4> acc;
+// x / 25 per lane by the shortcut of div25 (reciprocal 0.04, one correction step), exact for
+// a lane that is 0 or in [2^-83, 2^60]; CHECK sends other lanes to the literal division.
+template <bool CHECK>
+GLS_DI float2 div25_x2(float2 x) {
+    const float2 y = f2(0.04f, 0.04f);
+    const float2 q0 = mul2(x, y);  // a multiplicand and an fma addend only
+    float2 q = fma2(fma2(q0, f2(-25.0f, -25.0f), x), y, q0);
+    if (CHECK) {
+        if (!FastDiv::in_range(x.x)) q.x = glsm::div_slow(x.x, 25.0f);
+        if (!FastDiv::in_range(x.y)) q.y = glsm::div_slow(x.y, 25.0f);
+    }
+    return q;
+}
+
+template <class S, int BAYER>
+__global__ void __launch_bounds__(kT, 2) raw_pass1_kernel(RawPass1Args a) {  // 2 resident blocks per SM
+    __shared__ float4 s_q[RQS * RQS];
+    RawPass1Acc2 acc;
     acc.init();
     const int qw = a.w / 2, qh = a.h / 2;
     const int tiles_x = (qw + RQ - 1) / RQ, tiles_y = (qh + RQ - 1) / RQ;
     const int col = threadIdx.x & 31, row0 = (threadIdx.x >> 5) * 4;
     for (int t = blockIdx.x; t < tiles_x * tiles_y; t += gridDim.x) {
         const int qx0 = (t % tiles_x) * RQ, qy0 = (t / tiles_x) * RQ;
-        const int px0 = 2 * qx0 - 4, py0 = 2 * qy0 - 4;
-        for (int i = threadIdx.x; i < RP * RP; i += kT) {
-            const int r = i / RP, c = i - r * RP;
-            const int gx = clampi(px0 + c, 0, a.w - 1), gy = clampi(py0 + r, 0, a.h - 1);
-            const float v = scale_value(__ldg(a.raw + (size_t)gy * a.pitch + gx), a.sm[((gy & 1) << 1) | (gx & 1)],
-                                        a.black);
-            s_raw[i] = Storage<S>::round(v);
+        for (int i = threadIdx.x; i < RQS * RQS; i += kT) {
+            const int r = i / RQS, c = i - r * RQS;
+            const int px = 2 * (qx0 - 2 + c), py = 2 * (qy0 - 2 + r);
+            float v[4];
+#pragma unroll
+            for (int ch = 0; ch < 4; ch++) {  // the pixel of channel ch, clamped to the frame
+                const int gx = clampi(px + bayer_dx(BAYER, ch), 0, a.w - 1);
+                const int gy = clampi(py + bayer_dy(BAYER, ch), 0, a.h - 1);
+                v[ch] = Storage<S>::round(
+                    scale_value(__ldg(a.raw + (size_t)gy * a.pitch + gx), a.sm[((gy & 1) << 1) | (gx & 1)], a.black));
+            }
+            s_q[i] = make_float4(v[0], v[1], v[2], v[3]);
         }
         __syncthreads();
-        SAcc1 R{s_raw, px0, py0, RP};
+        // window sums of quads (qx0 + col, qy0 + row0 + j), j = 0..3
+        float2 s01[4], q01[4], s23[4], q23[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) s01[j] = q01[j] = s23[j] = q23[j] = f2(0.0f, 0.0f);
+#pragma unroll
+        for (int rr = 0; rr < 8; rr++) {
+#pragma unroll
+            for (int dx = 0; dx < 5; dx++) {
+                const float4 v = s_q[(row0 + rr) * RQS + col + dx];
+                const float2 a01 = f2(v.x, v.y), a23 = f2(v.z, v.w);
+                const float2 p01 = mul2s(a01, a01), p23 = mul2s(a23, a23);  // summed: scalar multiplies
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    if (rr - j >= 0 && rr - j <= 4) {
+                        s01[j] = add2(s01[j], a01);
+                        q01[j] = add2(q01[j], p01);
+                        s23[j] = add2(s23[j], a23);
+                        q23[j] = add2(q23[j], p23);
+                    }
+                }
+            }
+        }
 #pragma unroll
         for (int j = 0; j < 4; j++) {
             const int qx = qx0 + col, qy = qy0 + row0 + j;
             if (qx < qw && qy < qh) {
-                float m[4], v[4];
-                raw_stats_quad(R, qx, qy, a.bayer, m, v);
-                acc.add(m, v, a.th);
+                // mean = sum / 25, var = (sq - sum^2 / 25) / 25 (demosaic.cl:1288-1324)
+                float2 m[2], v[2];
+                const float2 sp[2] = {s01[j], s23[j]}, qp[2] = {q01[j], q23[j]};
+#pragma unroll
+                for (int p = 0; p < 2; p++) {
+                    if (a.sums_exact) {
+                        m[p] = div25_x2<false>(sp[p]);
+                        v[p] = div25_x2<true>(sub2(qp[p], div25_x2<false>(mul2(sp[p], sp[p]))));
+                    } else {
+                        m[p] = div25_x2<true>(sp[p]);
+                        v[p] = div25_x2<true>(sub2(qp[p], div25_x2<true>(mul2(sp[p], sp[p]))));
+                    }
+                }
+                const float mm[4] = {m[0].x, m[0].y, m[1].x, m[1].y}, vv[4] = {v[0].x, v[0].y, v[1].x, v[1].y};
+                if (in_range<4, 4>(mm, vv, a.th)) acc.add_selected(m, v);
             }
         }
         __syncthreads();
     }
-    pass1_epilogue<4, 4>(acc, a.nlf, a.nlf_out);
+    Pass1Acc<4, 4> out;
+    acc.unpack(out);
+    pass1_epilogue<4, 4>(out, a.nlf, a.nlf_out);
 }
 
 // =========================================================================================
@@ -301,7 +363,7 @@ constexpr int LP = LT + 4;
 template <class SIn, class SOut>
 __global__ void __launch_bounds__(kT) level_pass1_kernel(LevelPass1Args a) {
     __shared__ float4 s_in[LP * LP];
-    Pass1Acc<1, 3> acc;
+    LevelPass1Acc2 acc;
     acc.init();
     typedef typename Storage<SIn>::T4 TIn;
     const TIn* in = (const TIn*)a.in;
@@ -315,38 +377,40 @@ __global__ void __launch_bounds__(kT) level_pass1_kernel(LevelPass1Args a) {
             s_in[i] = gin.at(x0 - 2 + c, y0 - 2 + r);
         }
         __syncthreads();
-        // statistics for pixels (x0 + col, y0 + row0 + j), j = 0..3
-        float s0[4], s1[4], s2[4], q0[4], q1[4], q2[4];
+        // window sums for pixels (x0 + col, y0 + row0 + j), j = 0..3: (s0, s1), (q0, q1) and
+        // (s2, q2) as packed pairs, every window summed in the reference's row-major order
+        float2 s01[4], q01[4], s2q2[4];
 #pragma unroll
-        for (int j = 0; j < 4; j++) s0[j] = s1[j] = s2[j] = q0[j] = q1[j] = q2[j] = 0.0f;
+        for (int j = 0; j < 4; j++) s01[j] = q01[j] = s2q2[j] = f2(0.0f, 0.0f);
 #pragma unroll
         for (int rr = 0; rr < 8; rr++) {
 #pragma unroll
             for (int dx = 0; dx < 5; dx++) {
                 const float4 v = s_in[(row0 + rr) * LP + col + dx];
+                const float2 a01 = f2(v.x, v.y);
+                const float2 p01 = mul2s(a01, a01);  // summed: scalar multiplies
+                const float2 z = f2(v.z, __fmul_rn(v.z, v.z));
 #pragma unroll
                 for (int j = 0; j < 4; j++) {
                     if (rr - j >= 0 && rr - j <= 4) {
-                        s0[j] = s0[j] + v.x;
-                        q0[j] = q0[j] + v.x * v.x;
-                        s1[j] = s1[j] + v.y;
-                        q1[j] = q1[j] + v.y * v.y;
-                        s2[j] = s2[j] + v.z;
-                        q2[j] = q2[j] + v.z * v.z;
+                        s01[j] = add2(s01[j], a01);
+                        q01[j] = add2(q01[j], p01);
+                        s2q2[j] = add2(s2q2[j], z);
                     }
                 }
             }
         }
+        const FastDiv d25 = div25();
 #pragma unroll
         for (int j = 0; j < 4; j++) {
             const int x = x0 + col, y = y0 + row0 + j;
             if (x < a.w && y < a.h) {
-                float m[1], v[3];
-                m[0] = div_(s0[j], 25.0f);
-                v[0] = div_(q0[j] - div_(s0[j] * s0[j], 25.0f), 25.0f);
-                v[1] = div_(q1[j] - div_(s1[j] * s1[j], 25.0f), 25.0f);
-                v[2] = div_(q2[j] - div_(s2[j] * s2[j], 25.0f), 25.0f);
-                acc.add(m, v, a.th);
+                // noiseStatistics (demosaic.cl:1267-1286): mean Y = s0 / 25, var_k = (q_k - s_k^2 / 25) / 25
+                const float2 mt = div25_x2<true>(f2(s01[j].x, s2q2[j].x * s2q2[j].x));  // (mean Y, s2^2 / 25)
+                const float2 v01 = div25_x2<true>(sub2(q01[j], div25_x2<true>(mul2(s01[j], s01[j]))));
+                const float v2 = d25(s2q2[j].y - mt.y);
+                const float m[1] = {mt.x}, v[3] = {v01.x, v01.y, v2};
+                if (in_range<1, 3>(m, v, a.th)) acc.add_selected(mt.x, v01, v2);
             }
         }
         // downsample: the coarse 16x16 tile under this fine tile
@@ -360,7 +424,9 @@ __global__ void __launch_bounds__(kT) level_pass1_kernel(LevelPass1Args a) {
         }
         __syncthreads();
     }
-    pass1_epilogue<1, 3>(acc, a.nlf, a.nlf_out);
+    Pass1Acc<1, 3> out;
+    acc.unpack(out);
+    pass1_epilogue<1, 3>(out, a.nlf, a.nlf_out);
 }
 
 // =========================================================================================
@@ -463,7 +529,9 @@ __global__ void __launch_bounds__(kT) final_kernel(FinalArgs a) {
     for (int i = threadIdx.x; i < PW * PH; i += kT) {
         const int r = i / PW, c = i - r * PW;
         const int gx = clampi(x0 - 3 + c, 0, w - 1), gy = clampi(y0 - 3 + r, 0, h - 1);
-        s_l0[i] = Storage<__half>::cvt(a.level0[(size_t)gy * a.l0_pitch + gx]);
+        float4 v = Storage<__half>::cvt(a.level0[(size_t)gy * a.l0_pitch + gx]);
+        v.w = 1.0f;  // the denoisers read only .xyz; the bilateral counts its normaliser in .w
+        s_l0[i] = v;
     }
     // entry layout: rx[3][EW], ry[3][EH], lx[FW], ly[FH], gx[3][FW], gy[3][FH]
     constexpr int NRX = 3 * EW, NRY = 3 * EH, NLX = FW, NLY = FH, NGX = 3 * FW, NGY = 3 * FH;
@@ -547,7 +615,7 @@ __global__ void __launch_bounds__(kT) final_kernel(FinalArgs a) {
     __syncthreads();
 
     // ---- phase 3: denoise + reassemble over the tile and its ring ----
-    const SAcc4f L0{s_l0, x0 - 3, y0 - 3, PW};
+    const SAcc4f1 L0{{s_l0, x0 - 3, y0 - 3, PW}};
     Nlf6 n;
 #pragma unroll
     for (int k = 0; k < 3; k++) {
@@ -667,21 +735,41 @@ gls_status fused_raw_fit(gls_ctx* ctx, const RawPass1Args& args, bool half, NlfS
     a.th = nlf_thresholds();
     a.nlf = s;
     a.nlf_out = out_dev;
+    // Every scaled value is 0 or at least 2^-41 when each scale factor lies in [1/2, 2^15]
+    // (unorm16 values and the black level are multiples of 2^-40, so a positive difference
+    // is at least 2^-40), and at most 2^15 (finite in binary16 storage too); so a 5x5 sum is
+    // 0 or in [2^-41, 2^20] and its square 0 or in [2^-82, 2^40], where x / 25 has its exact
+    // shortcut.  Other scale factors take the checked path.
+    a.sums_exact = 1;
+    for (int k = 0; k < 4; k++)
+        if (!(a.sm[k] >= 0.5f && a.sm[k] <= 32768.0f)) a.sums_exact = 0;
     const int qw = a.w / 2, qh = a.h / 2;
     const long tiles = (long)((qw + RQ - 1) / RQ) * ((qh + RQ - 1) / RQ);
+#define GLS_RAWP1(SS, BY)                                                      \
+    {                                                                          \
+        const int grid = resident_grid<raw_pass1_kernel<SS, BY>>(ctx, tiles); \
+        raw_pass1_kernel<SS, BY><<<grid, kT, 0, ctx->stream>>>(a);            \
+    }
+#define GLS_RAWP1_B(SS)                 \
+    switch (a.bayer) {                  \
+        case 0: GLS_RAWP1(SS, 0) break; \
+        case 1: GLS_RAWP1(SS, 1) break; \
+        case 2: GLS_RAWP1(SS, 2) break; \
+        default: GLS_RAWP1(SS, 3) break; \
+    }
     if (half) {
-        const int grid = resident_grid<raw_pass1_kernel<__half>>(ctx, tiles);
-        raw_pass1_kernel<__half><<<grid, kT, 0, ctx->stream>>>(a);
+        GLS_RAWP1_B(__half)
         RawU16SrcS<__half> src{{a.raw, a.w, a.h, a.pitch}, {a.sm[0], a.sm[1], a.sm[2], a.sm[3]}, a.black, a.bayer};
         ctx->launches++;
         nlf_finish<4, 4>(ctx, src, qw, qh, s, out_dev);
     } else {
-        const int grid = resident_grid<raw_pass1_kernel<float>>(ctx, tiles);
-        raw_pass1_kernel<float><<<grid, kT, 0, ctx->stream>>>(a);
+        GLS_RAWP1_B(float)
         RawU16SrcS<float> src{{a.raw, a.w, a.h, a.pitch}, {a.sm[0], a.sm[1], a.sm[2], a.sm[3]}, a.black, a.bayer};
         ctx->launches++;
         nlf_finish<4, 4>(ctx, src, qw, qh, s, out_dev);
     }
+#undef GLS_RAWP1_B
+#undef GLS_RAWP1
     return check_launch(ctx, "raw noise statistics (fused)");
 }
 

@@ -63,6 +63,19 @@ def test_scale_raw(ctx, frame, half):
     assert mismatch(host(out), ref) == 0
 
 
+def test_unorm16_read_is_the_division(ctx):
+    """Every uint16 code through scaleRawData with unit scale and zero black: the device's
+    UNORM16 read (reciprocal and one correction step) equals the correctly rounded division
+    v / 65535 for all 65536 codes."""
+    import torch
+    raw = np.arange(65536, dtype=np.uint16).reshape(256, 256)
+    out = empty((256, 256), False)
+    ctx.scaleRawData(dev(raw), out, 2, [1.0, 1.0, 1.0, 1.0], np.float32(0.0))
+    torch.cuda.synchronize()
+    want = raw.astype(np.float32) / np.float32(65535.0)
+    assert np.array_equal(host(out).view(np.uint32), want.view(np.uint32))
+
+
 def test_raw_noise_statistics(ctx, frame):
     import torch
     s = frame["taps"]["scaled_raw"]
