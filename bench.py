@@ -50,6 +50,7 @@ def parse(argv=None):
     ap.add_argument("--no-awb", action="store_true")
     ap.add_argument("--no-dng", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-configs", action="store_true", help="skip the config-1 and precision-form lines")
     ap.add_argument("--profile-only", action="store_true", help="a short run for ncu: no clocks, no cpu leg")
     ap.add_argument("--cpu-replicas", action="store_true",
                     help="check the replica plumbing on the CPU (gloo): each rank runs the oracle on a tiny "
@@ -386,6 +387,93 @@ def run_cpu_replicas(args, cfg):
         dist.destroy_process_group()
 
 
+def single_frame_line(ctx, cfg, dev, args, flush):
+    """One configuration's own line: its frame alone per step through RawConverter::demosaicImage
+    (device-resident, CUDA events, L2 flushed between steps), the same through host buffers
+    (pinned raw in and output back, copies inside the timed region), and the whole-pipeline
+    algorithmic bandwidth with the configuration's storage and output bytes."""
+    import torch
+    from climage_gb300 import configs, gls
+    raw, _, spec = make_frames(cfg, 0)[0]
+    h, w = raw.shape
+    out_f32 = cfg["out"] == "rgba_f32"
+    half = cfg["storage"] == gls.STORAGE_F16
+    p = configs.to_gls_params(spec)
+    conv = gls.RawConverter(ctx)
+    raw_d = torch.from_numpy(raw).to(dev)
+    out_d = torch.empty((h, w, 4), dtype=torch.float32 if out_f32 else torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(args.warmup):
+        conv.demosaicImage(raw_d, p, out_d)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for a, b in ev:
+        flush.fill_(1)
+        a.record(stream)
+        conv.demosaicImage(raw_d, p, out_d)
+        b.record(stream)
+    torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in ev) / args.steps
+    # end to end: pinned host raw -> device, convert, output -> pinned host
+    raw_h = torch.from_numpy(raw).pin_memory()
+    out_h = torch.empty(out_d.shape, dtype=out_d.dtype).pin_memory()
+
+    def e2e_step():
+        raw_d.copy_(raw_h, non_blocking=True)
+        conv.demosaicImage(raw_d, p, out_d)
+        out_h.copy_(out_d, non_blocking=True)
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        e2e_step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    conv.close()
+    peak, _ = measured_peak_hbm()
+    S, O = (8 if half else 16), (16 if out_f32 else 4)
+    bpp = algorithmic_bytes_per_px(S, O, cfg["levels"])
+    achieved = bpp * w * h / (ms / 1e3) / 1e9
+    return {"workload": cfg["name"], "value": round(w * h / 1e3 / ms, 3), "unit": "MPix/s", "ms_per_frame": round(ms, 4),
+            "e2e": {"value": round(w * h / 1e3 / e2e_ms, 3), "unit": "MPix/s", "h2d_bytes_per_step": int(raw.nbytes),
+                    "d2h_bytes_per_step": int(out_d.numel() * out_d.element_size())},
+            "storage": "fp16" if half else "fp32", "output": "rgba_f32" if out_f32 else "rgba8", "levels": cfg["levels"],
+            "pipeline_roofline": {"algorithmic_bytes_per_px": round(bpp, 2), "achieved": round(achieved, 1),
+                                  "unit": "GB/s", "frac": round(achieved / peak, 4)},
+            "timing": "one frame per step, CUDA events, L2 flushed between steps; e2e by the host clock"}
+
+
+def burst_vs_oracle(burst, bouts):
+    """Four frames of the batched burst against the oracle, outside any timed region: the first
+    8064x6048 frame, the first 10-bit and the first 14-bit frames, and frames of the CFA phases
+    still missing, until every phase is covered or four frames are chosen."""
+    from oracle import oracle as orc
+    from tests.helpers import oracle_params
+    picks, phases = [], set()
+
+    def take(i):
+        if i is not None and i not in picks and len(picks) < 4:
+            picks.append(i)
+            phases.add(burst[i][1]["bayer_pattern"])
+
+    take(next((i for i, (r, _) in enumerate(burst) if r.shape[1] == 8064), None))
+    take(next((i for i, (_, sp) in enumerate(burst) if sp["white_level"] == 1023), None))
+    take(next((i for i, (_, sp) in enumerate(burst) if sp["white_level"] == 16383), None))
+    for i, (_, sp) in enumerate(burst):
+        if sp["bayer_pattern"] not in phases:
+            take(i)
+    res = []
+    for i in picks:
+        raw, sp = burst[i]
+        ref = orc.demosaic(raw.cpu().numpy(), oracle_params(sp), orc.F32, want=("rgba8",))["rgba8"]
+        got = bouts[i].cpu().numpy()
+        res.append({"frame": i, "size": "%dx%d" % (raw.shape[1], raw.shape[0]), "cfa": int(sp["bayer_pattern"]),
+                    "bits": {1023: 10, 4095: 12, 16383: 14}.get(int(sp["white_level"]), 0),
+                    "codes_differing": int((got[..., :3] != ref[..., :3]).sum())})
+    return {"bit_exact": all(r["codes_differing"] == 0 for r in res), "frames": res}
+
+
 def main(argv=None):
     argv = sys.argv[1:] if argv is None else argv
     args = parse(argv)
@@ -614,9 +702,17 @@ def main(argv=None):
                         "frame_data": "crops, 2x2 tilings and one-pixel shifts of the rendered 4032x3024 frames; "
                                       "10/14-bit by bit shifts; per-frame WB gains in [1, 3]"}
         del graph
+        if world == 1 and not args.no_cpu:
+            batched_line["bit_exact_vs_oracle"] = burst_vs_oracle(burst, bouts)
         bb.close()
         bctx.close()
         del braws, bouts, burst
+
+    # ---- configurations 1 and 3 on their own lines ----
+    config_lines = None
+    if rank == 0 and not args.no_configs and not args.profile_only:
+        config_lines = {"config1": single_frame_line(ctx, configs.CONFIG1, dev, args, flush),
+                        "precision_form": single_frame_line(ctx, configs.CONFIG3, dev, args, flush)}
 
     # ---- DNG ingest: the first frame as one lossless-JPEG strip (the layout the reference's
     # DNG writer uses), decoded from pinned host memory into the device frame ----
@@ -680,6 +776,8 @@ def main(argv=None):
             "auto_white_balance": awb_line,
             "dng_decode": dng_line,
             "batched_form": batched_line,
+            "config1": config_lines["config1"] if config_lines else None,
+            "precision_form": config_lines["precision_form"] if config_lines else None,
         }
         print(json.dumps(line), flush=True)
     conv.close()

@@ -127,7 +127,7 @@ def to_gls_params(spec):
     p.pyramid_levels = spec["pyramid_levels"]
     p.denoise_algorithm = spec["denoise_algorithm"]
     p.storage = spec["storage"]
-    p.rotate_180 = 0
+    p.rotate_180 = int(spec.get("rotate_180", 0))
     return p
 
 

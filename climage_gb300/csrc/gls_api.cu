@@ -320,7 +320,6 @@ gls_status gls_interpolate_green(gls_ctx* ctx, const gls_image_desc* scaled, con
 gls_status gls_interpolate_red_blue(gls_ctx* ctx, const gls_image_desc* scaled, const gls_image_desc* green,
                                     const gls_image_desc* rgb, int bayer, float chroma_variance, int rotate_180) {
     REQ_CTX
-    if (rotate_180) return set_error(ctx, GLS_ERR_UNSUPPORTED, "interpolateRedBlue: rotate_180 is not supported");
     GLS_CHECK(check_desc(ctx, scaled, "scaled", GLS_R_F32, GLS_R_F16));
     GLS_CHECK(check_desc(ctx, green, "green", GLS_R_F32, GLS_R_F16));
     GLS_CHECK(check_desc(ctx, rgb, "rgb", GLS_RGBA_F32, GLS_RGBA_F16));
@@ -329,7 +328,7 @@ gls_status gls_interpolate_red_blue(gls_ctx* ctx, const gls_image_desc* scaled, 
     GLS_CHECK(same_storage(ctx, scaled, green, "interpolateRedBlue"));
     GLS_CHECK(same_storage(ctx, scaled, rgb, "interpolateRedBlue"));
     GLS_CHECK(check_bayer(ctx, bayer));
-    launch_red_blue(ctx, ref_of(scaled), ref_of(green), ref_of(rgb), bayer, chroma_variance, nullptr);
+    launch_red_blue(ctx, ref_of(scaled), ref_of(green), ref_of(rgb), bayer, chroma_variance, nullptr, rotate_180 != 0);
     return check_launch(ctx, "interpolateRedBlue");
 }
 

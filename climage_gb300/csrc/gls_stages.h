@@ -33,8 +33,9 @@ void launch_scale_raw(gls_ctx* ctx, const uint16_t* raw, int w, int h, int rpitc
                       const float sm[4], float black);
 void launch_raw_stats(gls_ctx* ctx, const ImgRef& scaled, int bayer, float4* mean, int mpitch, float4* var, int vpitch);
 void launch_green(gls_ctx* ctx, const ImgRef& scaled, const ImgRef& green, int bayer, float lv, const float* lv_dev);
+// rotate_180: the output turned by 180 degrees as the reference writes it (row 0 and column 0 zero)
 void launch_red_blue(gls_ctx* ctx, const ImgRef& scaled, const ImgRef& green, const ImgRef& rgb, int bayer, float cv,
-                     const float* rawB_dev);
+                     const float* rawB_dev, int rotate_180 = 0);
 void launch_highlights(gls_ctx* ctx, const ImgRef& in, const ImgRef& out, float clip);
 void launch_transform(gls_ctx* ctx, const ImgRef& in, const ImgRef& out, const float m[9]);
 void launch_despeckle(gls_ctx* ctx, const ImgRef& in, const ImgRef& out, float va0, float vb0);

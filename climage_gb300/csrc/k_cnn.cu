@@ -506,11 +506,12 @@ struct FusedArgs {
     const float* bias[5];
 };
 
-// bounded wait on phase `parity` of an mbarrier: non-blocking polls (test_wait), so the
-// block resumes as soon as the MMAs complete; the verdict is block-uniform
-__device__ __forceinline__ bool fu_wait(uint32_t bar, uint32_t parity) {
+// bounded wait on phase `parity` of an mbarrier: at most `limit` non-blocking polls
+// (test_wait), so the block resumes as soon as the MMAs complete and gives up after the
+// limit; the verdict is block-uniform (every thread of the block calls it)
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity, uint32_t limit) {
     uint32_t done = 0;
-    for (uint32_t k = 0; k < 4 * kWaitLimit && !done; k++) {
+    for (uint32_t k = 0; k < limit && !done; k++) {
         asm volatile(
             "{\n.reg .pred p;\nmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
             : "=r"(done)
@@ -518,6 +519,22 @@ __device__ __forceinline__ bool fu_wait(uint32_t bar, uint32_t parity) {
             : "memory");
     }
     return __syncthreads_and(done) != 0;
+}
+
+__device__ __forceinline__ bool fu_wait(uint32_t bar, uint32_t parity) { return mbar_wait_bounded(bar, parity, 4 * kWaitLimit); }
+
+// The bounded wait of the tensor-core kernels on an mbarrier that nothing arrives at and to
+// which no MMA was committed: the wait runs out with nothing in flight, and the block
+// records the error as a block whose MMAs never completed does (gls_cnn_wait_probe).
+__global__ void __launch_bounds__(128) wait_probe_kernel(int* err, uint32_t limit) {
+    __shared__ __align__(8) uint64_t bar;
+    const uint32_t b = (uint32_t)__cvta_generic_to_shared(&bar);
+    if (threadIdx.x == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(b) : "memory");
+    __syncthreads();
+    const bool ok = mbar_wait_bounded(b, 0u, limit);
+    if (!ok && threadIdx.x == 0) atomicExch(err, 1);
+    __syncthreads();
+    if (threadIdx.x == 0) asm volatile("mbarrier.inval.shared::cta.b64 [%0];\n" ::"r"(b) : "memory");
 }
 
 __device__ __forceinline__ void fu_sync_for_mma() {
@@ -1232,8 +1249,19 @@ gls_status gls_cnn_status(gls_cnn* c) {
     GLS_CHECK(check_cuda(c->ctx, cudaMemcpyAsync(&e, c->err_dev, sizeof(int), cudaMemcpyDeviceToHost, c->ctx->stream),
                          "read CNN status"));
     GLS_CHECK(check_cuda(c->ctx, cudaStreamSynchronize(c->ctx->stream), "synchronize"));
-    if (e) return set_error(c->ctx, GLS_ERR_TIMEOUT, "CNN: a tensor-core wait ran out");
+    if (e) {
+        // reported once: the flag is cleared for the calls that follow
+        GLS_CHECK(check_cuda(c->ctx, cudaMemsetAsync(c->err_dev, 0, sizeof(int), c->ctx->stream), "clear CNN status"));
+        return set_error(c->ctx, GLS_ERR_TIMEOUT, "CNN: a tensor-core wait ran out");
+    }
     return GLS_OK;
+}
+
+gls_status gls_cnn_wait_probe(gls_cnn* c, unsigned polls) {
+    if (!c || polls == 0 || polls > kWaitLimit) return GLS_ERR_INVALID_ARGUMENT;
+    wait_probe_kernel<<<1, 128, 0, c->ctx->stream>>>(c->err_dev, polls);
+    c->ctx->launches++;
+    return check_launch(c->ctx, "CNN wait probe");
 }
 
 gls_status gls_cnn_set_params(gls_cnn* c, const float* params, int n) {

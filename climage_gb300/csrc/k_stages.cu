@@ -68,15 +68,23 @@ __global__ void green_kernel(GImg1<S> raw, S* out, int opitch, int bayer, float 
 }
 
 // ---- a8 ----
+// With rotate_180 the reference writes pixel (x, y) at (w - x, h - y) (demosaic.cl:310-313):
+// here each thread computes the output pixel (x, y) from the source pixel (w - x, h - y), and
+// row 0 and column 0 of the output, which the reference never writes, are zero.
 template <class S>
 __global__ void red_blue_kernel(GImg1<S> raw, GImg1<S> green, typename Storage<S>::T4* out, int opitch, int bayer,
-                                float cv_host, const float* rawB_dev) {
+                                float cv_host, const float* rawB_dev, int rotate_180) {
     PIXEL_XY
     if (x >= raw.w || y >= raw.h) return;
-    float cv = rawB_dev ? div_(rawB_dev[0] + rawB_dev[2], 2.0f) : cv_host;
-    cv = mmax(cv, 1e-6f);
-    const float3 p = red_blue_at(raw, green, x, y, bayer, cv);
-    Storage<S>::st4(out + (size_t)y * opitch + x, make_float4(p.x, p.y, p.z, 0.0f));
+    float4 o = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (!rotate_180 || (x > 0 && y > 0)) {
+        float cv = rawB_dev ? div_(rawB_dev[0] + rawB_dev[2], 2.0f) : cv_host;
+        cv = mmax(cv, 1e-6f);
+        const float3 p = rotate_180 ? red_blue_at(raw, green, raw.w - x, raw.h - y, bayer, cv)
+                                    : red_blue_at(raw, green, x, y, bayer, cv);
+        o = make_float4(p.x, p.y, p.z, 0.0f);
+    }
+    Storage<S>::st4(out + (size_t)y * opitch + x, o);
 }
 
 // ---- a9, a10 ----
@@ -408,9 +416,9 @@ void launch_green(gls_ctx* ctx, const ImgRef& scaled, const ImgRef& green, int b
 }
 
 void launch_red_blue(gls_ctx* ctx, const ImgRef& scaled, const ImgRef& green, const ImgRef& rgb, int bayer, float cv,
-                     const float* rawB_dev) {
+                     const float* rawB_dev, int rotate_180) {
     DISPATCH_S(scaled.half, (red_blue_kernel<S><<<grid2(scaled.w, scaled.h), dim3(BX, BY), 0, ctx->stream>>>(
-                                g1<S>(scaled), g1<S>(green), o4<S>(rgb), rgb.pitch, bayer, cv, rawB_dev)));
+                                g1<S>(scaled), g1<S>(green), o4<S>(rgb), rgb.pitch, bayer, cv, rawB_dev, rotate_180)));
     ctx->launches++;
 }
 

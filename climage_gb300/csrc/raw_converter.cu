@@ -281,11 +281,13 @@ struct gls_raw_converter {
     int mode = 0;  // 0 fused kernels, 1 one kernel per reference stage
 
     gls_status run(const uint16_t* raw, int rpitch, gls_demosaic_params* p, void* out, bool out_float, int opitch) {
-        if (mode == 0 && p->denoise_algorithm != GLS_DENOISE_GUIDED_PRECISE)
+        // rotate_180 turns the image at interpolateRedBlue; the later stages read the turned
+        // image, so a rotated frame takes the single-stage schedule
+        if (mode == 0 && p->denoise_algorithm != GLS_DENOISE_GUIDED_PRECISE && !p->rotate_180)
             return run_fused(raw, rpitch, p, out, out_float, opitch);
         if (cnn)
             return set_error(ctx, GLS_ERR_UNSUPPORTED,
-                             "the learned stage runs in the fused schedule only (not with GuidedPrecise)");
+                             "the learned stage runs in the fused schedule only (not with GuidedPrecise or rotate_180)");
         return run_staged(raw, rpitch, p, out, out_float, opitch);
     }
 
@@ -500,7 +502,7 @@ struct gls_raw_converter {
         launch_green(ctx, scaled, green, bayer, 0.0f, rawB + 1);
         mark("interpolateGreen");
         tap(1, green, 1);
-        launch_red_blue(ctx, scaled, green, linA, bayer, 0.0f, rawB);
+        launch_red_blue(ctx, scaled, green, linA, bayer, 0.0f, rawB, p->rotate_180 != 0);
         mark("interpolateRedBlue");
         launch_highlights(ctx, linA, linA, 1.0f);
         mark("blendHighlights");
@@ -653,7 +655,6 @@ static gls_status validate_params(gls_ctx* ctx, const gls_demosaic_params* p, in
         return set_error(ctx, GLS_ERR_INVALID_ARGUMENT, "unknown storage %d", p->storage);
     if (p->denoise_algorithm < 0 || p->denoise_algorithm > 2)
         return set_error(ctx, GLS_ERR_INVALID_ARGUMENT, "unknown denoise algorithm %d", p->denoise_algorithm);
-    if (p->rotate_180) return set_error(ctx, GLS_ERR_UNSUPPORTED, "rotate_180 is not supported");
     if (w <= 0 || h <= 0 || (w & 1) || (h & 1))
         return set_error(ctx, GLS_ERR_INVALID_SIZE, "raw frames must have positive, even width and height");
     if ((w >> (p->pyramid_levels - 1)) < 1 || (h >> (p->pyramid_levels - 1)) < 1)

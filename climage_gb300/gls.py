@@ -17,7 +17,13 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libgls_cuda.so")
 
 GLS_OK = 0
+GLS_ERR_INVALID_ARGUMENT = 1
 GLS_ERR_INVALID_SIZE = 2
+GLS_ERR_UNSUPPORTED = 3
+GLS_ERR_CUDA = 4
+GLS_ERR_OUT_OF_MEMORY = 5
+GLS_ERR_TIMEOUT = 6
+GLS_ERR_FORMAT = 7
 GLS_ERR_BAD_STREAM = 8
 # image size limit of Context.guidedFilterNoAlloc (gls_cuda.h)
 GUIDED_FILTER_NOALLOC_MAX_PIXELS = 116490
@@ -169,6 +175,7 @@ SIGNATURES = [
     ("gls_cnn_set_backend", _I, [_P, _I]),
     ("gls_cnn_get_backend", _I, [_P]),
     ("gls_cnn_status", _I, [_P]),
+    ("gls_cnn_wait_probe", _I, [_P, ctypes.c_uint]),
     ("gls_cnn_train_step", _I, [_P, _P, _P, _I, _I, _I, _F, _FP]),
     ("gls_raw_batch_plan", _I, [_I, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int), _I,
                                 ctypes.POINTER(ctypes.c_int)]),
@@ -663,6 +670,11 @@ class Cnn:
 
     def status(self):
         self.ctx.check(lib().gls_cnn_status(self.handle), "Cnn.status")
+
+    def wait_probe(self, polls):
+        """Runs the tensor-core kernels' bounded wait on a barrier that never completes; the
+        next status() raises GLS_ERR_TIMEOUT."""
+        self.ctx.check(lib().gls_cnn_wait_probe(self.handle, int(polls)), "Cnn.wait_probe")
 
     def train_step(self, inp, gt, lr):
         n, h, w, _ = inp.shape

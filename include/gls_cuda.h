@@ -101,7 +101,9 @@ typedef struct {
     int pyramid_levels;    /* 4..8 (the reference fixes 5) */
     int denoise_algorithm; /* gls_denoise_algorithm (PyramidalDenoise::DenoiseAlgorithm) */
     int storage;           /* gls_storage of the intermediate images */
-    int rotate_180;        /* must be 0 */
+    int rotate_180;        /* turn the image by 180 degrees at interpolateRedBlue, as the reference
+                              does (pixel (x, y) to (w - x, h - y); row 0 and column 0, which the
+                              reference leaves unwritten, are zero); runs the single-stage schedule */
 } gls_demosaic_params;
 
 typedef struct gls_ctx gls_ctx;
@@ -132,7 +134,8 @@ GLS_API gls_status gls_compute_raw_noise_statistics(gls_ctx* ctx, const gls_imag
 /* interpolateGreen (demosaic_cl.cpp:46-64) */
 GLS_API gls_status gls_interpolate_green(gls_ctx* ctx, const gls_image_desc* scaled, const gls_image_desc* green,
                                          int bayer_pattern, float luma_variance);
-/* interpolateRedBlue (demosaic_cl.cpp:66-86); rotate_180 must be 0 */
+/* interpolateRedBlue (demosaic_cl.cpp:66-86); rotate_180 turns the output by 180 degrees
+ * (demosaic.cl:310-313), row 0 and column 0 zero */
 GLS_API gls_status gls_interpolate_red_blue(gls_ctx* ctx, const gls_image_desc* scaled, const gls_image_desc* green,
                                             const gls_image_desc* rgb, int bayer_pattern, float chroma_variance,
                                             int rotate_180);
@@ -391,8 +394,14 @@ GLS_API gls_status gls_cnn_forward(gls_cnn* cnn, const float* in, int width, int
  * backward pass always uses mma.sync.  A converter given this network copies the choice. */
 GLS_API gls_status gls_cnn_set_backend(gls_cnn* cnn, int backend);
 GLS_API int gls_cnn_get_backend(gls_cnn* cnn);
-/* Synchronises; GLS_ERR_TIMEOUT when a tcgen05 block gave up waiting for its MMAs. */
+/* Synchronises; GLS_ERR_TIMEOUT when a tcgen05 block gave up waiting for its MMAs (reported
+ * once: the flag is cleared, and the next status is GLS_OK unless another wait ran out). */
 GLS_API gls_status gls_cnn_status(gls_cnn* cnn);
+/* Diagnostic of the bounded waits (no counterpart in the reference): runs the tensor-core
+ * kernels' mbarrier wait, limited to `polls` polls (1 .. 2^24), on a barrier that nothing
+ * arrives at and to which no MMA was committed, so the wait runs out with nothing in flight
+ * and the next gls_cnn_status returns GLS_ERR_TIMEOUT. */
+GLS_API gls_status gls_cnn_wait_probe(gls_cnn* cnn, unsigned polls);
 /* One Adam step (lr > 0; lr = 0 only computes the gradients) on a batch against the clean
  * RGB gt; loss[0] = mean squared error of (input RGB + residual), loss[1] = strength loss. */
 GLS_API gls_status gls_cnn_train_step(gls_cnn* cnn, const float* in, const float* gt, int width, int height, int n,

@@ -437,13 +437,13 @@ class RawConverter {
     cuda_image_2d<rgba_pixel>* demosaicImage(const image<luma_pixel_16>& rawImage, DemosaicParametersT<L>* params,
                                              const rectangle* gmb_position, bool rotate_180) {
         (void)gmb_position;  // the reference fits the noise model on every frame regardless
-        if (rotate_180) throw cuda_error(GLS_ERR_UNSUPPORTED, "rotate_180 is not supported");
         if (!_raw || _raw->width != rawImage.width || _raw->height != rawImage.height) {
             _raw = std::make_unique<cuda_image_2d<luma_pixel_16>>(_ctx, rawImage.width, rawImage.height);
             _rgb = std::make_unique<cuda_image_2d<rgba_pixel>>(_ctx, rawImage.width, rawImage.height);
         }
         _raw->copyPixelsFrom(rawImage);
         gls_demosaic_params p = params->to_c();
+        p.rotate_180 = rotate_180 ? 1 : 0;
         const gls_image_desc r = _raw->desc(), o = _rgb->desc();
         check(gls_raw_converter_demosaic(_conv, &r, &p, &o, 0), "RawConverter::demosaicImage", _ctx->ctx());
         params->update_noise_model(p);

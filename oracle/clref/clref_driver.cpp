@@ -54,10 +54,10 @@ int clref_interpolate_green(const float* scaled, int w, int h, int bayer, float 
 }
 
 int clref_interpolate_red_blue(const float* scaled, const float* green, int w, int h, int bayer, float chroma_variance,
-                               float* out) {
+                               int rotate_180, float* out) {
     cl_image in = img(scaled, w, h, 1, CLSHIM_F32), g = img(green, w, h, 1, CLSHIM_F32),
              o = img(out, w, h, 4, CLSHIM_F32);
-    return run2d(w, h, [&] { interpolateRedBlue(&in, &g, &o, bayer, chroma_variance, 0); });
+    return run2d(w, h, [&] { interpolateRedBlue(&in, &g, &o, bayer, chroma_variance, rotate_180); });
 }
 
 int clref_blend_highlights(const float* in_p, int w, int h, float clip, float* out) {

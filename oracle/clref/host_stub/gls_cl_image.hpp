@@ -5,6 +5,7 @@
 #ifndef GLS_CL_IMAGE_STUB_HPP
 #define GLS_CL_IMAGE_STUB_HPP
 
+#include <cstring>
 #include <memory>
 #include <span>
 #include <vector>
@@ -29,7 +30,14 @@ class cl_image_2d {
     const int width, height;
     mutable std::vector<T> pixels;
 
-    cl_image_2d(cl::Context, int w, int h) : width(w), height(h), pixels((size_t)w * h) {}
+    // A new image starts at zero.  The pixel types' own default constructors leave their
+    // channels unset, and the reference reads texels that no kernel has written in one
+    // place: with rotate_180, interpolateRedBlue never writes row 0 and column 0 of its
+    // output (demosaic.cl:310-313), whose contents OpenCL leaves undefined; zero is the
+    // convention the oracle and the CUDA path share.
+    cl_image_2d(cl::Context, int w, int h) : width(w), height(h), pixels((size_t)w * h) {
+        std::memset(static_cast<void*>(pixels.data()), 0, pixels.size() * sizeof(T));
+    }
     image<T> mapImage() const { return image<T>(width, height, std::span<T>(pixels.data(), pixels.size())); }
     void copyPixelsFrom(const image<T>& other) const {
         for (int y = 0; y < height; y++)

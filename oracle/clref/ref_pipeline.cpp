@@ -219,7 +219,7 @@ extern "C" {
 // exposure_multiplier, noise_level, scale_mul[4], rgb_cam[9], raw_nlf[4], pyramid_nlf[30],
 // denoise[25] (luma, chroma, chromaBoost, gradientBoost, sharpening per level), rgb[5],
 // ltm[4]; out: RGBA8; raw_nlf_out[4], pyramid_nlf_out[30]: the updated noise model.
-int ref_raw_converter(const uint16_t* raw, int w, int h, int bayer, const float* params, int local_tone_mapping,
+int ref_raw_converter(const uint16_t* raw, int w, int h, int bayer, const float* params, int local_tone_mapping, int rotate_180,
                       uint8_t* out, float* raw_nlf_out, float* pyramid_nlf_out) {
     g_mixed = false;
     const float* p = params;
@@ -258,7 +258,7 @@ int ref_raw_converter(const uint16_t* raw, int w, int h, int bayer, const float*
     gls::OpenCLContext ctx;
     RawConverter rc(&ctx);
     gls::image<gls::luma_pixel_16> rawImage(w, h, std::span<gls::luma_pixel_16>((gls::luma_pixel_16*)raw, (size_t)w * h));
-    const auto* rgba = rc.demosaicImage(rawImage, &dp, nullptr, false);
+    const auto* rgba = rc.demosaicImage(rawImage, &dp, nullptr, rotate_180 != 0);
     std::memcpy(out, rgba->pixels.data(), (size_t)w * h * 4);
     for (int i = 0; i < 4; i++) raw_nlf_out[i] = dp.noiseModel.rawNlf[i];
     for (int i = 0; i < 30; i++) pyramid_nlf_out[i] = dp.noiseModel.pyramidNlf[i / 6][i % 6];

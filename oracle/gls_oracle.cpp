@@ -600,11 +600,14 @@ void interpolate_green(const Pol& pol, const Img<C>& raw, int bayer, float lumaV
 }
 
 // ---------------------------------------------------------------------------------------
-// a8: interpolateRedBlue, demosaic.cl:229-318 (rotate_180 unsupported)
+// a8: interpolateRedBlue, demosaic.cl:229-318.  With rotate_180 the pixel (x, y) is written
+// at (w - x, h - y) (demosaic.cl:310-313): the writes of column 0 and row 0 fall outside the
+// image, and output column 0 and row 0 are never written -- they keep the image's initial
+// contents, zero here (the convention the CUDA path follows).
 // ---------------------------------------------------------------------------------------
 template <class C>
 void interpolate_red_blue(const Pol& pol, const Img<C>& raw, const Img<C>& gi, int bayer, float chromaVariance_,
-                          Img<C>& rgb) {
+                          Img<C>& rgb, bool rotate_180 = false) {
     rgb = Img<C>(raw.w, raw.h, 4);
     const C chromaVariance = mmaxc<C>((C)chromaVariance_, C(1e-6));
     const int rx = kBayer[bayer][raw_red][0], ry = kBayer[bayer][raw_red][1];
@@ -653,10 +656,12 @@ void interpolate_red_blue(const Pol& pol, const Img<C>& raw, const Img<C>& gi, i
                         red = c2;
                     }
                 }
-                rgb.ref(x, y, 0) = store(pol, red);
-                rgb.ref(x, y, 1) = store(pol, green);
-                rgb.ref(x, y, 2) = store(pol, blue);
-                rgb.ref(x, y, 3) = C(0);
+                const int ox = rotate_180 ? raw.w - x : x, oy = rotate_180 ? raw.h - y : y;
+                if (ox >= raw.w || oy >= raw.h) continue;  // the dropped writes of the rotation
+                rgb.ref(ox, oy, 0) = store(pol, red);
+                rgb.ref(ox, oy, 1) = store(pol, green);
+                rgb.ref(ox, oy, 2) = store(pol, blue);
+                rgb.ref(ox, oy, 3) = C(0);
             }
         }
     });
@@ -1313,7 +1318,6 @@ int demosaic(const uint16_t* raw, int w, int h, int stride, oracle_params* p, in
     const int L = p->pyramid_levels;
     if (w <= 0 || h <= 0 || (w & 1) || (h & 1) || L < 4 || L > ORACLE_MAX_LEVELS) return -1;
     if ((w >> (L - 1)) < 1 || (h >> (L - 1)) < 1) return -1;
-    if (p->rotate_180) return -2;
     const Pol pol{prec};
     const bool high_noise = p->noise_level > 0.6f;
 
@@ -1335,7 +1339,8 @@ int demosaic(const uint16_t* raw, int w, int h, int stride, oracle_params* p, in
     Img<C> green, lin, tmp;
     interpolate_green(pol, scaled, p->bayer_pattern, p->raw_nlf[1], green);
     if (taps && taps->green) to_float(green, taps->green);
-    interpolate_red_blue(pol, scaled, green, p->bayer_pattern, (p->raw_nlf[0] + p->raw_nlf[2]) / 2, lin);
+    interpolate_red_blue(pol, scaled, green, p->bayer_pattern, (p->raw_nlf[0] + p->raw_nlf[2]) / 2, lin,
+                         p->rotate_180 != 0);
     if (taps && taps->linear_rgb) to_float(lin, taps->linear_rgb);
     blend_highlights(pol, lin, C(1), tmp);
 
@@ -2288,9 +2293,11 @@ int oracle_interpolate_green(const float* s, int w, int h, int bayer, float lv, 
     return 0;
 }
 
-int oracle_interpolate_red_blue(const float* s, const float* g, int w, int h, int bayer, float cv, int prec, float* rgba) {
+int oracle_interpolate_red_blue(const float* s, const float* g, int w, int h, int bayer, float cv, int prec, int rotate_180,
+                                float* rgba) {
     Img<float> o;
-    interpolate_red_blue(Pol{prec}, from_float<float>(s, w, h, 1), from_float<float>(g, w, h, 1), bayer, cv, o);
+    interpolate_red_blue(Pol{prec}, from_float<float>(s, w, h, 1), from_float<float>(g, w, h, 1), bayer, cv, o,
+                         rotate_180 != 0);
     to_float(o, rgba);
     return 0;
 }

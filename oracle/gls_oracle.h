@@ -55,7 +55,7 @@ typedef struct {
     float noise_level;
     int pyramid_levels;     // 4..8
     int denoise_algorithm;  // 0 bilateral, 1 guided fast, 2 guided precise
-    int rotate_180;         // must be 0
+    int rotate_180;         // interpolateRedBlue writes the frame turned by 180 degrees
     float raw_nlf[4];                            // out
     float pyramid_nlf[ORACLE_MAX_LEVELS][6];     // in: [0] used by the despeckle; out: fitted
     oracle_denoise_params denoise[ORACLE_MAX_LEVELS];
@@ -94,7 +94,7 @@ int oracle_compute_raw_nlf(const float* scaled, int w, int h, int bayer, float o
 int oracle_interpolate_green(const float* scaled, int w, int h, int bayer, float luma_variance, int prec,
                              float* green);
 int oracle_interpolate_red_blue(const float* scaled, const float* green, int w, int h, int bayer,
-                                float chroma_variance, int prec, float* rgba);
+                                float chroma_variance, int prec, int rotate_180, float* rgba);
 int oracle_blend_highlights(const float* in, int w, int h, float clip, int prec, float* out);
 int oracle_transform(const float* in, int w, int h, const float m[9], int prec, float* out);
 int oracle_despeckle(const float* in, int w, int h, const float var_a[3], const float var_b[3], int prec,

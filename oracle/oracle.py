@@ -188,11 +188,12 @@ def interpolate_green(scaled, bayer, luma_variance, prec=F32):
     return out
 
 
-def interpolate_red_blue(scaled, green, bayer, chroma_variance, prec=F32):
+def interpolate_red_blue(scaled, green, bayer, chroma_variance, prec=F32, rotate_180=False):
     s, g = _f32(scaled), _f32(green)
     h, w = s.shape
     out = np.zeros((h, w, 4), np.float32)
-    lib().oracle_interpolate_red_blue(_p(s), _p(g), w, h, bayer, ctypes.c_float(chroma_variance), prec, _p(out))
+    lib().oracle_interpolate_red_blue(_p(s), _p(g), w, h, bayer, ctypes.c_float(chroma_variance), prec,
+                                      int(bool(rotate_180)), _p(out))
     return out
 
 
@@ -534,11 +535,12 @@ def clref_interpolate_green(scaled, bayer, luma_variance):
     return out
 
 
-def clref_interpolate_red_blue(scaled, green, bayer, chroma_variance):
+def clref_interpolate_red_blue(scaled, green, bayer, chroma_variance, rotate_180=False):
     s, g = _f32(scaled), _f32(green)
     h, w = s.shape
-    out = np.zeros((h, w, 4), np.float32)
-    _clref_call("clref_interpolate_red_blue", _p(s), _p(g), w, h, bayer, ctypes.c_float(chroma_variance), _p(out))
+    out = np.zeros((h, w, 4), np.float32)  # the rotation leaves row 0 and column 0 as they are: zero
+    _clref_call("clref_interpolate_red_blue", _p(s), _p(g), w, h, bayer, ctypes.c_float(chroma_variance),
+                int(bool(rotate_180)), _p(out))
     return out
 
 
@@ -736,10 +738,11 @@ def ref_pipeline_lib(prec=F32):
     return _pipelines.get(prec)
 
 
-def ref_raw_converter(raw, spec, prec=F32):
+def ref_raw_converter(raw, spec, prec=F32, rotate_180=False):
     """The reference's RawConverter::demosaicImage (5 pyramid levels, bilateral denoiser) on a
     uint16 frame with a spec dict (climage_gb300.configs.make_spec): (RGBA8, raw NLF (4,),
-    pyramid NLF (5, 6)); prec selects the image storage it was built with."""
+    pyramid NLF (5, 6)); prec selects the image storage it was built with, rotate_180 its
+    last argument (a converter made for the call: its images start at zero)."""
     raw = np.ascontiguousarray(raw, np.uint16)
     h, w = raw.shape
     p = [spec["black_level"], spec["white_level"], spec["exposure_multiplier"], spec["noise_level"]]
@@ -755,7 +758,8 @@ def ref_raw_converter(raw, spec, prec=F32):
     out = np.zeros((h, w, 4), np.uint8)
     rn, pn = np.zeros(4, np.float32), np.zeros(30, np.float32)
     rc = ref_pipeline_lib(prec).ref_raw_converter(_p(raw), w, h, int(spec["bayer_pattern"]), _p(params),
-                                              int(r["localToneMapping"]), _p(out), _p(rn), _p(pn))
+                                              int(r["localToneMapping"]), int(bool(rotate_180)), _p(out), _p(rn),
+                                              _p(pn))
     if rc != 0:
         raise ValueError("ref_raw_converter: a vector condition had components that disagree")
     return out, rn, pn.reshape(5, 6)

@@ -28,7 +28,7 @@ def oracle_params(spec):
         setattr(p.ltm, k, v)
     p.pyramid_levels = spec["pyramid_levels"]
     p.denoise_algorithm = spec["denoise_algorithm"]
-    p.rotate_180 = 0
+    p.rotate_180 = int(spec.get("rotate_180", 0))
     return p
 
 

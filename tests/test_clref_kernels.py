@@ -46,6 +46,14 @@ def test_demosaic_kernels(frame):
     same(orc.clref_interpolate_green(s, bayer, 0.001), g)
     rgb = orc.interpolate_red_blue(s, g, bayer, 0.0005)
     same(orc.clref_interpolate_red_blue(s, g, bayer, 0.0005), rgb)
+    # rotate_180 (demosaic.cl:310-313): pixel (x, y) written at (w - x, h - y); the writes of
+    # column 0 and row 0 fall outside the image, so output column 0 and row 0 keep the
+    # image's initial contents, zero on both sides
+    rot = orc.interpolate_red_blue(s, g, bayer, 0.0005, rotate_180=True)
+    same(orc.clref_interpolate_red_blue(s, g, bayer, 0.0005, rotate_180=True), rot)
+    h, w = s.shape
+    assert not rot[0].any() and not rot[:, 0].any()
+    same(rot[1:, 1:], rgb[:0:-1, :0:-1][:h - 1, :w - 1])
     same(orc.clref_fast_debayer(s, bayer), orc.fast_debayer(s, bayer))
     m, v = orc.raw_noise_statistics(s, bayer)
     cm, cv = orc.clref_raw_noise_statistics(s, bayer)

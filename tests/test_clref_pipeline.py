@@ -124,6 +124,23 @@ def test_oracle_equals_the_reference_raw_converter(bayer, noise_level, gain):
 
 
 @pytest.mark.skipif(orc.ref_pipeline_lib() is None, reason="the reference's RawConverter is not built here")
+@pytest.mark.parametrize("bayer,noise_level", [(2, 0.2), (1, 0.7)], ids=["rggb", "gbrg_high_noise"])
+def test_oracle_equals_the_reference_raw_converter_rotated(bayer, noise_level):
+    """RawConverter::demosaicImage(..., rotate_180 = true): interpolateRedBlue writes pixel
+    (x, y) at (w - x, h - y), so row 0 and column 0 of its image are never written and keep
+    the converter's initial (zero) contents; every later stage reads the turned image.  The
+    reference's own converter and the oracle agree on every RGBA8 code."""
+    raw, _, meta = synthetic.make_frame(256, 192, bayer=bayer, gain=4.0, read_sigma=6.0, seed=95 + bayer)
+    spec = configs.make_spec(meta, levels=5, noise_level=noise_level)
+    spec["rotate_180"] = 1
+    out, raw_nlf, pyr_nlf = orc.ref_raw_converter(raw, spec, rotate_180=True)
+    ref = orc.demosaic(raw, oracle_params(spec), orc.F32, want=("rgba8",))
+    np.testing.assert_array_equal(raw_nlf, ref["raw_nlf"])
+    np.testing.assert_array_equal(pyr_nlf, ref["pyramid_nlf"])
+    np.testing.assert_array_equal(out[..., :3], ref["rgba8"][..., :3])
+
+
+@pytest.mark.skipif(orc.ref_pipeline_lib() is None, reason="the reference's RawConverter is not built here")
 @pytest.mark.parametrize("width,height,bayer,noise_level,gain,sigma",
                          [(1024, 768, 2, 0.2, 2.0, 3.0), (4032, 3024, 2, 0.7, 16.0, 12.0)],
                          ids=["config1_1024x768", "bench_4032x3024_high_noise"])

@@ -134,3 +134,28 @@ def test_training_lowers_the_loss(cnn):
         cnn.train_step(torch.from_numpy(inp).cuda(), torch.from_numpy(gt).cuda(), 1e-3)
     after = cnn.train_step(vin_d, vgt_d, 0.0)[0]
     assert after < 0.7 * before, (before, after)
+
+
+def test_bounded_wait_runs_out_and_reports(cnn):
+    """A tensor-core wait that never completes: the kernels' bounded mbarrier wait, run on a
+    barrier that nothing arrives at (no MMA committed, nothing in flight), gives up after
+    its polls and flags the error; status() raises GLS_ERR_TIMEOUT once, and the network
+    then runs and reports normally (the context stays usable)."""
+    import torch
+    cnn.wait_probe(1 << 10)
+    with pytest.raises(gls.GlsError) as err:
+        cnn.status()
+    assert err.value.status == gls.GLS_ERR_TIMEOUT
+    cnn.status()  # reported once
+    rng = np.random.default_rng(13)
+    inp, _ = batch(rng, 1, 40, 56)
+    x = torch.from_numpy(inp).cuda()
+    cnn.set_params(gls.cnn_init(3))
+    first = cnn.forward(x, torch.empty_like(x)).cpu().numpy()
+    cnn.status()
+    again = cnn.forward(x, torch.empty_like(x)).cpu().numpy()
+    cnn.status()
+    np.testing.assert_array_equal(first, again)
+    with pytest.raises(gls.GlsError) as bad:
+        cnn.wait_probe(0)
+    assert bad.value.status == gls.GLS_ERR_INVALID_ARGUMENT

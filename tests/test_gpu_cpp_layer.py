@@ -37,12 +37,17 @@ def test_cpp_layer_raw_converter(cuda):
         res = subprocess.run([exe, d], capture_output=True, text=True, timeout=300)
         assert res.returncode == 0, res.stderr
         got = np.fromfile(os.path.join(d, "rgb.u8"), np.uint8).reshape(128, 192, 3)
+        got_rot = np.fromfile(os.path.join(d, "rgb_rot.u8"), np.uint8).reshape(128, 192, 3)
         nlf = np.array(open(os.path.join(d, "nlf.txt")).read().split(), np.float32)
         awb = np.array(open(os.path.join(d, "awb.txt")).read().split(), np.float32)
         patches = np.fromfile(os.path.join(d, "patches.f32"), np.float32).reshape(24, 2, 4)
     ref = orc.demosaic(raw, oracle_params(spec), orc.F32, want=("rgba8",))
     np.testing.assert_array_equal(got, ref["rgba8"][..., :3])
     np.testing.assert_allclose(nlf, ref["raw_nlf"], rtol=1e-6)
+    # demosaicImage(..., rotate_180 = true), the second call on the same converter
+    rspec = dict(spec, rotate_180=1)
+    ref_rot = orc.demosaic(raw, oracle_params(rspec), orc.F32, want=("rgba8",))
+    np.testing.assert_array_equal(got_rot, ref_rot["rgba8"][..., :3])
     # autoWhiteBalance: the gains and the highlight fraction (printed with 9 digits: exact floats)
     cy = gls.cam_ycbcr(np.array(spec["rgb_cam"], np.float32).reshape(3, 3))
     owb, ohl = orc.auto_white_balance(raw, cy, spec["scale_mul"], spec["white_level"], spec["black_level"],

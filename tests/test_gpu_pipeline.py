@@ -153,3 +153,16 @@ def test_pipeline_rejects_bad_input(ctx):
     tiny = torch.zeros((4, 4), dtype=torch.uint16, device="cuda")
     with pytest.raises(gls.GlsError):
         conv.demosaicImage(tiny, configs.to_gls_params(spec), torch.empty((4, 4, 4), dtype=torch.uint8, device="cuda"))
+
+
+@pytest.mark.parametrize("bayer,noise_level,gain", [(2, 0.2, 2.0), (1, 0.7, 16.0)], ids=["rggb", "gbrg_high_noise"])
+def test_pipeline_rotate_180(ctx, bayer, noise_level, gain):
+    """demosaicImage(..., rotate_180): interpolateRedBlue writes the frame turned by 180 degrees
+    and every later stage reads the turned image (the converter runs its single-stage
+    schedule for it); noise models, taps and output equal the oracle's, which the reference's
+    own RawConverter equals on the CPU (test_clref_pipeline.py)."""
+    raw, _, meta = synthetic.make_frame(200, 152, bayer=bayer, gain=gain, read_sigma=6.0, seed=140 + bayer)
+    spec = configs.make_spec(meta, levels=5, noise_level=noise_level)
+    spec["rotate_180"] = 1
+    check(ctx, raw, spec)
+    check(ctx, raw, spec, out_float=True)

@@ -119,6 +119,13 @@ def test_interpolate_red_blue(ctx, frame, half):
     torch.cuda.synchronize()
     ref = orc.interpolate_red_blue(s, g, frame["bayer"], 3.3e-4, orc.F16 if half else orc.F32)
     assert mismatch(host(out), ref) == 0
+    # rotate_180 (demosaic.cl:310-313): the output turned by 180 degrees, row 0 and column 0 zero
+    rot = empty((h, w, 4), half)
+    rot.fill_(7.0)
+    ctx.interpolateRedBlue(dev(s, half), dev(g, half), rot, frame["bayer"], 3.3e-4, rotate_180=True)
+    torch.cuda.synchronize()
+    ref_rot = orc.interpolate_red_blue(s, g, frame["bayer"], 3.3e-4, orc.F16 if half else orc.F32, rotate_180=True)
+    assert mismatch(host(rot), ref_rot) == 0
 
 
 @pytest.mark.parametrize("half", [False, True], ids=["f32", "f16"])
@@ -379,7 +386,7 @@ def test_invalid_arguments(ctx):
     with pytest.raises(gls.GlsError):
         ctx.scaleRawData(raw, empty((8, 8)), 7, [1, 1, 1, 1], 0.0)
     with pytest.raises(gls.GlsError):
-        ctx.interpolateRedBlue(empty((8, 8)), empty((8, 8)), empty((8, 8, 4)), 2, 1e-4, rotate_180=True)
+        ctx.interpolateRedBlue(empty((8, 8)), empty((8, 8)), empty((8, 6, 4)), 2, 1e-4, rotate_180=True)
     with pytest.raises(gls.GlsError):
         ctx.unpackRawBits(torch.zeros(3, dtype=torch.uint8, device="cuda"), 11, torch.zeros(2, dtype=torch.uint16,
                                                                                             device="cuda"))
