@@ -22,38 +22,35 @@ namespace gls {
 
 __device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
 
-__device__ __forceinline__ unsigned long long pk2(float2 a) {
-    return (unsigned long long)__float_as_uint(a.x) | ((unsigned long long)__float_as_uint(a.y) << 32);
-}
-__device__ __forceinline__ float2 up2(unsigned long long d) {
-    return make_float2(__uint_as_float((unsigned)d), __uint_as_float((unsigned)(d >> 32)));
-}
-
-__device__ __forceinline__ float2 add2(float2 a, float2 b) {
-    unsigned long long d;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk2(a)), "l"(pk2(b)));
-    return up2(d);
-}
-__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
-    unsigned long long d;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk2(a)), "l"(pk2(b)));
-    return up2(d);
-}
+// Each operation packs its float operands into 64-bit register pairs inside the PTX
+// (mov.b64 {lo, hi}), which the assembler allocates as adjacent registers at no cost.
+#define GLS_F32X2_BIN(NAME, OP)                                                                           \
+    __device__ __forceinline__ float2 NAME(float2 a, float2 b) {                                          \
+        float2 d;                                                                                         \
+        asm("{\n.reg .b64 ra, rb, rd;\nmov.b64 ra, {%2, %3};\nmov.b64 rb, {%4, %5};\n" OP " rd, ra, rb;\n" \
+            "mov.b64 {%0, %1}, rd;\n}\n"                                                                   \
+            : "=f"(d.x), "=f"(d.y)                                                                        \
+            : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));                                                    \
+        return d;                                                                                         \
+    }
+GLS_F32X2_BIN(add2, "add.rn.f32x2")
+GLS_F32X2_BIN(sub2, "sub.rn.f32x2")
 // a * b per lane; never add or subtract the result (see above)
-__device__ __forceinline__ float2 mul2(float2 a, float2 b) {
-    unsigned long long d;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk2(a)), "l"(pk2(b)));
-    return up2(d);
-}
+GLS_F32X2_BIN(mul2, "mul.rn.f32x2")
+#undef GLS_F32X2_BIN
+
 // a * b per lane as two scalar multiplies: safe to add or subtract afterwards
 __device__ __forceinline__ float2 mul2s(float2 a, float2 b) {
     return make_float2(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y));
 }
 // a * b + c per lane, one rounding
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
-    unsigned long long d;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(pk2(a)), "l"(pk2(b)), "l"(pk2(c)));
-    return up2(d);
+    float2 d;
+    asm("{\n.reg .b64 ra, rb, rc, rd;\nmov.b64 ra, {%2, %3};\nmov.b64 rb, {%4, %5};\nmov.b64 rc, {%6, %7};\n"
+        "fma.rn.f32x2 rd, ra, rb, rc;\nmov.b64 {%0, %1}, rd;\n}\n"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+    return d;
 }
 
 // Two float-float accumulators side by side: ff_add / ff_add_prod (gls_device.cuh) per lane.

@@ -116,18 +116,33 @@ struct SobelVal {
     float gx, gy, len;  // |sobel| components and their length
 };
 
-template <class Acc>
+// FINITE: the samples are finite (the fused pipeline's scaled raw tile), so each zero tap
+// of the kernels adds a zero to the sum and the taps of weight +-1 and +-2 add +-s and +-2s
+// exactly; the sums are evaluated with those taps only, in the kernels' order.  This can
+// change only the sign of a zero sum (and so of a zero |gradient| component), which no
+// value of interpolateGreen depends on: the gradient components are non-negative, a zero
+// luma direction is taken where the gradient vanishes and there the direction is mixed
+// away (lgt = 0).
+template <bool FINITE = false, class Acc>
 GLS_DI SobelVal sobel_abs(const Acc& im, int x, int y) {
-    const float kx[3][3] = {{1.0f, 0.0f, -1.0f}, {2.0f, 0.0f, -2.0f}, {1.0f, 0.0f, -1.0f}};
-    const float ky[3][3] = {{1.0f, 2.0f, 1.0f}, {0.0f, 0.0f, 0.0f}, {-1.0f, -2.0f, -1.0f}};
     float vx = 0.0f, vy = 0.0f;
+    if (FINITE) {
+        const float a = im.at(x - 1, y - 1), b = im.at(x, y - 1), c = im.at(x + 1, y - 1);
+        const float d = im.at(x - 1, y), f = im.at(x + 1, y);
+        const float g = im.at(x - 1, y + 1), h = im.at(x, y + 1), k = im.at(x + 1, y + 1);
+        vx = ((((a - c) + 2.0f * d) - 2.0f * f) + g) - k;
+        vy = ((((a + 2.0f * b) + c) - g) - 2.0f * h) - k;
+    } else {
+        const float kx[3][3] = {{1.0f, 0.0f, -1.0f}, {2.0f, 0.0f, -2.0f}, {1.0f, 0.0f, -1.0f}};
+        const float ky[3][3] = {{1.0f, 2.0f, 1.0f}, {0.0f, 0.0f, 0.0f}, {-1.0f, -2.0f, -1.0f}};
 #pragma unroll
-    for (int j = -1; j <= 1; j++) {
+        for (int j = -1; j <= 1; j++) {
 #pragma unroll
-        for (int i = -1; i <= 1; i++) {
-            const float s = im.at(x + i, y + j);
-            vx = vx + kx[j + 1][i + 1] * s;
-            vy = vy + ky[j + 1][i + 1] * s;
+            for (int i = -1; i <= 1; i++) {
+                const float s = im.at(x + i, y + j);
+                vx = vx + kx[j + 1][i + 1] * s;
+                vy = vy + ky[j + 1][i + 1] * s;
+            }
         }
     }
     FastDiv r;
@@ -355,8 +370,20 @@ GLS_DI void cswap(float& a, float& b) {
     b = mmax(t, b);
 }
 
-// HALF_EXACT: the accessor returns binary16 values already (a half4 tile), so the
-// rounding of every read to binary16 is the identity and is skipped.
+// the compare-exchange of the median network on (Cb, Cr) pairs: the hardware's half2
+// minimum and maximum.  For finite values it agrees with cswap's selects as values; on a
+// (-0, +0) tie it may keep the other zero, which no later value depends on (the chroma feeds
+// differences, squares, sums and products; the parity tests compare values).
+GLS_DI void cswap2(__half2& a, __half2& b) {
+    const __half2 lo = __hmin2(a, b), hi = __hmax2(a, b);
+    a = lo;
+    b = hi;
+}
+
+// HALF_EXACT: the accessor returns binary16 values already (a half4 tile of the fused
+// pipeline, finite by construction), so the rounding of every read to binary16 is the
+// identity and is skipped, and the chroma median runs on half2 pairs (cswap2).  Otherwise
+// (the single-stage entry point, any input) the reference's selects are evaluated as written.
 template <bool HALF_EXACT = false, class Acc4>
 GLS_DI float4 despeckle_px(const Acc4& im, int px, int py, float va0, float vb0) {
     using glsm::round_half;
@@ -364,11 +391,16 @@ GLS_DI float4 despeckle_px(const Acc4& im, int px, int py, float va0, float vb0)
     const float hinf = glsm::inf_();  // (half)(float)0xffff overflows to +inf
     float firstMin = hinf, secMin = hinf;
     float acb[6], acr[6];
-    auto rd = [&](int dx, int dy, float& cb, float& cr) {
+    __half2 ac[6];  // HALF_EXACT: (acb, acr) pairs
+    auto rd = [&](int dx, int dy, int k) {
         const float4 p = im.at(px + dx, py + dy);
         const float v = HALF_EXACT ? p.x : round_half(p.x);
-        cb = HALF_EXACT ? p.y : round_half(p.y);
-        cr = HALF_EXACT ? p.z : round_half(p.z);
+        if (HALF_EXACT) {
+            ac[k] = __floats2half2_rn(p.y, p.z);
+        } else {
+            acb[k] = round_half(p.y);
+            acr[k] = round_half(p.z);
+        }
         secMax = (v <= firstMax && v > secMax) ? v : secMax;
         secMax = v > firstMax ? firstMax : secMax;
         firstMax = v > firstMax ? v : firstMax;
@@ -377,31 +409,33 @@ GLS_DI float4 despeckle_px(const Acc4& im, int px, int py, float va0, float vb0)
         firstMin = v < firstMin ? v : firstMin;
         if (dx == 0 && dy == 0) sample = v;
     };
-    rd(0, -1, acb[0], acr[0]);
-    rd(1, -1, acb[1], acr[1]);
-    rd(0, 0, acb[2], acr[2]);
-    rd(1, 0, acb[3], acr[3]);
-    rd(0, 1, acb[4], acr[4]);
-    rd(1, 1, acb[5], acr[5]);
+    auto cs = [&](int a, int b) {
+        if (HALF_EXACT) {
+            cswap2(ac[a], ac[b]);
+        } else {
+            cswap(acb[a], acb[b]);
+            cswap(acr[a], acr[b]);
+        }
+    };
+    rd(0, -1, 0);
+    rd(1, -1, 1);
+    rd(0, 0, 2);
+    rd(1, 0, 3);
+    rd(0, 1, 4);
+    rd(1, 1, 5);
     // minMax6
-    cswap(acb[0], acb[1]); cswap(acb[2], acb[3]); cswap(acb[4], acb[5]);
-    cswap(acb[0], acb[2]); cswap(acb[1], acb[3]); cswap(acb[0], acb[4]); cswap(acb[3], acb[5]);
-    cswap(acr[0], acr[1]); cswap(acr[2], acr[3]); cswap(acr[4], acr[5]);
-    cswap(acr[0], acr[2]); cswap(acr[1], acr[3]); cswap(acr[0], acr[4]); cswap(acr[3], acr[5]);
-    rd(-1, 1, acb[0], acr[0]);
+    cs(0, 1); cs(2, 3); cs(4, 5);
+    cs(0, 2); cs(1, 3); cs(0, 4); cs(3, 5);
+    rd(-1, 1, 0);
     // minMax5
-    cswap(acb[0], acb[1]); cswap(acb[2], acb[3]); cswap(acb[0], acb[2]);
-    cswap(acb[1], acb[3]); cswap(acb[0], acb[4]); cswap(acb[3], acb[4]);
-    cswap(acr[0], acr[1]); cswap(acr[2], acr[3]); cswap(acr[0], acr[2]);
-    cswap(acr[1], acr[3]); cswap(acr[0], acr[4]); cswap(acr[3], acr[4]);
-    rd(-1, 0, acb[0], acr[0]);
+    cs(0, 1); cs(2, 3); cs(0, 2);
+    cs(1, 3); cs(0, 4); cs(3, 4);
+    rd(-1, 0, 0);
     // minMax4
-    cswap(acb[0], acb[1]); cswap(acb[2], acb[3]); cswap(acb[0], acb[2]); cswap(acb[1], acb[3]);
-    cswap(acr[0], acr[1]); cswap(acr[2], acr[3]); cswap(acr[0], acr[2]); cswap(acr[1], acr[3]);
-    rd(-1, -1, acb[0], acr[0]);
+    cs(0, 1); cs(2, 3); cs(0, 2); cs(1, 3);
+    rd(-1, -1, 0);
     // minMax3
-    cswap(acb[0], acb[1]); cswap(acb[0], acb[2]); cswap(acb[1], acb[2]);
-    cswap(acr[0], acr[1]); cswap(acr[0], acr[2]); cswap(acr[1], acr[2]);
+    cs(0, 1); cs(0, 2); cs(1, 2);
 
     const float sigma = round_half(sqrt_(va0 + vb0 * sample));
     const float four_sigma = round_half(4.0f * sigma);
@@ -413,6 +447,7 @@ GLS_DI float4 despeckle_px(const Acc4& im, int px, int py, float va0, float vb0)
     const float minVal = hmix(secMin, firstMin, hsmooth(sigma, four_sigma, round_half(secMin - firstMin)));
     const float maxVal = hmix(secMax, firstMax, hsmooth(sigma, four_sigma, round_half(firstMax - secMax)));
     sample = clamp_(sample, minVal, maxVal);
+    if (HALF_EXACT) return make_float4(sample, __low2float(ac[1]), __high2float(ac[1]), 0.0f);
     return make_float4(sample, acb[1], acr[1], 0.0f);
 }
 
@@ -481,15 +516,31 @@ struct unit_w<A, decltype((void)A::kUnitW)> {
     static constexpr bool value = A::kUnitW;
 };
 
+// 1 / v to within one unit in the last place (the hardware reciprocal approximation): the
+// bilateral's decision proxy needs 1 / sigma^2 to a few 2^-23 only.
+GLS_DI float rcp_approx(float v) {
+    float r;
+    asm("rcp.approx.f32 %0, %1;" : "=f"(r) : "f"(v));
+    return r;
+}
+
+template <class Acc4>
+__device__ __noinline__ float4 bilateral_literal_v(const Acc4& im, int px, int py, float v0, float v1, float v2,
+                                                   float e0, float e1) {
+    return bilateral_literal(im, px, py, sqrt_(v0), sqrt_(v1), sqrt_(v2), e0, e1);
+}
+
 template <class Acc4>
 GLS_DI float4 bilateral_px(const Acc4& im, int px, int py, const Nlf6& n, float chromaBoost, float gradientBoost) {
     constexpr bool UW = unit_w<Acc4>::value;
     const float4 c = im.at(px, py);
-    const float sig0 = sqrt_(n.a[0] + n.b[0] * c.x);
-    const float sig1 = sqrt_(n.a[1] + n.b[1] * c.x);
-    const float sig2 = sqrt_(n.a[2] + n.b[2] * c.x);
+    // sigma_k = sqrt(v_k) (demosaic.cl:741-743); the fast path below needs only 1 / v_k
+    const float v0 = n.a[0] + n.b[0] * c.x;
+    const float v1 = n.a[1] + n.b[1] * c.x;
+    const float v2 = n.a[2] + n.b[2] * c.x;
     float lumaBoost = 1.0f;
     if (gradientBoost > 1.0f) {
+        const float sig0 = sqrt_(v0);
         LumaOf<Acc4> l{im};
         const float2 g = sobel_signed(l, px, py);
         lumaBoost = gradientBoost -
@@ -497,27 +548,26 @@ GLS_DI float4 bilateral_px(const Acc4& im, int px, int py, const Nlf6& n, float 
     }
     // weight = 1 - step(edge, length(diff / sigma)) = !(sqrt_rn(q) >= edge), where
     // q = RN(RN(d0^2) + RN(d1^2)) + RN(d2^2) with d_k = RN(diff_k / sigma_k).  Each tap is
-    // decided on qa = sum diff_k^2 * RN(1/sigma_k)^2 instead: all terms are non-negative, so
-    // qa and q both lie within about 12 roundings (2^-20.4 relative) of the exact value, and
-    // a tap whose qa clears the square-root band of the edge (2^-20) widened by 2^-18 has the
-    // same weight either way.  The fast path keeps edges below 2^20 and 2^-60 <= sigma <= 2^30,
-    // so an overflowing diff^2 (or product) means d^2 > 2^68 and weight 0 on both sides, and
-    // qa is never NaN for finite samples.  A tap inside the band, or a NaN qa (the literal
-    // weight of a NaN sample is 1), is counted by !(qa > hi) but not by qa < lo: when the two
-    // counts differ the pixel takes the literal evaluation.  The weights are 0 or 1, so w * s
-    // is exact and the multiply-adds can be fused without changing a bit; channel pairs go
-    // through the packed fp32x2 operations, each lane rounded exactly as the scalar one.
+    // decided on qa = sum diff_k^2 * r_k instead, r_k = 1 / v_k to one ulp (1 / sigma_k^2 to
+    // about 2^-21.4, sigma_k being the rounded square root): all terms are non-negative, so
+    // qa and q both lie within about 2^-20 of the exact sum of (diff_k / sigma_k)^2, and a tap
+    // whose qa clears the square-root band of the edge (2^-20) widened by 2^-16 has the same
+    // weight either way.  The fast path keeps edges below 2^20 and 2^-120 <= v_k <= 2^60 (the
+    // sigmas in [2^-60, 2^30]), so an overflowing diff^2 (or product) means d^2 > 2^68 and
+    // weight 0 on both sides, and qa is never NaN for finite samples.  A tap inside the band,
+    // or a NaN qa (the literal weight of a NaN sample is 1), is counted by !(qa > hi) but not
+    // by qa < lo: when the two counts differ the pixel takes the literal evaluation.  The
+    // weights are 0 or 1, so w * s is exact and the multiply-adds can be fused without
+    // changing a bit; channel pairs go through the packed fp32x2 operations, each lane
+    // rounded exactly as the scalar one.
     SqrtGe ge0, ge1;
     ge0.init(lumaBoost * GLS_SQRT2_F);
     ge1.init(chromaBoost * GLS_SQRT2_F);
-    FastDiv dv0, dv1, dv2;
-    dv0.init(sig0);
-    dv1.init(sig1);
-    dv2.init(sig2);
-    if (!(dv0.ok && dv1.ok && dv2.ok && ge0.ok && ge1.ok && ge0.e < 1048576.0f && ge1.e < 1048576.0f))
-        return bilateral_literal(im, px, py, sig0, sig1, sig2, ge0.e, ge1.e);
-    constexpr float kWiden = 3.814697265625e-06f;  // 2^-18
-    const float r0 = dv0.y * dv0.y, r1 = dv1.y * dv1.y, r2 = dv2.y * dv2.y;
+    auto v_ok = [](float v) { return v >= 7.52316384526264e-37f && v <= 1.152921504606847e18f; };  // 2^-120, 2^60
+    if (!(v_ok(v0) && v_ok(v1) && v_ok(v2) && ge0.ok && ge1.ok && ge0.e < 1048576.0f && ge1.e < 1048576.0f))
+        return bilateral_literal_v(im, px, py, v0, v1, v2, ge0.e, ge1.e);
+    constexpr float kWiden = 1.52587890625e-05f;  // 2^-16
+    const float r0 = rcp_approx(v0), r1 = rcp_approx(v1), r2 = rcp_approx(v2);
     const float lo0 = ge0.lo * (1.0f - kWiden), hi0 = ge0.hi * (1.0f + kWiden);
     const float lo1 = ge1.lo * (1.0f - kWiden), hi1 = ge1.hi * (1.0f + kWiden);
     const float2 nc = make_float2(-c.x, -c.y);  // s - c == s + (-c), bit for bit
@@ -542,7 +592,7 @@ GLS_DI float4 bilateral_px(const Acc4& im, int px, int py, const Nlf6& n, float 
                 fzn = fma2(ww, make_float2(s.z, UW ? s.w : 1.0f), fzn);
             }
         }
-        if (nhi != fzn.y) return bilateral_literal(im, px, py, sig0, sig1, sig2, ge0.e, ge1.e);
+        if (nhi != fzn.y) return bilateral_literal_v(im, px, py, v0, v1, v2, ge0.e, ge1.e);
         return make_float4(div_(fxy.x, fzn.y), div_(fxy.y, fzn.y), div_(fzn.x, fzn.y), 0.0f);
     }
     float n0 = 0.0f, nhi0 = 0.0f, nhi1 = 0.0f;
@@ -563,7 +613,7 @@ GLS_DI float4 bilateral_px(const Acc4& im, int px, int py, const Nlf6& n, float 
             fzn = fma2(make_float2(w1, w1), make_float2(s.z, UW ? s.w : 1.0f), fzn);
         }
     }
-    if (nhi0 != n0 || nhi1 != fzn.y) return bilateral_literal(im, px, py, sig0, sig1, sig2, ge0.e, ge1.e);
+    if (nhi0 != n0 || nhi1 != fzn.y) return bilateral_literal_v(im, px, py, v0, v1, v2, ge0.e, ge1.e);
     return make_float4(div_(fxy.x, n0), div_(fxy.y, fzn.y), div_(fzn.x, fzn.y), 0.0f);
 }
 
@@ -707,7 +757,14 @@ GLS_DI float ltm_mask_from(const float (&gs)[9], float4 inp, const LtmParams& lp
     const float illuminance = div_(filtered, knorm);
     const float reflectance = div_(luma, illuminance);
     const float3 rgb = transform_px(m, make_float3(inp.x, inp.y, inp.z));
-    const float hc = mmin(length3_(sqrt_(2.0f * rgb.x), sqrt_(2.0f * rgb.y), sqrt_(2.0f * rgb.z)), 1.0f);
+    // hc = min(length(sqrt(2r), sqrt(2g), sqrt(2b)), 1), which is 1 without the square roots
+    // when a channel is negative or NaN (the length is NaN, and min(NaN, 1) selects 1) or
+    // when 2 (r + g + b) >= 1 + 2^-18 (each rounded sqrt(2c)^2 is within 2^-22 of 2c, so the
+    // rounded length is at least 1)
+    float hc = 1.0f;
+    if (rgb.x >= 0.0f && rgb.y >= 0.0f && rgb.z >= 0.0f &&
+        2.0f * ((rgb.x + rgb.y) + rgb.z) < 1.000003814697265625f)
+        hc = mmin(length3_(sqrt_(2.0f * rgb.x), sqrt_(2.0f * rgb.y), sqrt_(2.0f * rgb.z)), 1.0f);
     const float tc = mix_(lp.shadows, lp.highlights, hc);
     return div_(glsm::pow_(illuminance, div_(1.0f, tc)) * glsm::pow_(reflectance, lp.detail), luma);
 }

@@ -219,7 +219,7 @@ __global__ void __launch_bounds__(kT, 5) demosaic_kernel(DemosaicArgs a) {  // 5
     // 2. Sobel map (|gx|, |gy|, length) at every position a bilateralSobel may visit
     for (int i = tid; i < SH * SW; i += kT) {
         const int r = i / SW, c = i - r * SW;
-        const SobelVal sv = sobel_abs(R, x0 - 4 + c, y0 - 4 + r);
+        const SobelVal sv = sobel_abs<true>(R, x0 - 4 + c, y0 - 4 + r);  // finite scaled raw
         s_sob[i] = make_float4(sv.gx, sv.gy, sv.len, 0.0f);
     }
     if (a.tap_scaled) {
@@ -668,7 +668,14 @@ __global__ void __launch_bounds__(kT) final_kernel(FinalArgs a) {
             float gs[9];
 #pragma unroll
             for (int k = 0; k < 9; k++) gs[k] = tab_sample1(s_g, T.gx[k % 3][c], T.gy[k / 3][r]);
-            const float4 inp = tab_sample4(s_den, T.lx[c], T.ly[r]);
+            // the input is sampled at texel centres: after the 8-bit fraction each axis sits on
+            // one texel (fraction 0 or 1), and with the bilateral's finite outputs the sample is
+            // that texel's value (the other weights are zero)
+            const TabTap tx = T.lx[c], ty = T.ly[r];
+            const bool one_x = tx.a == 0.0f || tx.oma == 0.0f, one_y = ty.a == 0.0f || ty.oma == 0.0f;
+            const float4 inp = (ALGO == 0 && one_x && one_y)
+                                   ? s_den[(ty.a == 0.0f ? ty.i0 : ty.i1) + (tx.a == 0.0f ? tx.i0 : tx.i1)]
+                                   : tab_sample4(s_den, tx, ty);
             mask = Storage<S>::round(ltm_mask_from(gs, inp, a.ltm, a.icy));
             if (a.tap_mask) a.tap_mask[(size_t)y * a.tap_pitch + x] = mask;
         }
