@@ -208,27 +208,44 @@ GLS_DI float2 bilateral_sobel(const SobF& sob, float sigma) {
     const bool zero = e0 == 0.0f && e1 == 0.0f;
     if (!(fast || zero)) return bilateral_sobel_literal(sob, e0, e1);
     const SobelVal c = sob(0, 0);
-    float sx = 0.0f, sy = 0.0f, ws = 0.0f;
+    float2 sxy = make_float2(0.0f, 0.0f);  // (sx, sy): the products are scalar, the sums packed
+    float ws = 0.0f;
+    auto acc = [&](const SobelVal& g, float w) {
+        sxy = add2(sxy, mul2s(make_float2(w, w), make_float2(g.gx, g.gy)));
+        ws = ws + w;
+    };
+    if (fast) {
+        // the weights of two taps at a time as packed lanes (t from the shared-divisor
+        // shortcut, then 1 - t * t * (3 - 2 t) with 3 - 2 t = fma(-2, t, 3): 2 t is exact),
+        // accumulated tap by tap in the reference's order (rows, then columns)
+        const float2 e0v = make_float2(e0, e0), yv = make_float2(den.y, den.y), ndv = make_float2(-den.d, -den.d);
 #pragma unroll
-    for (int j = -2; j <= 2; j++) {
+        for (int k = 0; k < 25; k += 2) {
+            const bool two = k + 1 < 25;
+            const SobelVal ga = sob(k % 5 - 2, k / 5 - 2);
+            const SobelVal gb = two ? sob((k + 1) % 5 - 2, (k + 1) / 5 - 2) : ga;
+            const float2 num = sub2(make_float2(0.05f * mabs(ga.len - c.len), 0.05f * mabs(gb.len - c.len)), e0v);
+            const float2 q0 = mul2(num, yv);
+            const float2 q = fma2(fma2(q0, ndv, num), yv, q0);
+            const float2 t = make_float2(!(num.x > 0.0f) ? 0.0f : (num.x >= den.d ? 1.0f : q.x),
+                                         !(num.y > 0.0f) ? 0.0f : (num.y >= den.d ? 1.0f : q.y));
+            const float2 w = sub2(make_float2(1.0f, 1.0f),
+                                  mul2s(mul2(t, t), fma2(t, make_float2(-2.0f, -2.0f), make_float2(3.0f, 3.0f))));
+            acc(ga, w.x);
+            if (two) acc(gb, w.y);
+        }
+    } else {
 #pragma unroll
-        for (int i = -2; i <= 2; i++) {
-            const SobelVal g = sob(i, j);
-            const float x = 0.05f * mabs(g.len - c.len);
-            float w;
-            if (fast) {
-                const float num = x - e0;
-                const float t = !(num > 0.0f) ? 0.0f : (num >= den.d ? 1.0f : den.fast(num));
-                w = 1.0f - t * t * (3.0f - 2.0f * t);
-            } else {
-                w = x > 0.0f ? 0.0f : 1.0f;
+        for (int j = -2; j <= 2; j++) {
+#pragma unroll
+            for (int i = -2; i <= 2; i++) {
+                const SobelVal g = sob(i, j);
+                const float x = 0.05f * mabs(g.len - c.len);
+                acc(g, x > 0.0f ? 0.0f : 1.0f);
             }
-            sx = sx + w * g.gx;
-            sy = sy + w * g.gy;
-            ws = ws + w;
         }
     }
-    return make_float2(div_(sx, ws), div_(sy, ws));
+    return make_float2(div_(sxy.x, ws), div_(sxy.y, ws));
 }
 
 // True when (x, y) is a red or blue site, where green has to be interpolated.

@@ -363,6 +363,9 @@ constexpr int LP = LT + 4;
 template <class SIn, class SOut>
 __global__ void __launch_bounds__(kT) level_pass1_kernel(LevelPass1Args a) {
     __shared__ float4 s_in[LP * LP];
+    // downsampleImage's taps for the tile's 16 output columns and rows: [0] at -0.5 output
+    // pixel, [1] at +0.5 (downsample_px's px -+ sx), relative to the staged tile
+    __shared__ TabTap s_tx[2][LT / 2], s_ty[2][LT / 2];
     LevelPass1Acc2 acc;
     acc.init();
     typedef typename Storage<SIn>::T4 TIn;
@@ -375,6 +378,20 @@ __global__ void __launch_bounds__(kT) level_pass1_kernel(LevelPass1Args a) {
         for (int i = threadIdx.x; i < LP * LP; i += kT) {
             const int r = i / LP, c = i - r * LP;
             s_in[i] = gin.at(x0 - 2 + c, y0 - 2 + r);
+        }
+        if (a.out && threadIdx.x < 2 * LT) {
+            // the same float operations as downsample_px's coordinates and tap1, once per
+            // column (threads 0..31) and row (32..63)
+            const int e = threadIdx.x & (LT - 1), k = e >> 4, o = e & 15;
+            if (threadIdx.x < LT) {
+                const float n = div_(1.0f, (float)a.ow);
+                const float pc = ((float)(x0 / 2 + o) + 0.5f) * n, sh = 0.5f * n;
+                s_tx[k][o] = tab_tap(tap1(k ? pc + sh : pc + -sh, a.w), a.w, x0 - 2, LP, 1);
+            } else {
+                const float n = div_(1.0f, (float)a.oh);
+                const float pc = ((float)(y0 / 2 + o) + 0.5f) * n, sh = 0.5f * n;
+                s_ty[k][o] = tab_tap(tap1(k ? pc + sh : pc + -sh, a.h), a.h, y0 - 2, LP, LP);
+            }
         }
         __syncthreads();
         // window sums for pixels (x0 + col, y0 + row0 + j), j = 0..3: (s0, s1), (q0, q1) and
@@ -413,13 +430,23 @@ __global__ void __launch_bounds__(kT) level_pass1_kernel(LevelPass1Args a) {
                 if (in_range<1, 3>(m, v, a.th)) acc.add_selected(mt.x, v01, v2);
             }
         }
-        // downsample: the coarse 16x16 tile under this fine tile
+        // downsample: the coarse 16x16 tile under this fine tile, from the staged tile through
+        // the tap tables (downsample_px's samples and their average, bit for bit)
         if (a.out) {
-            const int ox = x0 / 2 + (threadIdx.x & 15), oy = y0 / 2 + (threadIdx.x >> 4);
+            const int oc = threadIdx.x & 15, orow = threadIdx.x >> 4;
+            const int ox = x0 / 2 + oc, oy = y0 / 2 + orow;
             if (ox < a.ow && oy < a.oh) {
+                const float4 t0 = tab_sample4(s_in, s_tx[0][oc], s_ty[0][orow]);
+                const float4 t1 = tab_sample4(s_in, s_tx[1][oc], s_ty[0][orow]);
+                const float4 t2 = tab_sample4(s_in, s_tx[0][oc], s_ty[1][orow]);
+                const float4 t3 = tab_sample4(s_in, s_tx[1][oc], s_ty[1][orow]);
+                float4 d;
+                d.x = 0.25f * (t0.x + t1.x + t2.x + t3.x);
+                d.y = 0.25f * (t0.y + t1.y + t2.y + t3.y);
+                d.z = 0.25f * (t0.z + t1.z + t2.z + t3.z);
+                d.w = 0.25f * (t0.w + t1.w + t2.w + t3.w);
                 typedef typename Storage<SOut>::T4 TOut;
-                Storage<SOut>::st4((TOut*)a.out + (size_t)oy * a.opitch + ox,
-                                   downsample_px(gin, ox, oy, a.ow, a.oh, a.w, a.h));
+                Storage<SOut>::st4((TOut*)a.out + (size_t)oy * a.opitch + ox, d);
             }
         }
         __syncthreads();
