@@ -704,6 +704,39 @@ def main(argv=None):
         del graph
         if world == 1 and not args.no_cpu:
             batched_line["bit_exact_vs_oracle"] = burst_vs_oracle(burst, bouts)
+        # the same burst with the learned stage (shipped parameters): batched + learned
+        if not args.no_learned:
+            from climage_gb300 import learned
+            prm = learned.load_params()
+            if prm is not None:
+                bcnn = gls.Cnn(bctx)
+                bcnn.set_params(prm)
+                bb.set_cnn(bcnn)
+                with torch.cuda.stream(bstream):
+                    bb.demosaic(braws, bparams, bouts)
+                torch.cuda.synchronize()
+                graph = torch.cuda.CUDAGraph()
+                with torch.cuda.graph(graph, stream=bstream):
+                    bb.demosaic(braws, bparams, bouts)
+                for _ in range(args.warmup):
+                    graph.replay()
+                torch.cuda.synchronize()
+                for k in range(args.steps):
+                    with torch.cuda.stream(bstream):
+                        flush.fill_(k & 0xFF)
+                        bs[k].record(bstream)
+                        graph.replay()
+                        be[k].record(bstream)
+                torch.cuda.synchronize()
+                lms = float(sum(a.elapsed_time(b) for a, b in zip(bs, be))) / args.steps
+                bcnn.status()
+                batched_line["learned"] = {"value": round(bpx / 1e3 / lms, 3), "unit": "MPix/s",
+                                           "ms_per_burst": round(lms, 3),
+                                           "vs_plain_value": round(bpx / 1e3 / lms / value, 3),
+                                           "launch": "one CUDA graph replay per burst, learned stage on every frame"}
+                del graph
+                bb.set_cnn(None)
+                bcnn.close()
         bb.close()
         bctx.close()
         del braws, bouts, burst

@@ -23,8 +23,8 @@ import math
 
 import numpy as np
 
-# image storage precision (gls_cuda.h GLS_STORAGE_F32 / GLS_STORAGE_F16)
-STORAGE_F32, STORAGE_F16 = 0, 1
+# image storage precision (gls_cuda.h GLS_STORAGE_F32 / _F16 / _F16_STATS)
+STORAGE_F32, STORAGE_F16, STORAGE_F16_STATS = 0, 1, 2
 
 CAM_XYZ = [1.4955, -0.6760, -0.1453, -0.1341, 1.0072, 0.1269, -0.0647, 0.1987, 0.4304]
 

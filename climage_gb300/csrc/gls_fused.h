@@ -17,6 +17,7 @@ struct RawPass1Args {
     NlfScratch nlf;  // regression scratch (set by the launcher)
     float* nlf_out;  // fitted {A0..3, B0..3}
     int sums_exact;  // set by the launcher: every 5x5 sum and its square lie where x / 25 has its exact shortcut
+    int stats_half;  // the statistics rounded to binary16 before the fit (GLS_STORAGE_F16_STATS)
 };
 
 struct DemosaicArgs {
@@ -63,6 +64,7 @@ struct LevelPass1Args {
     NlfThresholds th;
     NlfScratch nlf;  // regression scratch (set by the launcher)
     float* nlf_out;  // fitted {A0..2, B0..2}
+    int stats_half;  // the statistics rounded to binary16 before the fit (GLS_STORAGE_F16_STATS)
 };
 
 struct DenoiseArgs {

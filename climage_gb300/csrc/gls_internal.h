@@ -118,12 +118,14 @@ NlfThresholds nlf_thresholds();
 // Launchers of the regression (k_nlf.cu).  Raw: statistics of 2x2 quads of a scaled raw
 // image (fp32/fp16) or computed on the fly from uint16 raw; level: statistics of an RGBA
 // image.  The fitted {A.., B..} floats are written to out_dev (8 or 6 floats).
+// half_stats: the statistics rounded to binary16 before the fit (GLS_STORAGE_F16_STATS)
 gls_status nlf_fit_raw_scaled(gls_ctx* ctx, const void* scaled, bool half, int w, int h, int pitch, int bayer,
-                              NlfScratch s, float* out_dev);
+                              NlfScratch s, float* out_dev, bool half_stats = false);
 gls_status nlf_fit_raw_u16(gls_ctx* ctx, const uint16_t* raw, int w, int h, int pitch, int bayer,
-                           const float scale_mul[4], float black, bool half_storage, NlfScratch s, float* out_dev);
+                           const float scale_mul[4], float black, bool half_storage, NlfScratch s, float* out_dev,
+                           bool half_stats = false);
 gls_status nlf_fit_level(gls_ctx* ctx, const void* img, bool half, int w, int h, int pitch, NlfScratch s,
-                         float* out_dev);
+                         float* out_dev, bool half_stats = false);
 
 }  // namespace gls
 

@@ -18,11 +18,26 @@ constexpr int kTX = 32, kTY = 8, kThreads = kTX * kTY;
 
 // ---- statistics sources: stats(x, y, m[MC], v[NC]) over a (sw x sh) grid ----
 
+// The statistics as the fit reads them: fp32, or (half_stats) rounded to binary16, as the
+// reference's fp16 build stores its statistics images.
+template <int MC, int NC>
+GLS_DI void round_stats(float* m, float* v, bool half_stats) {
+    if (!half_stats) return;
+#pragma unroll
+    for (int c = 0; c < MC; c++) m[c] = glsm::round_half(m[c]);
+#pragma unroll
+    for (int c = 0; c < NC; c++) v[c] = glsm::round_half(v[c]);
+}
+
 template <class S>
 struct RawScaledSrc {
     GImg1<S> img;
     int bayer;
-    GLS_DI void stats(int qx, int qy, float* m, float* v) const { raw_stats_quad(img, qx, qy, bayer, m, v); }
+    bool half_stats;
+    GLS_DI void stats(int qx, int qy, float* m, float* v) const {
+        raw_stats_quad(img, qx, qy, bayer, m, v);
+        round_stats<4, 4>(m, v, half_stats);
+    }
 };
 
 // Raw uint16 read with scaleRawData applied on the fly (and the storage rounding of the
@@ -43,18 +58,24 @@ struct ScaledRawAcc {
 struct RawU16Src {
     ScaledRawAcc acc;
     int bayer;
-    GLS_DI void stats(int qx, int qy, float* m, float* v) const { raw_stats_quad(acc, qx, qy, bayer, m, v); }
+    bool half_stats;
+    GLS_DI void stats(int qx, int qy, float* m, float* v) const {
+        raw_stats_quad(acc, qx, qy, bayer, m, v);
+        round_stats<4, 4>(m, v, half_stats);
+    }
 };
 
 template <class S>
 struct LevelSrc {
     GImg4<S> img;
+    bool half_stats;
     GLS_DI void stats(int x, int y, float* m, float* v) const {
         const float4 s = noise_stats_px(img, x, y);
         m[0] = s.x;
         v[0] = s.y;
         v[1] = s.z;
         v[2] = s.w;
+        round_stats<1, 3>(m, v, half_stats);
     }
 };
 

@@ -168,6 +168,13 @@ __global__ void __launch_bounds__(kT, 2) raw_pass1_kernel(RawPass1Args a) {  // 
                         v[p] = div25_x2<true>(sub2(qp[p], div25_x2<true>(mul2(sp[p], sp[p]))));
                     }
                 }
+                if (a.stats_half) {  // the statistics as the reference's fp16 build stores them
+#pragma unroll
+                    for (int p = 0; p < 2; p++) {
+                        m[p] = __half22float2(__float22half2_rn(m[p]));
+                        v[p] = __half22float2(__float22half2_rn(v[p]));
+                    }
+                }
                 const float mm[4] = {m[0].x, m[0].y, m[1].x, m[1].y}, vv[4] = {v[0].x, v[0].y, v[1].x, v[1].y};
                 if (in_range<4, 4>(mm, vv, a.th)) acc.add_selected(m, v);
             }
@@ -424,10 +431,15 @@ __global__ void __launch_bounds__(kT) level_pass1_kernel(LevelPass1Args a) {
             if (x < a.w && y < a.h) {
                 // noiseStatistics (demosaic.cl:1267-1286): mean Y = s0 / 25, var_k = (q_k - s_k^2 / 25) / 25
                 const float2 mt = div25_x2<true>(f2(s01[j].x, s2q2[j].x * s2q2[j].x));  // (mean Y, s2^2 / 25)
-                const float2 v01 = div25_x2<true>(sub2(q01[j], div25_x2<true>(mul2(s01[j], s01[j]))));
-                const float v2 = d25(s2q2[j].y - mt.y);
-                const float m[1] = {mt.x}, v[3] = {v01.x, v01.y, v2};
-                if (in_range<1, 3>(m, v, a.th)) acc.add_selected(mt.x, v01, v2);
+                float2 v01 = div25_x2<true>(sub2(q01[j], div25_x2<true>(mul2(s01[j], s01[j]))));
+                float v2 = d25(s2q2[j].y - mt.y), my = mt.x;
+                if (a.stats_half) {  // the statistics as the reference's fp16 build stores them
+                    v01 = __half22float2(__float22half2_rn(v01));
+                    v2 = glsm::round_half(v2);
+                    my = glsm::round_half(my);
+                }
+                const float m[1] = {my}, v[3] = {v01.x, v01.y, v2};
+                if (in_range<1, 3>(m, v, a.th)) acc.add_selected(my, v01, v2);
             }
         }
         // downsample: the coarse 16x16 tile under this fine tile, from the staged tile through
@@ -750,12 +762,16 @@ struct RawU16SrcS {
     float sm[4];
     float black;
     int bayer;
+    bool half_stats;
     GLS_DI float at(int x, int y) const {
         x = clampi(x, 0, raw.w - 1);
         y = clampi(y, 0, raw.h - 1);
         return Storage<S>::round(scale_value(__ldg(raw.p + (size_t)y * raw.pitch + x), sm[((y & 1) << 1) | (x & 1)], black));
     }
-    GLS_DI void stats(int qx, int qy, float* m, float* v) const { raw_stats_quad(*this, qx, qy, bayer, m, v); }
+    GLS_DI void stats(int qx, int qy, float* m, float* v) const {
+        raw_stats_quad(*this, qx, qy, bayer, m, v);
+        round_stats<4, 4>(m, v, half_stats);
+    }
 };
 
 }  // namespace
@@ -793,12 +809,14 @@ gls_status fused_raw_fit(gls_ctx* ctx, const RawPass1Args& args, bool half, NlfS
     }
     if (half) {
         GLS_RAWP1_B(__half)
-        RawU16SrcS<__half> src{{a.raw, a.w, a.h, a.pitch}, {a.sm[0], a.sm[1], a.sm[2], a.sm[3]}, a.black, a.bayer};
+        RawU16SrcS<__half> src{{a.raw, a.w, a.h, a.pitch}, {a.sm[0], a.sm[1], a.sm[2], a.sm[3]}, a.black, a.bayer,
+                                  a.stats_half != 0};
         ctx->launches++;
         nlf_finish<4, 4>(ctx, src, qw, qh, s, out_dev);
     } else {
         GLS_RAWP1_B(float)
-        RawU16SrcS<float> src{{a.raw, a.w, a.h, a.pitch}, {a.sm[0], a.sm[1], a.sm[2], a.sm[3]}, a.black, a.bayer};
+        RawU16SrcS<float> src{{a.raw, a.w, a.h, a.pitch}, {a.sm[0], a.sm[1], a.sm[2], a.sm[3]}, a.black, a.bayer,
+                                 a.stats_half != 0};
         ctx->launches++;
         nlf_finish<4, 4>(ctx, src, qw, qh, s, out_dev);
     }
@@ -842,12 +860,12 @@ gls_status fused_level_fit(gls_ctx* ctx, const LevelPass1Args& args, bool in_hal
     if (in_half) {
         if (half) level_pass1_kernel<__half, __half><<<resident_grid<level_pass1_kernel<__half, __half>>(ctx, tiles), kT, 0, ctx->stream>>>(a);
         else level_pass1_kernel<__half, float><<<resident_grid<level_pass1_kernel<__half, float>>(ctx, tiles), kT, 0, ctx->stream>>>(a);
-        LevelSrc<__half> src{{(const half4*)a.in, a.w, a.h, a.pitch}};
+        LevelSrc<__half> src{{(const half4*)a.in, a.w, a.h, a.pitch}, a.stats_half != 0};
         ctx->launches++;
         nlf_finish<1, 3>(ctx, src, a.w, a.h, s, out_dev);
     } else {
         level_pass1_kernel<float, float><<<resident_grid<level_pass1_kernel<float, float>>(ctx, tiles), kT, 0, ctx->stream>>>(a);
-        LevelSrc<float> src{{(const float4*)a.in, a.w, a.h, a.pitch}};
+        LevelSrc<float> src{{(const float4*)a.in, a.w, a.h, a.pitch}, a.stats_half != 0};
         ctx->launches++;
         nlf_finish<1, 3>(ctx, src, a.w, a.h, s, out_dev);
     }

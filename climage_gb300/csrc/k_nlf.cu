@@ -33,18 +33,20 @@ NlfThresholds nlf_thresholds() {
 }
 
 gls_status nlf_fit_raw_scaled(gls_ctx* ctx, const void* scaled, bool half, int w, int h, int pitch, int bayer,
-                              NlfScratch s, float* out_dev) {
+                              NlfScratch s, float* out_dev, bool half_stats) {
     if (half) {
-        RawScaledSrc<__half> src{{(const __half*)scaled, w, h, pitch}, bayer};
+        RawScaledSrc<__half> src{{(const __half*)scaled, w, h, pitch}, bayer, half_stats};
         return run_fit<4, 4>(ctx, src, w / 2, h / 2, s, out_dev);
     }
-    RawScaledSrc<float> src{{(const float*)scaled, w, h, pitch}, bayer};
+    RawScaledSrc<float> src{{(const float*)scaled, w, h, pitch}, bayer, half_stats};
     return run_fit<4, 4>(ctx, src, w / 2, h / 2, s, out_dev);
 }
 
 gls_status nlf_fit_raw_u16(gls_ctx* ctx, const uint16_t* raw, int w, int h, int pitch, int bayer,
-                           const float scale_mul[4], float black, bool half_storage, NlfScratch s, float* out_dev) {
+                           const float scale_mul[4], float black, bool half_storage, NlfScratch s, float* out_dev,
+                           bool half_stats) {
     RawU16Src src;
+    src.half_stats = half_stats;
     src.acc.raw = GRaw16{raw, w, h, pitch};
     for (int c = 0; c < 4; c++) src.acc.sm[bayer_dy(bayer, c) * 2 + bayer_dx(bayer, c)] = scale_mul[c];
     src.acc.black = black;
@@ -54,12 +56,12 @@ gls_status nlf_fit_raw_u16(gls_ctx* ctx, const uint16_t* raw, int w, int h, int 
 }
 
 gls_status nlf_fit_level(gls_ctx* ctx, const void* img, bool half, int w, int h, int pitch, NlfScratch s,
-                         float* out_dev) {
+                         float* out_dev, bool half_stats) {
     if (half) {
-        LevelSrc<__half> src{{(const half4*)img, w, h, pitch}};
+        LevelSrc<__half> src{{(const half4*)img, w, h, pitch}, half_stats};
         return run_fit<1, 3>(ctx, src, w, h, s, out_dev);
     }
-    LevelSrc<float> src{{(const float4*)img, w, h, pitch}};
+    LevelSrc<float> src{{(const float4*)img, w, h, pitch}, half_stats};
     return run_fit<1, 3>(ctx, src, w, h, s, out_dev);
 }
 

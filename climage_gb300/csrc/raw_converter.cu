@@ -314,6 +314,7 @@ struct gls_raw_converter {
         ra.bayer = bayer;
         memcpy(ra.sm, sm, sizeof(sm));
         ra.black = black;
+        ra.stats_half = p->storage == GLS_STORAGE_F16_STATS;
         GLS_CHECK(fused_raw_fit(ctx, ra, half, nlf_scratch_at(nlf_scratch), nlf_dev));
         mark("rawNoiseStatistics+fit");
         const float* rawB = nlf_dev + 4;
@@ -394,6 +395,7 @@ struct gls_raw_converter {
                 la.oh = pyr[i].h;
                 la.opitch = pyr[i].pitch;
             }
+            la.stats_half = p->storage == GLS_STORAGE_F16_STATS;
             GLS_CHECK(fused_level_fit(ctx, la, src.half, half, nlf_scratch_at(nlf_scratch), nlf_dev + 8 * (1 + i)));
             mark(i == 0 ? "noiseStatistics+downsample L0" : "noiseStatistics+downsample L1+");
         }
@@ -488,7 +490,7 @@ struct gls_raw_converter {
         launch_scale_raw(ctx, raw, w, h, rpitch, scaled, bayer, p->scale_mul, p->black_level / 0xffff);
         mark("scaleRawData");
         GLS_CHECK(nlf_fit_raw_scaled(ctx, scaled.ptr, half, w, h, scaled.pitch, bayer, nlf_scratch_at(nlf_scratch),
-                                     nlf_dev));
+                                     nlf_dev, p->storage == GLS_STORAGE_F16_STATS));
         mark("rawNoiseStatistics+fit");
         const float* rawB = nlf_dev + 4;
         if (high_noise) {
@@ -522,7 +524,7 @@ struct gls_raw_converter {
             if (i < Lv - 1) launch_downsample(ctx, src, pyr[i]);
             mark("downsampleImage");
             GLS_CHECK(nlf_fit_level(ctx, src.ptr, half, src.w, src.h, src.pitch, nlf_scratch_at(nlf_scratch),
-                                    nlf_dev + 8 * (1 + i)));
+                                    nlf_dev + 8 * (1 + i), p->storage == GLS_STORAGE_F16_STATS));
             mark(i == 0 ? "noiseStatistics+fit L0" : "noiseStatistics+fit L1+");
         }
         const int algo = p->denoise_algorithm;
@@ -619,7 +621,7 @@ struct gls_raw_converter {
 
     // the staged raw frame through the pipeline, RGBA8 (or RGB8) back to the host
     gls_status finish_host(int fw, int fh, gls_demosaic_params* p, uint8_t* out, int out_channels) {
-        GLS_CHECK(ensure(fw, fh, p->pyramid_levels, p->storage == GLS_STORAGE_F16));
+        GLS_CHECK(ensure(fw, fh, p->pyramid_levels, p->storage != GLS_STORAGE_F32));
         GLS_CHECK(run(raw_dev, fw, p, out_dev, false, fw));
         const void* src = out_dev;
         if (out_channels == 3) {
@@ -651,7 +653,7 @@ static gls_status validate_params(gls_ctx* ctx, const gls_demosaic_params* p, in
         return set_error(ctx, GLS_ERR_INVALID_ARGUMENT, "unknown bayer pattern %d", p->bayer_pattern);
     if (p->pyramid_levels < 4 || p->pyramid_levels > GLS_MAX_LEVELS)
         return set_error(ctx, GLS_ERR_INVALID_ARGUMENT, "pyramid_levels must be in [4, %d]", GLS_MAX_LEVELS);
-    if (p->storage != GLS_STORAGE_F32 && p->storage != GLS_STORAGE_F16)
+    if (p->storage != GLS_STORAGE_F32 && p->storage != GLS_STORAGE_F16 && p->storage != GLS_STORAGE_F16_STATS)
         return set_error(ctx, GLS_ERR_INVALID_ARGUMENT, "unknown storage %d", p->storage);
     if (p->denoise_algorithm < 0 || p->denoise_algorithm > 2)
         return set_error(ctx, GLS_ERR_INVALID_ARGUMENT, "unknown denoise algorithm %d", p->denoise_algorithm);
@@ -719,7 +721,7 @@ gls_status gls_raw_converter_cnn_input(gls_raw_converter* c, const gls_image_des
     if (out->width != raw->width || out->height != raw->height || out->stride_bytes != out->width * 16)
         return set_error(ctx, GLS_ERR_INVALID_SIZE, "learned stage input: dense RGBA_F32 of the raw frame's size");
     GLS_CHECK(validate_params(ctx, params, raw->width, raw->height));
-    GLS_CHECK(c->ensure(raw->width, raw->height, params->pyramid_levels, params->storage == GLS_STORAGE_F16));
+    GLS_CHECK(c->ensure(raw->width, raw->height, params->pyramid_levels, params->storage != GLS_STORAGE_F32));
     gls_demosaic_params p = *params;
     return c->run_fused((const uint16_t*)raw->ptr, pitch_elems(raw), &p, nullptr, false, 0, (float*)out->ptr);
 }
@@ -782,7 +784,7 @@ gls_status gls_raw_converter_demosaic(gls_raw_converter* c, const gls_image_desc
     if (out->width != raw->width || out->height != raw->height)
         return set_error(ctx, GLS_ERR_INVALID_SIZE, "output size differs from the raw frame");
     GLS_CHECK(validate_params(ctx, p, raw->width, raw->height));
-    GLS_CHECK(c->ensure(raw->width, raw->height, p->pyramid_levels, p->storage == GLS_STORAGE_F16));
+    GLS_CHECK(c->ensure(raw->width, raw->height, p->pyramid_levels, p->storage != GLS_STORAGE_F32));
     GLS_CHECK(c->run((const uint16_t*)raw->ptr, pitch_elems(raw), p, out->ptr, out->format == GLS_RGBA_F32,
                      pitch_elems(out)));
     if (!defer) GLS_CHECK(c->fetch_noise_model(p));
@@ -841,7 +843,7 @@ gls_status gls_raw_converter_fast_demosaic(gls_raw_converter* c, const gls_image
     if (out->width != raw->width / 2 || out->height != raw->height / 2)
         return set_error(ctx, GLS_ERR_INVALID_SIZE, "fastDemosaicImage output must be half size");
     if (p->bayer_pattern < 0 || p->bayer_pattern > 3) return set_error(ctx, GLS_ERR_INVALID_ARGUMENT, "bayer pattern");
-    const bool half = p->storage == GLS_STORAGE_F16;
+    const bool half = p->storage != GLS_STORAGE_F32;
     GLS_CHECK(c->ensure(raw->width, raw->height, c->L ? c->L : 4, half));
     GLS_CHECK(c->ensure_staged());
     const int w = raw->width, h = raw->height;
@@ -1000,11 +1002,11 @@ gls_status gls_raw_batch_create(gls_ctx* ctx, int lanes, gls_raw_batch** out) {
 gls_status gls_raw_batch_reserve(gls_raw_batch* b, int width, int height, int levels, int storage) {
     if (!b) return GLS_ERR_INVALID_ARGUMENT;
     if (width <= 0 || height <= 0 || (width & 1) || (height & 1) || levels < 4 || levels > GLS_MAX_LEVELS ||
-        (storage != GLS_STORAGE_F32 && storage != GLS_STORAGE_F16))
+        (storage != GLS_STORAGE_F32 && storage != GLS_STORAGE_F16 && storage != GLS_STORAGE_F16_STATS))
         return set_error(b->ctx, GLS_ERR_INVALID_ARGUMENT, "reserve: bad frame size, levels or storage");
     for (size_t l = 0; l < b->lane.size(); l++) {
         gls_raw_converter* c = b->lane[l];
-        gls_status s = c->ensure(width, height, levels, storage == GLS_STORAGE_F16);
+        gls_status s = c->ensure(width, height, levels, storage != GLS_STORAGE_F32);
         if (s == GLS_OK) s = c->ensure_high_noise();
         if (s == GLS_OK) s = c->ensure_staging(width, height);
         if (s != GLS_OK) return batch_error(b, (int)l, s);
@@ -1039,7 +1041,7 @@ gls_status gls_raw_batch_demosaic(gls_raw_batch* b, int n, const gls_image_desc*
         const int l = b->lane_of[i];
         gls_raw_converter* c = b->lane[l];
         gls_demosaic_params p = params[i];
-        gls_status s = c->ensure(ws[i], hs[i], p.pyramid_levels, p.storage == GLS_STORAGE_F16);
+        gls_status s = c->ensure(ws[i], hs[i], p.pyramid_levels, p.storage != GLS_STORAGE_F32);
         if (s == GLS_OK)
             s = c->run((const uint16_t*)raws[i].ptr, pitch_elems(&raws[i]), &p, outs[i].ptr,
                        outs[i].format == GLS_RGBA_F32, pitch_elems(&outs[i]));

@@ -33,7 +33,7 @@ STATUS = {0: "ok", 1: "invalid argument", 2: "invalid size", 3: "unsupported", 4
 R16_UNORM, R_F32, R_F16, RGBA_F32, RGBA_F16, RGBA8_UNORM, RGB8_UNORM = range(7)
 GRBG, GBRG, RGGB, BGGR = range(4)
 BILATERAL, GUIDED_FAST, GUIDED_PRECISE = range(3)
-STORAGE_F32, STORAGE_F16 = 0, 1
+STORAGE_F32, STORAGE_F16, STORAGE_F16_STATS = 0, 1, 2
 MAX_LEVELS = 8
 
 

@@ -79,7 +79,11 @@ typedef struct {
 #define GLS_MAX_LEVELS 8
 
 typedef enum { GLS_DENOISE_BILATERAL = 0, GLS_DENOISE_GUIDED_FAST = 1, GLS_DENOISE_GUIDED_PRECISE = 2 } gls_denoise_algorithm;
-typedef enum { GLS_STORAGE_F32 = 0, GLS_STORAGE_F16 = 1 } gls_storage;
+/* Storage of the intermediate images: fp32; fp16 (USE_FP16_FLOATS, gls_image.hpp:32, 189-205)
+ * with the noise models fitted on fp32 statistics; or fp16 with the noise statistics in fp16
+ * as well, exactly as the reference ships (its meanImage/varImage and noise-statistics images
+ * are rgba_pixel_float too, pyramidal_denoise.cpp:162, 260-261). */
+typedef enum { GLS_STORAGE_F32 = 0, GLS_STORAGE_F16 = 1, GLS_STORAGE_F16_STATS = 2 } gls_storage;
 
 /* DemosaicParameters (demosaic.hpp:61-81), generalised from 5 to pyramid_levels levels.
  * raw_nlf and pyramid_nlf are in/out exactly as NoiseModel is in the reference:

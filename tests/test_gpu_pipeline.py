@@ -47,7 +47,7 @@ def run_gpu(ctx, raw, spec, out_float=False, taps=True, mode=0):
 
 
 def check(ctx, raw, spec, out_float=False, mode=0):
-    prec = orc.F16 if spec["storage"] == gls.STORAGE_F16 else orc.F32
+    prec = {gls.STORAGE_F16: orc.F16, gls.STORAGE_F16_STATS: orc.F16_STATS}.get(spec["storage"], orc.F32)
     ref = orc.demosaic(raw, oracle_params(spec), prec, want=("rgbaf" if out_float else "rgba8",),
                        taps=tuple(TAPS.values()))
     got = run_gpu(ctx, raw, spec, out_float, mode=mode)
@@ -83,6 +83,16 @@ def test_pipeline_config1_float_output(ctx, mode):
 def test_pipeline_fp16_storage(ctx, mode):
     raw, _, meta = synthetic.make_frame(320, 240, bayer=0, bits=14, seed=3)
     check(ctx, raw, configs.make_spec(meta, levels=6, storage=gls.STORAGE_F16), mode=mode)
+
+
+@pytest.mark.parametrize("bayer,noise_level,gain", [(0, 0.2, 2.0), (3, 0.7, 16.0)], ids=["grbg", "bggr_high_noise"])
+def test_pipeline_fp16_statistics(ctx, mode, bayer, noise_level, gain):
+    """GLS_STORAGE_F16_STATS: fp16 images and the noise statistics rounded to fp16 before the
+    fits, as the reference ships -- equal to the oracle's F16_STATS mode, which the reference's
+    own RawConverter built with fp16 storage equals on the CPU (test_clref_pipeline.py)."""
+    raw, _, meta = synthetic.make_frame(256, 192, bayer=bayer, gain=gain, read_sigma=6.0, seed=150 + bayer)
+    check(ctx, raw, configs.make_spec(meta, levels=5, storage=gls.STORAGE_F16_STATS, noise_level=noise_level),
+          mode=mode)
 
 
 def test_pipeline_high_noise_branch(ctx, mode):
