@@ -69,42 +69,43 @@ struct NlfFit {
     int pad;
 };
 
-// Scratch layout for one regression: fit state, the block ticket, and per-block partial
-// sums (pass 1 and 3: 128-bit fixed point + NaN masks; pass 2: doubles; pass 1: min/max).
-// The ticket must be zero before a pass starts; the last block of every pass resets it.
+// Scratch layout for one regression.  The header holds the fit state, the block ticket and
+// the running totals of passes 1 and 3, which every block adds its own sums to with integer
+// atomics (exact, so in any order): per column three 64-bit limbs of the 128-bit fixed-point
+// total, the pass-1 extremes as order-preserving words (atomic maximum; zero is the identity)
+// and the NaN mask.  Pass 2 keeps per-block FP64 rows.  The header must be zero before a
+// pass starts; the last block of every pass leaves it at zero (the fit state aside).
 constexpr int kNlfMaxBlocks = 1024;
 constexpr int kNlfK = 1 + 5 * 4;   // N + 5 sums x 4 channels
 constexpr int kNlfKF = 4 * 4;      // min/max of m and v per channel
-constexpr size_t kNlfHeaderBytes = 256;
-constexpr size_t kNlfPartIBytes = 16 * (size_t)kNlfMaxBlocks * kNlfK;
-constexpr size_t kNlfPartNanBytes = sizeof(unsigned) * (size_t)kNlfMaxBlocks;
+constexpr size_t kNlfTicketOff = 128;
+constexpr size_t kNlfLimbOff = 256;                                  // [kNlfK][3] u64
+constexpr size_t kNlfMmOff = kNlfLimbOff + 8 * 3 * (size_t)kNlfK;    // [kNlfKF] u32
+constexpr size_t kNlfNanOff = kNlfMmOff + 4 * (size_t)kNlfKF;        // u32
+constexpr size_t kNlfHeaderBytes = 1024;
 constexpr size_t kNlfPartDBytes = sizeof(double) * (size_t)kNlfMaxBlocks * kNlfK;
-constexpr size_t kNlfPartFBytes = sizeof(float) * (size_t)kNlfMaxBlocks * kNlfKF;
-constexpr size_t kNlfScratchBytes = kNlfHeaderBytes + kNlfPartIBytes + kNlfPartNanBytes + kNlfPartDBytes + kNlfPartFBytes;
-static_assert(sizeof(NlfFit) <= 128, "fit state and ticket share the 256-byte header");
+constexpr size_t kNlfScratchBytes = kNlfHeaderBytes + kNlfPartDBytes;
+static_assert(sizeof(NlfFit) <= kNlfTicketOff, "fit state overlaps the ticket");
+static_assert(kNlfNanOff + 4 <= kNlfHeaderBytes, "totals overflow the header");
 
 struct NlfScratch {
     NlfFit* fit;
-    unsigned* ticket;            // blocks of the current pass that have written their row
-    unsigned long long* part_i;  // [block][kNlfK] x {lo, hi}
-    unsigned* part_nan;          // [block]: bit k set when column k summed a NaN
-    double* part_d;              // [block][kNlfK]
-    float* part_f;               // [block][kNlfKF]
+    unsigned* ticket;              // blocks of the current pass that have added their sums
+    unsigned long long* tot_limb;  // [kNlfK][3]: bits 0-39, 40-79, and 80-127 (signed) of each block's sum
+    unsigned* tot_mm;              // a fit of NC channels: [0, 2 NC) ~ord(minimum), [2 NC, 4 NC) ord(maximum)
+    unsigned* tot_nan;             // bit k set when column k summed a NaN
+    double* part_d;                // [block][kNlfK], pass 2
 };
 
 inline NlfScratch nlf_scratch_at(void* base) {
     char* p = reinterpret_cast<char*>(base);
     NlfScratch s;
     s.fit = reinterpret_cast<NlfFit*>(p);
-    s.ticket = reinterpret_cast<unsigned*>(p + 128);
-    p += kNlfHeaderBytes;
-    s.part_i = reinterpret_cast<unsigned long long*>(p);
-    p += kNlfPartIBytes;
-    s.part_nan = reinterpret_cast<unsigned*>(p);
-    p += kNlfPartNanBytes;
-    s.part_d = reinterpret_cast<double*>(p);
-    p += kNlfPartDBytes;
-    s.part_f = reinterpret_cast<float*>(p);
+    s.ticket = reinterpret_cast<unsigned*>(p + kNlfTicketOff);
+    s.tot_limb = reinterpret_cast<unsigned long long*>(p + kNlfLimbOff);
+    s.tot_mm = reinterpret_cast<unsigned*>(p + kNlfMmOff);
+    s.tot_nan = reinterpret_cast<unsigned*>(p + kNlfNanOff);
+    s.part_d = reinterpret_cast<double*>(p + kNlfHeaderBytes);
     return s;
 }
 

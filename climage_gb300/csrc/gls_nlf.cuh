@@ -111,8 +111,17 @@ GLS_DI void block_reduce_write(double (&vals)[K], double* out) {
     __syncthreads();
 }
 
+// A float as an unsigned word with the same order (-0 below +0; NaN is never stored).
+GLS_DI unsigned ord_f32(float x) {
+    const unsigned b = __float_as_uint(x);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+GLS_DI float unord_f32(unsigned u) { return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u); }
+
+// The block's minima and maxima folded into the running extremes: tot[k] holds ~ord(min k)
+// and tot[K + k] ord(max k), both by atomic maximum, so zero is the identity of both.
 template <int K>
-GLS_DI void block_minmax_write(float (&mn)[K], float (&mx)[K], float* out) {
+GLS_DI void block_minmax_atomic(float (&mn)[K], float (&mx)[K], unsigned* tot) {
     __shared__ float rmn[kThreads / 32][K], rmx[kThreads / 32][K];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
@@ -130,11 +139,16 @@ GLS_DI void block_minmax_write(float (&mn)[K], float (&mx)[K], float* out) {
             a = fminf(a, rmn[w][threadIdx.x]);
             b = fmaxf(b, rmx[w][threadIdx.x]);
         }
-        out[threadIdx.x] = a;
-        out[K + threadIdx.x] = b;
+        atomicMax(tot + threadIdx.x, ~ord_f32(a));
+        atomicMax(tot + K + threadIdx.x, ord_f32(b));
     }
     __syncthreads();
 }
+
+// the running extremes back as floats (an untouched word: +inf for a minimum, -inf for a
+// maximum, as the empty reductions give)
+GLS_DI float tot_min(unsigned u) { return u ? unord_f32(~u) : glsm::inf_(); }
+GLS_DI float tot_max(unsigned u) { return u ? unord_f32(u) : -glsm::inf_(); }
 
 // ---- exact fixed-point partial sums ----
 // Each thread sums its pixels in float-float pairs.  From there on the pass-1 and pass-3
@@ -222,6 +236,26 @@ GLS_DI double fixed_to_f64(I128 a, int R) {
     return neg ? -d : d;
 }
 
+// A block's 128-bit sum added to a column's running total as three limbs: bits 0-39 and
+// 40-79 (unsigned) and bits 80-127 (signed).  With at most kNlfMaxBlocks (2^10) blocks the
+// two low limbs stay below 2^50, and the high limb's total is within one of the column total
+// / 2^80 (below 2^46 in magnitude by the column bounds), so no limb overflows and the
+// totals are exact whatever the order of the atomics.
+GLS_DI void tot_add(unsigned long long* limb, I128 v) {
+    const unsigned long long m40 = (1ull << 40) - 1ull;
+    atomicAdd(limb + 0, v.lo & m40);
+    atomicAdd(limb + 1, ((v.lo >> 40) | (v.hi << 24)) & m40);
+    atomicAdd(limb + 2, (unsigned long long)((long long)v.hi >> 16));
+}
+
+GLS_DI I128 tot_get(const unsigned long long* limb) {
+    const unsigned long long l0 = __ldcg(limb), l1 = __ldcg(limb + 1), l2 = __ldcg(limb + 2);
+    I128 t{l0, 0ull};
+    i128_add(t, I128{l1 << 40, l1 >> 24});
+    i128_add(t, I128{0ull, l2 << 16});
+    return t;
+}
+
 GLS_DI I128 warp_sum_i128(I128 v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -306,8 +340,8 @@ struct Pass1Acc {
         if (in_range<MC, NC>(m, v, th)) add_selected(m, v);
     }
 
-    // The block's fixed-point row (threads < K) and NaN mask (thread 0).
-    GLS_DI void write_fixed(unsigned long long* part_i, unsigned* part_nan) const {
+    // The block's fixed-point sums (threads < K) and NaN mask (thread 0) added to the totals.
+    GLS_DI void write_fixed(const NlfScratch& s) const {
         __shared__ I128 red[kWarps][K];
         __shared__ unsigned nanw[kWarps];
         unsigned nan = 0;
@@ -329,23 +363,21 @@ struct Pass1Acc {
         if ((threadIdx.x & 31) == 0) nanw[threadIdx.x >> 5] = nan;
         __syncthreads();
         if (threadIdx.x < K) {
-            I128 s = red[0][threadIdx.x];
+            I128 t = red[0][threadIdx.x];
 #pragma unroll
-            for (int w = 1; w < kWarps; w++) i128_add(s, red[w][threadIdx.x]);
-            unsigned long long* row = part_i + 2 * ((size_t)blockIdx.x * kNlfK + threadIdx.x);
-            row[0] = s.lo;
-            row[1] = s.hi;
+            for (int w = 1; w < kWarps; w++) i128_add(t, red[w][threadIdx.x]);
+            tot_add(s.tot_limb + 3 * threadIdx.x, t);
         }
         if (threadIdx.x == 0) {
             unsigned m = 0;
 #pragma unroll
             for (int w = 0; w < kWarps; w++) m |= nanw[w];
-            part_nan[blockIdx.x] = m;
+            if (m) atomicOr(s.tot_nan, m);
         }
         __syncthreads();
     }
 
-    GLS_DI void write_minmax(float* part_f) { block_minmax_write<2 * NC>(mn, mx, part_f + (size_t)blockIdx.x * kNlfKF); }
+    GLS_DI void write_minmax(const NlfScratch& s) { block_minmax_atomic<2 * NC>(mn, mx, s.tot_mm); }
 };
 
 // The raw fit's pass-1 accumulator with the four channels as two packed pairs (0, 1) and
@@ -566,43 +598,26 @@ __device__ void fit_totals(const double* tot, const float* fmm, int stage, NlfFi
 // column totals over the nblocks rows (warp w sums columns w, w + 8, ...), NaN masks, the
 // pass-1 extremes, then the fit.  Leaves the ticket at zero for the next pass.
 template <int NC>
-GLS_DI void solve_fixed(const NlfScratch& s, int nblocks, int stage, float* out) {
+GLS_DI void solve_fixed(const NlfScratch& s, int stage, float* out) {
     constexpr int K = 1 + 5 * NC;
     __shared__ double tot[K];
     __shared__ float fmm[4 * NC];
-    __shared__ unsigned nanw[kWarps];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int k = warp; k < K; k += kWarps) {
-        I128 acc{0ull, 0ull};
-        for (int b = lane; b < nblocks; b += 32) {
-            const unsigned long long* row = s.part_i + 2 * ((size_t)b * kNlfK + k);
-            i128_add(acc, I128{__ldcg(row), __ldcg(row + 1)});
-        }
-        acc = warp_sum_i128(acc);
-        if (lane == 0) tot[k] = fixed_to_f64(acc, fixed_scale(k));
+    __shared__ unsigned nan;
+    if (threadIdx.x < K) tot[threadIdx.x] = fixed_to_f64(tot_get(s.tot_limb + 3 * threadIdx.x), fixed_scale(threadIdx.x));
+    if (stage == 1 && threadIdx.x >= 32 && threadIdx.x < 32 + 4 * NC) {
+        const int k = threadIdx.x - 32;
+        const unsigned u = __ldcg(s.tot_mm + k);
+        fmm[k] = k < 2 * NC ? tot_min(u) : tot_max(u);
     }
-    if (stage == 1) {
-        for (int k = warp; k < 4 * NC; k += kWarps) {
-            const bool is_min = k < 2 * NC;
-            float v = is_min ? glsm::inf_() : -glsm::inf_();
-            for (int b = lane; b < nblocks; b += 32) {
-                const float x = __ldcg(s.part_f + (size_t)b * kNlfKF + k);
-                v = is_min ? fminf(v, x) : fmaxf(v, x);
-            }
-            v = is_min ? warp_min_f(v) : warp_max_f(v);
-            if (lane == 0) fmm[k] = v;
-        }
-    }
-    unsigned nan = 0;
-    for (int b = threadIdx.x; b < nblocks; b += kThreads) nan |= __ldcg(s.part_nan + b);
-    nan = __reduce_or_sync(0xffffffffu, nan);
-    if (lane == 0) nanw[warp] = nan;
+    if (threadIdx.x == 64) nan = __ldcg(s.tot_nan);
     __syncthreads();
+    // the totals are read: leave them (and the ticket) at zero for the next pass
+    if (threadIdx.x < 3 * K) s.tot_limb[threadIdx.x] = 0ull;
+    if (stage == 1 && threadIdx.x >= 96 && threadIdx.x < 96 + 4 * NC) s.tot_mm[threadIdx.x - 96] = 0u;
     if (threadIdx.x == 0) {
-        unsigned m = 0;
-        for (int w = 0; w < kWarps; w++) m |= nanw[w];
+        *s.tot_nan = 0u;
         for (int k = 0; k < K; k++)
-            if (m & (1u << k)) tot[k] = __longlong_as_double(0x7ff8000000000000ll);
+            if (nan & (1u << k)) tot[k] = __longlong_as_double(0x7ff8000000000000ll);
         fit_totals<NC>(tot, fmm, stage, s.fit, out);
         atomicExch(s.ticket, 0u);
     }
@@ -631,9 +646,9 @@ GLS_DI void solve_pass2(const NlfScratch& s, int nblocks) {
 // End of every pass-1 kernel: the block's rows, then the solve in the last block.
 template <int MC, int NC>
 GLS_DI void pass1_epilogue(Pass1Acc<MC, NC>& acc, const NlfScratch& s, float* out) {
-    acc.write_fixed(s.part_i, s.part_nan);
-    acc.write_minmax(s.part_f);
-    if (last_block(s.ticket)) solve_fixed<NC>(s, gridDim.x, 1, out);
+    acc.write_fixed(s);
+    acc.write_minmax(s);
+    if (last_block(s.ticket)) solve_fixed<NC>(s, 1, out);
 }
 
 template <int MC, int NC, class Src>
@@ -704,8 +719,8 @@ __global__ void __launch_bounds__(kThreads) nlf_pass3_kernel(Src src, int sw, in
         }
         if (ok) acc.add_selected(m, v);
     }
-    acc.write_fixed(s.part_i, s.part_nan);
-    if (last_block(s.ticket)) solve_fixed<NC>(s, gridDim.x, 3, out);
+    acc.write_fixed(s);
+    if (last_block(s.ticket)) solve_fixed<NC>(s, 3, out);
 }
 
 int grid_for(gls_ctx* ctx, int sw, int sh) {
@@ -732,8 +747,10 @@ template <int MC, int NC, class Src>
 gls_status run_fit(gls_ctx* ctx, const Src& src, int sw, int sh, NlfScratch s, float* out_dev) {
     const NlfThresholds th = nlf_thresholds();
     const int grid = grid_for(ctx, sw, sh);
-    // the scratch may have held other data (the context's scratch is shared): clear the ticket
-    GLS_CHECK(check_cuda(ctx, cudaMemsetAsync(s.ticket, 0, sizeof(unsigned), ctx->stream), "clear regression ticket"));
+    // the scratch may have held other data (the context's scratch is shared): clear the
+    // ticket and the running totals
+    GLS_CHECK(check_cuda(ctx, cudaMemsetAsync(s.ticket, 0, kNlfHeaderBytes - kNlfTicketOff, ctx->stream),
+                         "clear regression state"));
     nlf_pass1_kernel<MC, NC, Src><<<grid, kThreads, 0, ctx->stream>>>(src, sw, sh, th, s, out_dev);
     ctx->launches += 1;
     nlf_finish<MC, NC, Src>(ctx, src, sw, sh, s, out_dev);

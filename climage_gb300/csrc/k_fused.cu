@@ -368,7 +368,7 @@ constexpr int LT = 32;
 constexpr int LP = LT + 4;
 
 template <class SIn, class SOut>
-__global__ void __launch_bounds__(kT) level_pass1_kernel(LevelPass1Args a) {
+__global__ void __launch_bounds__(kT, 3) level_pass1_kernel(LevelPass1Args a) {  // 3 resident blocks per SM
     __shared__ float4 s_in[LP * LP];
     // downsampleImage's taps for the tile's 16 output columns and rows: [0] at -0.5 output
     // pixel, [1] at +0.5 (downsample_px's px -+ sx), relative to the staged tile
@@ -507,10 +507,14 @@ __global__ void __launch_bounds__(kT) denoise_reasm_kernel(DenoiseArgs a) {
 }
 
 // =========================================================================================
-// final: level-0 denoise + reassemble over the tile and a one-pixel ring (the local tone
-// mapping samples its input bilinearly), then the LTM mask, YCbCr -> camera and
-// convertTosRGB.  30x22 output tiles: with its ring the denoised tile is 32x24, three
-// positions per thread (the ring is 16 % of the denoised positions).
+// final: level-0 denoise + reassemble over the tile, then the LTM mask, YCbCr -> camera and
+// convertTosRGB.  32x24 output tiles, three positions per thread.  The local tone mapping
+// samples its input bilinearly, which in general needs the denoised tile with a one-pixel
+// ring (34x26).  Its sample points are the texel centres, though: when every column's and
+// row's sample falls on one texel (weight 0 or 1 after the 8-bit fraction) inside the tile
+// and the frame -- as it does for the bilateral denoiser at every practical frame width --
+// the value is that texel's (the other weight multiplies a finite value by zero), and the
+// block skips the ring (13 % of the positions it would otherwise denoise).
 //
 // Every bilinear sample here splits into an x part that depends only on the column and a y
 // part that depends only on the row (tap1).  The block evaluates those parts once per
@@ -521,7 +525,7 @@ __global__ void __launch_bounds__(kT) denoise_reasm_kernel(DenoiseArgs a) {
 // texels a tile reaches: with the pyramid's sizes (w >> 1, w >> 3) that is at most
 // FW / 2 + 4 half-resolution and FW / 8 + 5 guide texels across.
 // =========================================================================================
-constexpr int FW = 30, FH = 22;
+constexpr int FW = 32, FH = 24;
 constexpr int EW = FW + 2, EH = FH + 2;        // denoised level 0 with its ring
 constexpr int HTW = EW / 2 + 6, HTH = EH / 2 + 6;  // half-resolution tile capacity
 constexpr int GTW = FW / 8 + 8, GTH = FH / 8 + 8;  // guide tile capacity
@@ -547,6 +551,17 @@ GLS_DI float final_coord(int which, int k, int pos, float n) {
     return p + (off[k] + 0.5f) * n;
 }
 
+// Whether an LTM input tap reads one texel of the tile's interior that phase 3 denoises:
+// weight 0 or 1, the texel's offset (in units of ld) in [1, nf] and its coordinate
+// org - 1 + offset inside the frame of n texels.  Taps of positions outside the frame
+// (used = false) are never read.
+GLS_DI bool ring_free_tap(const TabTap& u, int ld, int nf, int org, int n, bool used) {
+    if (!used) return true;
+    if (!(u.a == 0.0f || u.oma == 0.0f)) return false;
+    const int off = (u.a == 0.0f ? u.i0 : u.i1) / ld;
+    return off >= 1 && off <= nf && org - 1 + off < n;
+}
+
 template <class S, int ALGO, bool LTM, bool OUT_F32>
 __global__ void __launch_bounds__(kT) final_kernel(FinalArgs a) {
     constexpr int PW = FW + 6, PH = FH + 6;  // level 0 (binary16 values, widened), origin (x0 - 3, y0 - 3)
@@ -556,6 +571,7 @@ __global__ void __launch_bounds__(kT) final_kernel(FinalArgs a) {
     __shared__ float4 s_i1[HTW * HTH], s_d1[HTW * HTH];
     __shared__ float s_g[GTW * GTH];
     __shared__ FinalTabs T;
+    __shared__ int s_ring_free;  // the LTM input reads only the tile's own texels
     // the raw table entries live only until the tables are built (phase 2); the denoised
     // tile is first written in phase 3
     static_assert(NRAW * sizeof(Tap1) <= sizeof(float4) * EW * EH, "raw table entries overflow the denoised tile");
@@ -594,6 +610,7 @@ __global__ void __launch_bounds__(kT) final_kernel(FinalArgs a) {
         }
         s_raw[e] = t;
     }
+    if (threadIdx.x == 0) s_ring_free = ALGO == 0 || !LTM;
     if (threadIdx.x < 8) {
         // extremes: the smallest index sits at the first column (row) and smallest offset,
         // the largest at the last one and the largest offset; clamped to the image
@@ -624,9 +641,13 @@ __global__ void __launch_bounds__(kT) final_kernel(FinalArgs a) {
         } else if ((q -= NRX) < NRY) {
             T.ry[q / EH][q % EH] = tab_tap(t, a.ch, hy0, HTH, HTW);
         } else if ((q -= NRY) < NLX) {
-            T.lx[q] = tab_tap_tile(t, x0 - 1, EW, 1);
+            const TabTap u = tab_tap_tile(t, x0 - 1, EW, 1);
+            T.lx[q] = u;
+            if (LTM && !ring_free_tap(u, 1, FW, x0, w, x0 + q < w)) s_ring_free = 0;
         } else if ((q -= NLX) < NLY) {
-            T.ly[q] = tab_tap_tile(t, y0 - 1, EH, EW);
+            const TabTap u = tab_tap_tile(t, y0 - 1, EH, EW);
+            T.ly[q] = u;
+            if (LTM && !ring_free_tap(u, EW, FH, y0, h, y0 + q < h)) s_ring_free = 0;
         } else if ((q -= NLY) < NGX) {
             T.gx[q / FW][q % FW] = tab_tap(t, a.gw, gx0, GTW, 1);
         } else {
@@ -661,8 +682,11 @@ __global__ void __launch_bounds__(kT) final_kernel(FinalArgs a) {
         n.a[k] = a.nlf_dev[k] * a.mul[k];
         n.b[k] = a.nlf_dev[3 + k] * a.mul[3 + k];
     }
-    for (int i = threadIdx.x; i < EW * EH; i += kT) {
-        const int r = i / EW, c = i - r * EW, x = x0 - 1 + c, y = y0 - 1 + r;
+    const bool ring_free = s_ring_free != 0;
+    for (int i = threadIdx.x; i < (ring_free ? FW * FH : EW * EH); i += kT) {
+        // position (r, c) of the denoised tile (origin x0 - 1, y0 - 1)
+        const int r = ring_free ? i / FW + 1 : i / EW, c = ring_free ? i - (r - 1) * FW + 1 : i - r * EW;
+        const int x = x0 - 1 + c, y = y0 - 1 + r;
         if (x < 0 || x >= w || y < 0 || y >= h) continue;
         Nlf6 nm = n;
         if (a.strength) {  // the learned stage's per-pixel multiplier of the noise model
@@ -683,10 +707,10 @@ __global__ void __launch_bounds__(kT) final_kernel(FinalArgs a) {
                                tab_sample_x(s_d1, T.rx[0][c], T.ry[1][r]), tab_sample_x(s_d1, T.rx[0][c], T.ry[2][r]));
         };
         d = round4<S>(reassemble_from(d, p1, pd1, sharp, a.sharpening, n.a[0], n.b[0]));
-        s_den[i] = d;
+        s_den[r * EW + c] = d;
     }
     __syncthreads();
-    if (x0 - 1 < 0 || y0 - 1 < 0 || x0 + FW + 1 > w || y0 + FH + 1 > h) {
+    if (!ring_free && (x0 - 1 < 0 || y0 - 1 < 0 || x0 + FW + 1 > w || y0 + FH + 1 > h)) {
         for (int i = threadIdx.x; i < EW * EH; i += kT) {
             const int r = i / EW, c = i - r * EW, x = x0 - 1 + c, y = y0 - 1 + r;
             if (x >= 0 && x < w && y >= 0 && y < h) continue;
