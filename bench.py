@@ -149,6 +149,19 @@ def make_frames(cfg, rank, reference=False):
     return frames
 
 
+def tuner_summary():
+    """The launch-shape tuner's choices made in this process: per kernel and frame size, the
+    chosen tile shape and the best time of every shape (ms, timed on the frame on first use)."""
+    from climage_gb300 import gls
+    names = {gls.TUNE_DEMOSAIC: "demosaic", gls.TUNE_FINAL: "final"}
+    out = []
+    for e in gls.tune_entries():
+        shapes = gls.TUNE_SHAPES[e["kernel"]]
+        out.append({"kernel": names[e["kernel"]], "size": "%dx%d" % (e["width"], e["height"]), "flags": e["flags"],
+                    "shape": shapes[e["shape"]], "ms": dict(zip(shapes, e["ms"]))})
+    return out
+
+
 def workload_config(cfg, world):
     """The line's config: the same dict on both arms (GPU and reference)."""
     return {"workload": cfg["name"], "frames_per_step": len(cfg["noise"]), "width": cfg["width"],
@@ -811,6 +824,7 @@ def main(argv=None):
             "batched_form": batched_line,
             "config1": config_lines["config1"] if config_lines else None,
             "precision_form": config_lines["precision_form"] if config_lines else None,
+            "tuner": tuner_summary(),
         }
         print(json.dumps(line), flush=True)
     conv.close()

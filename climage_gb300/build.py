@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgls_cuda.so")
 
-SOURCES = ["gls_api.cu", "k_stages.cu", "k_nlf.cu", "k_fused.cu", "raw_converter.cu", "k_noalloc.cu", "k_cnn.cu", "k_awb.cu", "k_lj92.cu", "k_calib.cu"]
+SOURCES = ["gls_api.cu", "k_stages.cu", "k_nlf.cu", "k_fused.cu", "k_fused_final.cu", "raw_converter.cu", "k_noalloc.cu", "k_cnn.cu", "k_awb.cu", "k_lj92.cu", "k_calib.cu", "k_tune.cu"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [

@@ -275,10 +275,18 @@ GLS_DI float green_at(const Acc& raw, int x, int y, float lumaVariance, const So
     const float g_hf_x = ((2.0f * c_xy - (c_left + c_right)) * 0.25f);
     const float g_hf_y = ((2.0f * c_xy - (c_up + c_down)) * 0.25f);
 
-    const float whiteness =
-        clamp_(div_(mmin(c_xy, mmin(g_ave, c2_ave)), mmax(c_xy, mmax(g_ave, c2_ave))), 0.0f, 1.0f);
     const float glen = length2_(grad.x, grad.y);
     const float lgt = smoothstep_(lumaStdDev, 4.0f * lumaStdDev, glen);
+    if (lgt == 0.0f && glen <= 3.40282347e38f) {
+        // Flat (lgt a zero of either sign) with a finite gradient: hf_gain below is lgt times a
+        // value in [+0, 1] (the clamped whiteness halved plus a smoothstep, capped at 1), so a
+        // zero of lgt's sign, and the direction is mix(0.5, d, lgt) with a finite d, which is
+        // 0.5; the whiteness, the angle and its smoothsteps do not change the result.
+        const float hf0 = lgt * 0.0f;
+        return mix_(g_lf_y + hf0 * g_hf_y, g_lf_x + hf0 * g_hf_x, 0.5f);
+    }
+    const float whiteness =
+        clamp_(div_(mmin(c_xy, mmin(g_ave, c2_ave)), mmax(c_xy, mmax(g_ave, c2_ave))), 0.0f, 1.0f);
     const float hf_gain = lgt * mmin(0.5f * whiteness + smoothstep_(0.0f, 0.3f, div_(glen, GLS_SQRT2_F)), 1.0f);
     const float g_est_x = g_lf_x + hf_gain * g_hf_x;
     const float g_est_y = g_lf_y + hf_gain * g_hf_y;

@@ -19,6 +19,7 @@
 //                  transformImage(YCbCr->camera), convertTosRGB -> RGBA8 / RGBA fp32
 #include "gls_fused.h"
 #include "gls_nlf.cuh"
+#include "gls_tune.h"
 
 namespace gls {
 namespace {
@@ -189,8 +190,16 @@ __global__ void __launch_bounds__(kT, 2) raw_pass1_kernel(RawPass1Args a) {  // 
 // =========================================================================================
 // demosaic: TW x TH output tile (44 x 28), 256 threads, 5 resident blocks per SM.
 // =========================================================================================
+// Shared memory of a demosaic tile and the blocks per SM it allows (at most 5: 48 registers)
+constexpr int demosaic_smem(int TW, int TH) {
+    return (TW + 10) * (TH + 10) * 4 + (TW + 4) * (TH + 4) * 4 + (TW + 8) * (TH + 8) * 16;
+}
+constexpr int demosaic_min_blocks(int TW, int TH) {
+    return (228 * 1024) / (demosaic_smem(TW, TH) + 1024) < 5 ? (228 * 1024) / (demosaic_smem(TW, TH) + 1024) : 5;
+}
+
 template <int TW, int TH, bool RAW_U16, class S, bool CNNIN>
-__global__ void __launch_bounds__(kT, 5) demosaic_kernel(DemosaicArgs a) {  // 5 resident blocks per SM
+__global__ void __launch_bounds__(kT, demosaic_min_blocks(TW, TH)) demosaic_kernel(DemosaicArgs a) {
     constexpr int RW = TW + 10, RH = TH + 10;  // scaled raw, origin (x0 - 5, y0 - 5)
     constexpr int SW = TW + 8, SH = TH + 8;    // Sobel map, origin (x0 - 4, y0 - 4)
     constexpr int GW = TW + 4, GH = TH + 4;    // green, origin (x0 - 2, y0 - 2)
@@ -525,14 +534,17 @@ __global__ void __launch_bounds__(kT) denoise_reasm_kernel(DenoiseArgs a) {
 // texels a tile reaches: with the pyramid's sizes (w >> 1, w >> 3) that is at most
 // FW / 2 + 4 half-resolution and FW / 8 + 5 guide texels across.
 // =========================================================================================
-constexpr int FW = 32, FH = 24;
-constexpr int EW = FW + 2, EH = FH + 2;        // denoised level 0 with its ring
-constexpr int HTW = EW / 2 + 6, HTH = EH / 2 + 6;  // half-resolution tile capacity
-constexpr int GTW = FW / 8 + 8, GTH = FH / 8 + 8;  // guide tile capacity
+// The output tile is FW x FH (a template parameter: the kernel is compiled for three
+// shapes, chosen per frame size by the launch-shape tuner).
+#define GLS_FINAL_TILE(FW, FH)                                                          \
+    constexpr int EW = FW + 2, EH = FH + 2;           /* denoised level 0 with its ring */ \
+    constexpr int HTW = EW / 2 + 6, HTH = EH / 2 + 6; /* half-resolution tile capacity */ \
+    constexpr int GTW = FW / 8 + 8, GTH = FH / 8 + 8; /* guide tile capacity */
 
 // tile origins (texels) and the table slots of one block
+template <int FW, int FH>
 struct FinalTabs {
-    TabTap rx[3][EW], ry[3][EH];  // reassemble: u = ipx, ipx + nx, ipx - nx (rows likewise)
+    TabTap rx[3][FW + 2], ry[3][FH + 2];  // reassemble: u = ipx, ipx + nx, ipx - nx (rows likewise)
     TabTap lx[FW], ly[FH];        // LTM input sample on the denoised tile
     TabTap gx[3][FW], gy[3][FH];  // LTM guide, offsets GLS_LTM_OFFSETS + 0.5
     int org[8];                   // half-res x0, x1, y0, y1; guide x0, x1, y0, y1
@@ -562,15 +574,16 @@ GLS_DI bool ring_free_tap(const TabTap& u, int ld, int nf, int org, int n, bool 
     return off >= 1 && off <= nf && org - 1 + off < n;
 }
 
-template <class S, int ALGO, bool LTM, bool OUT_F32>
+template <class S, int ALGO, bool LTM, bool OUT_F32, int FW, int FH>
 __global__ void __launch_bounds__(kT) final_kernel(FinalArgs a) {
+    GLS_FINAL_TILE(FW, FH)
     constexpr int PW = FW + 6, PH = FH + 6;  // level 0 (binary16 values, widened), origin (x0 - 3, y0 - 3)
     constexpr int NRAW = 3 * EW + 3 * EH + FW + FH + 3 * FW + 3 * FH;
     __shared__ float4 s_l0[PW * PH];
     __shared__ float4 s_den[EW * EH];            // origin (x0 - 1, y0 - 1)
     __shared__ float4 s_i1[HTW * HTH], s_d1[HTW * HTH];
     __shared__ float s_g[GTW * GTH];
-    __shared__ FinalTabs T;
+    __shared__ FinalTabs<FW, FH> T;
     __shared__ int s_ring_free;  // the LTM input reads only the tile's own texels
     // the raw table entries live only until the tables are built (phase 2); the denoised
     // tile is first written in phase 3
@@ -800,6 +813,8 @@ struct RawU16SrcS {
 
 }  // namespace
 
+#ifndef GLS_FUSED_FINAL_TU  // the final stage's launcher lives in k_fused_final.cu
+
 // ------------------------------------------------------------------------------------------
 // launchers
 // ------------------------------------------------------------------------------------------
@@ -849,12 +864,12 @@ gls_status fused_raw_fit(gls_ctx* ctx, const RawPass1Args& args, bool half, NlfS
     return check_launch(ctx, "raw noise statistics (fused)");
 }
 
-gls_status fused_demosaic(gls_ctx* ctx, const DemosaicArgs& a, bool raw_u16, bool half) {
-    constexpr int TW = 44, TH = 28;  // halos: green 1.25x, Sobel map 1.52x the tile; 44 KB, 5 blocks per SM
+// One compiled tile shape of the demosaic.
+template <int TW, int TH>
+void launch_demosaic(const DemosaicArgs& a, bool raw_u16, bool half, bool cnn, cudaStream_t st) {
     const dim3 grid((a.w + TW - 1) / TW, (a.h + TH - 1) / TH);
-    cudaStream_t st = ctx->stream;
-#define GLS_DEM(U16, SS)                                                               \
-    if (a.cnn_in) demosaic_kernel<TW, TH, U16, SS, true><<<grid, kT, 0, st>>>(a);     \
+#define GLS_DEM(U16, SS)                                                           \
+    if (cnn) demosaic_kernel<TW, TH, U16, SS, true><<<grid, kT, 0, st>>>(a);      \
     else demosaic_kernel<TW, TH, U16, SS, false><<<grid, kT, 0, st>>>(a);
     if (raw_u16) {
         if (half) { GLS_DEM(true, __half) } else { GLS_DEM(true, float) }
@@ -862,6 +877,22 @@ gls_status fused_demosaic(gls_ctx* ctx, const DemosaicArgs& a, bool raw_u16, boo
         if (half) { GLS_DEM(false, __half) } else { GLS_DEM(false, float) }
     }
 #undef GLS_DEM
+}
+
+// The learned stage's input path keeps the default shape; the plain path has three:
+// 0: 44x28 (halos: green 1.25x, Sobel map 1.52x the tile; 44 KB, 5 blocks per SM),
+// 1: 32x24 (more, smaller blocks: fills the GPU on small frames),
+// 2: 64x32 (least halo, 67 KB, 3 blocks per SM).
+void launch_demosaic_shape(int shape, const DemosaicArgs& a, bool raw_u16, bool half, cudaStream_t st) {
+    if (a.cnn_in || shape == 0) launch_demosaic<44, 28>(a, raw_u16, half, a.cnn_in != nullptr, st);
+    else if (shape == 1) launch_demosaic<32, 24>(a, raw_u16, half, false, st);
+    else launch_demosaic<64, 32>(a, raw_u16, half, false, st);
+}
+
+gls_status fused_demosaic(gls_ctx* ctx, const DemosaicArgs& a, bool raw_u16, bool half) {
+    const TuneKey key{kTuneDemosaic, a.w, a.h, (raw_u16 ? 1 : 0) | (half ? 2 : 0)};
+    const int shape = a.cnn_in ? 0 : tune_choose(ctx, key, [&](int v) { launch_demosaic_shape(v, a, raw_u16, half, ctx->stream); });
+    launch_demosaic_shape(shape, a, raw_u16, half, ctx->stream);
     ctx->launches++;
     return check_launch(ctx, "demosaic (fused)");
 }
@@ -915,23 +946,49 @@ gls_status fused_denoise(gls_ctx* ctx, const DenoiseArgs& a, bool in_half, bool 
     return check_launch(ctx, "denoise/reassemble (fused)");
 }
 
-gls_status fused_final(gls_ctx* ctx, const FinalArgs& a, bool half, int algo, bool ltm, bool out_f32) {
-    // the staged tiles are sized for the pyramid's levels 1 and 3
-    if (a.cw != a.w >> 1 || a.ch != a.h >> 1 || (ltm && (a.gw != a.w >> 3 || a.gh != a.h >> 3)))
-        return set_error(ctx, GLS_ERR_INVALID_SIZE, "final stage: levels 1 and 3 must be the pyramid's");
+#else
+
+template <int FW, int FH>
+void launch_final(const FinalArgs& a, bool half, int algo, bool ltm, bool out_f32, cudaStream_t st) {
     const dim3 grid((a.w + FW - 1) / FW, (a.h + FH - 1) / FH);
-    cudaStream_t st = ctx->stream;
-#define GLS_FIN(SS, AL) \
-    if (ltm) { if (out_f32) final_kernel<SS, AL, true, true><<<grid, kT, 0, st>>>(a); else final_kernel<SS, AL, true, false><<<grid, kT, 0, st>>>(a); } \
-    else { if (out_f32) final_kernel<SS, AL, false, true><<<grid, kT, 0, st>>>(a); else final_kernel<SS, AL, false, false><<<grid, kT, 0, st>>>(a); }
+#define GLS_FIN(SS, AL)                                                                          \
+    if (ltm) {                                                                                   \
+        if (out_f32) final_kernel<SS, AL, true, true, FW, FH><<<grid, kT, 0, st>>>(a);           \
+        else final_kernel<SS, AL, true, false, FW, FH><<<grid, kT, 0, st>>>(a);                  \
+    } else {                                                                                     \
+        if (out_f32) final_kernel<SS, AL, false, true, FW, FH><<<grid, kT, 0, st>>>(a);          \
+        else final_kernel<SS, AL, false, false, FW, FH><<<grid, kT, 0, st>>>(a);                 \
+    }
     if (half) {
         if (algo == 0) { GLS_FIN(__half, 0) } else { GLS_FIN(__half, 1) }
     } else {
         if (algo == 0) { GLS_FIN(float, 0) } else { GLS_FIN(float, 1) }
     }
 #undef GLS_FIN
+}
+
+// The bilateral path with the local tone mapping has three shapes (three, two and four
+// positions per thread): 0: 32x24, 1: 32x16, 2: 64x16; the other forms keep 32x24.
+void launch_final_shape(int shape, const FinalArgs& a, bool half, int algo, bool ltm, bool out_f32, cudaStream_t st) {
+    if (shape == 0 || algo != 0 || !ltm) launch_final<32, 24>(a, half, algo, ltm, out_f32, st);
+    else if (shape == 1) launch_final<32, 16>(a, half, 0, true, out_f32, st);
+    else launch_final<64, 16>(a, half, 0, true, out_f32, st);
+}
+
+gls_status fused_final(gls_ctx* ctx, const FinalArgs& a, bool half, int algo, bool ltm, bool out_f32) {
+    // the staged tiles are sized for the pyramid's levels 1 and 3
+    if (a.cw != a.w >> 1 || a.ch != a.h >> 1 || (ltm && (a.gw != a.w >> 3 || a.gh != a.h >> 3)))
+        return set_error(ctx, GLS_ERR_INVALID_SIZE, "final stage: levels 1 and 3 must be the pyramid's");
+    int shape = 0;
+    if (algo == 0 && ltm) {
+        const TuneKey key{kTuneFinal, a.w, a.h, (half ? 1 : 0) | (out_f32 ? 2 : 0)};
+        shape = tune_choose(ctx, key, [&](int v) { launch_final_shape(v, a, half, algo, ltm, out_f32, ctx->stream); });
+    }
+    launch_final_shape(shape, a, half, algo, ltm, out_f32, ctx->stream);
     ctx->launches++;
     return check_launch(ctx, "final (fused)");
 }
+
+#endif  // GLS_FUSED_FINAL_TU
 
 }  // namespace gls

@@ -179,7 +179,17 @@ SIGNATURES = [
     ("gls_cnn_train_step", _I, [_P, _P, _P, _I, _I, _I, _F, _FP]),
     ("gls_raw_batch_plan", _I, [_I, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int), _I,
                                 ctypes.POINTER(ctypes.c_int)]),
+    ("gls_tune_force", _I, [_I, _I]),
+    ("gls_tune_reset", _I, []),
+    ("gls_tune_count", _I, []),
+    ("gls_tune_entry", _I, [_I, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                            ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                            ctypes.POINTER(ctypes.c_int), _FP]),
 ]
+
+# launch-shape tuner: kernels and their compiled tile shapes (gls_tune_force / gls_tune_entry)
+TUNE_DEMOSAIC, TUNE_FINAL = 0, 1
+TUNE_SHAPES = {TUNE_DEMOSAIC: ("44x28", "32x24", "64x32"), TUNE_FINAL: ("32x24", "32x16", "64x16")}
 
 
 def lib():
@@ -551,6 +561,33 @@ class RawConverter:
             self.close()
         except Exception:
             pass
+
+
+def tune_force(kernel, shape):
+    """Pins a kernel's tile shape for every frame size (shape -1: the tuned choice again)."""
+    st = lib().gls_tune_force(int(kernel), int(shape))
+    if st != 0:
+        raise GlsError(st, "gls_tune_force(%d, %d)" % (kernel, shape))
+
+
+def tune_reset():
+    """Forgets every tuned choice and forced shape."""
+    lib().gls_tune_reset()
+
+
+def tune_entries():
+    """The tuner's choices: [{kernel, width, height, flags, shape, ms: [best ms per shape]}]."""
+    out = []
+    for i in range(lib().gls_tune_count()):
+        k, w, h, f, sh = (ctypes.c_int() for _ in range(5))
+        ms = (ctypes.c_float * 4)()
+        if lib().gls_tune_entry(i, ctypes.byref(k), ctypes.byref(w), ctypes.byref(h), ctypes.byref(f),
+                                ctypes.byref(sh), ms) != 0:
+            break
+        n = len(TUNE_SHAPES[k.value])
+        out.append(dict(kernel=k.value, width=w.value, height=h.value, flags=f.value, shape=sh.value,
+                        ms=[round(float(x), 4) for x in ms[:n]]))
+    return out
 
 
 def batch_plan(sizes, lanes):

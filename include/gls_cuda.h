@@ -417,6 +417,25 @@ GLS_API gls_status gls_raw_batch_set_cnn(gls_raw_batch* batch, gls_cnn* cnn);
  * to the lane with the fewest pixels so far; ties to the lower frame index and lane). */
 GLS_API gls_status gls_raw_batch_plan(int n, const int* widths, const int* heights, int lanes, int* lane_of);
 
+/* ---- launch-shape tuner (no counterpart in the reference; its work-group sizes come from
+ * src/gls_cl.cpp:227-261, computeWorkGroupSizes) ----
+ * The demosaic (kernel 0: tiles 44x28, 32x24, 64x32) and the final stage (kernel 1: tiles
+ * 32x16, 64x16) are compiled for several tile shapes that compute the same values.  On the
+ * first frame of a size (and storage/input form) the converter times every shape on that
+ * frame (best of three) and keeps the fastest for the process if it beats shape 0 by 3 %
+ * (shape 0 otherwise); frames converted while their stream is
+ * captured into a graph, and every frame when the environment sets GLS_TUNE=0, use shape 0
+ * until a size has been tuned. */
+/* pins kernel's shape for every size (-1: tuned choice again) */
+GLS_API gls_status gls_tune_force(int kernel, int shape);
+/* forgets every tuned choice and forced shape */
+GLS_API gls_status gls_tune_reset(void);
+/* number of tuned (kernel, size, flags) entries, and entry `index` with the best time of each
+ * shape in ms (zero for shapes the kernel does not have) */
+GLS_API int gls_tune_count(void);
+GLS_API gls_status gls_tune_entry(int index, int* kernel, int* width, int* height, int* flags, int* shape,
+                                  float ms[4]);
+
 #ifdef __cplusplus
 }
 #endif
