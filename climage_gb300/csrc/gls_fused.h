@@ -65,6 +65,7 @@ struct LevelPass1Args {
     NlfScratch nlf;  // regression scratch (set by the launcher)
     float* nlf_out;  // fitted {A0..2, B0..2}
     int stats_half;  // the statistics rounded to binary16 before the fit (GLS_STORAGE_F16_STATS)
+    int tma;         // the input's tensor map is valid (set by the launcher)
 };
 
 struct DenoiseArgs {

@@ -82,11 +82,12 @@ constexpr size_t kNlfTicketOff = 128;
 constexpr size_t kNlfLimbOff = 256;                                  // [kNlfK][3] u64
 constexpr size_t kNlfMmOff = kNlfLimbOff + 8 * 3 * (size_t)kNlfK;    // [kNlfKF] u32
 constexpr size_t kNlfNanOff = kNlfMmOff + 4 * (size_t)kNlfKF;        // u32
+constexpr size_t kNlfErrOff = kNlfNanOff + 4;                        // u32
 constexpr size_t kNlfHeaderBytes = 1024;
 constexpr size_t kNlfPartDBytes = sizeof(double) * (size_t)kNlfMaxBlocks * kNlfK;
 constexpr size_t kNlfScratchBytes = kNlfHeaderBytes + kNlfPartDBytes;
 static_assert(sizeof(NlfFit) <= kNlfTicketOff, "fit state overlaps the ticket");
-static_assert(kNlfNanOff + 4 <= kNlfHeaderBytes, "totals overflow the header");
+static_assert(kNlfErrOff + 4 <= kNlfHeaderBytes, "totals overflow the header");
 
 struct NlfScratch {
     NlfFit* fit;
@@ -94,6 +95,7 @@ struct NlfScratch {
     unsigned long long* tot_limb;  // [kNlfK][3]: bits 0-39, 40-79, and 80-127 (signed) of each block's sum
     unsigned* tot_mm;              // a fit of NC channels: [0, 2 NC) ~ord(minimum), [2 NC, 4 NC) ord(maximum)
     unsigned* tot_nan;             // bit k set when column k summed a NaN
+    unsigned* err;                 // nonzero once a bounded wait of a statistics kernel ran out
     double* part_d;                // [block][kNlfK], pass 2
 };
 
@@ -105,6 +107,7 @@ inline NlfScratch nlf_scratch_at(void* base) {
     s.tot_limb = reinterpret_cast<unsigned long long*>(p + kNlfLimbOff);
     s.tot_mm = reinterpret_cast<unsigned*>(p + kNlfMmOff);
     s.tot_nan = reinterpret_cast<unsigned*>(p + kNlfNanOff);
+    s.err = reinterpret_cast<unsigned*>(p + kNlfErrOff);
     s.part_d = reinterpret_cast<double*>(p + kNlfHeaderBytes);
     return s;
 }

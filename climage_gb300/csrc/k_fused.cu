@@ -17,6 +17,10 @@
 //   denoise_reasm  denoiseImage (+ reassembleImage) of levels >= 1
 //   final          denoiseImage + reassembleImage of level 0, localToneMappingMask,
 //                  transformImage(YCbCr->camera), convertTosRGB -> RGBA8 / RGBA fp32
+#include <cuda.h>
+
+#include <cstring>
+
 #include "gls_fused.h"
 #include "gls_nlf.cuh"
 #include "gls_tune.h"
@@ -372,28 +376,101 @@ __global__ void __launch_bounds__(kT) post_cnn_kernel(PostCnnArgs a) {
 // Persistent blocks walk 32x32 tiles; each thread owns a column of 4 pixels and reuses
 // the loaded rows across them (each output still sums its 5x5 window in the reference's
 // row-major order).
+//
+// Staging: the 36x36 input region of a tile is double-buffered.  Where the region lies inside
+// the image, one thread brings it in with a TMA tensor copy (cp.async.bulk.tensor) while the
+// block sums the previous tile, completing on an mbarrier; at the image's edges (clamped
+// reads) the block loads it itself.  A binary16 level is widened into a third buffer once
+// it has landed.
 // =========================================================================================
 constexpr int LT = 32;
 constexpr int LP = LT + 4;
+constexpr uint32_t kLevelWaitPolls = 1u << 22;  // bounded TMA wait (each poll a test_wait)
+
+GLS_DI void tma_issue_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(bytes) : "memory");
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];\n" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+        : "memory");
+}
+
+// every thread of the block calls it; true once phase `parity` of the barrier completed
+GLS_DI bool level_wait(uint32_t bar, uint32_t parity, uint32_t limit) {
+    uint32_t done = 0;
+    for (uint32_t k = 0; k < limit && !done; k++) {
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(bar), "r"(parity)
+            : "memory");
+    }
+    return __syncthreads_and(done) != 0;
+}
 
 template <class SIn, class SOut>
-__global__ void __launch_bounds__(kT, 3) level_pass1_kernel(LevelPass1Args a) {  // 3 resident blocks per SM
-    __shared__ float4 s_in[LP * LP];
+__global__ void __launch_bounds__(kT, 3) level_pass1_kernel(LevelPass1Args a, const __grid_constant__ CUtensorMap tmap) {
+    typedef typename Storage<SIn>::T4 TIn;
+    constexpr bool HALF_IN = sizeof(TIn) == 8;
+    constexpr uint32_t kStageBytes = LP * LP * sizeof(TIn);
+    __shared__ __align__(128) TIn s_stage[2][LP * LP];  // the tile's region as stored
+    __shared__ __align__(16) float4 s_wide[HALF_IN ? LP * LP : 1];  // a binary16 region widened
+    __shared__ __align__(8) uint64_t s_bar[2];
     // downsampleImage's taps for the tile's 16 output columns and rows: [0] at -0.5 output
     // pixel, [1] at +0.5 (downsample_px's px -+ sx), relative to the staged tile
     __shared__ TabTap s_tx[2][LT / 2], s_ty[2][LT / 2];
     LevelPass1Acc2 acc;
     acc.init();
-    typedef typename Storage<SIn>::T4 TIn;
     const TIn* in = (const TIn*)a.in;
     const GImg4<SIn> gin{in, a.w, a.h, a.pitch};
-    const int tiles_x = (a.w + LT - 1) / LT, tiles_y = (a.h + LT - 1) / LT;
+    const int tiles_x = (a.w + LT - 1) / LT, tiles_y = (a.h + LT - 1) / LT, ntiles = tiles_x * tiles_y;
     const int col = threadIdx.x & 31, row0 = (threadIdx.x >> 5) * 4;
-    for (int t = blockIdx.x; t < tiles_x * tiles_y; t += gridDim.x) {
+    const uint32_t bar0 = (uint32_t)__cvta_generic_to_shared(&s_bar[0]);
+    const uint32_t stage0 = (uint32_t)__cvta_generic_to_shared(&s_stage[0][0]);
+    if (threadIdx.x == 0 && a.tma) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar0) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar0 + 8) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+    // a tile's region by TMA when it lies inside the image (x in 8-byte units: even)
+    auto by_tma = [&](int t) {
         const int x0 = (t % tiles_x) * LT, y0 = (t / tiles_x) * LT;
-        for (int i = threadIdx.x; i < LP * LP; i += kT) {
-            const int r = i / LP, c = i - r * LP;
-            s_in[i] = gin.at(x0 - 2 + c, y0 - 2 + r);
+        return a.tma && x0 >= 2 && y0 >= 2 && x0 + LT + 2 <= a.w && y0 + LT + 2 <= a.h;
+    };
+    auto issue = [&](int t, int b) {  // thread 0
+        const int x0 = (t % tiles_x) * LT, y0 = (t / tiles_x) * LT;
+        tma_issue_2d(stage0 + (uint32_t)b * kStageBytes, &tmap, (x0 - 2) * (int)(sizeof(TIn) / 8), y0 - 2,
+                     bar0 + 8u * (uint32_t)b, kStageBytes);
+    };
+    uint32_t parity = 0;  // bit b: the phase of barrier b to wait for next
+    bool pending = false;  // this iteration's buffer is being filled by TMA
+    int buf = 0;
+    int t = blockIdx.x;
+    if (t < ntiles && by_tma(t)) {
+        if (threadIdx.x == 0) issue(t, 0);
+        pending = true;
+    }
+    for (; t < ntiles; t += gridDim.x, buf ^= 1) {
+        const int x0 = (t % tiles_x) * LT, y0 = (t / tiles_x) * LT;
+        TIn* const stage = s_stage[buf];
+        if (pending) {
+            const uint32_t par = (parity >> buf) & 1u;
+            parity ^= 1u << buf;
+            if (!level_wait(bar0 + 8u * (uint32_t)buf, par, kLevelWaitPolls)) {
+                // the copy did not complete: record it, give it one more bounded wait, and
+                // leave the tile loop (the sums so far still reach the totals, so the
+                // regression's ticket stays consistent)
+                if (threadIdx.x == 0) atomicOr(a.nlf.err, 1u);
+                level_wait(bar0 + 8u * (uint32_t)buf, par, kLevelWaitPolls);
+                break;
+            }
+        } else {
+            for (int i = threadIdx.x; i < LP * LP; i += kT) {
+                const int r = i / LP, c = i - r * LP;
+                const int gx = clampi(x0 - 2 + c, 0, a.w - 1), gy = clampi(y0 - 2 + r, 0, a.h - 1);
+                stage[i] = in[(size_t)gy * a.pitch + gx];
+            }
         }
         if (a.out && threadIdx.x < 2 * LT) {
             // the same float operations as downsample_px's coordinates and tap1, once per
@@ -410,6 +487,16 @@ __global__ void __launch_bounds__(kT, 3) level_pass1_kernel(LevelPass1Args a) { 
             }
         }
         __syncthreads();
+        if constexpr (HALF_IN) {
+            for (int i = threadIdx.x; i < LP * LP; i += kT) s_wide[i] = Storage<__half>::cvt(stage[i]);
+            __syncthreads();
+        }
+        const float4* const s_in = HALF_IN ? s_wide : reinterpret_cast<const float4*>(stage);
+        // the next tile's region streams into the other buffer while this one is summed (its
+        // previous contents were consumed before the barrier that ended the last iteration)
+        const int tn = t + gridDim.x;
+        pending = tn < ntiles && by_tma(tn);
+        if (pending && threadIdx.x == 0) issue(tn, buf ^ 1);
         // window sums for pixels (x0 + col, y0 + row0 + j), j = 0..3: (s0, s1), (q0, q1) and
         // (s2, q2) as packed pairs, every window summed in the reference's row-major order
         float2 s01[4], q01[4], s2q2[4];
@@ -470,6 +557,8 @@ __global__ void __launch_bounds__(kT, 3) level_pass1_kernel(LevelPass1Args a) { 
                 Storage<SOut>::st4((TOut*)a.out + (size_t)oy * a.opitch + ox, d);
             }
         }
+        // this tile's buffers may next be written by the async proxy (a TMA copy)
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
         __syncthreads();
     }
     Pass1Acc<1, 3> out;
@@ -905,21 +994,55 @@ gls_status fused_post_cnn(gls_ctx* ctx, const PostCnnArgs& a, bool half) {
     return check_launch(ctx, "after the learned stage");
 }
 
+// A 2D tensor map of an RGBA level (8 or 16 bytes per pixel) in 8-byte elements, with the
+// 36x36-pixel box of a level_pass1 tile; false where TMA does not apply (no driver entry
+// point, an unaligned base or pitch, a level smaller than a box).
+bool level_tensor_map(CUtensorMap* map, const void* base, int elem_bytes, int w, int h, int pitch) {
+    typedef CUresult (*EncodeFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+    static EncodeFn s_encode = nullptr;
+    static bool s_tried = false;
+    if (!s_tried) {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            s_encode = reinterpret_cast<EncodeFn>(f);
+        else
+            cudaGetLastError();
+        s_tried = true;
+    }
+    const int per = elem_bytes / 8;  // 8-byte elements per pixel
+    const uint64_t row_bytes = (uint64_t)pitch * (uint64_t)elem_bytes;
+    if (!s_encode || (reinterpret_cast<uintptr_t>(base) & 15u) || (row_bytes & 15u) || w < LP || h < LP) return false;
+    const cuuint64_t dims[2] = {(cuuint64_t)w * per, (cuuint64_t)h};
+    const cuuint64_t strides[1] = {row_bytes};
+    const cuuint32_t box[2] = {(cuuint32_t)(LP * per), (cuuint32_t)LP};
+    const cuuint32_t estr[2] = {1, 1};
+    return s_encode(map, CU_TENSOR_MAP_DATA_TYPE_UINT64, 2, const_cast<void*>(base), dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 gls_status fused_level_fit(gls_ctx* ctx, const LevelPass1Args& args, bool in_half, bool half, NlfScratch s,
                            float* out_dev) {
     LevelPass1Args a = args;
     a.th = nlf_thresholds();
     a.nlf = s;
     a.nlf_out = out_dev;
+    CUtensorMap map;
+    memset(&map, 0, sizeof(map));
+    a.tma = level_tensor_map(&map, a.in, in_half ? 8 : 16, a.w, a.h, a.pitch) ? 1 : 0;
     const long tiles = (long)((a.w + LT - 1) / LT) * ((a.h + LT - 1) / LT);
     if (in_half) {
-        if (half) level_pass1_kernel<__half, __half><<<resident_grid<level_pass1_kernel<__half, __half>>(ctx, tiles), kT, 0, ctx->stream>>>(a);
-        else level_pass1_kernel<__half, float><<<resident_grid<level_pass1_kernel<__half, float>>(ctx, tiles), kT, 0, ctx->stream>>>(a);
+        if (half) level_pass1_kernel<__half, __half><<<resident_grid<level_pass1_kernel<__half, __half>>(ctx, tiles), kT, 0, ctx->stream>>>(a, map);
+        else level_pass1_kernel<__half, float><<<resident_grid<level_pass1_kernel<__half, float>>(ctx, tiles), kT, 0, ctx->stream>>>(a, map);
         LevelSrc<__half> src{{(const half4*)a.in, a.w, a.h, a.pitch}, a.stats_half != 0};
         ctx->launches++;
         nlf_finish<1, 3>(ctx, src, a.w, a.h, s, out_dev);
     } else {
-        level_pass1_kernel<float, float><<<resident_grid<level_pass1_kernel<float, float>>(ctx, tiles), kT, 0, ctx->stream>>>(a);
+        level_pass1_kernel<float, float><<<resident_grid<level_pass1_kernel<float, float>>(ctx, tiles), kT, 0, ctx->stream>>>(a, map);
         LevelSrc<float> src{{(const float4*)a.in, a.w, a.h, a.pitch}, a.stats_half != 0};
         ctx->launches++;
         nlf_finish<1, 3>(ctx, src, a.w, a.h, s, out_dev);
