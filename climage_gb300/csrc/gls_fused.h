@@ -18,6 +18,7 @@ struct RawPass1Args {
     float* nlf_out;  // fitted {A0..3, B0..3}
     int sums_exact;  // set by the launcher: every 5x5 sum and its square lie where x / 25 has its exact shortcut
     int stats_half;  // the statistics rounded to binary16 before the fit (GLS_STORAGE_F16_STATS)
+    int tma;         // the raw image's tensor map is valid (set by the launcher)
 };
 
 struct DemosaicArgs {

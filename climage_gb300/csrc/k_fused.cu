@@ -85,6 +85,30 @@ GLS_DI float4 round4(float4 v) {
     return make_float4(Storage<S>::round(v.x), Storage<S>::round(v.y), Storage<S>::round(v.z), Storage<S>::round(v.w));
 }
 
+// ---- TMA tile staging (raw_pass1, level_pass1) ----
+constexpr uint32_t kStageWaitPolls = 1u << 22;  // bound of a staging wait (each poll a try_wait)
+
+GLS_DI void tma_issue_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(bytes) : "memory");
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];\n" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+        : "memory");
+}
+
+// every thread of the block calls it; true once phase `parity` of the barrier completed
+GLS_DI bool stage_wait(uint32_t bar, uint32_t parity, uint32_t limit) {
+    uint32_t done = 0;
+    for (uint32_t k = 0; k < limit && !done; k++) {
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(bar), "r"(parity)
+            : "memory");
+    }
+    return __syncthreads_and(done) != 0;
+}
+
 // =========================================================================================
 // raw_pass1: per 2x2 quad, the 5x5-quad statistics of the scaled raw planes and the
 // pass-1 sums of computeRawNoiseStatistics.  Tiles of 32x32 quads: the scaled values are
@@ -110,30 +134,89 @@ GLS_DI float2 div25_x2(float2 x) {
     return q;
 }
 
+// The raw region of a tile by TMA: 80 x 72 pixels from (2 qx0 - 8, 2 qy0 - 4), so that x is
+// a multiple of 8 pixels (16 bytes) and a row of the box is 160 bytes; the staged quads
+// start 4 pixels in.
+constexpr int RBW = 2 * RQS + 8, RBH = 2 * RQS;
+
 template <class S, int BAYER>
-__global__ void __launch_bounds__(kT, 2) raw_pass1_kernel(RawPass1Args a) {  // 2 resident blocks per SM
+__global__ void __launch_bounds__(kT, 2) raw_pass1_kernel(RawPass1Args a, const __grid_constant__ CUtensorMap tmap) {  // 2 resident blocks per SM
+    constexpr uint32_t kStageBytes = RBW * RBH * 2;
     __shared__ float4 s_q[RQS * RQS];
+    __shared__ __align__(128) uint16_t s_stage[2][RBW * RBH];
+    __shared__ __align__(8) uint64_t s_bar[2];
     RawPass1Acc2 acc;
     acc.init();
     const int qw = a.w / 2, qh = a.h / 2;
-    const int tiles_x = (qw + RQ - 1) / RQ, tiles_y = (qh + RQ - 1) / RQ;
+    const int tiles_x = (qw + RQ - 1) / RQ, tiles_y = (qh + RQ - 1) / RQ, ntiles = tiles_x * tiles_y;
     const int col = threadIdx.x & 31, row0 = (threadIdx.x >> 5) * 4;
-    for (int t = blockIdx.x; t < tiles_x * tiles_y; t += gridDim.x) {
+    const uint32_t bar0 = (uint32_t)__cvta_generic_to_shared(&s_bar[0]);
+    const uint32_t stage0 = (uint32_t)__cvta_generic_to_shared(&s_stage[0][0]);
+    if (threadIdx.x == 0 && a.tma) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar0) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar0 + 8) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+    auto by_tma = [&](int t) {
+        const int px0 = 2 * (t % tiles_x) * RQ, py0 = 2 * (t / tiles_x) * RQ;
+        return a.tma && px0 >= 8 && py0 >= 4 && px0 + 2 * RQ + 8 <= a.w && py0 + 2 * RQ + 4 <= a.h;
+    };
+    auto issue = [&](int t, int b) {  // thread 0
+        const int px0 = 2 * (t % tiles_x) * RQ, py0 = 2 * (t / tiles_x) * RQ;
+        tma_issue_2d(stage0 + (uint32_t)b * kStageBytes, &tmap, px0 - 8, py0 - 4, bar0 + 8u * (uint32_t)b, kStageBytes);
+    };
+    uint32_t parity = 0;
+    bool pending = false;
+    int buf = 0;
+    int t = blockIdx.x;
+    if (t < ntiles && by_tma(t)) {
+        if (threadIdx.x == 0) issue(t, 0);
+        pending = true;
+    }
+    for (; t < ntiles; t += gridDim.x, buf ^= 1) {
         const int qx0 = (t % tiles_x) * RQ, qy0 = (t / tiles_x) * RQ;
-        for (int i = threadIdx.x; i < RQS * RQS; i += kT) {
-            const int r = i / RQS, c = i - r * RQS;
-            const int px = 2 * (qx0 - 2 + c), py = 2 * (qy0 - 2 + r);
-            float v[4];
-#pragma unroll
-            for (int ch = 0; ch < 4; ch++) {  // the pixel of channel ch, clamped to the frame
-                const int gx = clampi(px + bayer_dx(BAYER, ch), 0, a.w - 1);
-                const int gy = clampi(py + bayer_dy(BAYER, ch), 0, a.h - 1);
-                v[ch] = Storage<S>::round(
-                    scale_value(__ldg(a.raw + (size_t)gy * a.pitch + gx), a.sm[((gy & 1) << 1) | (gx & 1)], a.black));
+        if (pending) {
+            const uint32_t par = (parity >> buf) & 1u;
+            parity ^= 1u << buf;
+            if (!stage_wait(bar0 + 8u * (uint32_t)buf, par, kStageWaitPolls)) {
+                if (threadIdx.x == 0) atomicOr(a.nlf.err, 1u);
+                stage_wait(bar0 + 8u * (uint32_t)buf, par, kStageWaitPolls);
+                break;
             }
-            s_q[i] = make_float4(v[0], v[1], v[2], v[3]);
+            // quads from the staged pixels: (2c + 4 + dx, 2r + dy); the pixel's parity is the
+            // channel's (dx, dy), as the frame's coordinates are even at the quad
+            const uint16_t* st = s_stage[buf];
+            for (int i = threadIdx.x; i < RQS * RQS; i += kT) {
+                const int r = i / RQS, c = i - r * RQS;
+                float v[4];
+#pragma unroll
+                for (int ch = 0; ch < 4; ch++) {
+                    const int dx = bayer_dx(BAYER, ch), dy = bayer_dy(BAYER, ch);
+                    v[ch] = Storage<S>::round(scale_value(st[(2 * r + dy) * RBW + 2 * c + 4 + dx], a.sm[(dy << 1) | dx], a.black));
+                }
+                s_q[i] = make_float4(v[0], v[1], v[2], v[3]);
+            }
+        } else {
+            for (int i = threadIdx.x; i < RQS * RQS; i += kT) {
+                const int r = i / RQS, c = i - r * RQS;
+                const int px = 2 * (qx0 - 2 + c), py = 2 * (qy0 - 2 + r);
+                float v[4];
+#pragma unroll
+                for (int ch = 0; ch < 4; ch++) {  // the pixel of channel ch, clamped to the frame
+                    const int gx = clampi(px + bayer_dx(BAYER, ch), 0, a.w - 1);
+                    const int gy = clampi(py + bayer_dy(BAYER, ch), 0, a.h - 1);
+                    v[ch] = Storage<S>::round(
+                        scale_value(__ldg(a.raw + (size_t)gy * a.pitch + gx), a.sm[((gy & 1) << 1) | (gx & 1)], a.black));
+                }
+                s_q[i] = make_float4(v[0], v[1], v[2], v[3]);
+            }
         }
         __syncthreads();
+        // the next tile's pixels stream into the other buffer while this one is summed
+        const int tn = t + gridDim.x;
+        pending = tn < ntiles && by_tma(tn);
+        if (pending && threadIdx.x == 0) issue(tn, buf ^ 1);
         // window sums of quads (qx0 + col, qy0 + row0 + j), j = 0..3
         float2 s01[4], q01[4], s23[4], q23[4];
 #pragma unroll
@@ -184,6 +267,8 @@ __global__ void __launch_bounds__(kT, 2) raw_pass1_kernel(RawPass1Args a) {  // 
                 if (in_range<4, 4>(mm, vv, a.th)) acc.add_selected(m, v);
             }
         }
+        // the staged pixels were read before this iteration's first barrier; s_q until here
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
         __syncthreads();
     }
     Pass1Acc<4, 4> out;
@@ -385,29 +470,6 @@ __global__ void __launch_bounds__(kT) post_cnn_kernel(PostCnnArgs a) {
 // =========================================================================================
 constexpr int LT = 32;
 constexpr int LP = LT + 4;
-constexpr uint32_t kLevelWaitPolls = 1u << 22;  // bounded TMA wait (each poll a test_wait)
-
-GLS_DI void tma_issue_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(bytes) : "memory");
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];\n" ::"r"(dst),
-        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
-        : "memory");
-}
-
-// every thread of the block calls it; true once phase `parity` of the barrier completed
-GLS_DI bool level_wait(uint32_t bar, uint32_t parity, uint32_t limit) {
-    uint32_t done = 0;
-    for (uint32_t k = 0; k < limit && !done; k++) {
-        asm volatile(
-            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
-            : "=r"(done)
-            : "r"(bar), "r"(parity)
-            : "memory");
-    }
-    return __syncthreads_and(done) != 0;
-}
-
 template <class SIn, class SOut>
 __global__ void __launch_bounds__(kT, 3) level_pass1_kernel(LevelPass1Args a, const __grid_constant__ CUtensorMap tmap) {
     typedef typename Storage<SIn>::T4 TIn;
@@ -457,12 +519,12 @@ __global__ void __launch_bounds__(kT, 3) level_pass1_kernel(LevelPass1Args a, co
         if (pending) {
             const uint32_t par = (parity >> buf) & 1u;
             parity ^= 1u << buf;
-            if (!level_wait(bar0 + 8u * (uint32_t)buf, par, kLevelWaitPolls)) {
+            if (!stage_wait(bar0 + 8u * (uint32_t)buf, par, kStageWaitPolls)) {
                 // the copy did not complete: record it, give it one more bounded wait, and
                 // leave the tile loop (the sums so far still reach the totals, so the
                 // regression's ticket stays consistent)
                 if (threadIdx.x == 0) atomicOr(a.nlf.err, 1u);
-                level_wait(bar0 + 8u * (uint32_t)buf, par, kLevelWaitPolls);
+                stage_wait(bar0 + 8u * (uint32_t)buf, par, kStageWaitPolls);
                 break;
             }
         } else {
@@ -908,6 +970,46 @@ struct RawU16SrcS {
 // launchers
 // ------------------------------------------------------------------------------------------
 
+// A 2D tensor map (elements of elem_bytes) of an image of w x h pixels of px_elems elements
+// each, pitch in pixels, with a box of box_w x box_h elements; false where TMA does not apply
+// (no driver entry point, an unaligned base or row, an image smaller than a box).
+bool tensor_map_2d(CUtensorMap* map, const void* base, CUtensorMapDataType type, int elem_bytes, int w_elems, int h,
+                   int pitch_elems, int box_w, int box_h) {
+    typedef CUresult (*EncodeFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+    static EncodeFn s_encode = nullptr;
+    static bool s_tried = false;
+    if (!s_tried) {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            s_encode = reinterpret_cast<EncodeFn>(f);
+        else
+            cudaGetLastError();
+        s_tried = true;
+    }
+    const uint64_t row_bytes = (uint64_t)pitch_elems * (uint64_t)elem_bytes;
+    if (!s_encode || (reinterpret_cast<uintptr_t>(base) & 15u) || (row_bytes & 15u) || w_elems < box_w || h < box_h ||
+        ((uint64_t)box_w * elem_bytes) % 16u != 0)
+        return false;
+    const cuuint64_t dims[2] = {(cuuint64_t)w_elems, (cuuint64_t)h};
+    const cuuint64_t strides[1] = {row_bytes};
+    const cuuint32_t box[2] = {(cuuint32_t)box_w, (cuuint32_t)box_h};
+    const cuuint32_t estr[2] = {1, 1};
+    return s_encode(map, type, 2, const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                    CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// A level (RGBA, 8 or 16 bytes per pixel) as 8-byte elements, with the 36x36-pixel box of a
+// level_pass1 tile.
+bool level_tensor_map(CUtensorMap* map, const void* base, int px_bytes, int w, int h, int pitch) {
+    const int per = px_bytes / 8;
+    return tensor_map_2d(map, base, CU_TENSOR_MAP_DATA_TYPE_UINT64, 8, w * per, h, pitch * per, LP * per, LP);
+}
+
 gls_status fused_raw_fit(gls_ctx* ctx, const RawPass1Args& args, bool half, NlfScratch s, float* out_dev) {
     RawPass1Args a = args;
     a.th = nlf_thresholds();
@@ -923,10 +1025,13 @@ gls_status fused_raw_fit(gls_ctx* ctx, const RawPass1Args& args, bool half, NlfS
         if (!(a.sm[k] >= 0.5f && a.sm[k] <= 32768.0f)) a.sums_exact = 0;
     const int qw = a.w / 2, qh = a.h / 2;
     const long tiles = (long)((qw + RQ - 1) / RQ) * ((qh + RQ - 1) / RQ);
+    CUtensorMap map;
+    memset(&map, 0, sizeof(map));
+    a.tma = tensor_map_2d(&map, a.raw, CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, a.w, a.h, a.pitch, RBW, RBH) ? 1 : 0;
 #define GLS_RAWP1(SS, BY)                                                      \
     {                                                                          \
         const int grid = resident_grid<raw_pass1_kernel<SS, BY>>(ctx, tiles); \
-        raw_pass1_kernel<SS, BY><<<grid, kT, 0, ctx->stream>>>(a);            \
+        raw_pass1_kernel<SS, BY><<<grid, kT, 0, ctx->stream>>>(a, map);       \
     }
 #define GLS_RAWP1_B(SS)                 \
     switch (a.bayer) {                  \
@@ -992,37 +1097,6 @@ gls_status fused_post_cnn(gls_ctx* ctx, const PostCnnArgs& a, bool half) {
     else post_cnn_kernel<float><<<grid, kT, 0, ctx->stream>>>(a);
     ctx->launches++;
     return check_launch(ctx, "after the learned stage");
-}
-
-// A 2D tensor map of an RGBA level (8 or 16 bytes per pixel) in 8-byte elements, with the
-// 36x36-pixel box of a level_pass1 tile; false where TMA does not apply (no driver entry
-// point, an unaligned base or pitch, a level smaller than a box).
-bool level_tensor_map(CUtensorMap* map, const void* base, int elem_bytes, int w, int h, int pitch) {
-    typedef CUresult (*EncodeFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
-                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
-                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-    static EncodeFn s_encode = nullptr;
-    static bool s_tried = false;
-    if (!s_tried) {
-        void* f = nullptr;
-        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            s_encode = reinterpret_cast<EncodeFn>(f);
-        else
-            cudaGetLastError();
-        s_tried = true;
-    }
-    const int per = elem_bytes / 8;  // 8-byte elements per pixel
-    const uint64_t row_bytes = (uint64_t)pitch * (uint64_t)elem_bytes;
-    if (!s_encode || (reinterpret_cast<uintptr_t>(base) & 15u) || (row_bytes & 15u) || w < LP || h < LP) return false;
-    const cuuint64_t dims[2] = {(cuuint64_t)w * per, (cuuint64_t)h};
-    const cuuint64_t strides[1] = {row_bytes};
-    const cuuint32_t box[2] = {(cuuint32_t)(LP * per), (cuuint32_t)LP};
-    const cuuint32_t estr[2] = {1, 1};
-    return s_encode(map, CU_TENSOR_MAP_DATA_TYPE_UINT64, 2, const_cast<void*>(base), dims, strides, box, estr,
-                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 gls_status fused_level_fit(gls_ctx* ctx, const LevelPass1Args& args, bool in_half, bool half, NlfScratch s,
