@@ -572,12 +572,14 @@ def main(argv=None):
     # ---- end to end through the host-buffer entry point ----
     e2e = None
     if not args.no_e2e and not args.profile_only:
+        # the host product is RGB8, as the reference's demosaicImage + convertToRGBImage give it
+        # (raw_converter.cpp:226-237): the alpha byte never crosses to the host
         hosts = [torch.from_numpy(f[0]).pin_memory() for f in frames]
-        houts = [torch.empty((h, w, 4), dtype=torch.uint8).pin_memory() for _ in frames]
+        houts = [torch.empty((h, w, 3), dtype=torch.uint8).pin_memory() for _ in frames]
 
         def host_step():
             batch.demosaic_host_ptr([t.data_ptr() for t in hosts], [(w, h)] * len(frames), params,
-                                    [t.data_ptr() for t in houts], 4)
+                                    [t.data_ptr() for t in houts], 3)
 
         for _ in range(args.warmup):
             host_step()
@@ -589,7 +591,9 @@ def main(argv=None):
         e2e_s = max_over_ranks(time.perf_counter() - t0, world, dev)
         e2e = {"value": round(replica_value(world, mpix_per_step, args.steps, 1e3 * e2e_s), 3), "unit": "MPix/s",
                "h2d_bytes_per_step": int(sum(f[0].nbytes for f in frames)),
-               "d2h_bytes_per_step": int(len(frames) * w * h * 4)}
+               "d2h_bytes_per_step": int(len(frames) * w * h * 3), "output": "rgb8 host buffers",
+               "overlap": "uploads one frame at a time; the final stage in 4 row bands, each copied back "
+                          "while the next band runs"}
         # the same burst from packed 12-bit host frames (an uncompressed DNG strip's layout):
         # the packed bytes cross to the device and are unpacked there
         from climage_gb300 import synthetic
@@ -599,7 +603,7 @@ def main(argv=None):
         def packed_step():
             batch.demosaic_packed_host_ptr([t.data_ptr() for t in packed], [t.numel() for t in packed],
                                            [cfg["bits"]] * len(frames), [(w, h)] * len(frames), params,
-                                           [t.data_ptr() for t in houts], 4)
+                                           [t.data_ptr() for t in houts], 3)
 
         for _ in range(args.warmup):
             packed_step()

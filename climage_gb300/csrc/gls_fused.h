@@ -103,6 +103,14 @@ struct FinalArgs {
     float* tap_mask;
     int tap_pitch;
     const float* strength;  // learned stage: level-0 noise-model multiplier per pixel (or null)
+    int tile_y0;            // first tile row of the launch (set by the launcher: bands of rows)
+};
+
+// Called after each band of output rows [y_begin, y_end) has been launched (the caller
+// enqueues work on the band, e.g. its copy to the host, behind it on the same stream).
+struct FinalBandFn {
+    gls_status (*fn)(void* user, int y_begin, int y_end);
+    void* user;
 };
 
 gls_status fused_raw_fit(gls_ctx* ctx, const RawPass1Args& a, bool half, NlfScratch s, float* out_dev);
@@ -111,7 +119,10 @@ gls_status fused_post_cnn(gls_ctx* ctx, const PostCnnArgs& a, bool half);
 gls_status fused_level_fit(gls_ctx* ctx, const LevelPass1Args& a, bool in_half, bool half, NlfScratch s,
                            float* out_dev);
 gls_status fused_denoise(gls_ctx* ctx, const DenoiseArgs& a, bool in_half, bool half, int algo, bool reasm);
-gls_status fused_final(gls_ctx* ctx, const FinalArgs& a, bool half, int algo, bool ltm, bool out_f32);
+// The final stage over the whole frame, or in `bands` bands of tile rows with band->fn
+// called after each (bands > 1 needs band).
+gls_status fused_final(gls_ctx* ctx, const FinalArgs& a, bool half, int algo, bool ltm, bool out_f32, int bands = 1,
+                       const FinalBandFn* band = nullptr);
 
 }  // namespace gls
 

@@ -740,7 +740,7 @@ __global__ void __launch_bounds__(kT) final_kernel(FinalArgs a) {
     // tile is first written in phase 3
     static_assert(NRAW * sizeof(Tap1) <= sizeof(float4) * EW * EH, "raw table entries overflow the denoised tile");
     Tap1* const s_raw = reinterpret_cast<Tap1*>(s_den);
-    const int x0 = blockIdx.x * FW, y0 = blockIdx.y * FH;
+    const int x0 = blockIdx.x * FW, y0 = (blockIdx.y + a.tile_y0) * FH;
     const int w = a.w, h = a.h;
     const float nx = div_(1.0f, (float)w), ny = div_(1.0f, (float)h);
 
@@ -1146,8 +1146,10 @@ gls_status fused_denoise(gls_ctx* ctx, const DenoiseArgs& a, bool in_half, bool 
 #else
 
 template <int FW, int FH>
-void launch_final(const FinalArgs& a, bool half, int algo, bool ltm, bool out_f32, cudaStream_t st) {
-    const dim3 grid((a.w + FW - 1) / FW, (a.h + FH - 1) / FH);
+void launch_final(const FinalArgs& args, bool half, int algo, bool ltm, bool out_f32, int ty0, int nty, cudaStream_t st) {
+    FinalArgs a = args;
+    a.tile_y0 = ty0;
+    const dim3 grid((a.w + FW - 1) / FW, nty);
 #define GLS_FIN(SS, AL)                                                                          \
     if (ltm) {                                                                                   \
         if (out_f32) final_kernel<SS, AL, true, true, FW, FH><<<grid, kT, 0, st>>>(a);           \
@@ -1166,24 +1168,39 @@ void launch_final(const FinalArgs& a, bool half, int algo, bool ltm, bool out_f3
 
 // The bilateral path with the local tone mapping has three shapes (three, two and four
 // positions per thread): 0: 32x24, 1: 32x16, 2: 64x16; the other forms keep 32x24.
-void launch_final_shape(int shape, const FinalArgs& a, bool half, int algo, bool ltm, bool out_f32, cudaStream_t st) {
-    if (shape == 0 || algo != 0 || !ltm) launch_final<32, 24>(a, half, algo, ltm, out_f32, st);
-    else if (shape == 1) launch_final<32, 16>(a, half, 0, true, out_f32, st);
-    else launch_final<64, 16>(a, half, 0, true, out_f32, st);
+int final_shape_h(int shape, int algo, bool ltm) { return (shape == 0 || algo != 0 || !ltm) ? 24 : 16; }
+
+// tile rows [ty0, ty0 + nty) of shape `shape` (nty < 0: the whole frame)
+void launch_final_shape(int shape, const FinalArgs& a, bool half, int algo, bool ltm, bool out_f32, int ty0, int nty,
+                        cudaStream_t st) {
+    if (nty < 0) nty = (a.h + final_shape_h(shape, algo, ltm) - 1) / final_shape_h(shape, algo, ltm);
+    if (shape == 0 || algo != 0 || !ltm) launch_final<32, 24>(a, half, algo, ltm, out_f32, ty0, nty, st);
+    else if (shape == 1) launch_final<32, 16>(a, half, 0, true, out_f32, ty0, nty, st);
+    else launch_final<64, 16>(a, half, 0, true, out_f32, ty0, nty, st);
 }
 
-gls_status fused_final(gls_ctx* ctx, const FinalArgs& a, bool half, int algo, bool ltm, bool out_f32) {
+gls_status fused_final(gls_ctx* ctx, const FinalArgs& a, bool half, int algo, bool ltm, bool out_f32, int bands,
+                       const FinalBandFn* band) {
     // the staged tiles are sized for the pyramid's levels 1 and 3
     if (a.cw != a.w >> 1 || a.ch != a.h >> 1 || (ltm && (a.gw != a.w >> 3 || a.gh != a.h >> 3)))
         return set_error(ctx, GLS_ERR_INVALID_SIZE, "final stage: levels 1 and 3 must be the pyramid's");
+    if (bands > 1 && !band) return set_error(ctx, GLS_ERR_INVALID_ARGUMENT, "final stage: bands without a callback");
     int shape = 0;
     if (algo == 0 && ltm) {
         const TuneKey key{kTuneFinal, a.w, a.h, (half ? 1 : 0) | (out_f32 ? 2 : 0)};
-        shape = tune_choose(ctx, key, [&](int v) { launch_final_shape(v, a, half, algo, ltm, out_f32, ctx->stream); });
+        shape = tune_choose(ctx, key, [&](int v) { launch_final_shape(v, a, half, algo, ltm, out_f32, 0, -1, ctx->stream); });
     }
-    launch_final_shape(shape, a, half, algo, ltm, out_f32, ctx->stream);
-    ctx->launches++;
-    return check_launch(ctx, "final (fused)");
+    const int fh = final_shape_h(shape, algo, ltm), tiles_y = (a.h + fh - 1) / fh;
+    if (bands < 1) bands = 1;
+    if (bands > tiles_y) bands = tiles_y;
+    for (int b = 0; b < bands; b++) {
+        const int ty0 = (int)((long)tiles_y * b / bands), ty1 = (int)((long)tiles_y * (b + 1) / bands);
+        launch_final_shape(shape, a, half, algo, ltm, out_f32, ty0, ty1 - ty0, ctx->stream);
+        ctx->launches++;
+        GLS_CHECK(check_launch(ctx, "final (fused)"));
+        if (band) GLS_CHECK(band->fn(band->user, ty0 * fh, ty1 * fh < a.h ? ty1 * fh : a.h));
+    }
+    return GLS_OK;
 }
 
 #endif  // GLS_FUSED_FINAL_TU

@@ -43,9 +43,10 @@ __global__ void tap_copy_kernel(const void* src, bool half, int channels, int w,
     }
 }
 
-__global__ void rgba8_to_rgb8_kernel(const uchar4* in, int w, int h, uint8_t* out) {
-    const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
-    if (x >= w || y >= h) return;
+// rows [y0, y1) of an RGBA8 frame packed to RGB8
+__global__ void rgba8_to_rgb8_kernel(const uchar4* in, int w, int y0, int y1, uint8_t* out) {
+    const int x = blockIdx.x * 32 + threadIdx.x, y = y0 + blockIdx.y * 8 + threadIdx.y;
+    if (x >= w || y >= y1) return;
     const uchar4 p = in[(size_t)y * w + x];
     uint8_t* o = out + ((size_t)y * w + x) * 3;
     o[0] = p.x;
@@ -111,6 +112,15 @@ struct gls_raw_converter {
 
     // level 0 of the pyramid in binary16 (the fused path: the despeckle output is binary16)
     ImgRef level0{};
+    // host-buffer conversions: where the final stage's row bands are copied (out null: none)
+    struct HostBand {
+        uint8_t* out = nullptr;
+        int channels = 4, w = 0, h = 0;
+        int bands = 0;  // bands whose copies were enqueued
+    } host_band;
+    static constexpr int kHostBands = 4;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t band_ev[kHostBands + 1] = {};  // after each band's launch; [kHostBands]: the last copy
     bool staged_alloc = false, high_noise_alloc = false;
 
     // Working images are allocated for a capacity (the largest frame, deepest pyramid seen so
@@ -471,7 +481,12 @@ struct gls_raw_converter {
         f.tap_pitch = w;
         f.strength = learned ? strength : nullptr;
         const int algo0 = (algo == GLS_DENOISE_GUIDED_FAST) ? 1 : 0;
-        GLS_CHECK(fused_final(ctx, f, half, algo0, rc.localToneMapping != 0, out_float));
+        if (host_band.out && !out_float && out == out_dev) {
+            const FinalBandFn band{&gls_raw_converter::copy_rows_cb, this};
+            GLS_CHECK(fused_final(ctx, f, half, algo0, rc.localToneMapping != 0, false, kHostBands, &band));
+        } else {
+            GLS_CHECK(fused_final(ctx, f, half, algo0, rc.localToneMapping != 0, out_float));
+        }
         mark("denoise L0+LTM+sRGB");
         collect();
         return GLS_OK;
@@ -591,11 +606,24 @@ struct gls_raw_converter {
     }
 
     // host raw in, host RGBA8/RGB8 out, all on this converter's stream (no synchronisation)
+    // after / copied: a burst's uploads go one at a time (each waits for the previous frame's
+    // copy), so the first frame's kernels start after one copy rather than after all of them
+    gls_status upload_order(cudaEvent_t after) {
+        if (!after) return GLS_OK;
+        return check_cuda(ctx, cudaStreamWaitEvent(ctx->stream, after, 0), "cudaStreamWaitEvent(upload)");
+    }
+    gls_status upload_done(cudaEvent_t copied) {
+        if (!copied) return GLS_OK;
+        return check_cuda(ctx, cudaEventRecord(copied, ctx->stream), "cudaEventRecord(upload)");
+    }
+
     gls_status run_host(const uint16_t* raw, int fw, int fh, int stride, gls_demosaic_params* p, uint8_t* out,
-                        int out_channels) {
+                        int out_channels, cudaEvent_t after = nullptr, cudaEvent_t copied = nullptr) {
         GLS_CHECK(ensure_staging(fw, fh));
+        GLS_CHECK(upload_order(after));
         GLS_CHECK(check_cuda(ctx, cudaMemcpy2DAsync(raw_dev, (size_t)fw * 2, raw, (size_t)stride * 2, (size_t)fw * 2,
                                                     fh, cudaMemcpyHostToDevice, ctx->stream), "copy raw frame"));
+        GLS_CHECK(upload_done(copied));
         return finish_host(fw, fh, p, out, out_channels);
     }
 
@@ -604,7 +632,8 @@ struct gls_raw_converter {
     // unpacked there into the staging frame (unpack12BitsInto16Bits and
     // unpack14BitsInto16Bits, src/gls_image_tiff.cpp:53-87)
     gls_status run_packed_host(const uint8_t* packed, size_t n_bytes, int bits, int fw, int fh,
-                               gls_demosaic_params* p, uint8_t* out, int out_channels) {
+                               gls_demosaic_params* p, uint8_t* out, int out_channels, cudaEvent_t after = nullptr,
+                               cudaEvent_t copied = nullptr) {
         GLS_CHECK(ensure_staging(fw, fh));
         if (packed_dev_bytes < n_bytes) {
             if (packed_dev) cudaFree(packed_dev);
@@ -613,26 +642,68 @@ struct gls_raw_converter {
             GLS_CHECK(check_cuda(ctx, cudaMalloc(&packed_dev, n_bytes), "cudaMalloc(packed raw)"));
             packed_dev_bytes = n_bytes;
         }
+        GLS_CHECK(upload_order(after));
         GLS_CHECK(check_cuda(ctx, cudaMemcpyAsync(packed_dev, packed, n_bytes, cudaMemcpyHostToDevice, ctx->stream),
                              "copy packed raw frame"));
+        GLS_CHECK(upload_done(copied));
         launch_unpack(ctx, packed_dev, n_bytes, bits, raw_dev, (size_t)fw * fh);
         return finish_host(fw, fh, p, out, out_channels);
     }
 
-    // the staged raw frame through the pipeline, RGBA8 (or RGB8) back to the host
+    // The host product of the final stage's rows [y0, y1): packed to RGB8 when asked and copied
+    // back on the converter's copy stream, which waits only for the rows' own launch, so the
+    // copy runs while the next band's kernel does.
+    gls_status ensure_copy_stream() {
+        if (copy_stream) return GLS_OK;
+        GLS_CHECK(check_cuda(ctx, cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking), "cudaStreamCreate(copy)"));
+        for (int k = 0; k <= kHostBands; k++)
+            GLS_CHECK(check_cuda(ctx, cudaEventCreateWithFlags(&band_ev[k], cudaEventDisableTiming), "cudaEventCreate(band)"));
+        return GLS_OK;
+    }
+    gls_status copy_rows(int y0, int y1, cudaStream_t st) {
+        const int fw = host_band.w, ch = host_band.channels;
+        const uint8_t* src = out_dev + (size_t)y0 * fw * 4;
+        if (ch == 3) {
+            uint8_t* rgb = out_dev + (size_t)fw * host_band.h * 4;
+            rgba8_to_rgb8_kernel<<<dim3((fw + 31) / 32, (y1 - y0 + 7) / 8), dim3(32, 8), 0, st>>>(
+                (const uchar4*)out_dev, fw, y0, y1, rgb);
+            ctx->launches++;
+            src = rgb + (size_t)y0 * fw * 3;
+        }
+        return check_cuda(ctx, cudaMemcpyAsync(host_band.out + (size_t)y0 * fw * ch, src, (size_t)(y1 - y0) * fw * ch,
+                                               cudaMemcpyDeviceToHost, st), "copy output rows");
+    }
+    static gls_status copy_rows_cb(void* self, int y0, int y1) {
+        gls_raw_converter* c = static_cast<gls_raw_converter*>(self);
+        const int k = c->host_band.bands++;
+        if (k >= kHostBands) return set_error(c->ctx, GLS_ERR_INVALID_ARGUMENT, "more output bands than events");
+        GLS_CHECK(check_cuda(c->ctx, cudaEventRecord(c->band_ev[k], c->ctx->stream), "cudaEventRecord(band)"));
+        GLS_CHECK(check_cuda(c->ctx, cudaStreamWaitEvent(c->copy_stream, c->band_ev[k], 0), "cudaStreamWaitEvent(band)"));
+        return c->copy_rows(y0, y1, c->copy_stream);
+    }
+
+    // the staged raw frame through the pipeline, RGBA8 (or RGB8) back to the host: the fused
+    // schedule runs its final stage in row bands whose copies overlap the following bands'
+    // kernels (the converter's stream then waits for the last copy); the other schedules copy
+    // the whole frame at the end
     gls_status finish_host(int fw, int fh, gls_demosaic_params* p, uint8_t* out, int out_channels) {
         GLS_CHECK(ensure(fw, fh, p->pyramid_levels, p->storage != GLS_STORAGE_F32));
-        GLS_CHECK(run(raw_dev, fw, p, out_dev, false, fw));
-        const void* src = out_dev;
-        if (out_channels == 3) {
-            uint8_t* rgb = out_dev + (size_t)fw * fh * 4;
-            rgba8_to_rgb8_kernel<<<dim3((fw + 31) / 32, (fh + 7) / 8), dim3(32, 8), 0, ctx->stream>>>(
-                (const uchar4*)out_dev, fw, fh, rgb);
-            ctx->launches++;
-            src = rgb;
+        GLS_CHECK(ensure_copy_stream());
+        host_band = HostBand{out, out_channels, fw, fh, 0};
+        const gls_status s = run(raw_dev, fw, p, out_dev, false, fw);
+        const int bands = host_band.bands;
+        if (bands > 0) {
+            GLS_CHECK(check_cuda(ctx, cudaEventRecord(band_ev[kHostBands], copy_stream), "cudaEventRecord(copied)"));
+            GLS_CHECK(check_cuda(ctx, cudaStreamWaitEvent(ctx->stream, band_ev[kHostBands], 0), "cudaStreamWaitEvent(copied)"));
         }
-        return check_cuda(ctx, cudaMemcpyAsync(out, src, (size_t)fw * fh * out_channels, cudaMemcpyDeviceToHost,
-                                               ctx->stream), "copy output");
+        GLS_CHECK(s);
+        if (bands > 0) {
+            host_band = HostBand{};
+            return GLS_OK;
+        }
+        const gls_status c = copy_rows(0, fh, ctx->stream);
+        host_band = HostBand{};
+        return c;
     }
 
     gls_status fetch_noise_model(gls_demosaic_params* p) {
@@ -686,6 +757,12 @@ gls_status gls_raw_converter_destroy(gls_raw_converter* c) {
     if (c->out_dev) cudaFree(c->out_dev);
     if (c->packed_dev) cudaFree(c->packed_dev);
     if (c->cnn) gls_cnn_destroy(c->cnn);
+    if (c->copy_stream) {
+        cudaStreamSynchronize(c->copy_stream);
+        cudaStreamDestroy(c->copy_stream);
+    }
+    for (cudaEvent_t e : c->band_ev)
+        if (e) cudaEventDestroy(e);
     delete c;
     return GLS_OK;
 }
@@ -873,6 +950,7 @@ struct gls_raw_batch {
     std::vector<gls_raw_converter*> lane;
     cudaEvent_t fork = nullptr;
     std::vector<cudaEvent_t> join;
+    std::vector<cudaEvent_t> copied;  // per lane: its latest host-to-device copy
     std::vector<int> lane_of;
 };
 
@@ -960,6 +1038,7 @@ gls_status gls_raw_batch_destroy(gls_raw_batch* b) {
         if (b->lane_ctx[l]) gls_ctx_destroy(b->lane_ctx[l]);
         if (b->lane_stream[l]) cudaStreamDestroy(b->lane_stream[l]);
         if (b->join[l]) cudaEventDestroy(b->join[l]);
+        if (b->copied[l]) cudaEventDestroy(b->copied[l]);
     }
     if (b->fork) cudaEventDestroy(b->fork);
     delete b;
@@ -976,6 +1055,7 @@ gls_status gls_raw_batch_create(gls_ctx* ctx, int lanes, gls_raw_batch** out) {
     b->lane_stream.assign(lanes, nullptr);
     b->lane.assign(lanes, nullptr);
     b->join.assign(lanes, nullptr);
+    b->copied.assign(lanes, nullptr);
     gls_status s = check_cuda(ctx, cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming), "cudaEventCreate");
     for (int l = 0; l < lanes && s == GLS_OK; l++) {
         s = gls_ctx_create(ctx->device, &b->lane_ctx[l]);
@@ -987,6 +1067,8 @@ gls_status gls_raw_batch_create(gls_ctx* ctx, int lanes, gls_raw_batch** out) {
         if (s != GLS_OK) break;
         b->lane_ctx[l]->stream = b->lane_stream[l];
         s = check_cuda(ctx, cudaEventCreateWithFlags(&b->join[l], cudaEventDisableTiming), "cudaEventCreate");
+        if (s != GLS_OK) break;
+        s = check_cuda(ctx, cudaEventCreateWithFlags(&b->copied[l], cudaEventDisableTiming), "cudaEventCreate");
         if (s != GLS_OK) break;
         s = gls_raw_converter_create(b->lane_ctx[l], &b->lane[l]);
         if (s != GLS_OK) batch_error(b, l, s);
@@ -1072,8 +1154,9 @@ gls_status gls_raw_batch_demosaic_host(gls_raw_batch* b, int n, const uint16_t* 
     for (int i = 0; i < n; i++) {
         const int l = b->lane_of[i];
         gls_demosaic_params p = params[i];
-        const gls_status s =
-            b->lane[l]->run_host(raws[i], widths[i], heights[i], raw_strides[i], &p, outs[i], out_channels);
+        const gls_status s = b->lane[l]->run_host(raws[i], widths[i], heights[i], raw_strides[i], &p, outs[i],
+                                                  out_channels, i > 0 ? b->copied[b->lane_of[i - 1]] : nullptr,
+                                                  b->copied[l]);
         if (s != GLS_OK) return batch_error(b, l, s);
     }
     GLS_CHECK(batch_join(b, l0));
@@ -1104,7 +1187,8 @@ gls_status gls_raw_batch_demosaic_packed_host(gls_raw_batch* b, int n, const uin
         const int l = b->lane_of[i];
         gls_demosaic_params p = params[i];
         const gls_status s = b->lane[l]->run_packed_host(packed[i], n_bytes[i], bits[i], widths[i], heights[i], &p,
-                                                         outs[i], out_channels);
+                                                         outs[i], out_channels,
+                                                         i > 0 ? b->copied[b->lane_of[i - 1]] : nullptr, b->copied[l]);
         if (s != GLS_OK) return batch_error(b, l, s);
     }
     GLS_CHECK(batch_join(b, l0));
