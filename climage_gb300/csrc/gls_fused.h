@@ -69,6 +69,36 @@ struct LevelPass1Args {
     int tma;         // the input's tensor map is valid (set by the launcher)
 };
 
+// Levels 1 .. L-1 of the pyramid's statistics in one launch (pyramid_stats_kernel): level p
+// of the launch is image level p + 1.
+struct PyrLevel {
+    const void* in;  // the level's image
+    int w, h, pitch;
+    void* out;  // the next level (null for the coarsest)
+    int ow, oh, opitch;
+    int tiles_x, first, count;  // its 32x32 tiles: work items [first, first + count)
+    NlfScratch nlf;              // its regression scratch (one per level: the fits run together)
+    float* nlf_out;              // fitted {A0..2, B0..2}
+    unsigned* done;              // per tile: the launch's mark once its downsampled block is written
+};
+// Device-side state of the launch, zero when first allocated; the last block to leave resets
+// the queue and advances the mark, so a captured graph can replay the launch.
+struct PyrCtl {
+    unsigned queue;  // next work item
+    unsigned exits;  // blocks that have left the work loop
+    unsigned mark;   // this launch's tiles are marked mark + 1
+    unsigned pad;
+    unsigned flushed[GLS_MAX_LEVELS];  // per level: tiles whose sums have reached the totals
+};
+struct PyramidArgs {
+    PyrLevel lv[GLS_MAX_LEVELS - 1];
+    int nlev, items;
+    NlfThresholds th;
+    int stats_half;
+    PyrCtl* ctl;
+    int tma;  // the first level's tensor map is valid
+};
+
 struct DenoiseArgs {
     const void* in;
     int w, h, pitch;
@@ -118,6 +148,7 @@ gls_status fused_demosaic(gls_ctx* ctx, const DemosaicArgs& a, bool raw_u16, boo
 gls_status fused_post_cnn(gls_ctx* ctx, const PostCnnArgs& a, bool half);
 gls_status fused_level_fit(gls_ctx* ctx, const LevelPass1Args& a, bool in_half, bool half, NlfScratch s,
                            float* out_dev);
+gls_status fused_pyramid_stats(gls_ctx* ctx, const PyramidArgs& a, bool half);
 gls_status fused_denoise(gls_ctx* ctx, const DenoiseArgs& a, bool in_half, bool half, int algo, bool reasm);
 // The final stage over the whole frame, or in `bands` bands of tile rows with band->fn
 // called after each (bands > 1 needs band).

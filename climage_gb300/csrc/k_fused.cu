@@ -470,6 +470,93 @@ __global__ void __launch_bounds__(kT) post_cnn_kernel(PostCnnArgs a) {
 // =========================================================================================
 constexpr int LT = 32;
 constexpr int LP = LT + 4;
+// downsampleImage's taps for a tile's 16 output columns and rows ([0] at -0.5 output pixel, [1]
+// at +0.5: downsample_px's px -+ sx), relative to the staged region; threads 0..63 of the block
+// (the same float operations as downsample_px's coordinates and tap1, once per column and row)
+GLS_DI void level_tables(int x0, int y0, int w, int h, int ow, int oh, TabTap (*s_tx)[LT / 2], TabTap (*s_ty)[LT / 2]) {
+    if (threadIdx.x >= 2 * LT) return;
+    const int e = threadIdx.x & (LT - 1), k = e >> 4, o = e & 15;
+    if (threadIdx.x < LT) {
+        const float n = div_(1.0f, (float)ow);
+        const float pc = ((float)(x0 / 2 + o) + 0.5f) * n, sh = 0.5f * n;
+        s_tx[k][o] = tab_tap(tap1(k ? pc + sh : pc + -sh, w), w, x0 - 2, LP, 1);
+    } else {
+        const float n = div_(1.0f, (float)oh);
+        const float pc = ((float)(y0 / 2 + o) + 0.5f) * n, sh = 0.5f * n;
+        s_ty[k][o] = tab_tap(tap1(k ? pc + sh : pc + -sh, h), h, y0 - 2, LP, LP);
+    }
+}
+
+// One 32x32 tile from its staged 36x36 region (fp32, origin (x0 - 2, y0 - 2)): the
+// noiseStatistics of its pixels added to acc, and its 16x16 downsampled block written to out
+// (when out is not null).
+template <class SOut>
+GLS_DI void level_tile(const float4* s_in, const TabTap (*s_tx)[LT / 2], const TabTap (*s_ty)[LT / 2], int x0, int y0,
+                       int w, int h, void* out, int ow, int oh, int opitch, const NlfThresholds& th, int stats_half,
+                       LevelPass1Acc2& acc) {
+    const int col = threadIdx.x & 31, row0 = (threadIdx.x >> 5) * 4;
+    // window sums for pixels (x0 + col, y0 + row0 + j), j = 0..3: (s0, s1), (q0, q1) and
+    // (s2, q2) as packed pairs, every window summed in the reference's row-major order
+    float2 s01[4], q01[4], s2q2[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) s01[j] = q01[j] = s2q2[j] = f2(0.0f, 0.0f);
+#pragma unroll
+    for (int rr = 0; rr < 8; rr++) {
+#pragma unroll
+        for (int dx = 0; dx < 5; dx++) {
+            const float4 v = s_in[(row0 + rr) * LP + col + dx];
+            const float2 a01 = f2(v.x, v.y);
+            const float2 p01 = mul2s(a01, a01);  // summed: scalar multiplies
+            const float2 z = f2(v.z, __fmul_rn(v.z, v.z));
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                if (rr - j >= 0 && rr - j <= 4) {
+                    s01[j] = add2(s01[j], a01);
+                    q01[j] = add2(q01[j], p01);
+                    s2q2[j] = add2(s2q2[j], z);
+                }
+            }
+        }
+    }
+    const FastDiv d25 = div25();
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        const int x = x0 + col, y = y0 + row0 + j;
+        if (x < w && y < h) {
+            // noiseStatistics (demosaic.cl:1267-1286): mean Y = s0 / 25, var_k = (q_k - s_k^2 / 25) / 25
+            const float2 mt = div25_x2<true>(f2(s01[j].x, s2q2[j].x * s2q2[j].x));  // (mean Y, s2^2 / 25)
+            float2 v01 = div25_x2<true>(sub2(q01[j], div25_x2<true>(mul2(s01[j], s01[j]))));
+            float v2 = d25(s2q2[j].y - mt.y), my = mt.x;
+            if (stats_half) {  // the statistics as the reference's fp16 build stores them
+                v01 = __half22float2(__float22half2_rn(v01));
+                v2 = glsm::round_half(v2);
+                my = glsm::round_half(my);
+            }
+            const float m[1] = {my}, v[3] = {v01.x, v01.y, v2};
+            if (in_range<1, 3>(m, v, th)) acc.add_selected(my, v01, v2);
+        }
+    }
+    // downsample: the coarse 16x16 block under this tile, from the staged region through the
+    // tap tables (downsample_px's samples and their average, bit for bit)
+    if (out) {
+        const int oc = threadIdx.x & 15, orow = threadIdx.x >> 4;
+        const int ox = x0 / 2 + oc, oy = y0 / 2 + orow;
+        if (ox < ow && oy < oh) {
+            const float4 t0 = tab_sample4(s_in, s_tx[0][oc], s_ty[0][orow]);
+            const float4 t1 = tab_sample4(s_in, s_tx[1][oc], s_ty[0][orow]);
+            const float4 t2 = tab_sample4(s_in, s_tx[0][oc], s_ty[1][orow]);
+            const float4 t3 = tab_sample4(s_in, s_tx[1][oc], s_ty[1][orow]);
+            float4 d;
+            d.x = 0.25f * (t0.x + t1.x + t2.x + t3.x);
+            d.y = 0.25f * (t0.y + t1.y + t2.y + t3.y);
+            d.z = 0.25f * (t0.z + t1.z + t2.z + t3.z);
+            d.w = 0.25f * (t0.w + t1.w + t2.w + t3.w);
+            typedef typename Storage<SOut>::T4 TOut;
+            Storage<SOut>::st4((TOut*)out + (size_t)oy * opitch + ox, d);
+        }
+    }
+}
+
 template <class SIn, class SOut>
 __global__ void __launch_bounds__(kT, 3) level_pass1_kernel(LevelPass1Args a, const __grid_constant__ CUtensorMap tmap) {
     typedef typename Storage<SIn>::T4 TIn;
@@ -478,15 +565,11 @@ __global__ void __launch_bounds__(kT, 3) level_pass1_kernel(LevelPass1Args a, co
     __shared__ __align__(128) TIn s_stage[2][LP * LP];  // the tile's region as stored
     __shared__ __align__(16) float4 s_wide[HALF_IN ? LP * LP : 1];  // a binary16 region widened
     __shared__ __align__(8) uint64_t s_bar[2];
-    // downsampleImage's taps for the tile's 16 output columns and rows: [0] at -0.5 output
-    // pixel, [1] at +0.5 (downsample_px's px -+ sx), relative to the staged tile
-    __shared__ TabTap s_tx[2][LT / 2], s_ty[2][LT / 2];
+    __shared__ TabTap s_tx[2][LT / 2], s_ty[2][LT / 2];  // downsampleImage's taps (level_tables)
     LevelPass1Acc2 acc;
     acc.init();
     const TIn* in = (const TIn*)a.in;
-    const GImg4<SIn> gin{in, a.w, a.h, a.pitch};
     const int tiles_x = (a.w + LT - 1) / LT, tiles_y = (a.h + LT - 1) / LT, ntiles = tiles_x * tiles_y;
-    const int col = threadIdx.x & 31, row0 = (threadIdx.x >> 5) * 4;
     const uint32_t bar0 = (uint32_t)__cvta_generic_to_shared(&s_bar[0]);
     const uint32_t stage0 = (uint32_t)__cvta_generic_to_shared(&s_stage[0][0]);
     if (threadIdx.x == 0 && a.tma) {
@@ -534,20 +617,7 @@ __global__ void __launch_bounds__(kT, 3) level_pass1_kernel(LevelPass1Args a, co
                 stage[i] = in[(size_t)gy * a.pitch + gx];
             }
         }
-        if (a.out && threadIdx.x < 2 * LT) {
-            // the same float operations as downsample_px's coordinates and tap1, once per
-            // column (threads 0..31) and row (32..63)
-            const int e = threadIdx.x & (LT - 1), k = e >> 4, o = e & 15;
-            if (threadIdx.x < LT) {
-                const float n = div_(1.0f, (float)a.ow);
-                const float pc = ((float)(x0 / 2 + o) + 0.5f) * n, sh = 0.5f * n;
-                s_tx[k][o] = tab_tap(tap1(k ? pc + sh : pc + -sh, a.w), a.w, x0 - 2, LP, 1);
-            } else {
-                const float n = div_(1.0f, (float)a.oh);
-                const float pc = ((float)(y0 / 2 + o) + 0.5f) * n, sh = 0.5f * n;
-                s_ty[k][o] = tab_tap(tap1(k ? pc + sh : pc + -sh, a.h), a.h, y0 - 2, LP, LP);
-            }
-        }
+        if (a.out) level_tables(x0, y0, a.w, a.h, a.ow, a.oh, s_tx, s_ty);
         __syncthreads();
         if constexpr (HALF_IN) {
             for (int i = threadIdx.x; i < LP * LP; i += kT) s_wide[i] = Storage<__half>::cvt(stage[i]);
@@ -559,66 +629,7 @@ __global__ void __launch_bounds__(kT, 3) level_pass1_kernel(LevelPass1Args a, co
         const int tn = t + gridDim.x;
         pending = tn < ntiles && by_tma(tn);
         if (pending && threadIdx.x == 0) issue(tn, buf ^ 1);
-        // window sums for pixels (x0 + col, y0 + row0 + j), j = 0..3: (s0, s1), (q0, q1) and
-        // (s2, q2) as packed pairs, every window summed in the reference's row-major order
-        float2 s01[4], q01[4], s2q2[4];
-#pragma unroll
-        for (int j = 0; j < 4; j++) s01[j] = q01[j] = s2q2[j] = f2(0.0f, 0.0f);
-#pragma unroll
-        for (int rr = 0; rr < 8; rr++) {
-#pragma unroll
-            for (int dx = 0; dx < 5; dx++) {
-                const float4 v = s_in[(row0 + rr) * LP + col + dx];
-                const float2 a01 = f2(v.x, v.y);
-                const float2 p01 = mul2s(a01, a01);  // summed: scalar multiplies
-                const float2 z = f2(v.z, __fmul_rn(v.z, v.z));
-#pragma unroll
-                for (int j = 0; j < 4; j++) {
-                    if (rr - j >= 0 && rr - j <= 4) {
-                        s01[j] = add2(s01[j], a01);
-                        q01[j] = add2(q01[j], p01);
-                        s2q2[j] = add2(s2q2[j], z);
-                    }
-                }
-            }
-        }
-        const FastDiv d25 = div25();
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-            const int x = x0 + col, y = y0 + row0 + j;
-            if (x < a.w && y < a.h) {
-                // noiseStatistics (demosaic.cl:1267-1286): mean Y = s0 / 25, var_k = (q_k - s_k^2 / 25) / 25
-                const float2 mt = div25_x2<true>(f2(s01[j].x, s2q2[j].x * s2q2[j].x));  // (mean Y, s2^2 / 25)
-                float2 v01 = div25_x2<true>(sub2(q01[j], div25_x2<true>(mul2(s01[j], s01[j]))));
-                float v2 = d25(s2q2[j].y - mt.y), my = mt.x;
-                if (a.stats_half) {  // the statistics as the reference's fp16 build stores them
-                    v01 = __half22float2(__float22half2_rn(v01));
-                    v2 = glsm::round_half(v2);
-                    my = glsm::round_half(my);
-                }
-                const float m[1] = {my}, v[3] = {v01.x, v01.y, v2};
-                if (in_range<1, 3>(m, v, a.th)) acc.add_selected(my, v01, v2);
-            }
-        }
-        // downsample: the coarse 16x16 tile under this fine tile, from the staged tile through
-        // the tap tables (downsample_px's samples and their average, bit for bit)
-        if (a.out) {
-            const int oc = threadIdx.x & 15, orow = threadIdx.x >> 4;
-            const int ox = x0 / 2 + oc, oy = y0 / 2 + orow;
-            if (ox < a.ow && oy < a.oh) {
-                const float4 t0 = tab_sample4(s_in, s_tx[0][oc], s_ty[0][orow]);
-                const float4 t1 = tab_sample4(s_in, s_tx[1][oc], s_ty[0][orow]);
-                const float4 t2 = tab_sample4(s_in, s_tx[0][oc], s_ty[1][orow]);
-                const float4 t3 = tab_sample4(s_in, s_tx[1][oc], s_ty[1][orow]);
-                float4 d;
-                d.x = 0.25f * (t0.x + t1.x + t2.x + t3.x);
-                d.y = 0.25f * (t0.y + t1.y + t2.y + t3.y);
-                d.z = 0.25f * (t0.z + t1.z + t2.z + t3.z);
-                d.w = 0.25f * (t0.w + t1.w + t2.w + t3.w);
-                typedef typename Storage<SOut>::T4 TOut;
-                Storage<SOut>::st4((TOut*)a.out + (size_t)oy * a.opitch + ox, d);
-            }
-        }
+        level_tile<SOut>(s_in, s_tx, s_ty, x0, y0, a.w, a.h, a.out, a.ow, a.oh, a.opitch, a.th, a.stats_half, acc);
         // this tile's buffers may next be written by the async proxy (a TMA copy)
         asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
         __syncthreads();
@@ -626,6 +637,194 @@ __global__ void __launch_bounds__(kT, 3) level_pass1_kernel(LevelPass1Args a, co
     Pass1Acc<1, 3> out;
     acc.unpack(out);
     pass1_epilogue<1, 3>(out, a.nlf, a.nlf_out);
+}
+
+// =========================================================================================
+// pyramid_stats: levels 1 .. L-1 of the pyramid (statistics, regression sums, downsample to
+// the next level) in one launch.  Blocks take 32x32 tiles from a work queue ordered by level
+// (an atomic counter); a tile of level p >= 2 first waits (bounded) for the tiles of level
+// p - 1 whose downsampled blocks its 36x36 region reads, which were all taken from the queue
+// before it by running blocks, so every wait ends.  A block keeps the sums of one level at a
+// time and adds them to that level's totals when it moves to another level or leaves; the
+// block whose addition completes a level's tile count solves that level's fit.  Level 1 was
+// written by the previous launch and comes in by TMA (the next item's region while the
+// current one is summed); the later levels are read through L2 (ld.global.cg).
+// =========================================================================================
+constexpr uint32_t kPyrWaitPolls = 1u << 20;  // bound of a dependency wait (polls of ~0.1-1 us)
+
+GLS_DI unsigned ld_acquire_u32(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+// a pixel through L2 only (ld.global.cg): data written by other blocks of the same launch
+GLS_DI float4 ld_cg(const float4* p) { return __ldcg(p); }
+GLS_DI half4 ld_cg(const half4* p) {
+    const uint2 u = __ldcg(reinterpret_cast<const uint2*>(p));
+    half4 h;
+    *reinterpret_cast<uint2*>(&h) = u;
+    return h;
+}
+GLS_DI void st_release_u32(unsigned* p, unsigned v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;\n" ::"l"(p), "r"(v) : "memory");
+}
+
+template <class S>
+__global__ void __launch_bounds__(kT, 3) pyramid_stats_kernel(const __grid_constant__ PyramidArgs a,
+                                                               const __grid_constant__ CUtensorMap tmap) {
+    typedef typename Storage<S>::T4 T4;
+    constexpr bool HALF = sizeof(T4) == 8;
+    constexpr uint32_t kStageBytes = LP * LP * sizeof(T4);
+    __shared__ __align__(128) T4 s_stage[2][LP * LP];
+    __shared__ __align__(16) float4 s_wide[HALF ? LP * LP : 1];
+    __shared__ __align__(8) uint64_t s_bar[2];
+    __shared__ TabTap s_tx[2][LT / 2], s_ty[2][LT / 2];
+    __shared__ int s_item, s_flag;
+    __shared__ unsigned s_mark;
+    const uint32_t bar0 = (uint32_t)__cvta_generic_to_shared(&s_bar[0]);
+    const uint32_t stage0 = (uint32_t)__cvta_generic_to_shared(&s_stage[0][0]);
+    if (threadIdx.x == 0) {
+        if (a.tma) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar0) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar0 + 8) : "memory");
+            asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        }
+        s_mark = ld_acquire_u32(&a.ctl->mark) + 1u;
+        s_item = (int)atomicAdd(&a.ctl->queue, 1u);
+    }
+    __syncthreads();
+    const unsigned mark = s_mark;
+    auto level_of = [&](int item) {
+        int p = 0;
+        while (p + 1 < a.nlev && item >= a.lv[p + 1].first) p++;
+        return p;
+    };
+    auto by_tma = [&](int item) {  // a level-1 tile inside the image
+        if (!a.tma || item >= a.lv[0].count) return false;
+        const PyrLevel& L = a.lv[0];
+        const int x0 = (item % L.tiles_x) * LT, y0 = (item / L.tiles_x) * LT;
+        return x0 >= 2 && y0 >= 2 && x0 + LT + 2 <= L.w && y0 + LT + 2 <= L.h;
+    };
+    auto issue = [&](int item, int b) {  // thread 0
+        const int x0 = (item % a.lv[0].tiles_x) * LT, y0 = (item / a.lv[0].tiles_x) * LT;
+        tma_issue_2d(stage0 + (uint32_t)b * kStageBytes, &tmap, (x0 - 2) * (int)(sizeof(T4) / 8), y0 - 2,
+                     bar0 + 8u * (uint32_t)b, kStageBytes);
+    };
+    // this block's sums of level `cur` (over `ntiles` of its tiles) to that level's totals, and
+    // the level's solve when they were the last
+    LevelPass1Acc2 acc;
+    acc.init();
+    int cur = -1, ntiles = 0;
+    auto flush = [&]() {
+        const PyrLevel& L = a.lv[cur];
+        Pass1Acc<1, 3> out;
+        acc.unpack(out);
+        out.write_fixed(L.nlf);
+        out.write_minmax(L.nlf);
+        if (threadIdx.x == 0) {
+            __threadfence();
+            s_flag = atomicAdd(&a.ctl->flushed[cur], (unsigned)ntiles) + (unsigned)ntiles == (unsigned)L.count;
+        }
+        __syncthreads();
+        if (s_flag) {
+            __threadfence();
+            solve_fixed<3>(L.nlf, 1, L.nlf_out);
+            if (threadIdx.x == 0) a.ctl->flushed[cur] = 0u;
+        }
+        __syncthreads();
+        acc.init();
+        ntiles = 0;
+    };
+    uint32_t parity = 0;
+    int buf = 0;
+    int item = s_item;
+    bool pending = item < a.items && by_tma(item);
+    if (pending && threadIdx.x == 0) issue(item, 0);
+    bool failed = false;
+    while (item < a.items) {
+        const int p = level_of(item);
+        const PyrLevel& L = a.lv[p];
+        const int t = item - L.first;
+        const int x0 = (t % L.tiles_x) * LT, y0 = (t / L.tiles_x) * LT;
+        if (p != cur) {
+            if (cur >= 0) flush();
+            cur = p;
+        }
+        T4* const stage = s_stage[buf];
+        if (pending) {
+            const uint32_t par = (parity >> buf) & 1u;
+            parity ^= 1u << buf;
+            if (!stage_wait(bar0 + 8u * (uint32_t)buf, par, kStageWaitPolls)) {
+                if (threadIdx.x == 0) atomicOr(L.nlf.err, 1u);
+                stage_wait(bar0 + 8u * (uint32_t)buf, par, kStageWaitPolls);
+                failed = true;
+                break;
+            }
+        } else {
+            if (p >= 1) {
+                // the tiles of level p - 1 whose 16x16 downsampled blocks cover this region
+                const PyrLevel& P = a.lv[p - 1];
+                const int ax0 = max(x0 - 2, 0) >> 4, ax1 = min(x0 + LT + 1, L.w - 1) >> 4;
+                const int by0 = max(y0 - 2, 0) >> 4, by1 = min(y0 + LT + 1, L.h - 1) >> 4;
+                const int na = ax1 - ax0 + 1, nb = by1 - by0 + 1;
+                bool ok = true;
+                if ((int)threadIdx.x < na * nb) {
+                    const unsigned* f = P.done + (by0 + (int)threadIdx.x / na) * P.tiles_x + ax0 + (int)threadIdx.x % na;
+                    uint32_t k = 0;
+                    while (ld_acquire_u32(f) != mark && k < kPyrWaitPolls) {
+                        __nanosleep(64);
+                        k++;
+                    }
+                    ok = k < kPyrWaitPolls;
+                }
+                if (!__syncthreads_and(ok)) {
+                    if (threadIdx.x == 0) atomicOr(L.nlf.err, 2u);
+                    failed = true;
+                    break;
+                }
+            }
+            const T4* in = (const T4*)L.in;
+            for (int i = threadIdx.x; i < LP * LP; i += kT) {
+                const int r = i / LP, c = i - r * LP;
+                const int gx = clampi(x0 - 2 + c, 0, L.w - 1), gy = clampi(y0 - 2 + r, 0, L.h - 1);
+                stage[i] = p == 0 ? in[(size_t)gy * L.pitch + gx] : ld_cg(in + (size_t)gy * L.pitch + gx);
+            }
+        }
+        if (L.out) level_tables(x0, y0, L.w, L.h, L.ow, L.oh, s_tx, s_ty);
+        if (threadIdx.x == 0) s_item = (int)atomicAdd(&a.ctl->queue, 1u);
+        __syncthreads();
+        const int next = s_item;
+        if constexpr (HALF) {
+            for (int i = threadIdx.x; i < LP * LP; i += kT) s_wide[i] = Storage<__half>::cvt(stage[i]);
+            __syncthreads();
+        }
+        const float4* const s_in = HALF ? s_wide : reinterpret_cast<const float4*>(stage);
+        pending = next < a.items && by_tma(next);
+        if (pending && threadIdx.x == 0) issue(next, buf ^ 1);
+        level_tile<S>(s_in, s_tx, s_ty, x0, y0, L.w, L.h, L.out, L.ow, L.oh, L.opitch, a.th, a.stats_half, acc);
+        ntiles++;
+        if (L.out && p + 1 < a.nlev) {
+            // publish the downsampled block to the next level's tiles: the barrier orders the
+            // block's stores before thread 0's release, which is cumulative over them
+            __syncthreads();
+            if (threadIdx.x == 0) st_release_u32(L.done + t, mark);
+        }
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        __syncthreads();
+        item = next;
+        buf ^= 1;
+    }
+    if (cur >= 0 && !failed) flush();
+    // the last block to leave resets the queue and advances the mark for the next launch
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(&a.ctl->exits, 1u) == gridDim.x - 1) {
+            a.ctl->queue = 0u;
+            a.ctl->exits = 0u;
+            __threadfence();
+            st_release_u32(&a.ctl->mark, mark);
+        }
+    }
 }
 
 // =========================================================================================
@@ -1122,6 +1321,33 @@ gls_status fused_level_fit(gls_ctx* ctx, const LevelPass1Args& args, bool in_hal
         nlf_finish<1, 3>(ctx, src, a.w, a.h, s, out_dev);
     }
     return check_launch(ctx, "level statistics (fused)");
+}
+
+gls_status fused_pyramid_stats(gls_ctx* ctx, const PyramidArgs& args, bool half) {
+    PyramidArgs a = args;
+    a.th = nlf_thresholds();
+    CUtensorMap map;
+    memset(&map, 0, sizeof(map));
+    a.tma = level_tensor_map(&map, a.lv[0].in, half ? 8 : 16, a.lv[0].w, a.lv[0].h, a.lv[0].pitch) ? 1 : 0;
+    if (half) {
+        pyramid_stats_kernel<__half><<<resident_grid<pyramid_stats_kernel<__half>>(ctx, a.items), kT, 0, ctx->stream>>>(a, map);
+    } else {
+        pyramid_stats_kernel<float><<<resident_grid<pyramid_stats_kernel<float>>(ctx, a.items), kT, 0, ctx->stream>>>(a, map);
+    }
+    ctx->launches++;
+    GLS_CHECK(check_launch(ctx, "pyramid statistics (fused)"));
+    // the explicit regression passes of every level (they exit at once unless needed)
+    for (int p = 0; p < a.nlev; p++) {
+        const PyrLevel& L = a.lv[p];
+        if (half) {
+            LevelSrc<__half> src{{(const half4*)L.in, L.w, L.h, L.pitch}, a.stats_half != 0};
+            nlf_finish<1, 3>(ctx, src, L.w, L.h, L.nlf, L.nlf_out);
+        } else {
+            LevelSrc<float> src{{(const float4*)L.in, L.w, L.h, L.pitch}, a.stats_half != 0};
+            nlf_finish<1, 3>(ctx, src, L.w, L.h, L.nlf, L.nlf_out);
+        }
+    }
+    return check_launch(ctx, "pyramid statistics (explicit passes)");
 }
 
 gls_status fused_denoise(gls_ctx* ctx, const DenoiseArgs& a, bool in_half, bool half, int algo, bool reasm) {

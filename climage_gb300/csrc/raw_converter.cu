@@ -65,6 +65,9 @@ struct gls_raw_converter {
     ImgRef pyr[GLS_MAX_LEVELS]{}, den[GLS_MAX_LEVELS]{};
     float* nlf_dev = nullptr;  // slot 0: raw {A0..A3, B0..B3}; slot 1+i: level i {A0..A2, B0..B2, -, -}
     void* nlf_scratch = nullptr;
+    void* pyr_state = nullptr;  // PyrCtl, then the per-tile marks of levels 1..cap_L-1
+    // a lane of a multi-lane burst (gls_raw_batch): levels 1.. take one launch each
+    bool overlapped = false;
     void* gf_scratch = nullptr;
     size_t gf_scratch_bytes = 0;
     float* nlf_host = nullptr;  // pinned
@@ -169,10 +172,18 @@ struct gls_raw_converter {
             void* p = nullptr;
             GLS_CHECK(alloc(&p, (1 + GLS_MAX_LEVELS) * 8 * sizeof(float)));
             nlf_dev = (float*)p;
-            GLS_CHECK(alloc(&nlf_scratch, kNlfScratchBytes));
-            // the regression ticket starts at zero; every pass leaves it at zero
-            GLS_CHECK(check_cuda(ctx, cudaMemsetAsync(nlf_scratch, 0, kNlfHeaderBytes, ctx->stream),
+            // one regression scratch for the raw fit, level 0 and the single-stage schedule, and
+            // one per pyramid level for the fused levels 1.. (their fits run in one launch)
+            GLS_CHECK(alloc(&nlf_scratch, kNlfScratchBytes * (1 + GLS_MAX_LEVELS)));
+            // the regression state starts at zero; every pass leaves it at zero
+            GLS_CHECK(check_cuda(ctx, cudaMemsetAsync(nlf_scratch, 0, kNlfScratchBytes * (1 + GLS_MAX_LEVELS), ctx->stream),
                                  "clear regression state"));
+            // the pyramid launch's control block and per-tile marks, zero to start with
+            size_t marks = 0;
+            for (int i = 1; i < nL; i++) marks += (size_t)(((nw >> i) + 31) / 32) * (((nh >> i) + 31) / 32);
+            GLS_CHECK(alloc(&pyr_state, sizeof(PyrCtl) + marks * sizeof(unsigned)));
+            GLS_CHECK(check_cuda(ctx, cudaMemsetAsync(pyr_state, 0, sizeof(PyrCtl) + marks * sizeof(unsigned), ctx->stream),
+                                 "clear pyramid state"));
             gf_scratch = nullptr;
             gf_scratch_bytes = 0;
             cap_w = nw;
@@ -391,23 +402,75 @@ struct gls_raw_converter {
         }
         tap(2, level0, 4);
 
-        // pyramid: noise model of every level, downsampled levels
-        for (int i = 0; i < Lv; i++) {
-            const ImgRef& src = i == 0 ? level0 : pyr[i - 1];
+        // pyramid: level 0's noise model and level 1 (one launch), then the noise models of
+        // levels 1 .. Lv-1 and their downsampled levels (one launch)
+        {
             LevelPass1Args la{};
-            la.in = src.ptr;
-            la.w = src.w;
-            la.h = src.h;
-            la.pitch = src.pitch;
-            if (i < Lv - 1) {
-                la.out = pyr[i].ptr;
-                la.ow = pyr[i].w;
-                la.oh = pyr[i].h;
-                la.opitch = pyr[i].pitch;
-            }
+            la.in = level0.ptr;
+            la.w = level0.w;
+            la.h = level0.h;
+            la.pitch = level0.pitch;
+            la.out = pyr[0].ptr;
+            la.ow = pyr[0].w;
+            la.oh = pyr[0].h;
+            la.opitch = pyr[0].pitch;
             la.stats_half = p->storage == GLS_STORAGE_F16_STATS;
-            GLS_CHECK(fused_level_fit(ctx, la, src.half, half, nlf_scratch_at(nlf_scratch), nlf_dev + 8 * (1 + i)));
-            mark(i == 0 ? "noiseStatistics+downsample L0" : "noiseStatistics+downsample L1+");
+            GLS_CHECK(fused_level_fit(ctx, la, true, half, nlf_scratch_at(nlf_scratch), nlf_dev + 8));
+            mark("noiseStatistics+downsample L0");
+        }
+        if (overlapped) {
+            // a lane of a burst: the other lanes' kernels fill the small levels' idle SMs, so
+            // the levels keep one launch each (measured faster there than the one-launch form,
+            // whose blocks hold every SM for the whole pyramid)
+            for (int i = 1; i < Lv; i++) {
+                const ImgRef& src = pyr[i - 1];
+                LevelPass1Args la{};
+                la.in = src.ptr;
+                la.w = src.w;
+                la.h = src.h;
+                la.pitch = src.pitch;
+                if (i < Lv - 1) {
+                    la.out = pyr[i].ptr;
+                    la.ow = pyr[i].w;
+                    la.oh = pyr[i].h;
+                    la.opitch = pyr[i].pitch;
+                }
+                la.stats_half = p->storage == GLS_STORAGE_F16_STATS;
+                GLS_CHECK(fused_level_fit(ctx, la, half, half, nlf_scratch_at(nlf_scratch), nlf_dev + 8 * (1 + i)));
+            }
+            mark("noiseStatistics+downsample L1+");
+        } else {
+            PyramidArgs pa{};
+            pa.nlev = Lv - 1;
+            pa.stats_half = p->storage == GLS_STORAGE_F16_STATS;
+            pa.ctl = (PyrCtl*)pyr_state;
+            unsigned* marks = (unsigned*)((char*)pyr_state + sizeof(PyrCtl));
+            int first = 0;
+            for (int q = 0; q < pa.nlev; q++) {
+                PyrLevel& lv = pa.lv[q];
+                const ImgRef& src = pyr[q];
+                lv.in = src.ptr;
+                lv.w = src.w;
+                lv.h = src.h;
+                lv.pitch = src.pitch;
+                if (q + 1 < pa.nlev) {
+                    lv.out = pyr[q + 1].ptr;
+                    lv.ow = pyr[q + 1].w;
+                    lv.oh = pyr[q + 1].h;
+                    lv.opitch = pyr[q + 1].pitch;
+                }
+                lv.tiles_x = (src.w + 31) / 32;
+                lv.first = first;
+                lv.count = lv.tiles_x * ((src.h + 31) / 32);
+                first += lv.count;
+                lv.nlf = nlf_scratch_at((char*)nlf_scratch + kNlfScratchBytes * (1 + q));
+                lv.nlf_out = nlf_dev + 8 * (2 + q);
+                lv.done = marks;
+                marks += (size_t)(((cap_w >> (q + 1)) + 31) / 32) * (((cap_h >> (q + 1)) + 31) / 32);
+            }
+            pa.items = first;
+            GLS_CHECK(fused_pyramid_stats(ctx, pa, half));
+            mark("noiseStatistics+downsample L1+");
         }
 
         // denoise coarse to fine
@@ -1072,6 +1135,7 @@ gls_status gls_raw_batch_create(gls_ctx* ctx, int lanes, gls_raw_batch** out) {
         if (s != GLS_OK) break;
         s = gls_raw_converter_create(b->lane_ctx[l], &b->lane[l]);
         if (s != GLS_OK) batch_error(b, l, s);
+        else b->lane[l]->overlapped = lanes > 1;
     }
     if (s != GLS_OK) {
         gls_raw_batch_destroy(b);
