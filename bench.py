@@ -817,6 +817,10 @@ def main(argv=None):
             "pipeline_roofline": {"algorithmic_bytes_per_px": round(bpp, 2), "achieved": round(pipe_achieved, 1),
                                   "unit": "GB/s", "frac": round(pipe_achieved / peak, 4), "ms_per_frame": round(frame_ms, 4)},
             "stages_ms_per_frame": {k: round(v[0] / (2 * len(frames)), 4) for k, v in prof.items()},
+            # per full-resolution stage: its compulsory bytes over its time, as a fraction of the
+            # measured HBM peak (the stages are issue-bound; issue_active_pct says by how much)
+            "stages_roofline_frac": {k: round(stage_bytes(k, S1, S4) * w * h / (v[0] / (2 * len(frames)) / 1e3) / 1e9 / peak, 4)
+                                     for k, v in prof.items() if stage_bytes(k, S1, S4) and v[0] > 0},
             "gpu_launches": int(launches),
             "clocks": sampler.summary(),
             "e2e": e2e,

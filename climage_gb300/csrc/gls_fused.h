@@ -149,6 +149,8 @@ gls_status fused_post_cnn(gls_ctx* ctx, const PostCnnArgs& a, bool half);
 gls_status fused_level_fit(gls_ctx* ctx, const LevelPass1Args& a, bool in_half, bool half, NlfScratch s,
                            float* out_dev);
 gls_status fused_pyramid_stats(gls_ctx* ctx, const PyramidArgs& a, bool half);
+// both bounded waits of the statistics kernels, made to run out (polls each): s's error word
+gls_status fused_wait_probe(gls_ctx* ctx, NlfScratch s, unsigned polls);
 gls_status fused_denoise(gls_ctx* ctx, const DenoiseArgs& a, bool in_half, bool half, int algo, bool reasm);
 // The final stage over the whole frame, or in `bands` bands of tile rows with band->fn
 // called after each (bands > 1 needs band).

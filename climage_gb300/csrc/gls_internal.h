@@ -83,11 +83,12 @@ constexpr size_t kNlfLimbOff = 256;                                  // [kNlfK][
 constexpr size_t kNlfMmOff = kNlfLimbOff + 8 * 3 * (size_t)kNlfK;    // [kNlfKF] u32
 constexpr size_t kNlfNanOff = kNlfMmOff + 4 * (size_t)kNlfKF;        // u32
 constexpr size_t kNlfErrOff = kNlfNanOff + 4;                        // u32
+constexpr size_t kNlfProbeOff = kNlfErrOff + 4;                      // u32, never written (wait probe)
 constexpr size_t kNlfHeaderBytes = 1024;
 constexpr size_t kNlfPartDBytes = sizeof(double) * (size_t)kNlfMaxBlocks * kNlfK;
 constexpr size_t kNlfScratchBytes = kNlfHeaderBytes + kNlfPartDBytes;
 static_assert(sizeof(NlfFit) <= kNlfTicketOff, "fit state overlaps the ticket");
-static_assert(kNlfErrOff + 4 <= kNlfHeaderBytes, "totals overflow the header");
+static_assert(kNlfProbeOff + 4 <= kNlfHeaderBytes, "totals overflow the header");
 
 struct NlfScratch {
     NlfFit* fit;

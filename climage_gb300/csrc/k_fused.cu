@@ -669,6 +669,34 @@ GLS_DI void st_release_u32(unsigned* p, unsigned v) {
     asm volatile("st.release.gpu.global.u32 [%0], %1;\n" ::"l"(p), "r"(v) : "memory");
 }
 
+// The statistics kernels' two bounded waits run out on purpose: a mark that nothing sets
+// (the pyramid's dependency wait) and an mbarrier that nothing arrives at and no copy
+// targets (the TMA staging wait), so nothing is in flight when they give up; each records
+// its bit in the error word exactly as the kernels do.
+__global__ void __launch_bounds__(kT) stage_wait_probe_kernel(NlfScratch s, uint32_t polls) {
+    __shared__ __align__(8) uint64_t bar;
+    const uint32_t b = (uint32_t)__cvta_generic_to_shared(&bar);
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(b) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+    const unsigned* word = reinterpret_cast<const unsigned*>(reinterpret_cast<const char*>(s.fit) + kNlfProbeOff);
+    bool ok = true;
+    if (threadIdx.x < 16) {
+        uint32_t k = 0;
+        while (ld_acquire_u32(word) != 1u && k < polls) {
+            __nanosleep(64);
+            k++;
+        }
+        ok = k < polls;
+    }
+    if (!__syncthreads_and(ok) && threadIdx.x == 0) atomicOr(s.err, 2u);
+    if (!stage_wait(b, 0u, polls) && threadIdx.x == 0) atomicOr(s.err, 1u);
+    __syncthreads();
+    if (threadIdx.x == 0) asm volatile("mbarrier.inval.shared::cta.b64 [%0];\n" ::"r"(b) : "memory");
+}
+
 template <class S>
 __global__ void __launch_bounds__(kT, 3) pyramid_stats_kernel(const __grid_constant__ PyramidArgs a,
                                                                const __grid_constant__ CUtensorMap tmap) {
@@ -1321,6 +1349,12 @@ gls_status fused_level_fit(gls_ctx* ctx, const LevelPass1Args& args, bool in_hal
         nlf_finish<1, 3>(ctx, src, a.w, a.h, s, out_dev);
     }
     return check_launch(ctx, "level statistics (fused)");
+}
+
+gls_status fused_wait_probe(gls_ctx* ctx, NlfScratch s, unsigned polls) {
+    stage_wait_probe_kernel<<<1, kT, 0, ctx->stream>>>(s, polls);
+    ctx->launches++;
+    return check_launch(ctx, "statistics wait probe");
 }
 
 gls_status fused_pyramid_stats(gls_ctx* ctx, const PyramidArgs& args, bool half) {

@@ -937,6 +937,33 @@ gls_status gls_raw_converter_noise_model(gls_raw_converter* c, gls_demosaic_para
     return c->fetch_noise_model(p);
 }
 
+gls_status gls_raw_converter_status(gls_raw_converter* c) {
+    if (!c) return GLS_ERR_INVALID_ARGUMENT;
+    if (!c->nlf_scratch) return GLS_OK;
+    gls_ctx* ctx = c->ctx;
+    GLS_CHECK(check_cuda(ctx, cudaStreamSynchronize(ctx->stream), "synchronize"));
+    unsigned any = 0;
+    for (int r = 0; r <= GLS_MAX_LEVELS; r++) {
+        unsigned* e = (unsigned*)((char*)c->nlf_scratch + kNlfScratchBytes * r + kNlfErrOff);
+        unsigned v = 0;
+        GLS_CHECK(check_cuda(ctx, cudaMemcpy(&v, e, sizeof(v), cudaMemcpyDeviceToHost), "read error word"));
+        if (v) {
+            any |= v;
+            GLS_CHECK(check_cuda(ctx, cudaMemset(e, 0, sizeof(v)), "clear error word"));
+        }
+    }
+    if (any)
+        return set_error(ctx, GLS_ERR_TIMEOUT, "a bounded wait of a statistics kernel ran out (%s)",
+                         (any & 1u) ? ((any & 2u) ? "tile copy and tile mark" : "tile copy") : "tile mark");
+    return GLS_OK;
+}
+
+gls_status gls_raw_converter_wait_probe(gls_raw_converter* c, unsigned polls) {
+    if (!c || polls == 0 || polls > (1u << 22)) return GLS_ERR_INVALID_ARGUMENT;
+    if (!c->nlf_scratch) return set_error(c->ctx, GLS_ERR_INVALID_ARGUMENT, "no frame processed yet");
+    return fused_wait_probe(c->ctx, nlf_scratch_at(c->nlf_scratch), polls);
+}
+
 gls_status gls_raw_converter_demosaic_host(gls_raw_converter* c, const uint16_t* raw, int w, int h, int stride,
                                            gls_demosaic_params* p, uint8_t* out, int out_channels) {
     if (!c || !raw || !out) return GLS_ERR_INVALID_ARGUMENT;

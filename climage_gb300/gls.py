@@ -143,6 +143,8 @@ SIGNATURES = [
     ("gls_raw_converter_destroy", _I, [_P]),
     ("gls_raw_converter_demosaic", _I, [_P, _D, ctypes.POINTER(DemosaicParams), _D, _I]),
     ("gls_raw_converter_noise_model", _I, [_P, ctypes.POINTER(DemosaicParams)]),
+    ("gls_raw_converter_status", _I, [_P]),
+    ("gls_raw_converter_wait_probe", _I, [_P, ctypes.c_uint]),
     ("gls_raw_converter_demosaic_host", _I, [_P, _P, _I, _I, _I, ctypes.POINTER(DemosaicParams), _P, _I]),
     ("gls_raw_converter_demosaic_packed_host", _I, [_P, _P, ctypes.c_size_t, _I, _I, _I,
                                                     ctypes.POINTER(DemosaicParams), _P, _I]),
@@ -494,6 +496,15 @@ class RawConverter:
 
     def noiseModel(self, params):
         self.ctx.check(lib().gls_raw_converter_noise_model(self.handle, ctypes.byref(params)), "noiseModel")
+
+    def status(self):
+        """Raises GLS_ERR_TIMEOUT (once) when a bounded wait of the statistics kernels ran out
+        since the last call."""
+        self.ctx.check(lib().gls_raw_converter_status(self.handle), "RawConverter.status")
+
+    def wait_probe(self, polls):
+        """Makes both bounded waits of the statistics kernels run out (after one converted frame)."""
+        self.ctx.check(lib().gls_raw_converter_wait_probe(self.handle, int(polls)), "RawConverter.wait_probe")
 
     def demosaicImageHost(self, raw, params, out):
         """raw: (H, W) uint16 numpy array (ideally pinned); out: (H, W, 3|4) uint8 numpy array."""

@@ -305,6 +305,15 @@ GLS_API gls_status gls_raw_converter_demosaic(gls_raw_converter* conv, const gls
                                               gls_demosaic_params* params, const gls_image_desc* out,
                                               int defer_noise_model);
 GLS_API gls_status gls_raw_converter_noise_model(gls_raw_converter* conv, gls_demosaic_params* params);
+/* Device-side status of the converter's statistics kernels (no counterpart in the reference):
+ * synchronises the converter's stream and returns GLS_ERR_TIMEOUT, once, when a bounded wait
+ * of those kernels ran out since the last call (a tile copy or a coarser tile's mark that
+ * did not arrive in time; the frame's noise model is then not valid), else GLS_OK. */
+GLS_API gls_status gls_raw_converter_status(gls_raw_converter* conv);
+/* Diagnostic of those waits: runs both, limited to `polls` polls (1 .. 2^22), on a mark that
+ * nothing sets and an mbarrier that nothing arrives at (nothing in flight), so the next
+ * gls_raw_converter_status returns GLS_ERR_TIMEOUT.  Needs one converted frame first. */
+GLS_API gls_status gls_raw_converter_wait_probe(gls_raw_converter* conv, unsigned polls);
 /* demosaicImage + convertToRGBImage on host buffers (demosaic.cpp:34-51): host uint16
  * raw in, host RGBA8 (out_channels 4) or RGB8 (3) out; copies go through pinned staging. */
 GLS_API gls_status gls_raw_converter_demosaic_host(gls_raw_converter* conv, const uint16_t* raw, int width, int height,

@@ -176,3 +176,32 @@ def test_pipeline_rotate_180(ctx, bayer, noise_level, gain):
     spec["rotate_180"] = 1
     check(ctx, raw, spec)
     check(ctx, raw, spec, out_float=True)
+
+
+def test_statistics_waits_run_out_and_report(ctx):
+    """The statistics kernels' bounded waits (a TMA tile copy on its mbarrier, a coarser
+    level's tile mark in the one-launch pyramid), made to run out on a mark that nothing sets
+    and a barrier that nothing arrives at: the error word is set, status() raises
+    GLS_ERR_TIMEOUT once, and the converter then converts frames as before."""
+    import torch
+    raw, _, meta = synthetic.make_frame(256, 192, bayer=2, seed=21)
+    spec = configs.make_spec(meta, levels=5)
+    conv = gls.RawConverter(ctx)
+    p = configs.to_gls_params(spec)
+    out = torch.empty((192, 256, 4), dtype=torch.uint8, device="cuda")
+    conv.demosaicImage(torch.from_numpy(raw).cuda(), p, out)
+    first = out.cpu().numpy()
+    conv.status()
+    conv.wait_probe(1 << 10)
+    with pytest.raises(gls.GlsError) as err:
+        conv.status()
+    assert err.value.status == gls.GLS_ERR_TIMEOUT
+    conv.status()  # reported once
+    p = configs.to_gls_params(spec)
+    conv.demosaicImage(torch.from_numpy(raw).cuda(), p, out)
+    conv.status()
+    np.testing.assert_array_equal(out.cpu().numpy(), first)
+    with pytest.raises(gls.GlsError) as bad:
+        conv.wait_probe(0)
+    assert bad.value.status == gls.GLS_ERR_INVALID_ARGUMENT
+    conv.close()
