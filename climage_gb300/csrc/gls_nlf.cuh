@@ -723,6 +723,79 @@ __global__ void __launch_bounds__(kThreads) nlf_pass3_kernel(Src src, int sw, in
     if (last_block(s.ticket)) solve_fixed<NC>(s, 3, out);
 }
 
+// The explicit passes 2 and 3 of several level fits in one launch each: every block takes
+// its share of every level whose fit needs the pass (the same per-level rows, tickets and
+// solves as the one-level kernels; a level whose solve proved the pass redundant is
+// skipped by every block alike).
+template <class S>
+struct LevelSet {
+    LevelSrc<S> src[GLS_MAX_LEVELS];
+    NlfScratch s[GLS_MAX_LEVELS];
+    float* out[GLS_MAX_LEVELS];
+    int n;
+};
+
+template <class S>
+__global__ void __launch_bounds__(kThreads) nlf_pass2_levels_kernel(const __grid_constant__ LevelSet<S> ls,
+                                                                    NlfThresholds th) {
+    const int tx = threadIdx.x % kTX, ty = threadIdx.x / kTX;
+    for (int l = 0; l < ls.n; l++) {
+        const NlfScratch& s = ls.s[l];
+        if (s.fit->mode != 1) continue;
+        const LevelSrc<S>& src = ls.src[l];
+        const int sw = src.img.w, sh = src.img.h;
+        double acc[3] = {0.0, 0.0, 0.0};
+        const int tiles_x = (sw + kTX - 1) / kTX, tiles_y = (sh + kTY - 1) / kTY;
+        for (int t = blockIdx.x; t < tiles_x * tiles_y; t += gridDim.x) {
+            const int x = (t % tiles_x) * kTX + tx, y = (t / tiles_x) * kTY + ty;
+            if (x >= sw || y >= sh) continue;
+            float m[1], v[3];
+            src.stats(x, y, m, v);
+            if (!in_range<1, 3>(m, v, th)) continue;
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                const double d = (s.fit->A[c] + s.fit->B[c] * (double)m[0]) - (double)v[c];
+                acc[c] += d * d;
+            }
+        }
+        block_reduce_write<3>(acc, s.part_d + (size_t)blockIdx.x * kNlfK);
+        if (last_block(s.ticket)) solve_pass2<3>(s, gridDim.x);
+        __syncthreads();
+    }
+}
+
+template <class S>
+__global__ void __launch_bounds__(kThreads) nlf_pass3_levels_kernel(const __grid_constant__ LevelSet<S> ls,
+                                                                    NlfThresholds th) {
+    const int tx = threadIdx.x % kTX, ty = threadIdx.x / kTX;
+    for (int l = 0; l < ls.n; l++) {
+        const NlfScratch& s = ls.s[l];
+        if (s.fit->mode != 2) continue;
+        const LevelSrc<S>& src = ls.src[l];
+        const int sw = src.img.w, sh = src.img.h;
+        Pass1Acc<1, 3> acc;
+        acc.init();
+        const int tiles_x = (sw + kTX - 1) / kTX, tiles_y = (sh + kTY - 1) / kTY;
+        for (int t = blockIdx.x; t < tiles_x * tiles_y; t += gridDim.x) {
+            const int x = (t % tiles_x) * kTX + tx, y = (t / tiles_x) * kTY + ty;
+            if (x >= sw || y >= sh) continue;
+            float m[1], v[3];
+            src.stats(x, y, m, v);
+            if (!in_range<1, 3>(m, v, th)) continue;
+            bool ok = true;
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                const double d = (s.fit->A[c] + s.fit->B[c] * (double)m[0]) - (double)v[c];
+                if (!(d * d <= s.fit->err2[c])) ok = false;
+            }
+            if (ok) acc.add_selected(m, v);
+        }
+        acc.write_fixed(s);
+        if (last_block(s.ticket)) solve_fixed<3>(s, 3, ls.out[l]);
+        __syncthreads();
+    }
+}
+
 int grid_for(gls_ctx* ctx, int sw, int sh) {
     const long tiles = (long)((sw + kTX - 1) / kTX) * ((sh + kTY - 1) / kTY);
     long g = 4L * (ctx->num_sms > 0 ? ctx->num_sms : 148);

@@ -1370,17 +1370,26 @@ gls_status fused_pyramid_stats(gls_ctx* ctx, const PyramidArgs& args, bool half)
     }
     ctx->launches++;
     GLS_CHECK(check_launch(ctx, "pyramid statistics (fused)"));
-    // the explicit regression passes of every level (they exit at once unless needed)
-    for (int p = 0; p < a.nlev; p++) {
-        const PyrLevel& L = a.lv[p];
-        if (half) {
-            LevelSrc<__half> src{{(const half4*)L.in, L.w, L.h, L.pitch}, a.stats_half != 0};
-            nlf_finish<1, 3>(ctx, src, L.w, L.h, L.nlf, L.nlf_out);
-        } else {
-            LevelSrc<float> src{{(const float4*)L.in, L.w, L.h, L.pitch}, a.stats_half != 0};
-            nlf_finish<1, 3>(ctx, src, L.w, L.h, L.nlf, L.nlf_out);
+    // the explicit regression passes of every level, one launch each (they exit at once
+    // unless a level's solve could not prove them redundant)
+    auto finish = [&](auto tag) {
+        typedef decltype(tag) SS;
+        typedef typename Storage<SS>::T4 T4;
+        LevelSet<SS> ls{};
+        ls.n = a.nlev;
+        for (int p = 0; p < a.nlev; p++) {
+            const PyrLevel& L = a.lv[p];
+            ls.src[p] = LevelSrc<SS>{{(const T4*)L.in, L.w, L.h, L.pitch}, a.stats_half != 0};
+            ls.s[p] = L.nlf;
+            ls.out[p] = L.nlf_out;
         }
-    }
+        const int grid = grid_for(ctx, a.lv[0].w, a.lv[0].h);
+        nlf_pass2_levels_kernel<SS><<<grid, kThreads, 0, ctx->stream>>>(ls, a.th);
+        nlf_pass3_levels_kernel<SS><<<grid, kThreads, 0, ctx->stream>>>(ls, a.th);
+        ctx->launches += 2;
+    };
+    if (half) finish(__half());
+    else finish(float());
     return check_launch(ctx, "pyramid statistics (explicit passes)");
 }
 
