@@ -145,6 +145,20 @@ GLS_HD float rcp_(float d) {
 #endif
 }
 
+// RN(1/d) for |d| in [2^-60, 2^30]: the hardware's reciprocal approximation refined by one
+// Newton-Raphson step, r + r (1 - d r) with both operations fused.  Equal to the correctly
+// rounded reciprocal for every d in that range (checked exhaustively against __frcp_rn on the
+// GPU by gls_selftest_reciprocal), at three instructions.
+GLS_HD float rcp_fast(float d) {
+#if defined(__CUDA_ARCH__)
+    float r;
+    asm("rcp.approx.f32 %0, %1;" : "=f"(r) : "f"(d));
+    return __fmaf_rn(__fmaf_rn(-d, r, 1.0f), r, r);
+#else
+    return 1.0f / d;
+#endif
+}
+
 // Division by a value shared by many numerators.  With y = RN(1/d) and q0 = RN(x*y), the
 // residual r = x - q0*d is exact and RN(q0 + r*y) is the correctly rounded x/d
 // (Markstein's correction, P. Markstein, "IA-64 and Elementary Functions", 2000); the
@@ -159,7 +173,15 @@ struct FastDiv {
         d = den;
         const float ad = fabs_(den);
         ok = ad >= 8.67361738e-19f && ad <= 1073741824.0f;
-        y = ok ? rcp_(den) : 0.0f;
+        y = ok ? rcp_fast(den) : 0.0f;
+    }
+    // a divisor known in advance: y = RN(1/den) and ok as init() computes them
+    GLS_HDM static FastDiv of(float den, float rcp, bool in_range) {
+        FastDiv f;
+        f.d = den;
+        f.y = rcp;
+        f.ok = in_range;
+        return f;
     }
     GLS_HDM float operator()(float x) const {
         if (!ok || !in_range(x)) return div_(x, d);

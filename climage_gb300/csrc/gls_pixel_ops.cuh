@@ -145,8 +145,9 @@ GLS_DI SobelVal sobel_abs(const Acc& im, int x, int y) {
             }
         }
     }
-    FastDiv r;
-    r.init(sqrt_(4.5f));
+    // division by sqrt(4.5) (the Sobel normalisation): 0x4007c3b6 = RN(sqrt(4.5)) and
+    // 0x3ef15bf0 = RN(1 / that), the values init(sqrt_(4.5f)) computes
+    const FastDiv r = FastDiv::of(__uint_as_float(0x4007c3b6u), __uint_as_float(0x3ef15bf0u), true);
     SobelVal o;
     o.gx = mabs(r(vx));
     o.gy = mabs(r(vy));
@@ -169,8 +170,7 @@ GLS_DI float2 sobel_signed(const Acc& im, int x, int y) {
             vy = vy + ky[j + 1][i + 1] * s;
         }
     }
-    FastDiv r;
-    r.init(sqrt_(4.5f));
+    const FastDiv r = FastDiv::of(__uint_as_float(0x4007c3b6u), __uint_as_float(0x3ef15bf0u), true);
     return make_float2(r(vx), r(vy));
 }
 
@@ -814,7 +814,9 @@ struct RgbParams {
     int localToneMapping;
     // per-frame constants of convertTosRGB, evaluated once (rgb_params_init): the exposure
     // factor powr(2, exposureBias) and the tone curve's sigmoid(0, s), sigmoid(1, s) - sigmoid(0, s)
-    float eb, sig0, sig_den;
+    // with its reciprocal RN(1 / that) and whether the shared-divisor shortcut applies to it
+    float eb, sig0, sig_den, sig_rcp;
+    int sig_ok;
 };
 
 __host__ __device__ inline float sigmoid_(float x, float s) { return 0.5f * (glsm::tanh_(s * x - 0.3f * s) + 1.0f); }
@@ -831,6 +833,10 @@ __host__ __device__ inline RgbParams rgb_params_init(float contrast, float satur
     r.eb = exposureBias != 0.0f ? glsm::powr_(2.0f, exposureBias) : 1.0f;
     r.sig0 = sigmoid_(0.0f, toneCurveSlope);
     r.sig_den = sigmoid_(1.0f, toneCurveSlope) - r.sig0;
+    FastDiv f;
+    f.init(r.sig_den);
+    r.sig_rcp = f.y;
+    r.sig_ok = f.ok ? 1 : 0;
     return r;
 }
 
@@ -860,8 +866,7 @@ GLS_DI float3 srgb_px(float3 in, float ltm, const Mat3& m, const RgbParams& rp) 
     }
     const float3 t = transform_px(m, make_float3(p[0], p[1], p[2]));
     float rgb[3] = {t.x, t.y, t.z};
-    FastDiv tden;
-    tden.init(rp.sig_den);
+    const FastDiv tden = FastDiv::of(rp.sig_den, rp.sig_rcp, rp.sig_ok != 0);
 #pragma unroll
     for (int k = 0; k < 3; k++) rgb[k] = clamp_(tone_curve_(rgb[k], rp.toneCurveSlope, rp.sig0, tden), 0.0f, 1.0f);
     if (rp.localToneMapping) {

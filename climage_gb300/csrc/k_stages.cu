@@ -662,8 +662,37 @@ __global__ void selftest_kernel(uint64_t n, uint64_t seed, unsigned long long* b
     if (b3) atomicAdd(&bad[3], b3);
 }
 
+// every divisor magnitude of the shared-divisor range [2^-60, 2^31), both signs: rcp_fast
+// against the correctly rounded reciprocal
+__global__ void selftest_reciprocal_kernel(unsigned long long* bad) {
+    constexpr uint64_t kCount = (uint64_t)(158 - 67) << 24;  // exponent fields 67..157, 2^23 mantissas, 2 signs
+    unsigned long long b = 0;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < kCount; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t bits = ((uint32_t)(67 + (i >> 24)) << 23) | (uint32_t)(i & 0x7fffffu) | ((uint32_t)(i >> 23) & 1u) << 31;
+        const float d = __uint_as_float(bits);
+        if (__float_as_uint(glsm::rcp_fast(d)) != __float_as_uint(__frcp_rn(d))) b++;
+    }
+    if (b) atomicAdd(bad, b);
+}
+
 }  // namespace
 }  // namespace gls
+
+extern "C" gls_status gls_selftest_reciprocal(gls_ctx* ctx, uint64_t* mismatches) {
+    using namespace gls;
+    if (!ctx || !mismatches) return GLS_ERR_INVALID_ARGUMENT;
+    unsigned long long* d = nullptr;
+    GLS_CHECK(check_cuda(ctx, cudaMalloc(&d, sizeof(unsigned long long)), "cudaMalloc(selftest)"));
+    cudaMemsetAsync(d, 0, sizeof(unsigned long long), ctx->stream);
+    selftest_reciprocal_kernel<<<8 * (ctx->num_sms > 0 ? ctx->num_sms : 148), 256, 0, ctx->stream>>>(d);
+    ctx->launches++;
+    unsigned long long h = 0;
+    gls_status s = check_cuda(ctx, cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream), "selftest copy");
+    if (s == GLS_OK) s = check_cuda(ctx, cudaStreamSynchronize(ctx->stream), "selftest");
+    cudaFree(d);
+    *mismatches = h;
+    return s;
+}
 
 extern "C" gls_status gls_selftest(gls_ctx* ctx, uint64_t n, uint64_t seed, uint64_t mismatches[4]) {
     using namespace gls;

@@ -136,6 +136,7 @@ SIGNATURES = [
     ("gls_color_checker_raw_stats", _I, [_P, _D, _F, _F, _I, ctypes.POINTER(ctypes.c_int), _I, _FP, _FP]),
     ("gls_estimate_raw_parameters", _I, [_P, _D, _F, _F, _I, ctypes.POINTER(ctypes.c_int), _I, _FP, _FP, _FP]),
     ("gls_selftest", _I, [_P, ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)]),
+    ("gls_selftest_reciprocal", _I, [_P, ctypes.POINTER(ctypes.c_uint64)]),
     ("gls_cam_xyz_coeff", _I, [_FP, _FP, _FP]),
     ("gls_cam_ycbcr", _I, [_FP, _FP]),
     ("gls_inverse3x3", _I, [_FP, _FP]),
@@ -322,6 +323,12 @@ class Context:
 
     def synchronize(self):
         self.check(self._lib.gls_ctx_synchronize(self.handle), "synchronize")
+
+    def selftest_reciprocal(self):
+        """Divisors of the shared-divisor range whose fast reciprocal differs from __frcp_rn."""
+        m = ctypes.c_uint64()
+        self.check(lib().gls_selftest_reciprocal(self.handle, ctypes.byref(m)), "selftest_reciprocal")
+        return m.value
 
     def selftest(self, n=1 << 24, seed=1):
         out = (ctypes.c_uint64 * 4)()

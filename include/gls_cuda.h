@@ -226,6 +226,10 @@ GLS_API gls_status gls_unpack_raw_bits(gls_ctx* ctx, const void* packed, size_t 
  * [1] the clamped smoothstep vs its literal form, [2] the squared-length edge test vs
  * sqrt-then-compare, [3] hardware float->half rounding vs the portable conversion. */
 GLS_API gls_status gls_selftest(gls_ctx* ctx, uint64_t n, uint64_t seed, uint64_t mismatches[4]);
+/* Exhaustive check of the three-instruction reciprocal the shared-divisor division uses:
+ * every float divisor of magnitude in [2^-60, 2^31), both signs, against __frcp_rn;
+ * *mismatches = the number that differ (0 expected). */
+GLS_API gls_status gls_selftest_reciprocal(gls_ctx* ctx, uint64_t* mismatches);
 
 /* autoWhiteBalance (demosaic_utils.cpp:976-1026): the white-balance gains of a raw
  * R16_UNORM frame (device) -- rgb_ycbcr is cam_ycbcr(rgb_cam), scale_mul the four channel

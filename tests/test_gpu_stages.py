@@ -375,6 +375,13 @@ def test_exact_shortcuts_selftest(ctx):
         assert ctx.selftest(1 << 26, seed) == [0, 0, 0, 0]
 
 
+def test_fast_reciprocal_is_correctly_rounded(ctx):
+    """The shared-divisor division takes its reciprocal from the hardware approximation and
+    one Newton step; for every divisor of its range (2^-60 <= |d| < 2^31, 1.5 G values) that
+    equals the correctly rounded reciprocal, which the Markstein correction needs."""
+    assert ctx.selftest_reciprocal() == 0
+
+
 def test_invalid_arguments(ctx):
     import torch
     raw = torch.zeros((9, 8), dtype=torch.uint16, device="cuda")
