@@ -219,7 +219,7 @@ def algorithmic_bytes_per_px(S, O, L):
 # DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum) and issue-slot use
 # of the two largest kernels, from one ncu capture of this workload (4032x3024, fp32
 # storage, RGBA8 out); the roofline fraction is computed live, these explain it.
-NCU_TRAFFIC = {"denoise L0+LTM+sRGB": (234833664, 77.1), "demosaic": (75758080, 77.2)}
+NCU_TRAFFIC = {"denoise L0+LTM+sRGB": (235532032, 76.9), "demosaic": (75923200, 78.7)}
 
 
 # Compulsory bytes per full-resolution pixel of each full-resolution kernel (what it must
