@@ -145,6 +145,9 @@ GLS_HD float rcp_(float d) {
 #endif
 }
 
+// the literal division, out of line (the rare paths of the shortcuts below)
+GLS_HDN float div_slow(float a, float b) { return div_(a, b); }
+
 // RN(1/d) for |d| in [2^-60, 2^30]: the hardware's reciprocal approximation refined by one
 // Newton-Raphson step, r + r (1 - d r) with both operations fused.  Equal to the correctly
 // rounded reciprocal for every d in that range (checked exhaustively against __frcp_rn on the
@@ -184,7 +187,7 @@ struct FastDiv {
         return f;
     }
     GLS_HDM float operator()(float x) const {
-        if (!ok || !in_range(x)) return div_(x, d);
+        if (!ok || !in_range(x)) return div_slow(x, d);
         return fast(x);
     }
     // the shortcut alone: exact when ok and in_range(x) (x == 0 gives a zero of either sign)
@@ -203,7 +206,6 @@ struct FastDiv {
 // division is only evaluated where the clamp does not decide the result by itself
 // (num <= 0 or NaN clamps to 0, num >= den > 0 clamps to 1, exactly as the literal form).
 // out-of-line literal operations for the rare paths (keeps the unrolled loops compact)
-GLS_HDN float div_slow(float a, float b) { return div_(a, b); }
 GLS_HDN float sqrt_slow(float a) { return sqrt_(a); }
 GLS_HDN float smoothstep_slow(float num, float den) {
     const float t = clamp_(div_(num, den), 0.0f, 1.0f);
@@ -360,8 +362,8 @@ GLS_HD float exp2_core(float x) {
 }
 
 // 2^x
-GLS_HD float exp2_(float x) {
-    if (fabs_(x) < 126.0f) return exp2_core(x);  // NaN goes on
+// the special cases and the edge of the range, out of line (the kernels rarely reach them)
+GLS_HDN float exp2_slow(float x) {
     if (isnan_(x)) return x;
     if (x >= 128.0f) return inf_();
     if (x < -150.0f) return 0.0f;
@@ -387,6 +389,11 @@ GLS_HD float exp2_(float x) {
     return p * u2f((uint32_t)(e + 127) << 23);
 }
 
+GLS_HD float exp2_(float x) {
+    if (fabs_(x) < 126.0f) return exp2_core(x);  // NaN goes on
+    return exp2_slow(x);
+}
+
 // true for a positive, normal, finite x (one unsigned compare on the bits)
 GLS_HD bool is_pos_normal_(float x) { return f2u(x) - 0x00800000u < 0x7f000000u; }
 
@@ -410,9 +417,8 @@ GLS_HD float log2_core(float x) {
     return (float)e + z * p;
 }
 
-// log2(x)
-GLS_HD float log2_(float x) {
-    if (is_pos_normal_(x)) return log2_core(x);
+// log2 of what is not a positive normal finite x, out of line
+GLS_HDN float log2_slow(float x) {
     if (isnan_(x)) return x;
     if (x < 0.0f) return nan_();
     if (x == 0.0f) return -inf_();
@@ -440,13 +446,16 @@ GLS_HD float log2_(float x) {
     return ((float)e + k) + z * p;
 }
 
+// log2(x)
+GLS_HD float log2_(float x) {
+    if (is_pos_normal_(x)) return log2_core(x);
+    return log2_slow(x);
+}
+
 GLS_HD bool is_integer_(float y) { return floor_(y) == y; }
 
-// OpenCL pow(x, y) for the cases the pipeline meets: finite or infinite x, finite y.
-GLS_HD float pow_(float x, float y) {
-    if (y == 0.0f || x == 1.0f) return 1.0f;
-    // positive normal x and finite y: the general case, without its special-case tests
-    if (is_pos_normal_(x) && fabs_(y) < inf_()) return exp2_(y * log2_core(x));
+// pow's special cases, out of line
+GLS_HDN float pow_slow(float x, float y) {
     if (isnan_(x) || isnan_(y)) return x + y;
     if (x == 0.0f) return y < 0.0f ? inf_() : 0.0f;
     if (x < 0.0f) {
@@ -457,6 +466,14 @@ GLS_HD float pow_(float x, float y) {
     }
     if (x == inf_()) return y < 0.0f ? 0.0f : x;
     return exp2_(y * log2_(x));
+}
+
+// OpenCL pow(x, y) for the cases the pipeline meets: finite or infinite x, finite y.
+GLS_HD float pow_(float x, float y) {
+    if (y == 0.0f || x == 1.0f) return 1.0f;
+    // positive normal x and finite y: the general case, without its special-case tests
+    if (is_pos_normal_(x) && fabs_(y) < inf_()) return exp2_(y * log2_core(x));
+    return pow_slow(x, y);
 }
 
 // OpenCL powr(x, y): defined for x >= 0 only.
