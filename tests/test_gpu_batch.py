@@ -112,6 +112,38 @@ def test_graph_capture_and_replay():
     cctx.close()
 
 
+def test_one_lane_graph_replays_the_pyramid_launch():
+    """A one-lane burst runs the pyramid statistics as one launch, whose work queue and tile
+    marks live on the device and are reset by the launch itself: captured once into a CUDA
+    graph, it replays correctly again and again (the burst holds frames of three sizes)."""
+    import torch
+    stream = torch.cuda.Stream()
+    cctx = gls.Context(0, stream=stream)
+    fr = frames(BURST[:3], seed0=2500)
+    want = single(cctx, fr)
+    batch = gls.RawBatch(cctx, 1)
+    batch.reserve(max(f["w"] for f in fr), max(f["h"] for f in fr), 5, gls.STORAGE_F32)
+    outs = empty_outs(fr)
+    raws, params = [f["raw"] for f in fr], [f["params"] for f in fr]
+    with torch.cuda.stream(stream):
+        batch.demosaic(raws, params, outs)
+    torch.cuda.synchronize()
+    for o, w in zip(outs, want):
+        assert same(o, w)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=stream):
+        batch.demosaic(raws, params, outs)
+    for _ in range(3):
+        for o in outs:
+            o.fill_(7)
+        g.replay()
+        torch.cuda.synchronize()
+        for k, (o, w) in enumerate(zip(outs, want)):
+            assert same(o, w), "replay, frame %d" % k
+    batch.close()
+    cctx.close()
+
+
 def test_host_buffers(ctx):
     import torch
     fr = frames(BURST[:4], seed0=3000)
