@@ -56,3 +56,22 @@ def test_host_colour_math_matches_oracle():
     np.testing.assert_array_equal(rc_g, rc_o)
     np.testing.assert_array_equal(gls.cam_ycbcr(rc_g), orc.cam_ycbcr(rc_o))
     np.testing.assert_array_equal(gls.inverse3x3(gls.cam_ycbcr(rc_g)), orc.inverse3x3(orc.cam_ycbcr(rc_o)))
+
+
+def test_tuner_cache_host_logic():
+    """The launch-shape tuner's process-wide cache runs on the host: forcing a shape, the
+    rejected shapes, reset, and an empty cache before any frame was converted."""
+    gls.tune_reset()
+    assert gls.tune_entries() == []
+    l = gls.lib()
+    for kernel, shapes in gls.TUNE_SHAPES.items():
+        for shape in range(-1, len(shapes)):
+            assert l.gls_tune_force(kernel, shape) == 0
+        assert l.gls_tune_force(kernel, len(shapes)) != 0
+        assert l.gls_tune_force(kernel, -2) != 0
+    assert l.gls_tune_force(len(gls.TUNE_SHAPES), 0) != 0
+    k, w, h, f, s = (ctypes.c_int() for _ in range(5))
+    ms = (ctypes.c_float * 4)()
+    assert l.gls_tune_entry(0, ctypes.byref(k), ctypes.byref(w), ctypes.byref(h), ctypes.byref(f), ctypes.byref(s),
+                            ms) != 0  # no entry 0 in an empty cache
+    gls.tune_reset()
