@@ -41,6 +41,9 @@ struct DemosaicArgs {
     // fitted raw noise model (rawA_dev = A[0..3])
     float* cnn_in;
     const float* rawA_dev;
+    // the split form (two kernels): the green image between them, in the storage precision
+    void* green;
+    int green_pitch;
 };
 
 // After the learned stage: linear RGB + the network's residual, blendHighlights,

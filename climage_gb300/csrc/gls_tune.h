@@ -24,7 +24,7 @@ namespace gls {
 
 enum TuneKernel { kTuneDemosaic = 0, kTuneFinal = 1, kTuneKernels = 2 };
 constexpr int kTuneMaxShapes = 4;
-constexpr int kTuneShapes[kTuneKernels] = {3, 3};
+constexpr int kTuneShapes[kTuneKernels] = {4, 3};
 
 struct TuneKey {
     int kernel, w, h, flags;  // flags: the kernel's variant bits (storage, input form, ...)

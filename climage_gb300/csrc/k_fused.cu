@@ -417,6 +417,129 @@ __global__ void __launch_bounds__(kT, demosaic_min_blocks(TW, TH)) demosaic_kern
 }
 
 // =========================================================================================
+// The split demosaic (a tile shape of the tuner): the green of every red/blue site computed
+// once by its own kernel (no halo of green recomputed: the fused kernel interpolates 1.25x
+// its tile's sites and evaluates its Sobel map over 1.52x its tile), written to the green
+// image in the storage precision -- where the fused kernel keeps it in shared memory, rounded
+// the same way -- then red/blue, highlights, cam -> YCbCr and the despeckle by a second
+// kernel reading that image (clamped to the frame, as the fused kernel's border copies do).
+// =========================================================================================
+constexpr int SGW = 64, SGH = 32;  // green kernel tile
+
+template <bool RAW_U16, class S>
+__global__ void __launch_bounds__(kT, 4) green_split_kernel(DemosaicArgs a) {
+    constexpr int RW = SGW + 6, RH = SGH + 6;  // scaled raw, origin (x0 - 3, y0 - 3)
+    constexpr int SW = SGW + 4, SH = SGH + 4;  // Sobel map, origin (x0 - 2, y0 - 2)
+    __shared__ float s_raw[RH * RW];
+    __shared__ float4 s_sob[SH * SW];
+    const int x0 = blockIdx.x * SGW, y0 = blockIdx.y * SGH;
+    const int w = a.w, h = a.h, bayer = a.bayer;
+    for (int i = threadIdx.x; i < RH * RW; i += kT) {
+        const int r = i / RW, c = i - r * RW;
+        const int gx = clampi(x0 - 3 + c, 0, w - 1), gy = clampi(y0 - 3 + r, 0, h - 1);
+        float v;
+        if (RAW_U16) {
+            v = Storage<S>::round(scale_value(__ldg((const uint16_t*)a.in + (size_t)gy * a.in_pitch + gx),
+                                              a.sm[((gy & 1) << 1) | (gx & 1)], a.black));
+        } else {
+            v = Storage<S>::ldg((const S*)a.in + (size_t)gy * a.in_pitch + gx);
+        }
+        s_raw[i] = v;
+    }
+    __syncthreads();
+    const SAcc1 R{s_raw, x0 - 3, y0 - 3, RW};
+    for (int i = threadIdx.x; i < SH * SW; i += kT) {
+        const int r = i / SW, c = i - r * SW;
+        const SobelVal sv = sobel_abs<true>(R, x0 - 2 + c, y0 - 2 + r);  // finite scaled raw
+        s_sob[i] = make_float4(sv.gx, sv.gy, sv.len, 0.0f);
+    }
+    __syncthreads();
+    const float lv = mmax(a.rawB_dev ? a.rawB_dev[1] : a.lv_host, 1e-4f);
+    S* const green = (S*)a.green;
+    for (int p = threadIdx.x; p < SGW * SGH / 2; p += kT) {
+        const int r = p / (SGW / 2), k = p - r * (SGW / 2);
+        const int y = y0 + r, xa = x0 + 2 * k;
+        if (y >= h) continue;
+        const int e_rb = green_needs_interp(xa, y, bayer) ? 0 : 1;
+        const int xr = xa + e_rb, xg = xa + (1 - e_rb);
+        if (xr < w) {
+            const SobelMap sob{s_sob, x0 - 2, y0 - 2, SW, xr, y};
+            const float g = Storage<S>::round(green_at(R, xr, y, lv, sob));
+            Storage<S>::st(green + (size_t)y * a.green_pitch + xr, g);
+            if (a.tap_green) a.tap_green[(size_t)y * a.tap_pitch + xr] = g;
+        }
+        if (xg < w) {
+            const float g = Storage<S>::round(R.at(xg, y));
+            Storage<S>::st(green + (size_t)y * a.green_pitch + xg, g);
+            if (a.tap_green) a.tap_green[(size_t)y * a.tap_pitch + xg] = g;
+        }
+    }
+    if (a.tap_scaled) {
+        for (int i = threadIdx.x; i < SGW * SGH; i += kT) {
+            const int r = i / SGW, c = i - r * SGW, x = x0 + c, y = y0 + r;
+            if (x < w && y < h) a.tap_scaled[(size_t)y * a.tap_pitch + x] = R.at(x, y);
+        }
+    }
+}
+
+template <bool RAW_U16, class S>
+__global__ void __launch_bounds__(kT, 5) rb_despeckle_kernel(DemosaicArgs a) {
+    constexpr int TW = 44, TH = 28;
+    constexpr int RW = TW + 4, RH = TH + 4;  // scaled raw and green, origin (x0 - 2, y0 - 2)
+    constexpr int CW = TW + 2, CH = TH + 2;  // YCbCr (binary16), origin (x0 - 1, y0 - 1)
+    __shared__ float s_raw[RH * RW];
+    __shared__ float s_green[RH * RW];
+    __shared__ half4 s_ycc[CH * CW];
+    const int x0 = blockIdx.x * TW, y0 = blockIdx.y * TH;
+    const int w = a.w, h = a.h, bayer = a.bayer;
+    const bool border = x0 - 2 < 0 || y0 - 2 < 0 || x0 + TW + 2 > w || y0 + TH + 2 > h;
+    const S* const green = (const S*)a.green;
+    for (int i = threadIdx.x; i < RH * RW; i += kT) {
+        const int r = i / RW, c = i - r * RW;
+        const int gx = clampi(x0 - 2 + c, 0, w - 1), gy = clampi(y0 - 2 + r, 0, h - 1);
+        float v;
+        if (RAW_U16) {
+            v = Storage<S>::round(scale_value(__ldg((const uint16_t*)a.in + (size_t)gy * a.in_pitch + gx),
+                                              a.sm[((gy & 1) << 1) | (gx & 1)], a.black));
+        } else {
+            v = Storage<S>::ldg((const S*)a.in + (size_t)gy * a.in_pitch + gx);
+        }
+        s_raw[i] = v;
+        s_green[i] = Storage<S>::ldg(green + (size_t)gy * a.green_pitch + gx);
+    }
+    __syncthreads();
+    const SAcc1 R{s_raw, x0 - 2, y0 - 2, RW};
+    const SAcc1 G{s_green, x0 - 2, y0 - 2, RW};
+    {
+        const float cv = mmax(a.rawB_dev ? div_(a.rawB_dev[0] + a.rawB_dev[2], 2.0f) : a.cv_host, 1e-6f);
+        for (int i = threadIdx.x; i < CH * CW; i += kT) {
+            const int r = i / CW, c = i - r * CW, x = x0 - 1 + c, y = y0 - 1 + r;
+            if (x < 0 || x >= w || y < 0 || y >= h) continue;
+            float3 p = round3<S>(red_blue_at(R, G, x, y, bayer, cv));
+            p = round3<S>(blend_highlights_px(p, 1.0f));
+            p = round3<S>(transform_px(a.cam_ycbcr, p));
+            s_ycc[i] = to_half4(make_float4(p.x, p.y, p.z, 0.0f));
+        }
+    }
+    __syncthreads();
+    if (border) {
+        for (int i = threadIdx.x; i < CH * CW; i += kT) {
+            const int r = i / CW, c = i - r * CW, x = x0 - 1 + c, y = y0 - 1 + r;
+            if (x >= 0 && x < w && y >= 0 && y < h) continue;
+            const int cx = clampi(x, 0, w - 1) - (x0 - 1), cy = clampi(y, 0, h - 1) - (y0 - 1);
+            s_ycc[i] = s_ycc[cy * CW + cx];
+        }
+        __syncthreads();
+    }
+    const SAcc4h Y{s_ycc, x0 - 1, y0 - 1, CW};
+    for (int i = threadIdx.x; i < TW * TH; i += kT) {
+        const int r = i / TW, c = i - r * TW, x = x0 + c, y = y0 + r;
+        if (x >= w || y >= h) continue;
+        a.level0[(size_t)y * a.l0_pitch + x] = to_half4(despeckle_px<true>(Y, x, y, a.va0, a.vb0));
+    }
+}
+
+// =========================================================================================
 // post_cnn: the learned stage's residual (its RGB output times the pixel's sigma) added to
 // the linear RGB, then blendHighlights,
 // cam -> YCbCr over the tile and a one-pixel ring (clamped reads: the same values the
@@ -1303,11 +1426,24 @@ void launch_demosaic(const DemosaicArgs& a, bool raw_u16, bool half, bool cnn, c
 // The learned stage's input path keeps the default shape; the plain path has three:
 // 0: 44x28 (halos: green 1.25x, Sobel map 1.52x the tile; 44 KB, 5 blocks per SM),
 // 1: 32x24 (more, smaller blocks: fills the GPU on small frames),
-// 2: 64x32 (least halo, 67 KB, 3 blocks per SM).
+// 2: 64x32 (least halo, 67 KB, 3 blocks per SM),
+// 3: split in two kernels through the green image (no green or Sobel halo recomputed).
 void launch_demosaic_shape(int shape, const DemosaicArgs& a, bool raw_u16, bool half, cudaStream_t st) {
-    if (a.cnn_in || shape == 0) launch_demosaic<44, 28>(a, raw_u16, half, a.cnn_in != nullptr, st);
+    if (a.cnn_in || shape == 0 || (shape == 3 && !a.green)) launch_demosaic<44, 28>(a, raw_u16, half, a.cnn_in != nullptr, st);
     else if (shape == 1) launch_demosaic<32, 24>(a, raw_u16, half, false, st);
-    else launch_demosaic<64, 32>(a, raw_u16, half, false, st);
+    else if (shape == 2) launch_demosaic<64, 32>(a, raw_u16, half, false, st);
+    else {
+        const dim3 g1((a.w + SGW - 1) / SGW, (a.h + SGH - 1) / SGH), g2((a.w + 43) / 44, (a.h + 27) / 28);
+#define GLS_SPLIT(U16, SS)                                        \
+    green_split_kernel<U16, SS><<<g1, kT, 0, st>>>(a);            \
+    rb_despeckle_kernel<U16, SS><<<g2, kT, 0, st>>>(a);
+        if (raw_u16) {
+            if (half) { GLS_SPLIT(true, __half) } else { GLS_SPLIT(true, float) }
+        } else {
+            if (half) { GLS_SPLIT(false, __half) } else { GLS_SPLIT(false, float) }
+        }
+#undef GLS_SPLIT
+    }
 }
 
 gls_status fused_demosaic(gls_ctx* ctx, const DemosaicArgs& a, bool raw_u16, bool half) {

@@ -61,7 +61,7 @@ struct gls_raw_converter {
     int w = 0, h = 0, L = 0;
     bool half = false;
     std::vector<DevBuf> owned;
-    ImgRef scaled{}, green{}, linA{}, linB{}, mask{}, hnA{}, hnB{};
+    ImgRef scaled{}, green{}, linA{}, linB{}, mask{}, hnA{}, hnB{}, split_green{};
     ImgRef pyr[GLS_MAX_LEVELS]{}, den[GLS_MAX_LEVELS]{};
     float* nlf_dev = nullptr;  // slot 0: raw {A0..A3, B0..B3}; slot 1+i: level i {A0..A2, B0..B2, -, -}
     void* nlf_scratch = nullptr;
@@ -159,7 +159,7 @@ struct gls_raw_converter {
             cudaStreamSynchronize(ctx->stream);
             release();
             for (int i = 0; i < GLS_MAX_LEVELS; i++) pyr[i] = den[i] = ImgRef{};
-            green = linA = linB = mask = scaled = hnA = hnB = ImgRef{};
+            green = linA = linB = mask = scaled = hnA = hnB = split_green = ImgRef{};
             staged_alloc = high_noise_alloc = learned_alloc = false;
             half = half_storage;
             {
@@ -194,6 +194,20 @@ struct gls_raw_converter {
         h = height;
         L = levels;
         set_views();
+        return GLS_OK;
+    }
+
+    // the green image between the split demosaic's two kernels (a tile shape of the tuner),
+    // allocated on first use at the capacity
+    gls_status ensure_split_green() {
+        if (split_green.ptr) {
+            split_green.w = w;
+            split_green.h = h;
+            return GLS_OK;
+        }
+        GLS_CHECK(img(split_green, cap_w, cap_h, 1));
+        split_green.w = w;
+        split_green.h = h;
         return GLS_OK;
     }
 
@@ -358,6 +372,9 @@ struct gls_raw_converter {
         da.tap_green = tap_ptr(1);
         da.tap_pitch = w;
         da.rawA_dev = nlf_dev;
+        GLS_CHECK(ensure_split_green());
+        da.green = split_green.ptr;
+        da.green_pitch = split_green.pitch;
         const bool learned = cnn != nullptr && !cnn_input_only;
         if (learned) GLS_CHECK(ensure_learned());
         da.cnn_in = cnn_input_only ? cnn_input_only : (learned ? cnn_in : nullptr);

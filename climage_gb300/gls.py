@@ -192,7 +192,7 @@ SIGNATURES = [
 
 # launch-shape tuner: kernels and their compiled tile shapes (gls_tune_force / gls_tune_entry)
 TUNE_DEMOSAIC, TUNE_FINAL = 0, 1
-TUNE_SHAPES = {TUNE_DEMOSAIC: ("44x28", "32x24", "64x32"), TUNE_FINAL: ("32x24", "32x16", "64x16")}
+TUNE_SHAPES = {TUNE_DEMOSAIC: ("44x28", "32x24", "64x32", "split"), TUNE_FINAL: ("32x24", "32x16", "64x16")}
 
 
 def lib():

@@ -432,7 +432,8 @@ GLS_API gls_status gls_raw_batch_plan(int n, const int* widths, const int* heigh
 
 /* ---- launch-shape tuner (no counterpart in the reference; its work-group sizes come from
  * src/gls_cl.cpp:227-261, computeWorkGroupSizes) ----
- * The demosaic (kernel 0: tiles 44x28, 32x24, 64x32) and the final stage (kernel 1: tiles
+ * The demosaic (kernel 0: tiles 44x28, 32x24, 64x32, or split in a green kernel and a
+ * red/blue + despeckle kernel through a green image) and the final stage (kernel 1: tiles
  * 32x16, 64x16) are compiled for several tile shapes that compute the same values.  On the
  * first frame of a size (and storage/input form) the converter times every shape on that
  * frame (best of three) and keeps the fastest for the process if it beats shape 0 by 3 %

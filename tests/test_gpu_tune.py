@@ -69,6 +69,6 @@ def test_a_frame_records_one_choice_per_kernel(ctx, unforced):
 
 
 def test_force_rejects_unknown_shapes(ctx):
-    for kernel, shape in ((gls.TUNE_DEMOSAIC, 3), (gls.TUNE_FINAL, -2), (2, 0)):
+    for kernel, shape in ((gls.TUNE_DEMOSAIC, len(gls.TUNE_SHAPES[gls.TUNE_DEMOSAIC])), (gls.TUNE_FINAL, -2), (2, 0)):
         with pytest.raises(gls.GlsError):
             gls.tune_force(kernel, shape)
