@@ -10,7 +10,7 @@ frame on its own stream).
 
 value: MPix/s with the raw frames already in HBM, CUDA-event timed per step with an L2
 flush (a 256 MB write) between steps, max over ranks.  e2e: the same frames through the
-host-buffer burst entry point (pinned uint16 in, RGBA8 out, copies inside the timed region).
+host-buffer burst entry point (pinned uint16 in, RGB8 out, copies inside the timed region).
 --impl reference times the CPU restatement of the reference pipeline (the oracle; the
 reference's OpenCL kernels cannot run on this machine) with every host thread, three frames
 per step as above; that arm imports no module of the product package and maps none of its
@@ -618,7 +618,7 @@ def main(argv=None):
         e2e = {"value": round(replica_value(world, mpix_per_step, args.steps, 1e3 * e2e_s), 3), "unit": "MPix/s",
                "h2d_bytes_per_step": int(sum(f[0].nbytes for f in frames)),
                "d2h_bytes_per_step": int(len(frames) * w * h * 3), "output": "rgb8 host buffers",
-               "overlap": "uploads one frame at a time; the final stage in 4 row bands, each copied back "
+               "overlap": "uploads one frame at a time; the final stage in 8 row bands, each copied back "
                           "while the next band runs"}
         # the same burst from packed 12-bit host frames (an uncompressed DNG strip's layout):
         # the packed bytes cross to the device and are unpacked there

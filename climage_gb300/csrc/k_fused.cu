@@ -970,6 +970,18 @@ __global__ void __launch_bounds__(kT, 3) pyramid_stats_kernel(const __grid_const
     if (threadIdx.x == 0) {
         __threadfence();
         if (atomicAdd(&a.ctl->exits, 1u) == gridDim.x - 1) {
+            __threadfence();
+            // a level whose tile count is still open was not solved (a block gave up a wait and
+            // recorded it in the error word): clear its count and the partial totals the other
+            // blocks added, so that the next launch starts from empty sums
+            for (int l = 0; l < a.nlev; l++) {
+                if (atomicExch(&a.ctl->flushed[l], 0u) == 0u) continue;
+                const NlfScratch& s = a.lv[l].nlf;
+                for (int k = 0; k < 3 * kNlfK; k++) s.tot_limb[k] = 0ull;
+                for (int k = 0; k < kNlfKF; k++) s.tot_mm[k] = 0u;
+                *s.tot_nan = 0u;
+                *s.ticket = 0u;
+            }
             a.ctl->queue = 0u;
             a.ctl->exits = 0u;
             __threadfence();

@@ -121,7 +121,7 @@ struct gls_raw_converter {
         int channels = 4, w = 0, h = 0;
         int bands = 0;  // bands whose copies were enqueued
     } host_band;
-    static constexpr int kHostBands = 4;
+    static constexpr int kHostBands = 8;
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t band_ev[kHostBands + 1] = {};  // after each band's launch; [kHostBands]: the last copy
     bool staged_alloc = false, high_noise_alloc = false;
