@@ -9,6 +9,7 @@
 #include <stdint.h>
 
 #include "gls_clmath.h"
+#include "gls_f32x2.cuh"
 
 namespace gls {
 
@@ -161,12 +162,16 @@ template <class Acc>
 GLS_DI float4 sample4(const Acc& im, const BilinearTap& t) {
     const float4 p00 = im.at(t.i0, t.j0), p10 = im.at(t.i0 + 1, t.j0);
     const float4 p01 = im.at(t.i0, t.j0 + 1), p11 = im.at(t.i0 + 1, t.j0 + 1);
-    float4 r;
-    r.x = t.w00 * p00.x + t.w10 * p10.x + t.w01 * p01.x + t.w11 * p11.x;
-    r.y = t.w00 * p00.y + t.w10 * p10.y + t.w01 * p01.y + t.w11 * p11.y;
-    r.z = t.w00 * p00.z + t.w10 * p10.z + t.w01 * p01.z + t.w11 * p11.z;
-    r.w = t.w00 * p00.w + t.w10 * p10.w + t.w01 * p01.w + t.w11 * p11.w;
-    return r;
+    // per channel w00 p00 + w10 p10 + w01 p01 + w11 p11, the channel pairs (x, y) and (z, w)
+    // as packed sums of scalar products
+    auto pair = [&](float2 a00, float2 a10, float2 a01, float2 a11) {
+        return add2(add2(add2(mul2s(f2(t.w00, t.w00), a00), mul2s(f2(t.w10, t.w10), a10)),
+                         mul2s(f2(t.w01, t.w01), a01)),
+                    mul2s(f2(t.w11, t.w11), a11));
+    };
+    const float2 xy = pair(f2(p00.x, p00.y), f2(p10.x, p10.y), f2(p01.x, p01.y), f2(p11.x, p11.y));
+    const float2 zw = pair(f2(p00.z, p00.w), f2(p10.z, p10.w), f2(p01.z, p01.w), f2(p11.z, p11.w));
+    return make_float4(xy.x, xy.y, zw.x, zw.y);
 }
 
 template <class Acc>
@@ -208,12 +213,15 @@ GLS_DI float4 tab_sample4(const float4* s, const TabTap& tx, const TabTap& ty) {
     const float w00 = tx.oma * ty.oma, w10 = tx.a * ty.oma, w01 = tx.oma * ty.a, w11 = tx.a * ty.a;
     const float4 p00 = s[ty.i0 + tx.i0], p10 = s[ty.i0 + tx.i1];
     const float4 p01 = s[ty.i1 + tx.i0], p11 = s[ty.i1 + tx.i1];
-    float4 r;
-    r.x = w00 * p00.x + w10 * p10.x + w01 * p01.x + w11 * p11.x;
-    r.y = w00 * p00.y + w10 * p10.y + w01 * p01.y + w11 * p11.y;
-    r.z = w00 * p00.z + w10 * p10.z + w01 * p01.z + w11 * p11.z;
-    r.w = w00 * p00.w + w10 * p10.w + w01 * p01.w + w11 * p11.w;
-    return r;
+    // the channel pairs (x, y) and (z, w) as packed sums of scalar products, each lane summed
+    // in the order of w00 p00 + w10 p10 + w01 p01 + w11 p11
+    auto pair = [&](float2 a00, float2 a10, float2 a01, float2 a11) {
+        return add2(add2(add2(mul2s(f2(w00, w00), a00), mul2s(f2(w10, w10), a10)), mul2s(f2(w01, w01), a01)),
+                    mul2s(f2(w11, w11), a11));
+    };
+    const float2 xy = pair(f2(p00.x, p00.y), f2(p10.x, p10.y), f2(p01.x, p01.y), f2(p11.x, p11.y));
+    const float2 zw = pair(f2(p00.z, p00.w), f2(p10.z, p10.w), f2(p01.z, p01.w), f2(p11.z, p11.w));
+    return make_float4(xy.x, xy.y, zw.x, zw.y);
 }
 
 GLS_DI float tab_sample_x(const float4* s, const TabTap& tx, const TabTap& ty) {
@@ -225,6 +233,27 @@ GLS_DI float tab_sample_x(const float4* s, const TabTap& tx, const TabTap& ty) {
 GLS_DI float tab_sample1(const float* s, const TabTap& tx, const TabTap& ty) {
     const float w00 = tx.oma * ty.oma, w10 = tx.a * ty.oma, w01 = tx.oma * ty.a, w11 = tx.a * ty.a;
     return w00 * s[ty.i0 + tx.i0] + w10 * s[ty.i0 + tx.i1] + w01 * s[ty.i1 + tx.i0] + w11 * s[ty.i1 + tx.i1];
+}
+
+// Two samples at once (a at (ax, ay), b at (bx, by)), each lane the value of tab_sample1 /
+// tab_sample_x: scalar weights and products, the sums as one packed chain.
+template <class V>
+GLS_DI float2 tab_sample_pair(V v, const TabTap& ax, const TabTap& ay, const TabTap& bx, const TabTap& by) {
+    const float a00 = ax.oma * ay.oma, a10 = ax.a * ay.oma, a01 = ax.oma * ay.a, a11 = ax.a * ay.a;
+    const float b00 = bx.oma * by.oma, b10 = bx.a * by.oma, b01 = bx.oma * by.a, b11 = bx.a * by.a;
+    return add2(add2(add2(mul2s(f2(a00, b00), f2(v(ay.i0 + ax.i0), v(by.i0 + bx.i0))),
+                          mul2s(f2(a10, b10), f2(v(ay.i0 + ax.i1), v(by.i0 + bx.i1)))),
+                     mul2s(f2(a01, b01), f2(v(ay.i1 + ax.i0), v(by.i1 + bx.i0)))),
+                mul2s(f2(a11, b11), f2(v(ay.i1 + ax.i1), v(by.i1 + bx.i1))));
+}
+
+GLS_DI float2 tab_sample1_x2(const float* s, const TabTap& ax, const TabTap& ay, const TabTap& bx, const TabTap& by) {
+    return tab_sample_pair([s](int i) { return s[i]; }, ax, ay, bx, by);
+}
+
+GLS_DI float2 tab_sample_x_x2(const float4* s, const TabTap& ax, const TabTap& ay, const TabTap& bx,
+                              const TabTap& by) {
+    return tab_sample_pair([s](int i) { return s[i].x; }, ax, ay, bx, by);
 }
 
 // ---------------------------------------------------------------------------------------

@@ -703,11 +703,10 @@ GLS_DI float4 guided_fast_px(const Acc4& im, int px, int py, const Nlf6& n) {
 template <class SharpF>
 GLS_DI float4 reassemble_from(float4 d0, float4 p1, float4 pd1, const SharpF& sharp, float sharpening, float nlf0,
                               float nlf1) {
-    float4 dp;
-    dp.x = d0.x - (p1.x - pd1.x);
-    dp.y = d0.y - (p1.y - pd1.y);
-    dp.z = d0.z - (p1.z - pd1.z);
-    dp.w = d0.w - (p1.w - pd1.w);
+    // dp = d0 - (p1 - pd1) per channel, the channel pairs packed
+    const float2 dxy = sub2(f2(d0.x, d0.y), sub2(f2(p1.x, p1.y), f2(pd1.x, pd1.y)));
+    const float2 dzw = sub2(f2(d0.z, d0.w), sub2(f2(p1.z, p1.w), f2(pd1.z, pd1.w)));
+    float4 dp = make_float4(dxy.x, dxy.y, dzw.x, dzw.y);
     if (sharpening > 1.0f) {
         const float4 g = sharp();
         const float dx = ((g.x - g.y) * 0.5f);
@@ -750,13 +749,13 @@ struct LtmParams {
 // the nine offsets, inp the denoised image at the pixel.
 GLS_DI float ltm_mask_from(const float (&gs)[9], float4 inp, const LtmParams& lp, const Mat3& m) {
     const float bw[9] = {0.16f, 0.16f, 0.08f, 0.16f, 0.16f, 0.08f, 0.08f, 0.08f, 0.04f};
-    float sum = 0.0f, sumSq = 0.0f;
+    float2 ss = f2(0.0f, 0.0f);  // (sum, sumSq) as one packed chain of scalar products
 #pragma unroll
     for (int i = 0; i < 9; i++) {
-        const float s = bw[i] * gs[i];
-        sum = sum + s;
-        sumSq = sumSq + s * s;
+        const float s = __fmul_rn(bw[i], gs[i]);
+        ss = add2(ss, f2(s, __fmul_rn(s, s)));
     }
+    const float sum = ss.x, sumSq = ss.y;
     const float mean = sum, var = sumSq - sum * sum;
     const float luma = inp.x;
     float filtered = 0.0f, knorm = 0.0f;
@@ -772,12 +771,37 @@ GLS_DI float ltm_mask_from(const float (&gs)[9], float4 inp, const LtmParams& lp
 #pragma unroll
     for (int i = 0; i < 9; i++) mag = mag + glsm::fabs_(gs[i]);
     const bool fast = dv.ok && den >= 9.5367431640625e-07f && mag <= 1048576.0f;  // 2^-20, 2^20; NaN fails
+    if (fast) {
+        // two taps per step: the numerators and the shortcut's quotients as packed lanes
+        // (num feeds a multiply and an fma only), the weights and the products that are
+        // summed as scalar multiplies, (filtered, knorm) as one packed chain
+        const float lm = luma - mean;
+        const float2 mv = f2(mean, mean), lmv = f2(lm, lm), yv = f2(dv.y, dv.y), ndv = f2(-dv.d, -dv.d);
+        float2 fk = f2(0.0f, 0.0f);
 #pragma unroll
-    for (int i = 0; i < 9; i++) {
-        const float num = (gs[i] - mean) * (luma - mean);
-        const float wgt = bw[i] * (1.0f + (fast ? dv.fast(num) : dv(num)));
-        filtered = filtered + wgt * gs[i];
-        knorm = knorm + wgt;
+        for (int i = 0; i < 9; i += 2) {
+            const bool two = i + 1 < 9;
+            const float2 g = f2(gs[i], two ? gs[i + 1] : gs[i]);
+            const float2 num = mul2(sub2(g, mv), lmv);
+            const float2 q0 = mul2(num, yv);
+            const float2 opq = add2(f2(1.0f, 1.0f), fma2(fma2(q0, ndv, num), yv, q0));
+            const float wa = __fmul_rn(bw[i], opq.x);
+            fk = add2(fk, f2(__fmul_rn(wa, g.x), wa));
+            if (two) {
+                const float wb = __fmul_rn(bw[i + 1], opq.y);
+                fk = add2(fk, f2(__fmul_rn(wb, g.y), wb));
+            }
+        }
+        filtered = fk.x;
+        knorm = fk.y;
+    } else {
+#pragma unroll
+        for (int i = 0; i < 9; i++) {
+            const float num = (gs[i] - mean) * (luma - mean);
+            const float wgt = bw[i] * (1.0f + dv(num));
+            filtered = filtered + wgt * gs[i];
+            knorm = knorm + wgt;
+        }
     }
     const float illuminance = div_(filtered, knorm);
     const float reflectance = div_(luma, illuminance);

@@ -669,11 +669,11 @@ GLS_DI void level_tile(const float4* s_in, const TabTap (*s_tx)[LT / 2], const T
             const float4 t1 = tab_sample4(s_in, s_tx[1][oc], s_ty[0][orow]);
             const float4 t2 = tab_sample4(s_in, s_tx[0][oc], s_ty[1][orow]);
             const float4 t3 = tab_sample4(s_in, s_tx[1][oc], s_ty[1][orow]);
-            float4 d;
-            d.x = 0.25f * (t0.x + t1.x + t2.x + t3.x);
-            d.y = 0.25f * (t0.y + t1.y + t2.y + t3.y);
-            d.z = 0.25f * (t0.z + t1.z + t2.z + t3.z);
-            d.w = 0.25f * (t0.w + t1.w + t2.w + t3.w);
+            // 0.25 (t0 + t1 + t2 + t3) per channel, the channel pairs packed
+            const float2 q = f2(0.25f, 0.25f);
+            const float2 xy = mul2(q, add2(add2(add2(f2(t0.x, t0.y), f2(t1.x, t1.y)), f2(t2.x, t2.y)), f2(t3.x, t3.y)));
+            const float2 zw = mul2(q, add2(add2(add2(f2(t0.z, t0.w), f2(t1.z, t1.w)), f2(t2.z, t2.w)), f2(t3.z, t3.w)));
+            const float4 d = make_float4(xy.x, xy.y, zw.x, zw.y);
             typedef typename Storage<SOut>::T4 TOut;
             Storage<SOut>::st4((TOut*)out + (size_t)oy * opitch + ox, d);
         }
@@ -1229,8 +1229,9 @@ __global__ void __launch_bounds__(kT) final_kernel(FinalArgs a) {
         const float4 p1 = tab_sample4(s_i1, T.rx[0][c], T.ry[0][r]);
         const float4 pd1 = tab_sample4(s_d1, T.rx[0][c], T.ry[0][r]);
         auto sharp = [&]() {
-            return make_float4(tab_sample_x(s_d1, T.rx[1][c], T.ry[0][r]), tab_sample_x(s_d1, T.rx[2][c], T.ry[0][r]),
-                               tab_sample_x(s_d1, T.rx[0][c], T.ry[1][r]), tab_sample_x(s_d1, T.rx[0][c], T.ry[2][r]));
+            const float2 gx = tab_sample_x_x2(s_d1, T.rx[1][c], T.ry[0][r], T.rx[2][c], T.ry[0][r]);
+            const float2 gy = tab_sample_x_x2(s_d1, T.rx[0][c], T.ry[1][r], T.rx[0][c], T.ry[2][r]);
+            return make_float4(gx.x, gx.y, gy.x, gy.y);
         };
         d = round4<S>(reassemble_from(d, p1, pd1, sharp, a.sharpening, n.a[0], n.b[0]));
         s_den[r * EW + c] = d;
@@ -1254,9 +1255,15 @@ __global__ void __launch_bounds__(kT) final_kernel(FinalArgs a) {
         if (a.tap_den) reinterpret_cast<float4*>(a.tap_den)[(size_t)y * a.tap_pitch + x] = den;
         float mask = 0.0f;
         if (LTM) {
-            float gs[9];
+            float gs[9];  // samples 0-7 in pairs: their sums as packed chains
 #pragma unroll
-            for (int k = 0; k < 9; k++) gs[k] = tab_sample1(s_g, T.gx[k % 3][c], T.gy[k / 3][r]);
+            for (int k = 0; k < 8; k += 2) {
+                const float2 v =
+                    tab_sample1_x2(s_g, T.gx[k % 3][c], T.gy[k / 3][r], T.gx[(k + 1) % 3][c], T.gy[(k + 1) / 3][r]);
+                gs[k] = v.x;
+                gs[k + 1] = v.y;
+            }
+            gs[8] = tab_sample1(s_g, T.gx[2][c], T.gy[2][r]);
             // the input is sampled at texel centres: after the 8-bit fraction each axis sits on
             // one texel (fraction 0 or 1), and with the bilateral's finite outputs the sample is
             // that texel's value (the other weights are zero)
