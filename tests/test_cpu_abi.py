@@ -6,6 +6,7 @@ import os
 import re
 
 import numpy as np
+import pytest
 
 from climage_gb300 import configs, gls
 
@@ -75,3 +76,23 @@ def test_tuner_cache_host_logic():
     assert l.gls_tune_entry(0, ctypes.byref(k), ctypes.byref(w), ctypes.byref(h), ctypes.byref(f), ctypes.byref(s),
                             ms) != 0  # no entry 0 in an empty cache
     gls.tune_reset()
+
+
+def test_bench_shapes_option():
+    """bench.py --shapes: 'kernel=shape' pairs by name reach the tuner's forced shapes; unknown
+    kernels or shapes are rejected before anything runs."""
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location(
+        "gls_bench_module", os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "bench.py"))
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    try:
+        bench.force_shapes(gls, "demosaic=split, final=32x16")
+        bench.force_shapes(gls, "")
+        with pytest.raises(KeyError):
+            bench.force_shapes(gls, "green=split")
+        with pytest.raises(ValueError):
+            bench.force_shapes(gls, "final=split")
+    finally:
+        gls.tune_reset()
