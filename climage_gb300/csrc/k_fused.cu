@@ -434,17 +434,41 @@ __global__ void __launch_bounds__(kT, 4) green_split_kernel(DemosaicArgs a) {
     __shared__ float4 s_sob[SH * SW];
     const int x0 = blockIdx.x * SGW, y0 = blockIdx.y * SGH;
     const int w = a.w, h = a.h, bayer = a.bayer;
-    for (int i = threadIdx.x; i < RH * RW; i += kT) {
-        const int r = i / RW, c = i - r * RW;
-        const int gx = clampi(x0 - 3 + c, 0, w - 1), gy = clampi(y0 - 3 + r, 0, h - 1);
-        float v;
-        if (RAW_U16) {
-            v = Storage<S>::round(scale_value(__ldg((const uint16_t*)a.in + (size_t)gy * a.in_pitch + gx),
-                                              a.sm[((gy & 1) << 1) | (gx & 1)], a.black));
-        } else {
-            v = Storage<S>::ldg((const S*)a.in + (size_t)gy * a.in_pitch + gx);
+    // An interior tile of uint16 raw whose rows start 8-byte aligned reads its region as
+    // 8-byte words: 72 pixels a row from x0 - 4 (x0 is a multiple of 64), one word per thread
+    // step, the first and last pixel of a row outside the staged 70; other tiles read pixel
+    // by pixel with the frame's edges clamped.
+    const bool words = RAW_U16 && x0 >= 4 && x0 + SGW + 4 <= w && y0 >= 3 && y0 + SGH + 3 <= h &&
+                       (reinterpret_cast<uintptr_t>(a.in) & 7u) == 0 && (a.in_pitch & 3) == 0;
+    if (words) {
+        constexpr int WPR = (RW + 2) / 4;  // words per row: 18
+        const uint16_t* base = (const uint16_t*)a.in + (size_t)(y0 - 3) * a.in_pitch + (x0 - 4);
+        for (int i = threadIdx.x; i < RH * WPR; i += kT) {
+            const int r = i / WPR, q = i - r * WPR;
+            const uint2 u = __ldg(reinterpret_cast<const uint2*>(base + (size_t)r * a.in_pitch) + q);
+            const int py = (y0 - 3 + r) & 1;
+            const float s0 = a.sm[py << 1], s1 = a.sm[(py << 1) | 1];  // even and odd columns
+            const uint16_t px[4] = {(uint16_t)(u.x & 0xffffu), (uint16_t)(u.x >> 16), (uint16_t)(u.y & 0xffffu),
+                                    (uint16_t)(u.y >> 16)};
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const int c = 4 * q + k - 1;  // staged column of pixel x0 - 4 + 4q + k
+                if (c >= 0 && c < RW) s_raw[r * RW + c] = Storage<S>::round(scale_value(px[k], (k & 1) ? s1 : s0, a.black));
+            }
         }
-        s_raw[i] = v;
+    } else {
+        for (int i = threadIdx.x; i < RH * RW; i += kT) {
+            const int r = i / RW, c = i - r * RW;
+            const int gx = clampi(x0 - 3 + c, 0, w - 1), gy = clampi(y0 - 3 + r, 0, h - 1);
+            float v;
+            if (RAW_U16) {
+                v = Storage<S>::round(scale_value(__ldg((const uint16_t*)a.in + (size_t)gy * a.in_pitch + gx),
+                                                  a.sm[((gy & 1) << 1) | (gx & 1)], a.black));
+            } else {
+                v = Storage<S>::ldg((const S*)a.in + (size_t)gy * a.in_pitch + gx);
+            }
+            s_raw[i] = v;
+        }
     }
     __syncthreads();
     const SAcc1 R{s_raw, x0 - 3, y0 - 3, RW};

@@ -23,6 +23,8 @@ CASES = [
     dict(w=338, h=246, bayer=1, bits=12, levels=4, storage=gls.STORAGE_F32, out_float=False, seed=61),
     dict(w=402, h=298, bayer=3, bits=14, levels=5, storage=gls.STORAGE_F16, out_float=False, seed=62),
     dict(w=290, h=214, bayer=0, bits=10, levels=4, storage=gls.STORAGE_F32, out_float=True, seed=63),
+    # rows a multiple of 4 pixels: interior tiles of the split green kernel read 8-byte words
+    dict(w=416, h=256, bayer=2, bits=12, levels=4, storage=gls.STORAGE_F32, out_float=False, seed=66),
 ]
 
 
