@@ -305,18 +305,55 @@ __global__ void __launch_bounds__(kT, demosaic_min_blocks(TW, TH)) demosaic_kern
     const int tid = threadIdx.x;
     const bool border = x0 - 5 < 0 || y0 - 5 < 0 || x0 + TW + 5 > w || y0 + TH + 5 > h;
 
-    // 1. scaled raw tile (clamped reads)
-    for (int i = tid; i < RH * RW; i += kT) {
-        const int r = i / RW, c = i - r * RW;
-        const int gx = clampi(x0 - 5 + c, 0, w - 1), gy = clampi(y0 - 5 + r, 0, h - 1);
-        float v;
-        if (RAW_U16) {
-            v = Storage<S>::round(scale_value(__ldg((const uint16_t*)a.in + (size_t)gy * a.in_pitch + gx),
-                                              a.sm[((gy & 1) << 1) | (gx & 1)], a.black));
-        } else {
-            v = Storage<S>::ldg((const S*)a.in + (size_t)gy * a.in_pitch + gx);
+    // 1. scaled raw tile: an interior tile whose rows start aligned reads words of 4 pixels
+    // (uint16 raw: 8 bytes; the scaled raw in the storage precision: a float4 or half4), TW + 16
+    // a row from x0 - 8 (TW and so x0 are multiples of 4), the pixels outside the staged
+    // region skipped; other tiles read pixel by pixel, clamped to the frame
+    typedef typename Storage<S>::T4 T4;
+    constexpr int WPR = (TW + 16) / 4;
+    static_assert(TW % 4 == 0, "tile columns in words of 4 pixels");
+    const bool words = x0 >= 8 && x0 + TW + 8 <= w && y0 >= 5 && y0 + TH + 5 <= h && (a.in_pitch & 3) == 0 &&
+                       (reinterpret_cast<uintptr_t>(a.in) & (uintptr_t)(RAW_U16 ? 7 : sizeof(T4) - 1)) == 0;
+    if (words) {
+        for (int i = tid; i < RH * WPR; i += kT) {
+            const int r = i / WPR, q = i - r * WPR;
+            float v[4];
+            if (RAW_U16) {
+                const uint16_t* row = (const uint16_t*)a.in + (size_t)(y0 - 5 + r) * a.in_pitch + (x0 - 8);
+                const uint2 u = __ldg(reinterpret_cast<const uint2*>(row) + q);
+                const int py = (y0 - 5 + r) & 1;
+                const float s0 = a.sm[py << 1], s1 = a.sm[(py << 1) | 1];  // even and odd columns
+                v[0] = Storage<S>::round(scale_value((uint16_t)(u.x & 0xffffu), s0, a.black));
+                v[1] = Storage<S>::round(scale_value((uint16_t)(u.x >> 16), s1, a.black));
+                v[2] = Storage<S>::round(scale_value((uint16_t)(u.y & 0xffffu), s0, a.black));
+                v[3] = Storage<S>::round(scale_value((uint16_t)(u.y >> 16), s1, a.black));
+            } else {
+                const S* row = (const S*)a.in + (size_t)(y0 - 5 + r) * a.in_pitch + (x0 - 8);
+                const float4 f = Storage<S>::ldg4(reinterpret_cast<const T4*>(row) + q);
+                v[0] = f.x;
+                v[1] = f.y;
+                v[2] = f.z;
+                v[3] = f.w;
+            }
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const int c = 4 * q + k - 3;  // staged column of pixel x0 - 8 + 4q + k
+                if (c >= 0 && c < RW) s_raw[r * RW + c] = v[k];
+            }
         }
-        s_raw[i] = v;
+    } else {
+        for (int i = tid; i < RH * RW; i += kT) {
+            const int r = i / RW, c = i - r * RW;
+            const int gx = clampi(x0 - 5 + c, 0, w - 1), gy = clampi(y0 - 5 + r, 0, h - 1);
+            float v;
+            if (RAW_U16) {
+                v = Storage<S>::round(scale_value(__ldg((const uint16_t*)a.in + (size_t)gy * a.in_pitch + gx),
+                                                  a.sm[((gy & 1) << 1) | (gx & 1)], a.black));
+            } else {
+                v = Storage<S>::ldg((const S*)a.in + (size_t)gy * a.in_pitch + gx);
+            }
+            s_raw[i] = v;
+        }
     }
     __syncthreads();
     const SAcc1 R{s_raw, x0 - 5, y0 - 5, RW};
@@ -518,18 +555,49 @@ __global__ void __launch_bounds__(kT, 5) rb_despeckle_kernel(DemosaicArgs a) {
     const int w = a.w, h = a.h, bayer = a.bayer;
     const bool border = x0 - 2 < 0 || y0 - 2 < 0 || x0 + TW + 2 > w || y0 + TH + 2 > h;
     const S* const green = (const S*)a.green;
-    for (int i = threadIdx.x; i < RH * RW; i += kT) {
-        const int r = i / RW, c = i - r * RW;
-        const int gx = clampi(x0 - 2 + c, 0, w - 1), gy = clampi(y0 - 2 + r, 0, h - 1);
-        float v;
-        if (RAW_U16) {
-            v = Storage<S>::round(scale_value(__ldg((const uint16_t*)a.in + (size_t)gy * a.in_pitch + gx),
-                                              a.sm[((gy & 1) << 1) | (gx & 1)], a.black));
-        } else {
-            v = Storage<S>::ldg((const S*)a.in + (size_t)gy * a.in_pitch + gx);
+    typedef typename Storage<S>::T4 T4;
+    // An interior tile of uint16 raw whose raw and green rows start aligned reads both regions
+    // as words of 4 pixels: 52 a row from x0 - 4 (x0 is a multiple of 44, so of 4), the two
+    // pixels each side outside the staged 48; other tiles read pixel by pixel, clamped.
+    const bool words = RAW_U16 && x0 >= 4 && x0 + TW + 4 <= w && y0 >= 2 && y0 + TH + 2 <= h &&
+                       (reinterpret_cast<uintptr_t>(a.in) & 7u) == 0 && (a.in_pitch & 3) == 0 &&
+                       (reinterpret_cast<uintptr_t>(green) & (sizeof(T4) - 1)) == 0 && (a.green_pitch & 3) == 0;
+    if (words) {
+        constexpr int WPR = (RW + 4) / 4;  // words per row: 13
+        const uint16_t* rbase = (const uint16_t*)a.in + (size_t)(y0 - 2) * a.in_pitch + (x0 - 4);
+        const S* gbase = green + (size_t)(y0 - 2) * a.green_pitch + (x0 - 4);
+        for (int i = threadIdx.x; i < RH * WPR; i += kT) {
+            const int r = i / WPR, q = i - r * WPR;
+            const uint2 u = __ldg(reinterpret_cast<const uint2*>(rbase + (size_t)r * a.in_pitch) + q);
+            const float4 g4 = Storage<S>::ldg4(reinterpret_cast<const T4*>(gbase + (size_t)r * a.green_pitch) + q);
+            const int py = (y0 - 2 + r) & 1;
+            const float s0 = a.sm[py << 1], s1 = a.sm[(py << 1) | 1];  // even and odd columns
+            const uint16_t px[4] = {(uint16_t)(u.x & 0xffffu), (uint16_t)(u.x >> 16), (uint16_t)(u.y & 0xffffu),
+                                    (uint16_t)(u.y >> 16)};
+            const float gv[4] = {g4.x, g4.y, g4.z, g4.w};
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const int c = 4 * q + k - 2;  // staged column of pixel x0 - 4 + 4q + k
+                if (c >= 0 && c < RW) {
+                    s_raw[r * RW + c] = Storage<S>::round(scale_value(px[k], (k & 1) ? s1 : s0, a.black));
+                    s_green[r * RW + c] = gv[k];
+                }
+            }
         }
-        s_raw[i] = v;
-        s_green[i] = Storage<S>::ldg(green + (size_t)gy * a.green_pitch + gx);
+    } else {
+        for (int i = threadIdx.x; i < RH * RW; i += kT) {
+            const int r = i / RW, c = i - r * RW;
+            const int gx = clampi(x0 - 2 + c, 0, w - 1), gy = clampi(y0 - 2 + r, 0, h - 1);
+            float v;
+            if (RAW_U16) {
+                v = Storage<S>::round(scale_value(__ldg((const uint16_t*)a.in + (size_t)gy * a.in_pitch + gx),
+                                                  a.sm[((gy & 1) << 1) | (gx & 1)], a.black));
+            } else {
+                v = Storage<S>::ldg((const S*)a.in + (size_t)gy * a.in_pitch + gx);
+            }
+            s_raw[i] = v;
+            s_green[i] = Storage<S>::ldg(green + (size_t)gy * a.green_pitch + gx);
+        }
     }
     __syncthreads();
     const SAcc1 R{s_raw, x0 - 2, y0 - 2, RW};

@@ -39,10 +39,13 @@ def test_every_tile_shape_equals_the_oracle(ctx, unforced, kernel, case):
         check(ctx, raw, spec, out_float=c["out_float"])
 
 
-def test_high_noise_branch_every_demosaic_shape(ctx, unforced):
-    # the high-noise branch feeds the demosaic pre-scaled, denoised raw (the other input form)
-    raw, _, meta = synthetic.make_frame(258, 194, bayer=2, gain=16.0, read_sigma=12.0, seed=64)
-    spec = configs.make_spec(meta, levels=4, noise_level=0.7)
+@pytest.mark.parametrize("w,h,storage", [(258, 194, gls.STORAGE_F32), (416, 256, gls.STORAGE_F16)],
+                         ids=["258x194-fp32", "416x256-fp16"])
+def test_high_noise_branch_every_demosaic_shape(ctx, unforced, w, h, storage):
+    # the high-noise branch feeds the demosaic pre-scaled, denoised raw (the other input form);
+    # rows a multiple of 4 pixels let interior tiles read it in words of 4 pixels
+    raw, _, meta = synthetic.make_frame(w, h, bayer=2, gain=16.0, read_sigma=12.0, seed=64)
+    spec = configs.make_spec(meta, levels=4, noise_level=0.7, storage=storage)
     for shape in range(len(gls.TUNE_SHAPES[gls.TUNE_DEMOSAIC])):
         gls.tune_force(gls.TUNE_DEMOSAIC, shape)
         check(ctx, raw, spec)
