@@ -224,7 +224,7 @@ def algorithmic_bytes_per_px(S, O, L):
 # storage, RGBA8 out; the demosaic in its split shape, the green kernel and the red/blue +
 # despeckle kernel together, issue use weighted by time); the roofline fraction is computed
 # live, these explain it.
-NCU_TRAFFIC = {"denoise L0+LTM+sRGB": (235657984, 76.4), "demosaic": (153797120, 78.3)}
+NCU_TRAFFIC = {"denoise L0+LTM+sRGB": (235657984, 76.4), "demosaic": (151781632, 80.1)}
 
 
 # Compulsory bytes per full-resolution pixel of each full-resolution kernel (what it must
